@@ -1,0 +1,587 @@
+// erlbm_abi.cu -- C ABI of the single-lattice engine (include/erlbm_gb300.h).
+//
+// A handle owns one lattice on the device: two SoA population buffers (ping-pong), an optional
+// solid mask and fluid-index map, a staging buffer for the caller's AoS arrays, reduction
+// scratch, a run-status block and its own CUDA stream.
+//
+// State machine.  The reference's drivers hold post-stream populations at the top of each step.
+// The kernels here fuse "stream of step s-1" with "boundary + collision of step s", so between
+// launches the buffer holds post-collision populations with the stream still pending:
+//   after erlbm_set_populations: kind = PRE   (buffer = post-stream populations, as given)
+//   after >= 1 step:             kind = POST  (buffer = post-collision populations of the last step)
+// The first step after a set collides the given populations in place (mode 1); every later step
+// pulls (mode 0).  Post-stream populations of a POST state are produced on demand by a stream-only
+// pass into the spare buffer, so nothing the caller can observe differs from the reference loop.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/erlbm_gb300.h"
+#include "abi_internal.h"
+#include "kernels_api.h"
+
+using namespace erlbm;
+
+namespace erlbm {
+
+static thread_local std::string g_last_error;
+
+void set_error(const char *fmt, const char *a, const char *b)
+{
+    char buf[512];
+    snprintf(buf, sizeof(buf), fmt, a ? a : "", b ? b : "");
+    g_last_error = buf;
+}
+
+int cuda_fail(cudaError_t e, const char *where)
+{
+    set_error("CUDA error in %s: %s", where, cudaGetErrorString(e));
+    return ERLBM_E_CUDA;
+}
+
+}  // namespace erlbm
+
+#define CK(call)                                              \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+#define CKL(rc, what)                                                                  \
+    do {                                                                               \
+        int r_ = (rc);                                                                 \
+        if (r_ != 0) {                                                                 \
+            cudaError_t e_ = cudaGetLastError();                                       \
+            if (e_ != cudaSuccess) return cuda_fail(e_, what);                         \
+            set_error("launch of %s rejected its arguments%s", what, "");              \
+            return ERLBM_E_INVAL;                                                      \
+        }                                                                              \
+    } while (0)
+
+struct erlbm_handle {
+    int q = 0, prec = 0, op = 0, device = 0;
+    double tau = 0, tau_nh = 0;
+    Relax R{};
+    Geo g{};
+    long long n_fluid = 0;
+    uint8_t *d_solid = nullptr;
+    int *d_nof = nullptr;            // node of fluid index (null for periodic boxes)
+    void *d_buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    int kind = 0;                    // 0 PRE (post-stream), 1 POST (post-collision, stream pending)
+    long long steps_done = 0;
+    double *d_aos = nullptr;         // staging: n_fluid * q doubles
+    double *d_scr = nullptr;         // n_fluid doubles of per-node values + 4096 reduction scratch
+    double *d_out = nullptr;         // small device result block
+    RunStatus *d_status = nullptr;
+    cudaStream_t stream = nullptr;
+    size_t elem() const { return prec == ERLBM_FP64 ? sizeof(double) : sizeof(float); }
+};
+
+namespace {
+
+int check_handle(const erlbm_handle *h)
+{
+    if (!h) {
+        set_error("null handle%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    return ERLBM_OK;
+}
+
+int check_op(int op)
+{
+    if (op == ERLBM_OP_BGK || op == ERLBM_OP_REG || op == ERLBM_OP_EXTREG) return ERLBM_OK;
+    if (op == ERLBM_OP_MRT) {
+        set_error("collision operator MRT is not provided by this library%s%s", "", "");
+        return ERLBM_E_UNSUPPORTED;
+    }
+    set_error("unknown collision operator (use BGK=1, REG=3, EXTREG=4)%s%s", "", "");
+    return ERLBM_E_INVAL;
+}
+
+void free_handle(erlbm_handle *h)
+{
+    if (!h) return;
+    cudaFree(h->d_solid);
+    cudaFree(h->d_nof);
+    cudaFree(h->d_buf[0]);
+    cudaFree(h->d_buf[1]);
+    cudaFree(h->d_aos);
+    cudaFree(h->d_scr);
+    cudaFree(h->d_out);
+    cudaFree(h->d_status);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+// Buffer holding the populations of `stage`; may run the stream-only pass into the spare buffer.
+int stage_buffer(erlbm_handle *h, int stage, const void **out)
+{
+    if (stage != ERLBM_STAGE_POST_STREAM && stage != ERLBM_STAGE_POST_COLLISION) {
+        set_error("unknown stage%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    if (h->kind == 0) {
+        if (stage == ERLBM_STAGE_POST_COLLISION) {
+            set_error("no collision has run since the populations were set%s%s", "", "");
+            return ERLBM_E_STATE;
+        }
+        *out = h->d_buf[h->cur];
+        return ERLBM_OK;
+    }
+    if (stage == ERLBM_STAGE_POST_COLLISION) {
+        *out = h->d_buf[h->cur];
+        return ERLBM_OK;
+    }
+    void *spare = h->d_buf[h->cur ^ 1];
+    if (h->prec == ERLBM_FP64)
+        CKL(launch_stream_only_fp64(h->q, h->g, (const double *)h->d_buf[h->cur], (double *)spare, h->stream),
+            "stream_only");
+    else
+        CKL(launch_stream_only_fp32(h->q, h->g, (const float *)h->d_buf[h->cur], (float *)spare, h->stream),
+            "stream_only");
+    *out = spare;
+    return ERLBM_OK;
+}
+
+int node_fields(erlbm_handle *h, const void *buf, double *e, double *rho, double *u)
+{
+    if (h->prec == ERLBM_FP64)
+        CKL(launch_node_fields_fp64(h->q, h->g, h->n_fluid, h->d_nof, (const double *)buf, e, rho, u, h->stream),
+            "node_fields");
+    else
+        CKL(launch_node_fields_fp32(h->q, h->g, h->n_fluid, h->d_nof, (const float *)buf, e, rho, u, h->stream),
+            "node_fields");
+    return ERLBM_OK;
+}
+
+int ensure_aos(erlbm_handle *h)
+{
+    if (h->d_aos) return ERLBM_OK;
+    const size_t bytes = (size_t)h->n_fluid * h->q * sizeof(double);
+    if (cudaMalloc(&h->d_aos, bytes ? bytes : 8) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("out of device memory for the staging buffer%s%s", "", "");
+        return ERLBM_E_OOM;
+    }
+    return ERLBM_OK;
+}
+
+int validate_bc(const erlbm_handle *h, const erlbm_bc *bc, BCp *out)
+{
+    out->inlet_x = -1;
+    out->outlet_x = -1;
+    out->u_in = 0;
+    out->rho_out = 1;
+    if (!bc) return ERLBM_OK;
+    if (bc->inlet_x >= 0) {
+        if (h->q != 19) {
+            set_error("the Zou-He inlet is a D3Q19 boundary (ZouHeD3Q19_vx_x)%s%s", "", "");
+            return ERLBM_E_UNSUPPORTED;
+        }
+        if (bc->inlet_x >= h->g.nx) {
+            set_error("inlet plane outside the box%s%s", "", "");
+            return ERLBM_E_INVAL;
+        }
+        out->inlet_x = bc->inlet_x;
+        out->u_in = bc->u_in;
+    }
+    if (bc->outlet_x >= 0) {
+        if (bc->outlet_x >= h->g.nx || h->g.nx < 2) {
+            set_error("outlet plane outside the box%s%s", "", "");
+            return ERLBM_E_INVAL;
+        }
+        const int nb = bc->outlet_x + (bc->outlet_x < h->g.nx / 2 ? 1 : -1);
+        if (nb < 0 || nb >= h->g.nx) {
+            set_error("outlet plane has no inner neighbour%s%s", "", "");
+            return ERLBM_E_INVAL;
+        }
+        out->outlet_x = bc->outlet_x;
+        out->rho_out = bc->rho_out;
+    }
+    return ERLBM_OK;
+}
+
+// Enqueue one step.  status/check_density are used by erlbm_run.
+int enqueue_step(erlbm_handle *h, const BCp &bc, int check_density, double density_limit, bool stop_on_flag)
+{
+    StepArgs a;
+    a.mode = h->kind == 0 ? 1 : 0;
+    a.step_index = (int)h->steps_done;
+    a.check_density = check_density;
+    a.density_limit = density_limit;
+    a.status = (check_density || stop_on_flag) ? h->d_status : nullptr;
+    a.stop_on_flag = stop_on_flag ? 1 : 0;
+    void *src = h->d_buf[h->cur], *dst = h->d_buf[h->cur ^ 1];
+    const bool plain = bc.inlet_x < 0 && bc.outlet_x < 0 && !check_density && !stop_on_flag && a.mode == 0;
+    if (h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && plain && periodic_d2q9_fp32_ok(h->g)) {
+        CKL(launch_periodic_d2q9_fp32(h->op, h->g, h->R, (const float *)src, (float *)dst, h->stream), "periodic_d2q9");
+    } else if (h->prec == ERLBM_FP64) {
+        CKL(launch_step_fp64(h->q, h->op, h->g, bc, h->R, a, (const double *)src, (double *)dst, h->stream), "step");
+    } else {
+        CKL(launch_step_fp32(h->q, h->op, h->g, bc, h->R, a, (const float *)src, (float *)dst, h->stream), "step");
+    }
+    h->cur ^= 1;
+    h->kind = 1;
+    h->steps_done++;
+    return ERLBM_OK;
+}
+
+int energy_now(erlbm_handle *h, int stage, double *E)
+{
+    const void *buf;
+    int rc = stage_buffer(h, stage, &buf);
+    if (rc) return rc;
+    if ((rc = node_fields(h, buf, h->d_scr, nullptr, nullptr))) return rc;
+    // serial order (the reference's) up to 2^16 nodes, fixed-shape tree above
+    CKL(launch_sum(h->d_scr, h->n_fluid, 1 << 16, h->d_scr + h->n_fluid, h->d_out, h->stream), "sum");
+    CK(cudaMemcpyAsync(E, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return ERLBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int erlbm_version(void) { return 10000; }
+
+const char *erlbm_strerror(int code)
+{
+    switch (code) {
+    case ERLBM_OK: return "ok";
+    case ERLBM_E_INVAL: return "invalid argument";
+    case ERLBM_E_OOM: return "out of memory";
+    case ERLBM_E_CUDA: return "CUDA error";
+    case ERLBM_E_TIMEOUT: return "timeout";
+    case ERLBM_E_NONFINITE: return "non-finite value";
+    case ERLBM_E_UNSUPPORTED: return "unsupported";
+    case ERLBM_E_STATE: return "invalid state";
+    default: return "unknown error";
+    }
+}
+
+const char *erlbm_last_error(void) { return g_last_error.c_str(); }
+
+int erlbm_create(const erlbm_desc *d, erlbm_handle **out)
+{
+    if (!d || !out) {
+        set_error("null argument%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    *out = nullptr;
+    if (d->q != 9 && d->q != 19) {
+        set_error("q must be 9 (D2Q9) or 19 (D3Q19)%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    if (d->nx < 1 || d->ny < 1 || d->nz < 1 || (d->q == 9 && d->nz != 1)) {
+        set_error("bad lattice extent (D2Q9 needs nz = 1)%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    if ((long long)d->nx * d->ny * d->nz > (1LL << 31) - 1) {
+        set_error("lattice too large for 32-bit node indices%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    if (d->precision != ERLBM_FP64 && d->precision != ERLBM_FP32_SHIFTED) {
+        set_error("unknown precision%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    int rc = check_op(d->op);
+    if (rc) return rc;
+    if (!(d->tau > 0) || !std::isfinite(d->tau) || !std::isfinite(d->tau_nh) || d->tau_nh == 0) {
+        set_error("tau and tau_nh must be finite and non-zero%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    erlbm_handle *h = new (std::nothrow) erlbm_handle();
+    if (!h) return ERLBM_E_OOM;
+    h->q = d->q;
+    h->prec = d->precision;
+    h->op = d->op;
+    h->tau = d->tau;
+    h->tau_nh = d->tau_nh;
+    h->R = make_relax(d->tau, d->tau_nh, d->op);
+    h->g.nx = d->nx;
+    h->g.ny = d->ny;
+    h->g.nz = d->nz;
+    h->g.nbox = (long long)d->nx * d->ny * d->nz;
+    h->g.plane = (h->g.nbox + 63) / 64 * 64;
+    h->g.solid = nullptr;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&h->device)) != cudaSuccess) {
+        free_handle(h);
+        return cuda_fail(e, "cudaGetDevice");
+    }
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        free_handle(h);
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    std::vector<int> nof;
+    h->n_fluid = h->g.nbox;
+    if (d->solid) {
+        bool any = false;
+        for (long long k = 0; k < h->g.nbox; k++) any |= d->solid[k] != 0;
+        if (any) {
+            nof.reserve(h->g.nbox);
+            for (long long k = 0; k < h->g.nbox; k++)
+                if (!d->solid[k]) nof.push_back((int)k);
+            h->n_fluid = (long long)nof.size();
+        }
+    }
+    const size_t pop_bytes = (size_t)h->q * h->g.plane * h->elem();
+    bool ok = cudaMalloc(&h->d_buf[0], pop_bytes) == cudaSuccess && cudaMalloc(&h->d_buf[1], pop_bytes) == cudaSuccess &&
+              cudaMalloc(&h->d_scr, ((size_t)h->n_fluid + 4096) * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&h->d_out, 64 * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&h->d_status, sizeof(RunStatus)) == cudaSuccess;
+    if (ok && !nof.empty()) {
+        ok = cudaMalloc(&h->d_solid, h->g.nbox) == cudaSuccess &&
+             cudaMalloc(&h->d_nof, nof.size() * sizeof(int)) == cudaSuccess;
+        if (ok) {
+            ok = cudaMemcpy(h->d_solid, d->solid, h->g.nbox, cudaMemcpyHostToDevice) == cudaSuccess &&
+                 cudaMemcpy(h->d_nof, nof.data(), nof.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
+            h->g.solid = h->d_solid;
+        }
+    }
+    if (!ok) {
+        cudaError_t le = cudaGetLastError();
+        free_handle(h);
+        if (le == cudaErrorMemoryAllocation) {
+            set_error("out of device memory%s%s", "", "");
+            return ERLBM_E_OOM;
+        }
+        return cuda_fail(le, "erlbm_create");
+    }
+    // populations start as zeros (new double[] of the reference is uninitialised; callers set them)
+    if ((e = cudaMemsetAsync(h->d_buf[0], 0, pop_bytes, h->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(h->d_buf[1], 0, pop_bytes, h->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(h->stream)) != cudaSuccess) {
+        free_handle(h);
+        return cuda_fail(e, "erlbm_create");
+    }
+    *out = h;
+    return ERLBM_OK;
+}
+
+int erlbm_destroy(erlbm_handle *h)
+{
+    if (!h) return ERLBM_OK;
+    cudaStreamSynchronize(h->stream);
+    free_handle(h);
+    return ERLBM_OK;
+}
+
+int erlbm_fluid_count(const erlbm_handle *h, int64_t *n)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!n) return ERLBM_E_INVAL;
+    *n = h->n_fluid;
+    return ERLBM_OK;
+}
+
+int erlbm_set_params(erlbm_handle *h, double tau, double tau_nh, int op)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if ((rc = check_op(op))) return rc;
+    if (!(tau > 0) || !std::isfinite(tau) || !std::isfinite(tau_nh) || tau_nh == 0) {
+        set_error("tau and tau_nh must be finite and non-zero%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    h->tau = tau;
+    h->tau_nh = tau_nh;
+    h->op = op;
+    h->R = make_relax(tau, tau_nh, op);
+    return ERLBM_OK;
+}
+
+int erlbm_set_populations(erlbm_handle *h, const double *aos, size_t n)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!aos || n != (size_t)h->n_fluid * h->q) {
+        set_error("population array must hold n_fluid * q doubles%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    if ((rc = ensure_aos(h))) return rc;
+    CK(cudaMemcpyAsync(h->d_aos, aos, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (h->prec == ERLBM_FP64)
+        CKL(launch_aos_to_soa_fp64(h->q, h->g, h->n_fluid, h->d_nof, h->d_aos, (double *)h->d_buf[h->cur], h->stream),
+            "aos_to_soa");
+    else
+        CKL(launch_aos_to_soa_fp32(h->q, h->g, h->n_fluid, h->d_nof, h->d_aos, (float *)h->d_buf[h->cur], h->stream),
+            "aos_to_soa");
+    h->kind = 0;
+    h->steps_done = 0;
+    // the caller may reuse its buffer as soon as we return
+    CK(cudaStreamSynchronize(h->stream));
+    return ERLBM_OK;
+}
+
+int erlbm_get_populations(erlbm_handle *h, double *aos, size_t n, int stage)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!aos || n != (size_t)h->n_fluid * h->q) {
+        set_error("population array must hold n_fluid * q doubles%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    if ((rc = ensure_aos(h))) return rc;
+    const void *buf;
+    if ((rc = stage_buffer(h, stage, &buf))) return rc;
+    if (h->prec == ERLBM_FP64)
+        CKL(launch_soa_to_aos_fp64(h->q, h->g, h->n_fluid, h->d_nof, (const double *)buf, h->d_aos, h->stream),
+            "soa_to_aos");
+    else
+        CKL(launch_soa_to_aos_fp32(h->q, h->g, h->n_fluid, h->d_nof, (const float *)buf, h->d_aos, h->stream),
+            "soa_to_aos");
+    CK(cudaMemcpyAsync(aos, h->d_aos, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return ERLBM_OK;
+}
+
+int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n_steps < 0) return ERLBM_E_INVAL;
+    BCp b;
+    if ((rc = validate_bc(h, bc, &b))) return rc;
+    for (int s = 0; s < n_steps; s++)
+        if ((rc = enqueue_step(h, b, 0, 0.0, false))) return rc;
+    return ERLBM_OK;
+}
+
+int erlbm_sync(erlbm_handle *h)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    return ERLBM_OK;
+}
+
+int erlbm_kinetic_energy(erlbm_handle *h, int stage, double *E)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!E) return ERLBM_E_INVAL;
+    return energy_now(h, stage, E);
+}
+
+int erlbm_max_abs_density(erlbm_handle *h, int stage, double *m, int *nonfinite)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    const void *buf;
+    if ((rc = stage_buffer(h, stage, &buf))) return rc;
+    if ((rc = node_fields(h, buf, nullptr, h->d_scr, nullptr))) return rc;
+    CKL(launch_maxabs(h->d_scr, h->n_fluid, h->d_scr + h->n_fluid, h->d_out, h->stream), "maxabs");
+    double r[2];
+    CK(cudaMemcpyAsync(r, h->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (m) *m = r[0];
+    if (nonfinite) *nonfinite = r[1] != 0.0;
+    return ERLBM_OK;
+}
+
+int erlbm_macroscopic(erlbm_handle *h, int stage, double *rho, double *u)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if ((rc = ensure_aos(h))) return rc;
+    const void *buf;
+    if ((rc = stage_buffer(h, stage, &buf))) return rc;
+    // d_aos holds n_fluid * q >= 4 * n_fluid doubles: rho first, then u
+    double *d_rho = h->d_aos, *d_u = h->d_aos + h->n_fluid;
+    if ((rc = node_fields(h, buf, nullptr, rho ? d_rho : nullptr, u ? d_u : nullptr))) return rc;
+    if (rho) CK(cudaMemcpyAsync(rho, d_rho, h->n_fluid * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (u) CK(cudaMemcpyAsync(u, d_u, 3 * h->n_fluid * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return ERLBM_OK;
+}
+
+int erlbm_run(erlbm_handle *h, int n_steps, const erlbm_bc *bc, const erlbm_checks *chk, erlbm_run_result *res)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n_steps < 0 || !res) return ERLBM_E_INVAL;
+    BCp b;
+    if ((rc = validate_bc(h, bc, &b))) return rc;
+    erlbm_checks c{};
+    if (chk) c = *chk;
+    if (c.energy_every < 0) return ERLBM_E_INVAL;
+    res->label = 0;
+    res->decided_step = n_steps;
+    res->steps_done = 0;
+    res->margin = 0.0;
+    RunStatus st0{0, 0x7fffffff, 0ull};
+    CK(cudaMemcpyAsync(h->d_status, &st0, sizeof(st0), cudaMemcpyHostToDevice, h->stream));
+    const long long base = h->steps_done;
+    const int cur0 = h->cur;
+    double E0 = 0.0;
+    if (c.energy_every > 0)
+        if ((rc = energy_now(h, ERLBM_STAGE_POST_STREAM, &E0))) return rc;
+    // Steps are enqueued in chunks ending at the next energy check; with density checks the
+    // kernels stop themselves one step after a failing step, and the host reads the status
+    // once per chunk.
+    const int chunk = c.energy_every > 0 ? c.energy_every : 512;
+    int s = 0;
+    while (s < n_steps) {
+        if (c.energy_every > 0 && s % c.energy_every == 0 && s > 0) {
+            double E;
+            if ((rc = energy_now(h, ERLBM_STAGE_POST_STREAM, &E))) return rc;
+            const double r = std::isfinite(E) ? E / (c.energy_factor * E0) : INFINITY;
+            if (r > res->margin) res->margin = r;
+            if (E > c.energy_factor * E0 || !std::isfinite(E)) {
+                res->label = 1;
+                res->decided_step = s;
+                res->steps_done = s;
+                return ERLBM_OK;
+            }
+        }
+        int m = chunk - (s % chunk);
+        if (s + m > n_steps) m = n_steps - s;
+        // keep the step numbering of the run itself in the kernels' step index
+        for (int k = 0; k < m; k++) {
+            h->steps_done = base + s + k;
+            if ((rc = enqueue_step(h, b, c.density_check, c.density_limit, c.density_check != 0))) return rc;
+        }
+        h->steps_done = base + s + m;
+        s += m;
+        if (c.density_check) {
+            RunStatus st;
+            CK(cudaMemcpyAsync(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            if (st.flags) {
+                double mx;
+                memcpy(&mx, &st.max_abs_rho_bits, sizeof(mx));
+                res->label = 1;
+                res->decided_step = st.decided_step - (int)base;
+                res->steps_done = res->decided_step + 1;
+                res->margin = (st.flags & 2) ? INFINITY : mx / c.density_limit;
+                h->steps_done = base + res->steps_done;
+                // launches after the failing step did nothing: the last written buffer is the one
+                // of step decided_step
+                h->cur = cur0 ^ (res->steps_done & 1);
+                CK(cudaStreamSynchronize(h->stream));
+                return ERLBM_OK;
+            }
+        }
+    }
+    if (c.density_check) {
+        RunStatus st;
+        CK(cudaMemcpyAsync(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        double mx;
+        memcpy(&mx, &st.max_abs_rho_bits, sizeof(mx));
+        res->margin = mx / c.density_limit;
+    }
+    res->steps_done = n_steps;
+    CK(cudaStreamSynchronize(h->stream));
+    return ERLBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+// k_fp32.cu -- FP32 shifted-population kernels (compiled with FMA contraction on).
+//
+// Besides the generic single-lattice kernels of lattice_kernels.cuh, this file holds the fused
+// periodic D2Q9 kernel used for the double-shear-layer lattices (L = 512 ... 2048): one warp
+// owns 128 consecutive nodes of a row, every lane four of them, so each direction plane is read
+// and written with 128-bit accesses.  The pull from x - c_x needs one neighbour column per
+// lane; it comes from the adjacent lane by a warp shuffle, and only the two warp-edge lanes
+// issue an extra 4-byte load (an L2 hit: the neighbouring warp reads that line too).
+// Algorithmic traffic is 2 * 9 * 4 = 72 bytes per lattice update.
+#include "lattice_kernels.cuh"
+
+namespace erlbm {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Pull one direction plane for the four nodes x0..x0+3 of row y (periodic in x and y).
+template <int CX>
+__device__ __forceinline__ float4 pull4(const float *__restrict__ row, int x0, int xl, int xr, int lane)
+{
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(row + x0));
+    if (CX == 0) return a;
+    if (CX == 1) {  // values at x0-1 .. x0+2
+        const float e = (lane == 0) ? __ldg(row + xl) : 0.f;
+        float p = __shfl_up_sync(FULL, a.w, 1);
+        if (lane == 0) p = e;
+        return make_float4(p, a.x, a.y, a.z);
+    }
+    // CX == -1: values at x0+1 .. x0+4
+    const float e = (lane == 31) ? __ldg(row + xr) : 0.f;
+    float n = __shfl_down_sync(FULL, a.x, 1);
+    if (lane == 31) n = e;
+    return make_float4(a.y, a.z, a.w, n);
+}
+
+__device__ __forceinline__ float comp(const float4 &v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+
+__device__ __forceinline__ void setc(float4 &v, int k, float x)
+{
+    if (k == 0)
+        v.x = x;
+    else if (k == 1)
+        v.y = x;
+    else if (k == 2)
+        v.z = x;
+    else
+        v.w = x;
+}
+
+template <int OP>
+__global__ void __launch_bounds__(256) k_periodic_d2q9(const float *__restrict__ src, float *__restrict__ dst, int nx,
+                                                        int ny, long long plane, shifted::Coef k)
+{
+    const int lane = threadIdx.x & 31;
+    const int wpr = nx >> 7;  // warps per row
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= (long long)wpr * ny) return;  // whole warps only
+    const int y = (int)(gw / wpr);
+    const int xw = (int)(gw % wpr) << 7;
+    const int x0 = xw + 4 * lane;
+    const int ym = (y == 0) ? ny - 1 : y - 1;  // row of populations moving +y
+    const int yp = (y == ny - 1) ? 0 : y + 1;  // row of populations moving -y
+    const int xl = (xw == 0) ? nx - 1 : xw - 1;
+    const int xr = (xw + 128 == nx) ? 0 : xw + 128;
+    const long long ry = (long long)y * nx, rm = (long long)ym * nx, rp = (long long)yp * nx;
+
+    float4 v[9];
+    v[0] = pull4<0>(src + 0 * plane + ry, x0, xl, xr, lane);
+    v[1] = pull4<1>(src + 1 * plane + ry, x0, xl, xr, lane);
+    v[2] = pull4<-1>(src + 2 * plane + ry, x0, xl, xr, lane);
+    v[3] = pull4<0>(src + 3 * plane + rm, x0, xl, xr, lane);
+    v[4] = pull4<0>(src + 4 * plane + rp, x0, xl, xr, lane);
+    v[5] = pull4<1>(src + 5 * plane + rm, x0, xl, xr, lane);
+    v[6] = pull4<-1>(src + 6 * plane + rp, x0, xl, xr, lane);
+    v[7] = pull4<1>(src + 7 * plane + rp, x0, xl, xr, lane);
+    v[8] = pull4<-1>(src + 8 * plane + rm, x0, xl, xr, lane);
+
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        float g[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) g[i] = comp(v[i], c);
+        shifted::collide9<OP>(g, k);
+#pragma unroll
+        for (int i = 0; i < 9; i++) setc(v[i], c, g[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; i++) *reinterpret_cast<float4 *>(dst + i * plane + ry + x0) = v[i];
+}
+
+}  // namespace
+
+bool periodic_d2q9_fp32_ok(const Geo &g)
+{
+    return g.solid == nullptr && g.nz == 1 && g.nx % 128 == 0 && g.ny >= 2 && g.plane % 4 == 0;
+}
+
+int launch_periodic_d2q9_fp32(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s)
+{
+    if (!periodic_d2q9_fp32_ok(g)) return -1;
+    const shifted::Coef k = shifted::make_coef(R);
+    const long long warps = (long long)(g.nx / 128) * g.ny;
+    const unsigned nb = (unsigned)((warps * 32 + 255) / 256);
+    switch (op) {
+    case OP_BGK:
+        k_periodic_d2q9<OP_BGK><<<nb, 256, 0, s>>>(src, dst, g.nx, g.ny, g.plane, k);
+        break;
+    case OP_REG:
+        k_periodic_d2q9<OP_REG><<<nb, 256, 0, s>>>(src, dst, g.nx, g.ny, g.plane, k);
+        break;
+    case OP_EXTREG:
+        k_periodic_d2q9<OP_EXTREG><<<nb, 256, 0, s>>>(src, dst, g.nx, g.ny, g.plane, k);
+        break;
+    default:
+        return -1;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+int launch_step_fp32(int q, int op, const Geo &g, const BCp &bc, const Relax &R, const StepArgs &a, const float *src,
+                     float *dst, cudaStream_t s)
+{
+    return step_any<PrecShifted32>(q, op, g, bc, R, a, src, dst, s);
+}
+
+int launch_stream_only_fp32(int q, const Geo &g, const float *src, float *dst, cudaStream_t s)
+{
+    return stream_only_any<PrecShifted32>(q, g, src, dst, s);
+}
+
+int launch_aos_to_soa_fp32(int q, const Geo &g, long long n, const int *nof, const double *aos, float *soa,
+                           cudaStream_t s)
+{
+    return aos_to_soa_any<PrecShifted32>(q, g, n, nof, aos, soa, s);
+}
+
+int launch_soa_to_aos_fp32(int q, const Geo &g, long long n, const int *nof, const float *soa, double *aos,
+                           cudaStream_t s)
+{
+    return soa_to_aos_any<PrecShifted32>(q, g, n, nof, soa, aos, s);
+}
+
+int launch_node_fields_fp32(int q, const Geo &g, long long n, const int *nof, const float *buf, double *e,
+                            double *rho, double *u, cudaStream_t s)
+{
+    return node_fields_any<PrecShifted32>(q, g, n, nof, buf, e, rho, u, s);
+}
+
+}  // namespace erlbm

@@ -1,0 +1,143 @@
+// k_fp64.cu -- plain FP64 kernels.  This translation unit is compiled with --fmad=false so that
+// every multiply and add is rounded on its own, as in the reference's GCC -std=c++17 build.
+#include "lattice_kernels.cuh"
+
+namespace erlbm {
+
+int launch_step_fp64(int q, int op, const Geo &g, const BCp &bc, const Relax &R, const StepArgs &a, const double *src,
+                     double *dst, cudaStream_t s)
+{
+    return step_any<PrecExact64>(q, op, g, bc, R, a, src, dst, s);
+}
+
+int launch_stream_only_fp64(int q, const Geo &g, const double *src, double *dst, cudaStream_t s)
+{
+    return stream_only_any<PrecExact64>(q, g, src, dst, s);
+}
+
+int launch_aos_to_soa_fp64(int q, const Geo &g, long long n, const int *nof, const double *aos, double *soa,
+                           cudaStream_t s)
+{
+    return aos_to_soa_any<PrecExact64>(q, g, n, nof, aos, soa, s);
+}
+
+int launch_soa_to_aos_fp64(int q, const Geo &g, long long n, const int *nof, const double *soa, double *aos,
+                           cudaStream_t s)
+{
+    return soa_to_aos_any<PrecExact64>(q, g, n, nof, soa, aos, s);
+}
+
+int launch_node_fields_fp64(int q, const Geo &g, long long n, const int *nof, const double *buf, double *e,
+                            double *rho, double *u, cudaStream_t s)
+{
+    return node_fields_any<PrecExact64>(q, g, n, nof, buf, e, rho, u, s);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Reductions (FP64; deterministic)
+// ------------------------------------------------------------------------------------------------
+
+namespace {
+
+// Serial sum in index order: the reference's kinectic_energy loop (Other_functions.cpp:100-115).
+__global__ void k_sum_serial(const double *__restrict__ x, long long n, double *out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0;
+    for (long long i = 0; i < n; i++) s = s + x[i];
+    *out = s;
+}
+
+constexpr int RB = 256;   // threads per reduction block
+constexpr int RG = 1024;  // reduction blocks (fixed, so the tree shape does not depend on the GPU)
+
+__global__ void __launch_bounds__(RB) k_sum_partial(const double *__restrict__ x, long long n, double *part)
+{
+    __shared__ double sh[RB];
+    double s = 0;
+    for (long long i = (long long)blockIdx.x * RB + threadIdx.x; i < n; i += (long long)RG * RB) s += x[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = RB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(RB) k_sum_final(const double *__restrict__ part, double *out)
+{
+    __shared__ double sh[RB];
+    double s = 0;
+    for (int i = threadIdx.x; i < RG; i += RB) s += part[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = RB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+__global__ void __launch_bounds__(RB) k_maxabs_partial(const double *__restrict__ x, long long n, double *part)
+{
+    __shared__ double sm[RB];
+    __shared__ int snf[RB];
+    double m = 0;
+    int nf = 0;
+    for (long long i = (long long)blockIdx.x * RB + threadIdx.x; i < n; i += (long long)RG * RB) {
+        const double v = x[i];
+        if (!isfinite(v))
+            nf = 1;
+        else
+            m = fmax(m, fabs(v));
+    }
+    sm[threadIdx.x] = m;
+    snf[threadIdx.x] = nf;
+    __syncthreads();
+    for (int o = RB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
+            snf[threadIdx.x] |= snf[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = sm[0];
+        part[2 * blockIdx.x + 1] = snf[0] ? 1.0 : 0.0;
+    }
+}
+
+__global__ void k_maxabs_final(const double *__restrict__ part, double *out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double m = 0, nf = 0;
+    for (int i = 0; i < RG; i++) {
+        m = fmax(m, part[2 * i]);
+        nf = fmax(nf, part[2 * i + 1]);
+    }
+    out[0] = m;
+    out[1] = nf;
+}
+
+}  // namespace
+
+int launch_sum(const double *x, long long n, long long serial_limit, double *scratch, double *out, cudaStream_t s)
+{
+    if (n <= serial_limit) {
+        k_sum_serial<<<1, 32, 0, s>>>(x, n, out);
+    } else {
+        k_sum_partial<<<RG, RB, 0, s>>>(x, n, scratch);
+        k_sum_final<<<1, RB, 0, s>>>(scratch, out);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+int launch_maxabs(const double *x, long long n, double *scratch, double *out, cudaStream_t s)
+{
+    k_maxabs_partial<<<RG, RB, 0, s>>>(x, n, scratch);
+    k_maxabs_final<<<1, 32, 0, s>>>(scratch, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+}  // namespace erlbm

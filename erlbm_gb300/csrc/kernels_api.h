@@ -1,0 +1,84 @@
+// kernels_api.h -- host-side launchers of the single-lattice and batched kernels.
+//
+// The FP64 kernels live in k_fp64.cu (compiled with --fmad=false, the reference's rounding) and
+// the FP32-shifted kernels in k_fp32.cu.  Everything here is internal to liberlbm_gb300.so.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lattice.cuh"
+
+namespace erlbm {
+
+// Box geometry of one lattice on the device.  Populations are SoA: direction plane i starts at
+// i * plane, node index = x + nx (y + ny z).  solid is null for a fully periodic box.
+struct Geo {
+    int nx, ny, nz;
+    long long nbox, plane;
+    const uint8_t *solid;
+};
+
+// Boundary planes of one step (ZouHeD3Q19_vx_x and devnull_rho_x); -1 disables a plane.
+struct BCp {
+    int inlet_x;
+    double u_in;
+    int outlet_x;
+    double rho_out;
+};
+
+// Per-run device status used by the stability checks and early stop.
+struct RunStatus {
+    int flags;            // bit 0: |rho| above limit, bit 1: non-finite density, bit 2: energy check failed
+    int decided_step;     // first step that set a flag (INT32_MAX when none)
+    unsigned long long max_abs_rho_bits;  // max |rho| seen, as the bit pattern of a non-negative double
+};
+
+struct StepArgs {
+    int mode;             // 0: stream (pull) + BC + collide;  1: BC + collide on local populations
+    int step_index;       // reference step number of this launch
+    int check_density;    // per-node |rho| > density_limit or non-finite, post-collision
+    double density_limit;
+    RunStatus *status;    // may be null when no check and no early stop
+    int stop_on_flag;     // return without work when a check failed in an earlier step
+};
+
+// FP64 (exact) and FP32-shifted launchers.  src/dst are device SoA buffers of the precision.
+int launch_step_fp64(int q, int op, const Geo &g, const BCp &bc, const Relax &R, const StepArgs &a, const double *src,
+                     double *dst, cudaStream_t s);
+int launch_step_fp32(int q, int op, const Geo &g, const BCp &bc, const Relax &R, const StepArgs &a, const float *src,
+                     float *dst, cudaStream_t s);
+
+// Fused periodic D2Q9 FP32 kernel (nx % 128 == 0, no solids, no boundary planes).
+int launch_periodic_d2q9_fp32(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s);
+bool periodic_d2q9_fp32_ok(const Geo &g);
+
+// Stream only: dst = post-stream populations of the post-collision state src (no BC, no collision).
+int launch_stream_only_fp64(int q, const Geo &g, const double *src, double *dst, cudaStream_t s);
+int launch_stream_only_fp32(int q, const Geo &g, const float *src, float *dst, cudaStream_t s);
+
+// Layout conversion between the caller's AoS fluid-index populations (double, reference order)
+// and the device SoA box layout.  node_of_fluid is null for a periodic box (identity).
+int launch_aos_to_soa_fp64(int q, const Geo &g, long long n_fluid, const int *node_of_fluid, const double *aos,
+                           double *soa, cudaStream_t s);
+int launch_soa_to_aos_fp64(int q, const Geo &g, long long n_fluid, const int *node_of_fluid, const double *soa,
+                           double *aos, cudaStream_t s);
+int launch_aos_to_soa_fp32(int q, const Geo &g, long long n_fluid, const int *node_of_fluid, const double *aos,
+                           float *soa, cudaStream_t s);
+int launch_soa_to_aos_fp32(int q, const Geo &g, long long n_fluid, const int *node_of_fluid, const float *soa,
+                           double *aos, cudaStream_t s);
+
+// Per-fluid-node kinetic energy 1/2 |u|^2, density and velocity of the populations in buf,
+// written in fluid-index order into e_out / rho_out / u_out (3 per node); any may be null.
+int launch_node_fields_fp64(int q, const Geo &g, long long n_fluid, const int *node_of_fluid, const double *buf,
+                            double *e_out, double *rho_out, double *u_out, cudaStream_t s);
+int launch_node_fields_fp32(int q, const Geo &g, long long n_fluid, const int *node_of_fluid, const float *buf,
+                            double *e_out, double *rho_out, double *u_out, cudaStream_t s);
+
+// Sum of n doubles: serial in index order when n <= serial_limit (the reference's order), else a
+// fixed-shape tree (deterministic).  scratch holds >= 1024 doubles.  Result in *out (device).
+int launch_sum(const double *x, long long n, long long serial_limit, double *scratch, double *out, cudaStream_t s);
+// max |x| over n doubles and a non-finite flag: out[0] = max, out[1] = 1.0 if any non-finite.
+int launch_maxabs(const double *x, long long n, double *scratch, double *out, cudaStream_t s);
+
+}  // namespace erlbm

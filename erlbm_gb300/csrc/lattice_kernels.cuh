@@ -1,0 +1,412 @@
+// lattice_kernels.cuh -- single-lattice kernels, written once for both precisions.
+//
+// One launch = one step of the reference's loop for every node: stream (pull) from the
+// post-collision populations of the previous step, boundary planes, collision, optional density
+// check, store.  The pull form is the push of propag_site (LBM_functions.cpp:3886-3955) through
+// the map of def_dir_prop (:1967-2311) read from the receiving side: population i of node x comes
+// from x - c_i (periodic wrap) or, when that node is solid, from direction opp(i) of x itself
+// (halfway bounce-back).  The buffer between launches therefore holds post-collision populations,
+// which is exactly what the reference's drivers measure after the collision of their last step.
+//
+// Included by k_fp64.cu (P = PrecExact64) and k_fp32.cu (P = PrecShifted32).
+#pragma once
+
+#include <cfloat>
+#include <climits>
+#include <cstdint>
+
+#include "collide_fp32.cuh"
+#include "collide_fp64.cuh"
+#include "kernels_api.h"
+#include "lattice.cuh"
+
+namespace erlbm {
+
+struct CollParams {
+    Relax R;
+    shifted::Coef k;
+};
+
+// ------------------------------------------------------------------------------------------------
+// Precision policies
+// ------------------------------------------------------------------------------------------------
+
+struct PrecExact64 {
+    using T = double;
+    template <int Q, int OP>
+    __device__ static __forceinline__ void collide(T *f, const CollParams &p)
+    {
+        exact::collide<Q, OP>(f, p.R);
+    }
+    template <int Q>
+    __device__ static __forceinline__ double density(const T *f)
+    {
+        return exact::node_density<Q>(f);
+    }
+    template <int Q>
+    __device__ static __forceinline__ double energy(const T *f)
+    {
+        return exact::node_energy<Q>(f);
+    }
+    // calcula (LBM_functions.cpp:3518-3589)
+    template <int Q>
+    __device__ static __forceinline__ void macro(const T *f, double &rho, double &ux, double &uy, double &uz)
+    {
+        if constexpr (Q == 9) {
+            exact::moments9(f, rho, ux, uy);
+            uz = 0.0;
+        } else {
+            exact::moments19(f, rho, ux, uy, uz);
+        }
+    }
+    __device__ static __forceinline__ void zou_he(T *f, double vx, bool left)
+    {
+        if (left)
+            exact::zou_he_left(f, vx);
+        else
+            exact::zou_he_right(f, vx);
+    }
+    // devnull_rho_x (Boundary_conditions.cpp:119-125): f = f_adj * (rho / density(f_adj)).
+    template <int Q>
+    __device__ static __forceinline__ void outlet(T *f, double rho)
+    {
+        const double fator = rho / exact::node_density<Q>(f);
+#pragma unroll
+        for (int i = 0; i < Q; i++) f[i] = f[i] * fator;
+    }
+    // dist_eq(f, rho) (LBM_functions.cpp:3015-3024): f_i = w_i rho.
+    template <int Q>
+    __device__ static __forceinline__ void rest(T *f, double rho)
+    {
+#pragma unroll
+        for (int i = 0; i < Q; i++) f[i] = Lat<Q>::w(i) * rho;
+    }
+    template <int Q>
+    __device__ static __forceinline__ T from_f(double f, int) { return f; }
+    template <int Q>
+    __device__ static __forceinline__ double to_f(T v, int) { return v; }
+};
+
+struct PrecShifted32 {
+    using T = float;
+    template <int Q, int OP>
+    __device__ static __forceinline__ void collide(T *f, const CollParams &p)
+    {
+        shifted::collide<Q, OP>(f, p.k);
+    }
+    template <int Q>
+    __device__ static __forceinline__ double density(const T *f)
+    {
+        return 1.0 + (double)shifted::node_drho<Q>(f);
+    }
+    template <int Q>
+    __device__ static __forceinline__ double energy(const T *f)
+    {
+        return shifted::node_energy<Q>(f);
+    }
+    template <int Q>
+    __device__ static __forceinline__ void macro(const T *f, double &rho, double &ux, double &uy, double &uz)
+    {
+        float drho, mx, my, mz = 0.f, fx, fy, fz = 0.f;
+        if constexpr (Q == 9)
+            shifted::moments9(f, drho, mx, my, fx, fy);
+        else
+            shifted::moments19(f, drho, mx, my, mz, fx, fy, fz);
+        rho = 1.0 + (double)drho;
+        ux = fx;
+        uy = fy;
+        uz = fz;
+    }
+    __device__ static __forceinline__ void zou_he(T *f, double vx, bool left) { shifted::zou_he(f, vx, left); }
+    template <int Q>
+    __device__ static __forceinline__ void outlet(T *f, double rho)
+    {
+        double r = 1.0;
+#pragma unroll
+        for (int i = 0; i < Q; i++) r += (double)f[i];
+        const double s = rho / r;
+#pragma unroll
+        for (int i = 0; i < Q; i++) f[i] = (float)(((double)f[i] + Lat<Q>::w(i)) * s - Lat<Q>::w(i));
+    }
+    template <int Q>
+    __device__ static __forceinline__ void rest(T *f, double rho)
+    {
+#pragma unroll
+        for (int i = 0; i < Q; i++) f[i] = (float)(Lat<Q>::w(i) * rho - Lat<Q>::w(i));
+    }
+    template <int Q>
+    __device__ static __forceinline__ T from_f(double f, int i) { return (float)(f - Lat<Q>::w(i)); }
+    template <int Q>
+    __device__ static __forceinline__ double to_f(T v, int i) { return (double)v + Lat<Q>::w(i); }
+};
+
+// ------------------------------------------------------------------------------------------------
+// Helpers
+// ------------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ int wrap1(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+// Post-stream populations of node (x, y, z) gathered from the post-collision buffer.
+template <class P, int Q>
+__device__ __forceinline__ void gather(const typename P::T *__restrict__ src, const Geo &g, int mode, int x, int y,
+                                       int z, long long node, typename P::T *f)
+{
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        if (mode == 1) {
+            f[i] = src[(long long)i * g.plane + node];
+            continue;
+        }
+        const int xs = wrap1(x - Lat<Q>::cx(i), g.nx);
+        const int ys = wrap1(y - Lat<Q>::cy(i), g.ny);
+        const int zs = (Q == 19) ? wrap1(z - Lat<Q>::cz(i), g.nz) : 0;
+        const long long s = (long long)xs + (long long)g.nx * ((long long)ys + (long long)g.ny * zs);
+        if (g.solid != nullptr && g.solid[s])
+            f[i] = src[(long long)Lat<Q>::opp(i) * g.plane + node];
+        else
+            f[i] = src[(long long)i * g.plane + s];
+    }
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Generic step kernel: any box, solid mask, boundary planes, density check
+// ------------------------------------------------------------------------------------------------
+
+template <class P, int Q, int OP>
+__global__ void __launch_bounds__(256) k_step(const typename P::T *__restrict__ src, typename P::T *__restrict__ dst,
+                                              Geo g, BCp bc, CollParams prm, StepArgs a)
+{
+    using T = typename P::T;
+    if (a.stop_on_flag && a.status != nullptr) {
+        // A check failed in an EARLIER step: nothing to do.  (Blocks of the failing step itself
+        // still finish it, as the reference finishes the step in which it flags a node.)  One
+        // value per warp, so that the warp reductions below see every lane or none.
+        const int ds = __shfl_sync(0xffffffffu, *(volatile int *)&a.status->decided_step, 0);
+        if (ds < a.step_index) return;
+    }
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = node < g.nbox;
+    if (active && g.solid != nullptr && g.solid[node]) active = false;
+    unsigned long long rho_bits = 0;
+    int flag = 0;
+    if (active) {
+        const int x = (int)(node % g.nx);
+        const long long r = node / g.nx;
+        const int y = (int)(r % g.ny);
+        const int z = (int)(r / g.ny);
+        T f[Q];
+        int gx = x;
+        const bool outlet = (x == bc.outlet_x);
+        if (outlet) gx = x + ((bc.outlet_x < g.nx / 2) ? 1 : -1);
+        const long long gnode = node + (gx - x);
+        if (outlet && g.solid != nullptr && g.solid[gnode]) {
+            P::template rest<Q>(f, bc.rho_out);
+        } else {
+            gather<P, Q>(src, g, a.mode, gx, y, z, gnode, f);
+            if (Q == 19 && gx == bc.inlet_x) P::zou_he(f, bc.u_in, bc.inlet_x < g.nx / 2);
+            if (outlet) P::template outlet<Q>(f, bc.rho_out);
+        }
+        P::template collide<Q, OP>(f, prm);
+        if (a.check_density) {
+            const double rho = P::template density<Q>(f);
+            if (!isfinite(rho)) {
+                flag = 2;
+            } else {
+                const double ar = fabs(rho);
+                rho_bits = (unsigned long long)__double_as_longlong(ar);
+                if (ar > a.density_limit) flag = 1;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < Q; i++) dst[(long long)i * g.plane + node] = f[i];
+    }
+    if (a.check_density) {
+        const unsigned long long m = warp_max_u64(rho_bits);
+        const int any = __reduce_or_sync(0xffffffffu, flag);
+        if ((threadIdx.x & 31) == 0) {
+            if (m) atomicMax(&a.status->max_abs_rho_bits, m);
+            if (any) {
+                atomicOr(&a.status->flags, any);
+                atomicMin(&a.status->decided_step, a.step_index);
+            }
+        }
+    }
+}
+
+template <class P, int Q>
+__global__ void __launch_bounds__(256) k_stream_only(const typename P::T *__restrict__ src,
+                                                     typename P::T *__restrict__ dst, Geo g)
+{
+    using T = typename P::T;
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= g.nbox) return;
+    if (g.solid != nullptr && g.solid[node]) return;
+    const int x = (int)(node % g.nx);
+    const long long r = node / g.nx;
+    const int y = (int)(r % g.ny);
+    const int z = (int)(r / g.ny);
+    T f[Q];
+    gather<P, Q>(src, g, 0, x, y, z, node, f);
+#pragma unroll
+    for (int i = 0; i < Q; i++) dst[(long long)i * g.plane + node] = f[i];
+}
+
+// ------------------------------------------------------------------------------------------------
+// Layout conversion and per-node fields
+// ------------------------------------------------------------------------------------------------
+
+template <class P, int Q>
+__global__ void __launch_bounds__(256) k_aos_to_soa(Geo g, long long n_fluid, const int *__restrict__ nof,
+                                                    const double *__restrict__ aos, typename P::T *__restrict__ soa)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_fluid) return;
+    const long long node = nof ? nof[p] : p;
+#pragma unroll
+    for (int i = 0; i < Q; i++) soa[(long long)i * g.plane + node] = P::template from_f<Q>(aos[p * Q + i], i);
+}
+
+template <class P, int Q>
+__global__ void __launch_bounds__(256) k_soa_to_aos(Geo g, long long n_fluid, const int *__restrict__ nof,
+                                                    const typename P::T *__restrict__ soa, double *__restrict__ aos)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_fluid) return;
+    const long long node = nof ? nof[p] : p;
+#pragma unroll
+    for (int i = 0; i < Q; i++) aos[p * Q + i] = P::template to_f<Q>(soa[(long long)i * g.plane + node], i);
+}
+
+template <class P, int Q>
+__global__ void __launch_bounds__(256) k_node_fields(Geo g, long long n_fluid, const int *__restrict__ nof,
+                                                     const typename P::T *__restrict__ buf, double *e_out,
+                                                     double *rho_out, double *u_out)
+{
+    using T = typename P::T;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_fluid) return;
+    const long long node = nof ? nof[p] : p;
+    T f[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) f[i] = buf[(long long)i * g.plane + node];
+    if (e_out) e_out[p] = P::template energy<Q>(f);
+    if (rho_out || u_out) {
+        double rho, ux, uy, uz;
+        P::template macro<Q>(f, rho, ux, uy, uz);
+        if (rho_out) rho_out[p] = u_out ? rho : P::template density<Q>(f);
+        if (u_out) {
+            u_out[3 * p] = ux;
+            u_out[3 * p + 1] = uy;
+            u_out[3 * p + 2] = uz;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Launch helpers
+// ------------------------------------------------------------------------------------------------
+
+inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+template <class P, int Q>
+int step_dispatch(int op, const Geo &g, const BCp &bc, const Relax &R, const StepArgs &a,
+                  const typename P::T *src, typename P::T *dst, cudaStream_t s)
+{
+    CollParams prm;
+    prm.R = R;
+    prm.k = shifted::make_coef(R);
+    const unsigned nb = blocks_for(g.nbox, 256);
+    switch (op) {
+    case OP_BGK:
+        k_step<P, Q, OP_BGK><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, a);
+        break;
+    case OP_REG:
+        k_step<P, Q, OP_REG><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, a);
+        break;
+    case OP_EXTREG:
+        k_step<P, Q, OP_EXTREG><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, a);
+        break;
+    default:
+        return -1;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+template <class P>
+int step_any(int q, int op, const Geo &g, const BCp &bc, const Relax &R, const StepArgs &a,
+             const typename P::T *src, typename P::T *dst, cudaStream_t s)
+{
+    if (q == 9) return step_dispatch<P, 9>(op, g, bc, R, a, src, dst, s);
+    if (q == 19) return step_dispatch<P, 19>(op, g, bc, R, a, src, dst, s);
+    return -1;
+}
+
+template <class P>
+int stream_only_any(int q, const Geo &g, const typename P::T *src, typename P::T *dst, cudaStream_t s)
+{
+    const unsigned nb = blocks_for(g.nbox, 256);
+    if (q == 9)
+        k_stream_only<P, 9><<<nb, 256, 0, s>>>(src, dst, g);
+    else if (q == 19)
+        k_stream_only<P, 19><<<nb, 256, 0, s>>>(src, dst, g);
+    else
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+template <class P>
+int aos_to_soa_any(int q, const Geo &g, long long n, const int *nof, const double *aos, typename P::T *soa,
+                   cudaStream_t s)
+{
+    if (n == 0) return 0;
+    const unsigned nb = blocks_for(n, 256);
+    if (q == 9)
+        k_aos_to_soa<P, 9><<<nb, 256, 0, s>>>(g, n, nof, aos, soa);
+    else if (q == 19)
+        k_aos_to_soa<P, 19><<<nb, 256, 0, s>>>(g, n, nof, aos, soa);
+    else
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+template <class P>
+int soa_to_aos_any(int q, const Geo &g, long long n, const int *nof, const typename P::T *soa, double *aos,
+                   cudaStream_t s)
+{
+    if (n == 0) return 0;
+    const unsigned nb = blocks_for(n, 256);
+    if (q == 9)
+        k_soa_to_aos<P, 9><<<nb, 256, 0, s>>>(g, n, nof, soa, aos);
+    else if (q == 19)
+        k_soa_to_aos<P, 19><<<nb, 256, 0, s>>>(g, n, nof, soa, aos);
+    else
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+template <class P>
+int node_fields_any(int q, const Geo &g, long long n, const int *nof, const typename P::T *buf, double *e,
+                    double *rho, double *u, cudaStream_t s)
+{
+    if (n == 0) return 0;
+    const unsigned nb = blocks_for(n, 256);
+    if (q == 9)
+        k_node_fields<P, 9><<<nb, 256, 0, s>>>(g, n, nof, buf, e, rho, u);
+    else if (q == 19)
+        k_node_fields<P, 19><<<nb, 256, 0, s>>>(g, n, nof, buf, e, rho, u);
+    else
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+}  // namespace erlbm

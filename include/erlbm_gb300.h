@@ -1,0 +1,154 @@
+/*
+ * erlbm_gb300.h -- C ABI of the GB300 E-RLBM collide-stream engine (liberlbm_gb300.so).
+ *
+ * Plain C: pointers, sizes and PODs only; no C++ or CUDA types cross this boundary, and nothing
+ * depends on the reference's nvel/dim macros.  Every function returns an int status
+ * (ERLBM_OK = 0, negative on error) and never throws.  The caller owns every host buffer; the
+ * library owns device memory.  A handle is used by one host thread at a time; different handles
+ * may be driven from different threads (each has its own CUDA stream).
+ *
+ * Granularity.  The reference's interface is per site -- coll_Ext_Reg(f, ax, ay, az, LATTICE,
+ * PARAMETERS) (SimBoltz_Functions/Definitions.cpp:697), propag_site (:509), ZouHeD3Q19_vx_x
+ * (:922), devnull_rho_x (:907), kinectic_energy (:1005), density (:582) -- called by the
+ * drivers' node loops (src/main_*.cpp).  A per-site call cannot run on a GPU, so this ABI sits
+ * one level up, at sweep and run granularity: one erlbm_step() replaces one pass of a driver's
+ * "for pto: colisao_sitio; propag_site" loop plus the pointer swap, and erlbm_map_run() replaces
+ * a whole OpenMP map loop.  Population arrays crossing the ABI use the reference layout:
+ * AoS in fluid-index order, f[pto * q + i], velocity order of def_lattice_d2q9 / def_lattice_d3q19.
+ */
+#ifndef ERLBM_GB300_H
+#define ERLBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------- */
+#define ERLBM_OK 0
+#define ERLBM_E_INVAL (-1)       /* bad argument (the reference exit(1)s on a bad operator name) */
+#define ERLBM_E_OOM (-2)         /* device or host allocation failed */
+#define ERLBM_E_CUDA (-3)        /* CUDA error; erlbm_last_error() has the text */
+#define ERLBM_E_TIMEOUT (-4)     /* a bounded device wait ran out */
+#define ERLBM_E_NONFINITE (-5)   /* non-finite value where a finite one was required */
+#define ERLBM_E_UNSUPPORTED (-6) /* valid request this build does not provide */
+#define ERLBM_E_STATE (-7)       /* call not valid in the handle's current state */
+
+/* ---- collision operators: same numbers as COLISAO (src/erlbm_common.h:42) ------------------- */
+#define ERLBM_OP_BGK 1    /* coll_BGK     Collision_operators.cpp:12-49 */
+#define ERLBM_OP_MRT 2    /* coll_MRT: not provided (ERLBM_E_UNSUPPORTED) */
+#define ERLBM_OP_REG 3    /* coll_Reg     Collision_operators.cpp:860-967 (E-RLBM with tau_nh = 1) */
+#define ERLBM_OP_EXTREG 4 /* coll_Ext_Reg Collision_operators.cpp:1182-1307 */
+
+/* ---- precisions --------------------------------------------------------------------------- */
+#define ERLBM_FP64 0         /* plain path: bit-identical to the reference's FP64 CPU results */
+#define ERLBM_FP32_SHIFTED 1 /* populations stored and collided in FP32 as f_i - w_i */
+
+/* ---- population stages (which populations a query reads) ---------------------------------- */
+#define ERLBM_STAGE_POST_STREAM 0    /* lattice.inif at the top of a driver's step loop */
+#define ERLBM_STAGE_POST_COLLISION 1 /* lattice.inif after the last step's collision, before the swap
+                                        (what main_taylor-green.cpp and main_double-shear-layer.cpp
+                                        measure) */
+
+typedef struct erlbm_handle erlbm_handle;
+
+/* Lattice description; replaces GEOMETRY + LATTICE + PARAMETERS of define_rede / aloca_populacoes
+ * (src/erlbm_common.h:123-157).  solid: nx*ny*nz bytes, x fastest, 1 = solid, NULL = all fluid
+ * (geometria_periodica, src/erlbm_common.h:101-114).  Fluid indices number the non-solid nodes
+ * in that order, as numera_fluido does (src/erlbm_common.h:89-99). */
+typedef struct erlbm_desc {
+    int q;              /* 9 (D2Q9, nz must be 1) or 19 (D3Q19) */
+    int nx, ny, nz;
+    const uint8_t *solid;
+    double tau, tau_nh; /* PARAMETERS.tau, PARAMETERS.tau_nh */
+    int op;             /* ERLBM_OP_* */
+    int precision;      /* ERLBM_FP64 or ERLBM_FP32_SHIFTED */
+} erlbm_desc;
+
+/* Boundary planes applied to the post-stream populations at the start of each step, in this
+ * order (main_stability-map_obstacle.cpp:92-94).  -1 disables a plane. */
+typedef struct erlbm_bc {
+    int inlet_x;    /* ZouHeD3Q19_vx_x(inlet_x, u_in) (Boundary_conditions.cpp:350-442); D3Q19 only */
+    double u_in;
+    int outlet_x;   /* devnull_rho_x(outlet_x, rho_out) (Boundary_conditions.cpp:68-141) */
+    double rho_out;
+} erlbm_bc;
+
+/* Stability checks of a run (roda_ponto, main_stability-map_taylor-green.cpp:41-104 and
+ * main_stability-map_obstacle.cpp:75-123). */
+typedef struct erlbm_checks {
+    int energy_every;     /* E of the post-stream populations at step % energy_every == 0 && step > 0;
+                             unstable when E > energy_factor * E0 or E non-finite; 0 = off */
+    double energy_factor; /* 2 in the reference */
+    int density_check;    /* |rho| > density_limit or non-finite at any node, post-collision, every step */
+    double density_limit; /* 10 rho0 in the reference */
+} erlbm_checks;
+
+typedef struct erlbm_run_result {
+    int label;        /* 1 unstable, 0 stable */
+    int decided_step; /* step of the failing check, or the step count when stable */
+    int steps_done;   /* steps executed */
+    double margin;    /* max over checks of E / (factor E0), or max |rho| / density_limit; +inf if non-finite */
+} erlbm_run_result;
+
+/* ---- library ------------------------------------------------------------------------------ */
+int erlbm_version(void);
+const char *erlbm_strerror(int code);
+const char *erlbm_last_error(void); /* text of the last error on this host thread */
+
+/* ---- single lattice ------------------------------------------------------------------------ */
+/* define_rede + aloca_populacoes (src/erlbm_common.h:123-148) */
+int erlbm_create(const erlbm_desc *d, erlbm_handle **h);
+/* libera_populacoes (src/erlbm_common.h:150-157) */
+int erlbm_destroy(erlbm_handle *h);
+int erlbm_fluid_count(const erlbm_handle *h, int64_t *n_fluid);
+/* new PARAMETERS for the next steps (colisao_sitio's parameters argument, src/erlbm_common.h:69) */
+int erlbm_set_params(erlbm_handle *h, double tau, double tau_nh, int op);
+/* writes lattice.inif: n = n_fluid * q post-stream populations (the state a step starts from) */
+int erlbm_set_populations(erlbm_handle *h, const double *aos, size_t n);
+/* reads the populations of the chosen stage into aos (n = n_fluid * q) */
+int erlbm_get_populations(erlbm_handle *h, double *aos, size_t n, int stage);
+/* n_steps driver steps: [boundary planes] -> colisao_sitio at every node -> propag_site -> swap
+ * (replaces e.g. main_double-shear-layer.cpp:382-449 without the output block).  bc may be NULL. */
+int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc);
+/* kinectic_energy (Other_functions.cpp:100-115) of the chosen stage */
+int erlbm_kinetic_energy(erlbm_handle *h, int stage, double *energy);
+/* max over fluid nodes of |density| (LBM_functions.cpp:5544-5552) and a non-finite flag */
+int erlbm_max_abs_density(erlbm_handle *h, int stage, double *max_abs_rho, int *nonfinite);
+/* per-fluid-node density and velocity (calcula, LBM_functions.cpp:3518-3589) of the chosen stage:
+ * rho[n_fluid] and u[3 * n_fluid] (ux, uy, uz per node); either may be NULL */
+int erlbm_macroscopic(erlbm_handle *h, int stage, double *rho, double *u);
+/* roda_ponto on this lattice: up to n_steps steps with the given checks; stops at the first
+ * failing check as the reference does */
+int erlbm_run(erlbm_handle *h, int n_steps, const erlbm_bc *bc, const erlbm_checks *chk, erlbm_run_result *res);
+/* wait for the handle's queued work */
+int erlbm_sync(erlbm_handle *h);
+
+/* ---- program inputs (host functions; what the reference's drivers build around their loops) --- */
+/* inicializa_taylor_green (main_taylor-green.cpp:57-100) on an L x L (x nz) periodic box, AoS in
+ * fluid-index order.  variant 1 is the same vortex translated by (L/4, L/4):
+ * u = U0 (-cos kx sin ky, sin kx cos ky), rho = 1 - 3/4 U0^2 (cos 2kx + cos 2ky). */
+int erlbm_init_taylor_green(int q, int L, int nz, double u0, double tau, int poisson, int neq, int variant,
+                            double *aos);
+/* initial_double_shear_layer (main_double-shear-layer.cpp:48-66), U0 = 1/32, lambda = 80, epsilon = 0.05 */
+int erlbm_init_double_shear(int L, double rho_ini, double *aos);
+/* dist_eq (LBM_functions.cpp:2945-3000) of one node */
+int erlbm_equilibrium(int q, double ux, double uy, double uz, double rho, double *feq);
+/* geometria_obstaculo (main_stability-map_obstacle.cpp:42-70) scaled by (sx, sy): nx = 20 sx + 2,
+ * ny = 12 sy; solid may be NULL to query the extent */
+int erlbm_obstacle_geometry(int sx, int sy, int *nx, int *ny, uint8_t *solid);
+/* E_vector, E_magnitude and nu_ef/nu - 1 of a Taylor-Green field (main_taylor-green.cpp:178-213) */
+int erlbm_taylor_green_error(int q, int L, const double *aos, double u0, double visc, int step, int variant,
+                             double *out3);
+/* map axes of main_stability-map_taylor-green.cpp:134-164 and main_stability-map_obstacle.cpp:147-173 */
+int erlbm_tg_map_params(int i, int j, int n_ma, int n_nu, int op, double tau_nh_in, double *u0, double *tau,
+                        double *tau_nh);
+int erlbm_obstacle_map_params(int i, int j, int n_tau, int n_nu, double ma, double *u_imp, double *tau,
+                              double *tau_nh);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ERLBM_GB300_H */

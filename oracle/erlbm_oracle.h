@@ -1,0 +1,66 @@
+/*
+ * erlbm_oracle.h -- TEST INFRASTRUCTURE, NOT THE PRODUCT.
+ * C interface of the CPU oracle (erlbm_oracle.c).  Loaded by tests/, smoke() and bench.py's
+ * CPU-baseline leg only.
+ */
+#ifndef ERLBM_ORACLE_H
+#define ERLBM_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* operator numbers of COLISAO (src/erlbm_common.h:42) */
+#define ORC_OP_BGK 1
+#define ORC_OP_REG 3
+#define ORC_OP_EXTREG 4
+
+typedef struct orc_lattice orc_lattice;
+
+typedef struct orc_bc {
+    int inlet_x;    /* Zou-He velocity inlet plane, -1 = none */
+    double u_in;    /* imposed x velocity */
+    int outlet_x;   /* copy-and-rescale outlet plane, -1 = none */
+    double rho_out; /* density the outlet is rescaled to */
+} orc_bc;
+
+orc_lattice *orc_create(int q, int nx, int ny, int nz, const uint8_t *solid, double tau, double tau_nh, int op);
+void orc_destroy(orc_lattice *L);
+int orc_fluid_count(const orc_lattice *L);
+void orc_set_params(orc_lattice *L, double tau, double tau_nh, int op);
+void orc_set_populations(orc_lattice *L, const double *aos);
+void orc_get_populations(const orc_lattice *L, double *aos, int stage);
+void orc_step(orc_lattice *L, int n_steps, const orc_bc *bc, int nthreads);
+double orc_kinetic_energy(const orc_lattice *L, int stage);
+double orc_max_abs_density(const orc_lattice *L, int stage, int *nonfinite);
+void orc_equilibrium(int q, double ux, double uy, double uz, double rho, double *feq);
+void orc_collide_site(int q, double *f, int op, double tau, double tau_nh);
+
+void orc_init_taylor_green(int q, int L, int nz, double u_0, double tau, int poisson, int neq, int variant,
+                           double *aos);
+void orc_taylor_green_error(int q, int L, const double *aos, double u_0, double visc, int step, int variant,
+                            double *out);
+void orc_taylor_green_program(int q, int L, int op, double tau_nh, double Re, double u_0, int tau_mode,
+                              double tau_in, int neq, int poisson, int variant, int nthreads, double *out);
+void orc_init_double_shear(int L, double rho_ini, double *aos);
+
+void orc_tg_map_params(int i, int j, int n_ma, int n_nu, int op, double tau_nh_in, double *u0, double *tau,
+                       double *tau_nh);
+void orc_obstacle_map_params(int i, int j, int n_tau, int n_nu, double ma, double *u_imp, double *tau,
+                             double *tau_nh);
+int orc_tg_map_point(int L, int op, double tau, double tau_nh, double u_0, int *decided_step, double *margin);
+void orc_obstacle_geometry(int sx, int sy, int *nx, int *ny, uint8_t *solid);
+int orc_obstacle_map_point(int sx, int sy, double tau, double tau_nh, double u_imp, int max_steps,
+                           int *decided_step, double *margin);
+void orc_tg_map(int L, int op, double tau_nh, int n_ma, int n_nu, int n_pts, const int *pi, const int *pj,
+                int nthreads, int *labels, int *decided, double *margins);
+void orc_obstacle_map(int n_tau, int n_nu, double ma, int n_pts, const int *pi, const int *pj, int max_steps,
+                      int nthreads, int *labels, int *decided, double *margins);
+int orc_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
