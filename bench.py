@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""bench.py -- throughput of the E-RLBM collide-stream hot path on GB300.
+
+Workload (one bench step): `inner` steps of the double shear layer (D2Q9, E-RLBM tau_nh = 0.65,
+Re = 80000, U0 = 1/32, lambda = 80, epsilon = 0.05; main_double-shear-layer.cpp) on an L x L
+periodic lattice, L = 2048 by default, FP32-shifted populations.  The metric is MLUPS (million
+lattice updates per second); `value` is device-timed with CUDA events on the stream the kernels
+run on, with the populations already resident in HBM.  The working set (2 x 9 x 4 B x L^2 =
+302 MB at L = 2048) is larger than the 129 MB L2, so no flush is needed between steps.
+
+`e2e` is the same metric through the C ABI as a caller uses it: each bench step copies the
+initial populations from pinned host memory (erlbm_set_populations, AoS doubles), runs `inner`
+steps (erlbm_step) and reads the kinetic energy back (erlbm_kinetic_energy), wall-clock timed.
+
+`cpu_baseline` times the CPU restatement of the reference's algorithm (oracle/, AoS + push map,
+OpenMP over all host cores) on a bounded sample of the same workload.  `--impl reference` runs the
+reference's own CPU code when it could be compiled from its sources here (oracle/_ref), otherwise
+that same restatement, and prints the same JSON line with "impl": "reference".
+
+Multi-GPU: one lattice does not shard, so N GPUs run N independent replicas (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_LU = {"fp32": 2 * 9 * 4, "fp64": 2 * 9 * 8}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--L", type=int, default=2048)
+    p.add_argument("--inner", type=int, default=1000, help="LBM steps per bench step")
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-extras", action="store_true")
+    return p.parse_args()
+
+
+def tau_of(L: int) -> float:
+    # main_double-shear-layer.cpp:307: tau = 1/2 + 3 U0 L / Re
+    return 0.5 + 3.0 * (1.0 / 32.0) * L / 80000.0
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(L: int, precision: str):
+    """DRAM bytes per launch from the committed ncu summary of the same kernel, scaled to L."""
+    path = os.path.join(ROOT, "profiles", "dsl_periodic_d2q9_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        rec = d[precision]
+        return rec["dram_bytes_per_lu"] * L * L
+    except Exception:
+        return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        if not shutil.which("nvidia-smi"):
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.fh = open(self.path, "w")
+        self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                     stderr=subprocess.DEVNULL)
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx = float(parts[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU legs (the only places bench.py executes oracle/)
+# ------------------------------------------------------------------------------------------------
+
+def cpu_sample(L: int, seconds: float, prefer_reference: bool):
+    """Time the reference's CPU algorithm on this host's cores: the reference library compiled from
+    its sources (oracle/_ref, only where it was built) or the oracle's restatement of it."""
+    import numpy as np
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    tau = tau_of(L)
+    f0 = O.init_double_shear(L)
+    kind = "port"
+    if prefer_reference and O.ref_available(9):
+        import ctypes as C
+        lib = O.load_ref(9)
+        fn = lib.ref9_run_threads
+        fn.restype = C.c_int
+        fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_int,
+                       C.c_int, C.c_double, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+
+        def run(n):
+            t = time.perf_counter()
+            fn(L, L, 1, None, 4, tau, 0.65, f0.ctypes.data, n, -1, 0.0, -1, 1.0, None, None, None, threads)
+            return time.perf_counter() - t
+        kind = "reference"
+    else:
+        lat = O.Lattice(9, L, L, 1, None, tau, 0.65, O.OP_EXTREG)
+        lat.set(f0)
+
+        def run(n):
+            t = time.perf_counter()
+            lat.step(n, threads=threads)
+            return time.perf_counter() - t
+    t1 = run(2) / 2
+    n = max(2, min(2000, int(seconds / max(t1, 1e-6))))
+    dt = run(n)
+    if kind == "reference":  # the harness includes set-up and output copies; subtract a 1-step run
+        dt = max(dt - run(1) + t1, 1e-9)
+    mlups = L * L * n / dt / 1e6
+    return {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": kind,
+            "sample": f"double shear layer D2Q9 E-RLBM FP64, L={L}, {n} steps, {threads} OpenMP threads"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    W, K = args.warmup, args.steps
+    # each bench step is a bounded sample; warm-up samples are shorter
+    per = max(1.0, min(8.0, 120.0 / max(1, K + W)))
+    for _ in range(W):
+        cpu_sample(args.L, per / 4, True)
+    vals = [cpu_sample(args.L, per, True) for _ in range(K)]
+    v = statistics.median(x["value"] for x in vals)
+    cb = dict(vals[-1])
+    cb["value"] = v
+    L = args.L
+    line = {"metric": "MLUPS", "value": v, "unit": "MLUPS", "n_gpus": args.gpus, "steps": K, "warmup": W,
+            "ms_per_step": L * L * args.inner / (v * 1e6) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (double shear layer initial condition)",
+            "config": {"workload": f"double shear layer D2Q9 E-RLBM tau_nh=0.65 Re=80000 L={L}", "L": L,
+                       "lbm_steps_per_step": args.inner, "precision": "fp64 (reference CPU path)"},
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------------------
+# GPU leg
+# ------------------------------------------------------------------------------------------------
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import erlbm_gb300 as E
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+
+    L, inner, K, W = args.L, args.inner, args.steps, args.warmup
+    prec = E.FP32_SHIFTED if args.precision == "fp32" else E.FP64
+    tau = tau_of(L)
+    f0 = E.init_double_shear(L)
+    stream = torch.cuda.Stream()
+    lat = E.Lattice(9, L, L, 1, None, tau, 0.65, E.OP_EXTREG, prec)
+    lat.set_stream(stream.cuda_stream)
+    lat.set_populations(f0)
+    lat.step(1)  # the first step collides the given populations in place; later ones are fused
+    for _ in range(W):
+        lat.step(inner)
+    lat.sync()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-timed region -------------------------------------------------------------------
+    barrier()
+    clocks = Clocks(dev)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(K):
+        lat.step(inner)
+    ev1.record(stream)
+    stream.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    launches = K * inner
+    value = world * L * L * inner * K / (ms / 1e3) / 1e6
+    launch_ms = ms / launches
+    algo_bytes = BYTES_PER_LU[args.precision] * L * L
+    peak, peak_kind = peaks()
+    achieved = algo_bytes / (launch_ms / 1e3) / 1e9
+
+    # ---- end to end through the C ABI with host buffers ------------------------------------------
+    pinned = torch.empty(f0.size, dtype=torch.float64, pin_memory=True)
+    pinned.numpy()[:] = f0
+    host = pinned.numpy()
+    for _ in range(max(1, min(W, 2))):
+        lat.set_populations(host)
+        lat.step(inner)
+        lat.kinetic_energy(E.STAGE_POST_COLLISION)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        lat.set_populations(host)
+        lat.step(inner)
+        lat.kinetic_energy(E.STAGE_POST_COLLISION)
+    t_e2e = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = {"value": world * L * L * inner * K / t_e2e / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": int(f0.nbytes),
+           "d2h_bytes_per_step": 8}
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        extras = gpu_extras(E, torch, L, f0, tau, prec)
+    lat.close()
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        cpu = cpu_sample(L, args.cpu_seconds, False)
+    line = {
+        "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "fp32" else "f64",
+        "data": "synthetic (double shear layer initial condition, main_double-shear-layer.cpp:48-66)",
+        "config": {"workload": f"double shear layer D2Q9 E-RLBM tau_nh=0.65 Re=80000 L={L}, "
+                               f"{'FP32-shifted' if args.precision == 'fp32' else 'FP64 plain'}",
+                   "L": L, "lbm_steps_per_step": inner, "parallelism": f"replicas x{world}",
+                   "l2": f"working set {2 * BYTES_PER_LU[args.precision] // 2 * L * L / 1e6:.0f} MB > 129 MB L2, "
+                         "no flush"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": ncu_traffic(L, args.precision),
+                     "algorithmic_bytes_per_launch": algo_bytes, "launch_us": launch_ms * 1e3,
+                     "kernel": "k_periodic_d2q9" if args.precision == "fp32" else "k_step<PrecExact64,9,EXTREG>"},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if extras:
+        line["extras"] = extras
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def gpu_extras(E, torch, L, f0, tau, prec):
+    """Secondary figures of the metric line: the plain FP64 path on the same lattice and the
+    FP32-shifted velocity error against it after a short common run."""
+    import numpy as np
+    out = {}
+    n64 = 200
+    s = torch.cuda.Stream()
+    with E.Lattice(9, L, L, 1, None, tau, 0.65, E.OP_EXTREG, E.FP64) as l64:
+        l64.set_stream(s.cuda_stream)
+        l64.set_populations(f0)
+        l64.step(1 + 10)
+        l64.sync()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        l64.step(n64)
+        b.record(s)
+        s.synchronize()
+        ms = a.elapsed_time(b)
+        out["fp64_plain_mlups"] = L * L * n64 / (ms / 1e3) / 1e6
+        out["fp64_plain_launch_us"] = ms / n64 * 1e3
+        # velocity error of FP32-shifted vs FP64 after the same 1 + 10 + n64 steps
+        _, u64 = l64.macroscopic(E.STAGE_POST_COLLISION)
+    with E.Lattice(9, L, L, 1, None, tau, 0.65, E.OP_EXTREG, E.FP32_SHIFTED) as l32:
+        l32.set_populations(f0)
+        l32.step(1 + 10 + n64)
+        _, u32 = l32.macroscopic(E.STAGE_POST_COLLISION)
+    out["fp32_vs_fp64_rel_l2_velocity"] = float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64))
+    out["fp32_vs_fp64_steps"] = 1 + 10 + n64
+    return out
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -13,13 +13,14 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import (FP32_SHIFTED, FP64, MAP_OBSTACLE, MAP_TAYLOR_GREEN, OP_BGK, OP_EXTREG, OP_MRT, OP_REG,
-                   STAGE_POST_COLLISION, STAGE_POST_STREAM, ErlbmError, check, lib)
+from ._lib import (FP32_SHIFTED, FP64, INIT_AOS, INIT_REST, INIT_TG_MAP, MAP_OBSTACLE, MAP_TAYLOR_GREEN, OP_BGK,
+                   OP_EXTREG, OP_MRT, OP_REG, STAGE_POST_COLLISION, STAGE_POST_STREAM, ErlbmError, check, lib)
 
 __all__ = ["Lattice", "ErlbmError", "lib", "OP_BGK", "OP_MRT", "OP_REG", "OP_EXTREG", "FP64", "FP32_SHIFTED",
            "STAGE_POST_STREAM", "STAGE_POST_COLLISION", "MAP_TAYLOR_GREEN", "MAP_OBSTACLE", "init_taylor_green",
            "init_double_shear", "equilibrium", "obstacle_geometry", "taylor_green_error", "tg_map_params",
-           "obstacle_map_params", "operator_from_name"]
+           "obstacle_map_params", "operator_from_name", "map_run", "batch_run", "INIT_REST", "INIT_TG_MAP",
+           "INIT_AOS"]
 
 _OPS = {"bgk": OP_BGK, "mrt": OP_MRT, "reg": OP_REG, "erlbm": OP_EXTREG}
 
@@ -94,6 +95,11 @@ class Lattice:
 
     def sync(self) -> None:
         check(lib().erlbm_sync(self._h), "erlbm_sync")
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        """Queue the lattice's work on a caller's cudaStream_t (an int handle; None = own stream)."""
+        check(lib().erlbm_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None),
+              "erlbm_set_stream")
 
     def kinetic_energy(self, stage: int = STAGE_POST_STREAM) -> float:
         e = C.c_double()
@@ -188,3 +194,59 @@ def obstacle_map_params(i: int, j: int, n_tau: int = 400, n_nu: int = 400, ma: f
     a, b, c = C.c_double(), C.c_double(), C.c_double()
     check(fn(i, j, n_tau, n_nu, ma, C.byref(a), C.byref(b), C.byref(c)), "erlbm_obstacle_map_params")
     return a.value, b.value, c.value
+
+
+# ---- batched runs and stability maps --------------------------------------------------------------
+
+def map_run(kind: int, points=None, precision: int = FP64, op: int = OP_EXTREG, tau_nh: float = 0.65, L: int = 16,
+            ma: float = 0.1, n_i: int = 400, n_j: int = 400, max_steps: int = 0, slots: int = 0):
+    """A stability map (or a subset of its points) in one batched launch.
+
+    kind: MAP_TAYLOR_GREEN (main_stability-map_taylor-green.cpp) or MAP_OBSTACLE
+    (main_stability-map_obstacle.cpp).  points: list of (i, j) map indices, or None for the whole
+    n_i x n_j grid (i fastest).  op = 0 on the Taylor-Green map runs every point with RLBM and with
+    E-RLBM (results concatenated, RLBM first).  Returns (labels, decided_step, margins) arrays.
+    """
+    if points is None:
+        n, pi, pj = n_i * n_j, None, None
+    else:
+        pi = np.ascontiguousarray([p[0] for p in points], dtype=np.int32)
+        pj = np.ascontiguousarray([p[1] for p in points], dtype=np.int32)
+        n = len(points)
+    d = _lib.MapDesc(kind, precision, op, tau_nh, L, ma, n_i, n_j, 0 if points is None else n,
+                     None if pi is None else pi.ctypes.data, None if pj is None else pj.ctypes.data, max_steps, slots)
+    m = n * (2 if (kind == MAP_TAYLOR_GREEN and op == 0) else 1)
+    labels = np.zeros(m, np.int32)
+    dec = np.zeros(m, np.int32)
+    mg = np.zeros(m, np.float64)
+    check(lib().erlbm_map_run(C.byref(d), _dptr(labels), _dptr(dec), _dptr(mg)), "erlbm_map_run")
+    return labels, dec, mg
+
+
+def batch_run(q: int, nx: int, ny: int, runs, precision: int = FP64, solid=None, inlet_x: int = -1,
+              outlet_x: int = -1, rho0: float = 1.0, energy_every: int = 0, energy_factor: float = 2.0,
+              density_check: bool = False, density_limit: float = 10.0, init: int = INIT_REST, aos=None,
+              slots: int = 0):
+    """Independent runs of one small geometry in one persistent launch.
+
+    runs: iterable of dicts with op, tau, tau_nh, u0, n_steps and (for INIT_AOS) aos_offset.
+    Returns a list of result dicts (label, decided_step, steps_done, status, margin, energy).
+    """
+    runs = list(runs)
+    specs = (_lib.RunSpec * max(1, len(runs)))()
+    for k, r in enumerate(runs):
+        specs[k] = _lib.RunSpec(int(r.get("op", OP_EXTREG)), float(r["tau"]), float(r.get("tau_nh", 1.0)),
+                                float(r.get("u0", 0.0)), int(r["n_steps"]), int(r.get("aos_offset", 0)))
+    sol = None
+    if solid is not None:
+        sol = np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1)
+    d = _lib.BatchDesc(q, nx, ny, None if sol is None else sol.ctypes.data, inlet_x, outlet_x, rho0, energy_every,
+                       energy_factor, int(bool(density_check)), density_limit, init, precision, slots)
+    a = None
+    if aos is not None:
+        a = np.ascontiguousarray(aos, dtype=np.float64).reshape(-1)
+    out = (_lib.BatchResult * max(1, len(runs)))()
+    check(lib().erlbm_batch_run(C.byref(d), len(runs), specs, None if a is None else a.ctypes.data,
+                                0 if a is None else a.size, out), "erlbm_batch_run")
+    return [dict(label=o.label, decided_step=o.decided_step, steps_done=o.steps_done, status=o.status,
+                 margin=o.margin, energy=o.energy) for o in out[:len(runs)]]

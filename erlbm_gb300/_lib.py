@@ -17,6 +17,7 @@ OP_BGK, OP_MRT, OP_REG, OP_EXTREG = 1, 2, 3, 4
 FP64, FP32_SHIFTED = 0, 1
 STAGE_POST_STREAM, STAGE_POST_COLLISION = 0, 1
 MAP_TAYLOR_GREEN, MAP_OBSTACLE = 1, 2
+INIT_REST, INIT_TG_MAP, INIT_AOS = 0, 1, 2
 
 
 class ErlbmError(RuntimeError):
@@ -49,9 +50,21 @@ class MapDesc(C.Structure):
                 ("pi", C.c_void_p), ("pj", C.c_void_p), ("max_steps", C.c_int), ("slots", C.c_int)]
 
 
+class BatchDesc(C.Structure):
+    _fields_ = [("q", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("solid", C.c_void_p), ("inlet_x", C.c_int),
+                ("outlet_x", C.c_int), ("rho0", C.c_double), ("energy_every", C.c_int),
+                ("energy_factor", C.c_double), ("density_check", C.c_int), ("density_limit", C.c_double),
+                ("init", C.c_int), ("precision", C.c_int), ("slots", C.c_int)]
+
+
 class RunSpec(C.Structure):
-    _fields_ = [("kind", C.c_int), ("op", C.c_int), ("tau", C.c_double), ("tau_nh", C.c_double),
-                ("u0", C.c_double), ("n_steps", C.c_int), ("sx", C.c_int), ("sy", C.c_int)]
+    _fields_ = [("op", C.c_int), ("tau", C.c_double), ("tau_nh", C.c_double), ("u0", C.c_double),
+                ("n_steps", C.c_int), ("aos_offset", C.c_int64)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("label", C.c_int), ("decided_step", C.c_int), ("steps_done", C.c_int), ("status", C.c_int),
+                ("margin", C.c_double), ("energy", C.c_double)]
 
 
 class ServerDesc(C.Structure):
@@ -90,6 +103,10 @@ _SIGS = {
     "erlbm_macroscopic": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "erlbm_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(BC), C.POINTER(Checks), C.POINTER(RunResult)]),
     "erlbm_sync": (C.c_int, [C.c_void_p]),
+    "erlbm_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "erlbm_batch_run": (C.c_int, [C.POINTER(BatchDesc), C.c_int, C.POINTER(RunSpec), C.c_void_p, C.c_size_t,
+                                  C.POINTER(BatchResult)]),
+    "erlbm_map_run": (C.c_int, [C.POINTER(MapDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 

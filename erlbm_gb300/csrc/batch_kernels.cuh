@@ -1,0 +1,354 @@
+// batch_kernels.cuh -- many small independent lattices in one persistent launch.
+//
+// This replaces the stability-map loops of the reference: "#pragma omp parallel for collapse(2)
+// schedule(dynamic)" over map points (main_stability-map_taylor-green.cpp:150-177,
+// main_stability-map_obstacle.cpp:161-186), each point running roda_ponto (TG map :41-104,
+// obstacle map :75-123) on its own populations.
+//
+// Layout.  One CTA owns one lattice "slot": the whole lattice (nx * ny <= NPT * blockDim nodes,
+// nz = 1) lives in shared memory as one SoA buffer buf[i * NB + node].  A step is
+//   gather (pull; bounce-back from the solid mask) into registers -> barrier ->
+//   [energy check] -> boundary planes -> collide -> [density check] -> write own nodes -> barrier,
+// so one buffer suffices.  When a run ends (budget reached, or a check failed), thread 0 claims the
+// next run index from a global counter and the slot is refilled: the launch is persistent, with
+// grid = SMs x resident CTAs, and the host orders runs longest-first so the tail is short.
+//
+// Checks (the reference's, per run):
+//   energy: E = sum 1/2 |u|^2 of the post-stream populations at step % every == 0 && step > 0;
+//           unstable when E > factor * E0 or E is not finite (TG map :69-81).  FP64: per-node
+//           energies are summed serially in node order, as kinectic_energy does.
+//   density: |rho| > limit or non-finite at any node after its collision; the step is finished
+//           and the run stops (obstacle map :98-106, :88).
+// Every loop is bounded by the run's step budget; nothing waits on another CTA.
+#pragma once
+
+#include <cstdint>
+
+#include "lattice_kernels.cuh"
+
+namespace erlbm {
+
+enum BatchInit : int { INIT_REST = 0, INIT_TG_MAP = 1, INIT_AOS = 2 };
+
+// Geometry and checks shared by every run of a launch.
+struct BatchGeo {
+    int nx, ny, nb;               // box (nz = 1), nb = nx * ny
+    const uint8_t *solid;         // nb bytes, 1 = solid; null = fully periodic
+    int inlet_x, outlet_x;        // boundary planes, -1 = none (D3Q19 inlet only)
+    double rho0;                  // outlet density and rest density
+    int energy_every;             // 0 = off
+    double energy_factor;
+    int density_check;
+    double density_limit;
+    int init;                     // BatchInit
+    const double *sinx, *cosx;    // INIT_TG_MAP: sin(2 pi x / L), cos(2 pi x / L) for x < nx
+};
+
+// One run, prepared on the host.
+struct BatchRun {
+    Relax R;
+    shifted::Coef k;
+    double u0;          // TG amplitude (INIT_TG_MAP) or inlet velocity (inlet_x >= 0)
+    long long aos_off;  // INIT_AOS: offset (in doubles) of this run's initial AoS populations
+    int n_steps;
+    int op;
+    int out;            // result slot
+    int pad;
+};
+
+struct BatchResult {
+    int label;          // 1 unstable
+    int decided_step;   // failing step, or n_steps
+    int steps_done;
+    int status;         // bit 0 density, bit 1 non-finite density, bit 2 energy
+    double margin;      // max E/(factor E0) or max |rho|/limit (+inf for non-finite)
+    double energy;      // last energy computed (E0 when no check ran)
+};
+
+template <class P, int Q>
+__device__ __forceinline__ void batch_collide(typename P::T *f, const BatchRun &r)
+{
+    CollParams prm;
+    prm.R = r.R;
+    prm.k = r.k;
+    if (r.op == OP_BGK)
+        P::template collide<Q, OP_BGK>(f, prm);
+    else if (r.op == OP_REG)
+        P::template collide<Q, OP_REG>(f, prm);
+    else
+        P::template collide<Q, OP_EXTREG>(f, prm);
+}
+
+// Initial equilibrium of the Taylor-Green map (main_stability-map_taylor-green.cpp:49-61): rho = 1,
+// u_x = U0 sin(kx) cos(ky), u_y = -U0 cos(kx) sin(ky), u_z = 0.
+template <class P, int Q>
+__device__ __forceinline__ void tg_map_init(typename P::T *f, int x, int y, double u0, const BatchGeo &g)
+{
+    const double ux = u0 * g.sinx[x] * g.cosx[y];
+    const double uy = -u0 * g.cosx[x] * g.sinx[y];
+    double feq[Q];
+    if constexpr (Q == 19)
+        exact::equilibrium19(1.0, ux, uy, 0.0, feq);
+    else
+        exact::equilibrium9(1.0, ux, uy, feq);
+#pragma unroll
+    for (int i = 0; i < Q; i++) f[i] = P::template from_f<Q>(feq[i], i);
+}
+
+// Deterministic block sum of one double per thread.  Exact path: serial in node order (thread
+// order), like kinectic_energy; FP32 path: fixed shuffle tree + serial over warps.
+template <bool SERIAL>
+__device__ double block_sum(double v, double *sh, int n_vals)
+{
+    const int tid = threadIdx.x;
+    double total;
+    if (SERIAL) {
+        sh[tid] = v;
+        __syncthreads();
+        if (tid == 0) {
+            double s = 0;
+            for (int k = 0; k < n_vals; k++) s = s + sh[k];
+            sh[blockDim.x] = s;
+        }
+        __syncthreads();
+        total = sh[blockDim.x];
+    } else {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0) sh[tid >> 5] = v;
+        __syncthreads();
+        if (tid == 0) {
+            double s = 0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[k];
+            sh[blockDim.x] = s;
+        }
+        __syncthreads();
+        total = sh[blockDim.x];
+    }
+    __syncthreads();
+    return total;
+}
+
+__device__ __forceinline__ double block_max(double v, double *sh)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int tid = threadIdx.x;
+    if ((tid & 31) == 0) sh[tid >> 5] = v;
+    __syncthreads();
+    if (tid == 0) {
+        double s = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) s = fmax(s, sh[k]);
+        sh[blockDim.x] = s;
+    }
+    __syncthreads();
+    const double t = sh[blockDim.x];
+    __syncthreads();
+    return t;
+}
+
+// Shared memory: populations Q * NB of T, the solid mask (NB bytes), reduction scratch.
+template <class P, int Q>
+__host__ __device__ inline size_t batch_smem_bytes(int nb, int block)
+{
+    const size_t pop = (size_t)Q * nb * sizeof(typename P::T);
+    const size_t red = ((size_t)block + 1) * sizeof(double);
+    const size_t mask = ((size_t)nb + 15) / 16 * 16;
+    return (pop + 15) / 16 * 16 + red + mask + 16;
+}
+
+// Register budget: one node per thread (the map lattices: 256 or 264 nodes) wants several
+// resident CTAs per SM to overlap their barriers, so it is bounded to 288 threads x 3 CTAs (FP32)
+// or x 2 (FP64, whose exact collision needs more registers); larger lattices get 512 x 1.
+template <int NPT, int BYTES>
+struct BatchBounds {
+    static constexpr int MAXT = NPT == 1 ? 288 : 512;
+    static constexpr int MINB = NPT == 1 ? (BYTES == 8 ? 2 : 3) : 1;
+};
+
+template <class P, int Q, int NPT>
+__global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
+                                  BatchBounds<NPT, sizeof(typename P::T)>::MINB) k_batch(BatchGeo g, const BatchRun *__restrict__ runs, int n_runs,
+                                               int *__restrict__ counter, BatchResult *__restrict__ res,
+                                               const double *__restrict__ aos)
+{
+    using T = typename P::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int NB = g.nb;
+    T *buf = reinterpret_cast<T *>(smem_raw);
+    double *red = reinterpret_cast<double *>(smem_raw + ((size_t)Q * NB * sizeof(T) + 15) / 16 * 16);
+    uint8_t *solid = reinterpret_cast<uint8_t *>(red + blockDim.x + 1);
+    __shared__ int s_run;
+    const int tid = threadIdx.x;
+
+    for (int k = tid; k < NB; k += blockDim.x) solid[k] = g.solid ? g.solid[k] : 0;
+    const bool any_solid = g.solid != nullptr;
+
+    // per-thread node slots
+    int node[NPT], nx_[NPT], ny_[NPT];
+    bool fluid[NPT];
+#pragma unroll
+    for (int s = 0; s < NPT; s++) {
+        node[s] = tid + s * blockDim.x;
+        nx_[s] = node[s] % g.nx;
+        ny_[s] = node[s] / g.nx;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < NPT; s++) fluid[s] = node[s] < NB && !solid[node[s]];
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_run = atomicAdd(counter, 1);
+        __syncthreads();
+        const int ri = s_run;
+        if (ri >= n_runs) break;
+        const BatchRun r = runs[ri];
+
+        // ---- initial populations (post-stream state of step 0) ----
+        T f[NPT][Q];
+#pragma unroll
+        for (int s = 0; s < NPT; s++) {
+            if (!fluid[s]) continue;
+            if (g.init == INIT_TG_MAP) {
+                tg_map_init<P, Q>(f[s], nx_[s], ny_[s], r.u0, g);
+            } else if (g.init == INIT_AOS) {
+                // fluid index of this node: count of fluid nodes before it (solid masks are small)
+                int p = 0;
+                for (int k = 0; k < node[s]; k++) p += !solid[k];
+                const double *src = aos + r.aos_off + (long long)p * Q;
+#pragma unroll
+                for (int i = 0; i < Q; i++) f[s][i] = P::template from_f<Q>(src[i], i);
+            } else {
+#pragma unroll
+                for (int i = 0; i < Q; i++) f[s][i] = P::template from_f<Q>(Lat<Q>::w(i) * g.rho0, i);
+            }
+#pragma unroll
+            for (int i = 0; i < Q; i++) buf[i * NB + node[s]] = f[s][i];
+        }
+        __syncthreads();
+
+        double E0 = 0.0, E = 0.0, margin = 0.0, max_rho = 0.0;
+        int label = 0, decided = r.n_steps, status = 0, steps_done = r.n_steps;
+        if (g.energy_every > 0) {
+            double e = 0.0;
+#pragma unroll
+            for (int s = 0; s < NPT; s++)
+                if (fluid[s]) e += P::template energy<Q>(f[s]);
+            E0 = block_sum<NPT == 1 && sizeof(T) == 8>(e, red, NB);
+            E = E0;
+        }
+
+        for (int step = 0; step < r.n_steps; step++) {
+            // ---- stream: post-stream populations of this step ----
+            if (step > 0) {
+#pragma unroll
+                for (int s = 0; s < NPT; s++) {
+                    if (!fluid[s]) continue;
+                    int x = nx_[s];
+                    const int y = ny_[s];
+                    int me = node[s];
+                    if (x == g.outlet_x) {  // the outlet copies its inner neighbour (devnull_rho_x)
+                        x += (g.outlet_x < g.nx / 2) ? 1 : -1;
+                        me = node[s] + (x - nx_[s]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < Q; i++) {
+                        const int xs = wrap1(x - Lat<Q>::cx(i), g.nx);
+                        const int ys = wrap1(y - Lat<Q>::cy(i), g.ny);
+                        const int src = xs + g.nx * ys;
+                        f[s][i] = (any_solid && solid[src]) ? buf[Lat<Q>::opp(i) * NB + me] : buf[i * NB + src];
+                    }
+                }
+            } else if (g.outlet_x >= 0) {
+#pragma unroll
+                for (int s = 0; s < NPT; s++) {
+                    if (!fluid[s] || nx_[s] != g.outlet_x) continue;
+                    const int me = node[s] + ((g.outlet_x < g.nx / 2) ? 1 : -1);
+#pragma unroll
+                    for (int i = 0; i < Q; i++) f[s][i] = buf[i * NB + me];
+                }
+            }
+            __syncthreads();
+
+            // ---- energy check on the post-stream populations ----
+            if (g.energy_every > 0 && step > 0 && step % g.energy_every == 0) {
+                double e = 0.0;
+#pragma unroll
+                for (int s = 0; s < NPT; s++)
+                    if (fluid[s]) e += P::template energy<Q>(f[s]);
+                E = block_sum<NPT == 1 && sizeof(T) == 8>(e, red, NB);
+                const double lim = g.energy_factor * E0;
+                const double rr = isfinite(E) ? E / lim : INFINITY;
+                margin = fmax(margin, rr);
+                if (E > lim || !isfinite(E)) {
+                    label = 1;
+                    decided = step;
+                    steps_done = step;
+                    status |= 4;
+                    break;
+                }
+            }
+
+            // ---- boundary planes, collision, density check, store ----
+            int flag = 0;
+#pragma unroll
+            for (int s = 0; s < NPT; s++) {
+                if (!fluid[s]) continue;
+                const int x = nx_[s];
+                if (x == g.outlet_x) {
+                    const int xn = x + ((g.outlet_x < g.nx / 2) ? 1 : -1);
+                    if (Q == 19 && xn == g.inlet_x) P::zou_he(f[s], r.u0, g.inlet_x < g.nx / 2);
+                    if (any_solid && solid[node[s] + (xn - x)])
+                        P::template rest<Q>(f[s], g.rho0);
+                    else
+                        P::template outlet<Q>(f[s], g.rho0);
+                } else if (Q == 19 && x == g.inlet_x) {
+                    P::zou_he(f[s], r.u0, g.inlet_x < g.nx / 2);
+                }
+                batch_collide<P, Q>(f[s], r);
+                if (g.density_check) {
+                    const double rho = P::template density<Q>(f[s]);
+                    if (!isfinite(rho)) {
+                        flag |= 2;
+                    } else {
+                        const double a = fabs(rho);
+                        max_rho = fmax(max_rho, a);
+                        if (a > g.density_limit) flag |= 1;
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < Q; i++) buf[i * NB + node[s]] = f[s][i];
+            }
+            if (g.density_check) {
+                // finish the step everywhere, then stop if any node failed
+                const int any = __syncthreads_or(flag);
+                if (any) {
+                    label = 1;
+                    decided = step;
+                    steps_done = step + 1;
+                    status |= __syncthreads_or(flag & 2) ? 3 : 1;
+                    break;
+                }
+            } else {
+                __syncthreads();
+            }
+        }
+        if (g.density_check) {
+            max_rho = block_max(max_rho, red);
+            margin = (status & 2) ? INFINITY : max_rho / g.density_limit;
+        }
+        if (tid == 0) {
+            BatchResult o;
+            o.label = label;
+            o.decided_step = decided;
+            o.steps_done = steps_done;
+            o.status = status;
+            o.margin = margin;
+            o.energy = E;
+            res[r.out] = o;
+        }
+    }
+}
+
+}  // namespace erlbm

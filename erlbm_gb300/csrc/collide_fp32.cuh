@@ -1,16 +1,26 @@
 // collide_fp32.cuh -- FP32 collision on shifted populations g_i = f_i - w_i (rho_ref = 1).
 //
 // Same operators as the reference (coll_Ext_Reg, Collision_operators.cpp:1182-1307; coll_Reg,
-// :860-967; coll_BGK, :12-49), rewritten for storage and arithmetic in FP32 without losing the
-// small quantities to cancellation against the O(w_i) rest populations:
-//   drho = sum g,  m = sum c g,  u = m / (1 + drho);
-//   Pi^neq_ab = sum c_a c_b g - (drho / 3) delta_ab - m_a u_b      (second moment of f_eq - w:
-//               exact for the second-order equilibrium on D2Q9 and D3Q19);
-//   geq_i = w_i (drho + 3 c.m + 4.5 (c.m)(c.u) - 1.5 m.u)          (= f_eq_i - w_i);
-//   f1_i  = 4.5 w_i Q_i : Pi^neq,  Q_i = c c - delta / 3;
-//   E-RLBM: g*_i = (1 - w_gt1) geq_i + w_gt1 g_i + (w_1 - w_gt1) f1_i
-//   RLBM:   g*_i = geq_i + w_1 f1_i;   BGK: g*_i = (1 - 1/tau) g_i + geq_i / tau.
-// Opposite directions share c.m c.u and f1, which halves that work.
+// :860-967; coll_BGK, :12-49), rewritten for FP32 storage and arithmetic.  In exact arithmetic
+//   f* = f_eq + w_1 f1 + w_gt1 (f - f_eq - f1)  =  f + k_d d + k_f f1,   d = f - f_eq,
+// with k_d = w_gt1 - 1, k_f = w_1 - w_gt1 (RLBM: k_d = -1, k_f = w_1; BGK: k_d = -1/tau, k_f = 0).
+// The increment form is what keeps FP32 honest: the update adds a small correction to the stored
+// population instead of rebuilding it from O(1) pieces.
+//
+// Each opposite pair (i, j) is split into an even part e = (g_i + g_j)/2 and an odd part
+// o = (g_i - g_j)/2 (both exact).  Then
+//   drho = g_0 + 2 sum e,   m = 2 sum c o,   u = m / (1 + drho),
+//   non-equilibrium even part  de = e - w (drho + 4.5 (c.m)(c.u) - 1.5 m.u),
+//   non-equilibrium odd part   do = o - 3 w (c.m),
+//   Pi^neq = 2 sum c c de  (odd parts do not enter even moments),  f1 = 4.5 w Q_i : Pi^neq.
+// The non-equilibrium part must carry no mass and no momentum.  That holds in exact arithmetic,
+// but the rounding of c.m = m_x +- m_y is a fixed function of the local state, so in a region of
+// uniform flow it would push momentum the same way every step (a drift linear in time, measured at
+// ~1e-8 relative velocity per step on the double shear layer).  So the axis pairs' odd parts and
+// the rest population's even part are not computed but closed:
+//   do_x = -(sum of the other c_x do),  ...,  de_0 = -2 sum de,
+// which makes the update conserve mass and momentum up to the rounding of small quantities; the
+// remaining error is the unbiased rounding of the stored populations (growth ~ sqrt(t)).
 #pragma once
 
 #include "lattice.cuh"
@@ -18,61 +28,38 @@
 namespace erlbm {
 namespace shifted {
 
-// Coefficients of the shifted update, formed in FP64 and rounded once.
+// Increment coefficients, formed in FP64 and rounded once.
 struct Coef {
-    float a, b, c;  // E-RLBM: a = 1 - w_gt1, b = w_gt1, c = w_1 - w_gt1; RLBM: a = 1, b = 0, c = w_1;
-                    // BGK: a = 1/tau, b = 1 - 1/tau, c = 0
+    float kd, kf;
 };
 
 inline Coef make_coef(const Relax &R)
 {
     Coef k;
     if (R.op == OP_BGK) {
-        k.a = (float)R.inv_tau;
-        k.b = (float)(1.0 - R.inv_tau);
-        k.c = 0.f;
+        k.kd = (float)(-R.inv_tau);
+        k.kf = 0.f;
     } else if (R.op == OP_REG) {
-        k.a = 1.f;
-        k.b = 0.f;
-        k.c = (float)R.omega_1;
+        k.kd = -1.f;
+        k.kf = (float)R.omega_1;
     } else {
-        k.a = (float)(1.0 - R.omega_gt1);
-        k.b = (float)R.omega_gt1;
-        k.c = (float)(R.omega_1 - R.omega_gt1);
+        k.kd = (float)(R.omega_gt1 - 1.0);
+        k.kf = (float)(R.omega_1 - R.omega_gt1);
     }
     return k;
 }
 
-template <int OP>
-__device__ __forceinline__ float update(float geq, float g, float f1, const Coef &k)
-{
-    if (OP == OP_BGK) return fmaf(k.b, g, k.a * geq);
-    if (OP == OP_REG) return fmaf(k.c, f1, geq);
-    return fmaf(k.a, geq, fmaf(k.b, g, k.c * f1));
-}
-
-// Equilibrium deviation of an opposite pair (cm = c.m, cu = c.u of the first member).
-__device__ __forceinline__ void geq_pair(float cm, float cu, float base, float w, float &ga, float &gb)
-{
-    const float s = fmaf(4.5f * cm, cu, base);
-    const float ws = w * s;
-    ga = fmaf(3.f * w, cm, ws);
-    gb = fmaf(-3.f * w, cm, ws);
-}
-
-// Moments of the shifted populations; returns drho, u and the node's kinetic energy 1/2 |u|^2.
-template <int Q>
-struct Mom;
-
 // ------------------------------------------------------------------------------------------------
-// D2Q9
+// D2Q9: pairs X = (1,2) c = (1,0); Y = (3,4) c = (0,1); P = (5,6) c = (1,1); M = (7,8) c = (1,-1)
 // ------------------------------------------------------------------------------------------------
 
 __device__ __forceinline__ void moments9(const float g[9], float &drho, float &mx, float &my, float &ux, float &uy)
 {
-    drho = ((g[0] + (g[1] + g[2])) + (g[3] + g[4])) + ((g[5] + g[6]) + (g[7] + g[8]));
-    mx = ((g[1] - g[2]) + (g[5] - g[6])) + (g[7] - g[8]);
-    my = ((g[3] - g[4]) + (g[5] - g[6])) + (g[8] - g[7]);
+    const float eX = g[1] + g[2], eY = g[3] + g[4], eP = g[5] + g[6], eM = g[7] + g[8];
+    const float oX = g[1] - g[2], oY = g[3] - g[4], oP = g[5] - g[6], oM = g[7] - g[8];
+    drho = g[0] + ((eX + eY) + (eP + eM));
+    mx = oX + (oP + oM);
+    my = oY + (oP - oM);
     const float inv = __frcp_rn(1.f + drho);
     ux = mx * inv;
     uy = my * inv;
@@ -81,52 +68,70 @@ __device__ __forceinline__ void moments9(const float g[9], float &drho, float &m
 template <int OP>
 __device__ __forceinline__ void collide9(float g[9], const Coef &k)
 {
-    float drho, mx, my, ux, uy;
-    moments9(g, drho, mx, my, ux, uy);
-    const float base = fmaf(-1.5f, fmaf(mx, ux, my * uy), drho);
-    float geq[9];
-    geq[0] = (4.f / 9.f) * base;
-    geq_pair(mx, ux, base, 1.f / 9.f, geq[1], geq[2]);
-    geq_pair(my, uy, base, 1.f / 9.f, geq[3], geq[4]);
-    geq_pair(mx + my, ux + uy, base, 1.f / 36.f, geq[5], geq[6]);
-    geq_pair(mx - my, ux - uy, base, 1.f / 36.f, geq[7], geq[8]);
-    float f1[9];
+    constexpr float W1 = 1.f / 9.f, W2 = 1.f / 36.f;
+    const float eX = 0.5f * (g[1] + g[2]), oX = 0.5f * (g[1] - g[2]);
+    const float eY = 0.5f * (g[3] + g[4]), oY = 0.5f * (g[3] - g[4]);
+    const float eP = 0.5f * (g[5] + g[6]), oP = 0.5f * (g[5] - g[6]);
+    const float eM = 0.5f * (g[7] + g[8]), oM = 0.5f * (g[7] - g[8]);
+    const float drho = g[0] + 2.f * ((eX + eY) + (eP + eM));
+    const float mx = 2.f * (oX + (oP + oM));
+    const float my = 2.f * (oY + (oP - oM));
+    const float inv = __frcp_rn(1.f + drho);
+    const float ux = mx * inv, uy = my * inv;
+    const float mu15 = -1.5f * fmaf(mx, ux, my * uy);
+    // even non-equilibrium parts
+    const float deX = fmaf(-W1, fmaf(4.5f * mx, ux, mu15), fmaf(-W1, drho, eX));
+    const float deY = fmaf(-W1, fmaf(4.5f * my, uy, mu15), fmaf(-W1, drho, eY));
+    const float cmP = mx + my, cmM = mx - my;
+    const float deP = fmaf(-W2, fmaf(4.5f * cmP, ux + uy, mu15), fmaf(-W2, drho, eP));
+    const float deM = fmaf(-W2, fmaf(4.5f * cmM, ux - uy, mu15), fmaf(-W2, drho, eM));
+    const float de0 = -2.f * ((deX + deY) + (deP + deM));
+    // odd non-equilibrium parts; the axis pairs close the momentum
+    const float doP = fmaf(-3.f * W2, cmP, oP);
+    const float doM = fmaf(-3.f * W2, cmM, oM);
+    const float doX = -(doP + doM);
+    const float doY = -(doP - doM);
+    float f10 = 0.f, f1X = 0.f, f1Y = 0.f, f1P = 0.f, f1M = 0.f;
     if (OP != OP_BGK) {
-        const float a56 = g[5] + g[6], a78 = g[7] + g[8];
-        const float dd = a56 + a78;
-        const float c3 = drho * (1.f / 3.f);
-        const float pxx = fmaf(-mx, ux, ((g[1] + g[2]) + dd) - c3);
-        const float pyy = fmaf(-my, uy, ((g[3] + g[4]) + dd) - c3);
-        const float pxy = fmaf(-mx, uy, a56 - a78);
+        const float pxx = 2.f * (deX + (deP + deM));
+        const float pyy = 2.f * (deY + (deP + deM));
+        const float pxy = 2.f * (deP - deM);
         const float tr = pxx + pyy;
-        f1[0] = (-2.f / 3.f) * tr;
-        f1[1] = f1[2] = fmaf(pxx, 1.f / 3.f, pyy * (-1.f / 6.f));
-        f1[3] = f1[4] = fmaf(pyy, 1.f / 3.f, pxx * (-1.f / 6.f));
+        f10 = (-2.f / 3.f) * tr;
+        f1X = fmaf(pxx, 1.f / 3.f, pyy * (-1.f / 6.f));
+        f1Y = fmaf(pyy, 1.f / 3.f, pxx * (-1.f / 6.f));
         const float t12 = tr * (1.f / 12.f);
-        f1[5] = f1[6] = fmaf(pxy, 0.25f, t12);
-        f1[7] = f1[8] = fmaf(pxy, -0.25f, t12);
+        f1P = fmaf(pxy, 0.25f, t12);
+        f1M = fmaf(pxy, -0.25f, t12);
     }
-#pragma unroll
-    for (int i = 0; i < 9; i++) g[i] = update<OP>(geq[i], g[i], OP != OP_BGK ? f1[i] : 0.f, k);
+    const float kd = k.kd, kf = k.kf;
+    g[0] = fmaf(kd, de0, fmaf(kf, f10, g[0]));
+    g[1] = fmaf(kd, deX + doX, fmaf(kf, f1X, g[1]));
+    g[2] = fmaf(kd, deX - doX, fmaf(kf, f1X, g[2]));
+    g[3] = fmaf(kd, deY + doY, fmaf(kf, f1Y, g[3]));
+    g[4] = fmaf(kd, deY - doY, fmaf(kf, f1Y, g[4]));
+    g[5] = fmaf(kd, deP + doP, fmaf(kf, f1P, g[5]));
+    g[6] = fmaf(kd, deP - doP, fmaf(kf, f1P, g[6]));
+    g[7] = fmaf(kd, deM + doM, fmaf(kf, f1M, g[7]));
+    g[8] = fmaf(kd, deM - doM, fmaf(kf, f1M, g[8]));
 }
 
 // ------------------------------------------------------------------------------------------------
-// D3Q19
+// D3Q19: pairs X (1,2), Y (3,4), Z (5,6); A (7,8) c = (1,1,0); B (9,10) c = (1,-1,0);
+// C (11,12) c = (1,0,1); D (13,14) c = (1,0,-1); E (16,15) c = (0,1,1); F (17,18) c = (0,-1,1)
 // ------------------------------------------------------------------------------------------------
 
 __device__ __forceinline__ void moments19(const float g[19], float &drho, float &mx, float &my, float &mz, float &ux,
                                           float &uy, float &uz)
 {
-    const float s12 = g[1] + g[2], s34 = g[3] + g[4], s56 = g[5] + g[6];
-    const float s78 = g[7] + g[8], s910 = g[9] + g[10], s1112 = g[11] + g[12], s1314 = g[13] + g[14];
-    const float s1516 = g[15] + g[16], s1718 = g[17] + g[18];
-    drho = ((g[0] + (s12 + s34)) + (s56 + s78)) + ((s910 + s1112) + ((s1314 + s1516) + s1718));
-    const float d12 = g[1] - g[2], d34 = g[3] - g[4], d56 = g[5] - g[6];
-    const float d78 = g[7] - g[8], d910 = g[9] - g[10], d1112 = g[11] - g[12], d1314 = g[13] - g[14];
-    const float d1615 = g[16] - g[15], d1718 = g[17] - g[18];
-    mx = (d12 + (d78 + d910)) + (d1112 + d1314);
-    my = (d34 + (d78 - d910)) + (d1615 - d1718);
-    mz = (d56 + (d1112 - d1314)) + (d1615 + d1718);
+    const float oX = g[1] - g[2], oY = g[3] - g[4], oZ = g[5] - g[6], oA = g[7] - g[8], oB = g[9] - g[10];
+    const float oC = g[11] - g[12], oD = g[13] - g[14], oE = g[16] - g[15], oF = g[17] - g[18];
+    const float e1 = (g[1] + g[2]) + (g[3] + g[4]), e2 = (g[5] + g[6]) + (g[7] + g[8]);
+    const float e3 = (g[9] + g[10]) + (g[11] + g[12]), e4 = (g[13] + g[14]) + (g[15] + g[16]);
+    drho = (g[0] + (e1 + e2)) + ((e3 + e4) + (g[17] + g[18]));
+    mx = (oX + (oA + oB)) + (oC + oD);
+    my = (oY + (oA - oB)) + (oE - oF);
+    mz = (oZ + (oC - oD)) + (oE + oF);
     const float inv = __frcp_rn(1.f + drho);
     ux = mx * inv;
     uy = my * inv;
@@ -136,52 +141,78 @@ __device__ __forceinline__ void moments19(const float g[19], float &drho, float 
 template <int OP>
 __device__ __forceinline__ void collide19(float g[19], const Coef &k)
 {
-    float drho, mx, my, mz, ux, uy, uz;
-    moments19(g, drho, mx, my, mz, ux, uy, uz);
-    const float base = fmaf(-1.5f, fmaf(mx, ux, fmaf(my, uy, mz * uz)), drho);
-    float geq[19];
     constexpr float W1 = 1.f / 18.f, W2 = 1.f / 36.f;
-    geq[0] = (1.f / 3.f) * base;
-    geq_pair(mx, ux, base, W1, geq[1], geq[2]);
-    geq_pair(my, uy, base, W1, geq[3], geq[4]);
-    geq_pair(mz, uz, base, W1, geq[5], geq[6]);
-    geq_pair(mx + my, ux + uy, base, W2, geq[7], geq[8]);
-    geq_pair(mx - my, ux - uy, base, W2, geq[9], geq[10]);
-    geq_pair(mx + mz, ux + uz, base, W2, geq[11], geq[12]);
-    geq_pair(mx - mz, ux - uz, base, W2, geq[13], geq[14]);
-    geq_pair(my + mz, uy + uz, base, W2, geq[16], geq[15]);
-    geq_pair(mz - my, uz - uy, base, W2, geq[17], geq[18]);
-    float f1[19];
+    const float eX = 0.5f * (g[1] + g[2]), oX = 0.5f * (g[1] - g[2]);
+    const float eY = 0.5f * (g[3] + g[4]), oY = 0.5f * (g[3] - g[4]);
+    const float eZ = 0.5f * (g[5] + g[6]), oZ = 0.5f * (g[5] - g[6]);
+    const float eA = 0.5f * (g[7] + g[8]), oA = 0.5f * (g[7] - g[8]);
+    const float eB = 0.5f * (g[9] + g[10]), oB = 0.5f * (g[9] - g[10]);
+    const float eC = 0.5f * (g[11] + g[12]), oC = 0.5f * (g[11] - g[12]);
+    const float eD = 0.5f * (g[13] + g[14]), oD = 0.5f * (g[13] - g[14]);
+    const float eE = 0.5f * (g[16] + g[15]), oE = 0.5f * (g[16] - g[15]);
+    const float eF = 0.5f * (g[17] + g[18]), oF = 0.5f * (g[17] - g[18]);
+    const float drho = g[0] + 2.f * (((eX + eY) + (eZ + eA)) + ((eB + eC) + (eD + (eE + eF))));
+    const float mx = 2.f * ((oX + (oA + oB)) + (oC + oD));
+    const float my = 2.f * ((oY + (oA - oB)) + (oE - oF));
+    const float mz = 2.f * ((oZ + (oC - oD)) + (oE + oF));
+    const float inv = __frcp_rn(1.f + drho);
+    const float ux = mx * inv, uy = my * inv, uz = mz * inv;
+    const float mu15 = -1.5f * fmaf(mx, ux, fmaf(my, uy, mz * uz));
+    const float r1 = -W1 * drho, r2 = -W2 * drho;
+    const float deX = fmaf(-W1, fmaf(4.5f * mx, ux, mu15), eX + r1);
+    const float deY = fmaf(-W1, fmaf(4.5f * my, uy, mu15), eY + r1);
+    const float deZ = fmaf(-W1, fmaf(4.5f * mz, uz, mu15), eZ + r1);
+    const float cmA = mx + my, cmB = mx - my, cmC = mx + mz, cmD = mx - mz, cmE = my + mz, cmF = mz - my;
+    const float deA = fmaf(-W2, fmaf(4.5f * cmA, ux + uy, mu15), eA + r2);
+    const float deB = fmaf(-W2, fmaf(4.5f * cmB, ux - uy, mu15), eB + r2);
+    const float deC = fmaf(-W2, fmaf(4.5f * cmC, ux + uz, mu15), eC + r2);
+    const float deD = fmaf(-W2, fmaf(4.5f * cmD, ux - uz, mu15), eD + r2);
+    const float deE = fmaf(-W2, fmaf(4.5f * cmE, uy + uz, mu15), eE + r2);
+    const float deF = fmaf(-W2, fmaf(4.5f * cmF, uz - uy, mu15), eF + r2);
+    const float de0 = -2.f * (((deX + deY) + (deZ + deA)) + ((deB + deC) + (deD + (deE + deF))));
+    const float doA = fmaf(-3.f * W2, cmA, oA), doB = fmaf(-3.f * W2, cmB, oB);
+    const float doC = fmaf(-3.f * W2, cmC, oC), doD = fmaf(-3.f * W2, cmD, oD);
+    const float doE = fmaf(-3.f * W2, cmE, oE), doF = fmaf(-3.f * W2, cmF, oF);
+    const float doX = -((doA + doB) + (doC + doD));
+    const float doY = -((doA - doB) + (doE - doF));
+    const float doZ = -((doC - doD) + (doE + doF));
+    float f10 = 0.f, f1X = 0.f, f1Y = 0.f, f1Z = 0.f, f1A = 0.f, f1B = 0.f, f1C = 0.f, f1D = 0.f, f1E = 0.f,
+          f1F = 0.f;
     if (OP != OP_BGK) {
-        const float s78 = g[7] + g[8], s910 = g[9] + g[10], s1112 = g[11] + g[12], s1314 = g[13] + g[14];
-        const float s1516 = g[15] + g[16], s1718 = g[17] + g[18];
-        const float c3 = drho * (1.f / 3.f);
-        const float sxx = ((g[1] + g[2]) + (s78 + s910)) + (s1112 + s1314);
-        const float syy = ((g[3] + g[4]) + (s78 + s910)) + (s1516 + s1718);
-        const float szz = ((g[5] + g[6]) + (s1112 + s1314)) + (s1516 + s1718);
-        const float pxx = fmaf(-mx, ux, sxx - c3);
-        const float pyy = fmaf(-my, uy, syy - c3);
-        const float pzz = fmaf(-mz, uz, szz - c3);
-        const float pxy = fmaf(-mx, uy, s78 - s910);
-        const float pxz = fmaf(-mx, uz, s1112 - s1314);
-        const float pyz = fmaf(-my, uz, s1516 - s1718);
+        const float pxx = 2.f * ((deX + (deA + deB)) + (deC + deD));
+        const float pyy = 2.f * ((deY + (deA + deB)) + (deE + deF));
+        const float pzz = 2.f * ((deZ + (deC + deD)) + (deE + deF));
+        const float pxy = 2.f * (deA - deB), pxz = 2.f * (deC - deD), pyz = 2.f * (deE - deF);
         const float tr3 = (pxx + pyy + pzz) * (1.f / 3.f);
-        f1[0] = -0.5f * (3.f * tr3);
-        f1[1] = f1[2] = 0.25f * (pxx - tr3);
-        f1[3] = f1[4] = 0.25f * (pyy - tr3);
-        f1[5] = f1[6] = 0.25f * (pzz - tr3);
+        f10 = -1.5f * tr3;
+        f1X = 0.25f * (pxx - tr3);
+        f1Y = 0.25f * (pyy - tr3);
+        f1Z = 0.25f * (pzz - tr3);
         const float bxy = 0.125f * ((pxx + pyy) - tr3);
-        f1[7] = f1[8] = fmaf(0.25f, pxy, bxy);
-        f1[9] = f1[10] = fmaf(-0.25f, pxy, bxy);
         const float bxz = 0.125f * ((pxx + pzz) - tr3);
-        f1[11] = f1[12] = fmaf(0.25f, pxz, bxz);
-        f1[13] = f1[14] = fmaf(-0.25f, pxz, bxz);
         const float byz = 0.125f * ((pyy + pzz) - tr3);
-        f1[15] = f1[16] = fmaf(0.25f, pyz, byz);
-        f1[17] = f1[18] = fmaf(-0.25f, pyz, byz);
+        f1A = fmaf(0.25f, pxy, bxy);
+        f1B = fmaf(-0.25f, pxy, bxy);
+        f1C = fmaf(0.25f, pxz, bxz);
+        f1D = fmaf(-0.25f, pxz, bxz);
+        f1E = fmaf(0.25f, pyz, byz);
+        f1F = fmaf(-0.25f, pyz, byz);
     }
-#pragma unroll
-    for (int i = 0; i < 19; i++) g[i] = update<OP>(geq[i], g[i], OP != OP_BGK ? f1[i] : 0.f, k);
+    const float kd = k.kd, kf = k.kf;
+    g[0] = fmaf(kd, de0, fmaf(kf, f10, g[0]));
+#define ERLBM_PAIR(I, J, DE, DO, F1)                  \
+    g[I] = fmaf(kd, DE + DO, fmaf(kf, F1, g[I]));     \
+    g[J] = fmaf(kd, DE - DO, fmaf(kf, F1, g[J]));
+    ERLBM_PAIR(1, 2, deX, doX, f1X)
+    ERLBM_PAIR(3, 4, deY, doY, f1Y)
+    ERLBM_PAIR(5, 6, deZ, doZ, f1Z)
+    ERLBM_PAIR(7, 8, deA, doA, f1A)
+    ERLBM_PAIR(9, 10, deB, doB, f1B)
+    ERLBM_PAIR(11, 12, deC, doC, f1C)
+    ERLBM_PAIR(13, 14, deD, doD, f1D)
+    ERLBM_PAIR(16, 15, deE, doE, f1E)
+    ERLBM_PAIR(17, 18, deF, doF, f1F)
+#undef ERLBM_PAIR
 }
 
 template <int Q, int OP>

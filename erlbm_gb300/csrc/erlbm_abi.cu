@@ -78,6 +78,7 @@ struct erlbm_handle {
     double *d_out = nullptr;         // small device result block
     RunStatus *d_status = nullptr;
     cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;  // the stream created at erlbm_create
     size_t elem() const { return prec == ERLBM_FP64 ? sizeof(double) : sizeof(float); }
 };
 
@@ -114,7 +115,7 @@ void free_handle(erlbm_handle *h)
     cudaFree(h->d_scr);
     cudaFree(h->d_out);
     cudaFree(h->d_status);
-    if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
 }
 
@@ -315,10 +316,11 @@ int erlbm_create(const erlbm_desc *d, erlbm_handle **out)
         free_handle(h);
         return cuda_fail(e, "cudaGetDevice");
     }
-    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    if ((e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking)) != cudaSuccess) {
         free_handle(h);
         return cuda_fail(e, "cudaStreamCreate");
     }
+    h->stream = h->own_stream;
     std::vector<int> nof;
     h->n_fluid = h->g.nbox;
     if (d->solid) {
@@ -452,6 +454,15 @@ int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc)
     if ((rc = validate_bc(h, bc, &b))) return rc;
     for (int s = 0; s < n_steps; s++)
         if ((rc = enqueue_step(h, b, 0, 0.0, false))) return rc;
+    return ERLBM_OK;
+}
+
+int erlbm_set_stream(erlbm_handle *h, void *stream)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    h->stream = stream ? (cudaStream_t)stream : h->own_stream;
     return ERLBM_OK;
 }
 

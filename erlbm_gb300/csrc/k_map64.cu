@@ -1,0 +1,60 @@
+// k_map64.cu -- batched persistent kernel instantiations, plain FP64 (compiled with --fmad=false, the reference's rounding).
+#include "batch_kernels.cuh"
+
+namespace erlbm {
+
+namespace {
+
+template <int Q, int NPT>
+cudaError_t go(const BatchGeo &g, const BatchRun *runs, int n_runs, int *counter, BatchResult *res, const double *aos,
+               int grid, int block, size_t smem, cudaStream_t s)
+{
+    auto k = k_batch<PrecExact64, Q, NPT>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, block, smem, s>>>(g, runs, n_runs, counter, res, aos);
+    return cudaGetLastError();
+}
+
+template <int Q, int NPT>
+int occ(int block, size_t smem)
+{
+    auto k = k_batch<PrecExact64, Q, NPT>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+}  // namespace
+
+int launch_batch_fp64(int q, int npt, const BatchGeo &g, const BatchRun *runs, int n_runs, int *counter,
+                      BatchResult *res, const double *aos, int grid, int block, size_t smem, cudaStream_t s)
+{
+    cudaError_t e;
+    if (q == 19 && npt == 1) e = go<19, 1>(g, runs, n_runs, counter, res, aos, grid, block, smem, s);
+    else if (q == 19 && npt == 2) e = go<19, 2>(g, runs, n_runs, counter, res, aos, grid, block, smem, s);
+    else if (q == 9 && npt == 1) e = go<9, 1>(g, runs, n_runs, counter, res, aos, grid, block, smem, s);
+    else if (q == 9 && npt == 2) e = go<9, 2>(g, runs, n_runs, counter, res, aos, grid, block, smem, s);
+    else if (q == 9 && npt == 4) e = go<9, 4>(g, runs, n_runs, counter, res, aos, grid, block, smem, s);
+    else return -1;
+    return e == cudaSuccess ? 0 : -3;
+}
+
+int batch_occupancy_fp64(int q, int npt, int block, size_t smem)
+{
+    if (q == 19 && npt == 1) return occ<19, 1>(block, smem);
+    if (q == 19 && npt == 2) return occ<19, 2>(block, smem);
+    if (q == 9 && npt == 1) return occ<9, 1>(block, smem);
+    if (q == 9 && npt == 2) return occ<9, 2>(block, smem);
+    if (q == 9 && npt == 4) return occ<9, 4>(block, smem);
+    return 0;
+}
+
+}  // namespace erlbm

@@ -82,3 +82,21 @@ int launch_sum(const double *x, long long n, long long serial_limit, double *scr
 int launch_maxabs(const double *x, long long n, double *scratch, double *out, cudaStream_t s);
 
 }  // namespace erlbm
+
+namespace erlbm {
+
+struct BatchGeo;
+struct BatchRun;
+struct BatchResult;
+
+// Persistent batched launch (batch_kernels.cuh).  block = threads per CTA, npt = nodes per thread,
+// grid = CTAs; smem = dynamic shared bytes.  Returns 0, -1 (no such instantiation) or -3.
+int launch_batch_fp64(int q, int npt, const BatchGeo &g, const BatchRun *runs, int n_runs, int *counter,
+                      BatchResult *res, const double *aos, int grid, int block, size_t smem, cudaStream_t s);
+int launch_batch_fp32(int q, int npt, const BatchGeo &g, const BatchRun *runs, int n_runs, int *counter,
+                      BatchResult *res, const double *aos, int grid, int block, size_t smem, cudaStream_t s);
+// Resident CTAs per SM for a configuration (0 if it cannot run).
+int batch_occupancy(int prec, int q, int npt, int block, size_t smem);
+size_t batch_smem(int prec, int q, int nb, int block);
+
+}  // namespace erlbm

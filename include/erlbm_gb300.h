@@ -125,6 +125,77 @@ int erlbm_macroscopic(erlbm_handle *h, int stage, double *rho, double *u);
 int erlbm_run(erlbm_handle *h, int n_steps, const erlbm_bc *bc, const erlbm_checks *chk, erlbm_run_result *res);
 /* wait for the handle's queued work */
 int erlbm_sync(erlbm_handle *h);
+/* run the handle's work on the caller's CUDA stream (a cudaStream_t; NULL = the handle's own
+ * stream).  Waits for the work queued so far first.  No counterpart in the reference, whose loops
+ * are synchronous; it lets a caller order the engine with its own GPU work and time it with events. */
+int erlbm_set_stream(erlbm_handle *h, void *stream);
+
+/* ---- batched independent runs (stability maps) ------------------------------------------- */
+/* Many small lattices of one geometry, each its own run, in one persistent GPU launch: the
+ * replacement for the maps' "#pragma omp parallel for collapse(2) schedule(dynamic)" loops over
+ * roda_ponto (main_stability-map_taylor-green.cpp:150-177, main_stability-map_obstacle.cpp:161-186).
+ * nx * ny <= 4096 nodes (the lattice lives in one CTA's shared memory), nz = 1. */
+#define ERLBM_INIT_REST 0     /* f_i = w_i rho0 (main_stability-map_obstacle.cpp:81-82) */
+#define ERLBM_INIT_TG_MAP 1   /* equilibrium, rho = 1, u = u0 (sin kx cos ky, -cos kx sin ky)
+                                 (main_stability-map_taylor-green.cpp:49-61) */
+#define ERLBM_INIT_AOS 2      /* each run's initial post-stream populations from aos[aos_offset...] */
+
+typedef struct erlbm_batch_desc {
+    int q, nx, ny;
+    const uint8_t *solid;       /* nx*ny bytes, 1 = solid; NULL = periodic */
+    int inlet_x, outlet_x;      /* boundary planes as in erlbm_bc (-1 = none); inlet velocity = run's u0 */
+    double rho0;                /* outlet and rest density */
+    int energy_every;           /* energy check period (0 = off) */
+    double energy_factor;
+    int density_check;          /* per-step density check (0 = off) */
+    double density_limit;
+    int init;                   /* ERLBM_INIT_* */
+    int precision;
+    int slots;                  /* resident lattices per SM; 0 = as many as fit */
+} erlbm_batch_desc;
+
+typedef struct erlbm_run_spec {
+    int op;                     /* ERLBM_OP_* of this run */
+    double tau, tau_nh;
+    double u0;                  /* TG amplitude (ERLBM_INIT_TG_MAP) or inlet velocity */
+    int n_steps;                /* step budget */
+    int64_t aos_offset;         /* ERLBM_INIT_AOS: offset in doubles of n_fluid * q populations */
+} erlbm_run_spec;
+
+typedef struct erlbm_batch_result {
+    int label;                  /* 1 unstable */
+    int decided_step;           /* failing step, or n_steps */
+    int steps_done;
+    int status;                 /* bit 0 |rho| > limit, bit 1 non-finite density, bit 2 energy check */
+    double margin;              /* as in erlbm_run_result */
+    double energy;              /* last kinetic energy computed (E0 if no check ran) */
+} erlbm_batch_result;
+
+int erlbm_batch_run(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec *runs, const double *aos,
+                    size_t n_aos, erlbm_batch_result *out);
+
+/* The reference's stability maps with their axes (main_stability-map_taylor-green.cpp:134-166,
+ * main_stability-map_obstacle.cpp:147-175). */
+#define ERLBM_MAP_TAYLOR_GREEN 1
+#define ERLBM_MAP_OBSTACLE 2
+
+typedef struct erlbm_map_desc {
+    int kind;                   /* ERLBM_MAP_* */
+    int precision;
+    int op;                     /* TG map: ERLBM_OP_REG or ERLBM_OP_EXTREG, or 0 for both (results
+                                   of all RLBM runs first, then all E-RLBM runs); obstacle: ignored */
+    double tau_nh;              /* TG map E-RLBM tau_nh (0.65) */
+    int L;                      /* TG map lattice side (16) */
+    double ma;                  /* obstacle Mach number (0.1) */
+    int n_i, n_j;               /* map axes (400 x 400) */
+    int n_points;               /* 0: the whole n_i x n_j grid, i fastest; else the points pi[k], pj[k] */
+    const int32_t *pi, *pj;
+    int max_steps;              /* cap on each run's budget, 0 = the reference's count */
+    int slots;                  /* as in erlbm_batch_desc */
+} erlbm_map_desc;
+
+/* labels (and optionally decided steps and margins) of n_points (x 2 when op = 0) runs */
+int erlbm_map_run(const erlbm_map_desc *d, int32_t *labels, int32_t *decided_step, double *margins);
 
 /* ---- program inputs (host functions; what the reference's drivers build around their loops) --- */
 /* inicializa_taylor_green (main_taylor-green.cpp:57-100) on an L x L (x nz) periodic box, AoS in

@@ -660,11 +660,13 @@ void orc_obstacle_map_params(int i, int j, int n_tau, int n_nu, double ma, doubl
 }
 
 /* roda_ponto of the Taylor-Green map (main_stability-map_taylor-green.cpp:41-104) on an L x L x 1
- * D3Q19 box.  Equilibrium start with rho = 1; n_steps = (int)(100 ny / U0); the energy of the
+ * D3Q19 box.  Equilibrium start with rho = 1; n_steps = (int)(100 ny / U0) unless max_steps > 0
+ * caps it; the energy of the
  * post-stream populations is checked when step % 100 == 0 && step > 0.
  * Outputs: label (1 unstable), decided step (the failing check, or n_steps), and the margin
  * max over checks of E / (2 E0) (non-finite E gives +inf). */
-int orc_tg_map_point(int L_, int op, double tau, double tau_nh, double u_0, int *decided_step, double *margin)
+int orc_tg_map_point(int L_, int op, double tau, double tau_nh, double u_0, int max_steps, int *decided_step,
+                     double *margin)
 {
     orc_lattice *lat = orc_create(19, L_, L_, 1, NULL, tau, tau_nh, op);
     const double L = (double)L_;
@@ -676,7 +678,8 @@ int orc_tg_map_point(int L_, int op, double tau, double tau_nh, double u_0, int 
             const double u[3] = {u_x, u_y, 0.0};
             equilibrium(lat->t, u, rho_ini, lat->f + (size_t)(lat->ini[x + y * L_] - 1) * 19);
         }
-    const int n_steps = (int)((double)(100 * L_) / u_0);
+    int n_steps = (int)((double)(100 * L_) / u_0);
+    if (max_steps > 0 && max_steps < n_steps) n_steps = max_steps;
     const double energy_ini = orc_kinetic_energy(lat, 0);
     int unstable = 0, dstep = n_steps;
     double mg = 0.0;
@@ -759,7 +762,7 @@ int orc_obstacle_map_point(int sx, int sy, double tau, double tau_nh, double u_i
 /* Map sweeps over a list of grid points, OpenMP dynamic over points like the reference
  * (main_stability-map_taylor-green.cpp:150-177, main_stability-map_obstacle.cpp:161-186). */
 void orc_tg_map(int L_, int op, double tau_nh, int n_ma, int n_nu, int n_pts, const int *pi, const int *pj,
-                int nthreads, int *labels, int *decided, double *margins)
+                int max_steps, int nthreads, int *labels, int *decided, double *margins)
 {
 #pragma omp parallel for schedule(dynamic) num_threads(nthreads > 0 ? nthreads : 1)
     for (int k = 0; k < n_pts; k++) {
@@ -767,7 +770,7 @@ void orc_tg_map(int L_, int op, double tau_nh, int n_ma, int n_nu, int n_pts, co
         orc_tg_map_params(pi[k], pj[k], n_ma, n_nu, op, tau_nh, &u0, &tau, &tnh);
         int ds;
         double mg;
-        labels[k] = orc_tg_map_point(L_, op, tau, tnh, u0, &ds, &mg);
+        labels[k] = orc_tg_map_point(L_, op, tau, tnh, u0, max_steps, &ds, &mg);
         if (decided) decided[k] = ds;
         if (margins) margins[k] = mg;
     }

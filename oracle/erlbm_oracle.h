@@ -50,12 +50,13 @@ void orc_tg_map_params(int i, int j, int n_ma, int n_nu, int op, double tau_nh_i
                        double *tau_nh);
 void orc_obstacle_map_params(int i, int j, int n_tau, int n_nu, double ma, double *u_imp, double *tau,
                              double *tau_nh);
-int orc_tg_map_point(int L, int op, double tau, double tau_nh, double u_0, int *decided_step, double *margin);
+int orc_tg_map_point(int L, int op, double tau, double tau_nh, double u_0, int max_steps, int *decided_step,
+                     double *margin);
 void orc_obstacle_geometry(int sx, int sy, int *nx, int *ny, uint8_t *solid);
 int orc_obstacle_map_point(int sx, int sy, double tau, double tau_nh, double u_imp, int max_steps,
                            int *decided_step, double *margin);
 void orc_tg_map(int L, int op, double tau_nh, int n_ma, int n_nu, int n_pts, const int *pi, const int *pj,
-                int nthreads, int *labels, int *decided, double *margins);
+                int max_steps, int nthreads, int *labels, int *decided, double *margins);
 void orc_obstacle_map(int n_tau, int n_nu, double ma, int n_pts, const int *pi, const int *pj, int max_steps,
                       int nthreads, int *labels, int *decided, double *margins);
 int orc_max_threads(void);

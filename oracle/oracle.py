@@ -64,13 +64,13 @@ def load():
                                      C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "orc_obstacle_map_params": (None, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                            C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
-        "orc_tg_map_point": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+        "orc_tg_map_point": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
                                        C.POINTER(C.c_int), C.POINTER(C.c_double)]),
         "orc_obstacle_geometry": (None, [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), vp]),
         "orc_obstacle_map_point": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
                                              C.POINTER(C.c_int), C.POINTER(C.c_double)]),
         "orc_tg_map": (None, [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, _ip, _ip, C.c_int,
-                              _ip, _ip, _dp]),
+                              C.c_int, _ip, _ip, _dp]),
         "orc_obstacle_map": (None, [C.c_int, C.c_int, C.c_double, C.c_int, _ip, _ip, C.c_int, C.c_int,
                                     _ip, _ip, _dp]),
         "orc_max_threads": (C.c_int, []),
@@ -176,9 +176,9 @@ def obstacle_map_params(i, j, n_tau, n_nu, ma=0.1):
     return a.value, b.value, c.value  # u_imp, tau, tau_nh
 
 
-def tg_map_point(L, op, tau, tau_nh, u0):
+def tg_map_point(L, op, tau, tau_nh, u0, max_steps=0):
     ds, mg = C.c_int(), C.c_double()
-    lab = load().orc_tg_map_point(L, op, tau, tau_nh, u0, C.byref(ds), C.byref(mg))
+    lab = load().orc_tg_map_point(L, op, tau, tau_nh, u0, max_steps, C.byref(ds), C.byref(mg))
     return lab, ds.value, mg.value
 
 
@@ -196,13 +196,13 @@ def obstacle_map_point(tau, tau_nh, u_imp, sx=1, sy=1, max_steps=0):
     return lab, ds.value, mg.value
 
 
-def tg_map(points, L=16, op=OP_EXTREG, tau_nh=0.65, n_ma=400, n_nu=400, threads=0):
+def tg_map(points, L=16, op=OP_EXTREG, tau_nh=0.65, n_ma=400, n_nu=400, max_steps=0, threads=0):
     pi = np.ascontiguousarray([p[0] for p in points], dtype=np.int32)
     pj = np.ascontiguousarray([p[1] for p in points], dtype=np.int32)
     n = len(points)
     lab, dec, mg = np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.float64)
     threads = threads or load().orc_max_threads()
-    load().orc_tg_map(L, op, tau_nh, n_ma, n_nu, n, pi, pj, threads, lab, dec, mg)
+    load().orc_tg_map(L, op, tau_nh, n_ma, n_nu, n, pi, pj, max_steps, threads, lab, dec, mg)
     return lab, dec, mg
 
 

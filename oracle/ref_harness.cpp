@@ -76,9 +76,22 @@ int REF_PREFIX(q)(void) { return nvel; }
 // node, pointer swap.  f_in: post-stream AoS populations (n_fluid * nvel).  Outputs (nullable):
 // post-stream populations after the last step, post-collision populations of the last step, and
 // the kinetic energy (kinectic_energy) of the post-stream populations.
+int REF_PREFIX(run_threads)(int nx, int ny, int nz, const uint8_t *solid, int col, double tau, double tau_nh,
+                            const double *f_in, int n_steps, int inlet_x, double u_in, int outlet_x, double rho_out,
+                            double *f_post_stream, double *f_post_collision, double *energy, int threads);
+
 int REF_PREFIX(run)(int nx, int ny, int nz, const uint8_t *solid, int col, double tau, double tau_nh,
                     const double *f_in, int n_steps, int inlet_x, double u_in, int outlet_x, double rho_out,
                     double *f_post_stream, double *f_post_collision, double *energy)
+{
+    return REF_PREFIX(run_threads)(nx, ny, nz, solid, col, tau, tau_nh, f_in, n_steps, inlet_x, u_in, outlet_x,
+                                   rho_out, f_post_stream, f_post_collision, energy, 1);
+}
+
+// threads > 1: the node loop runs under "omp parallel for", as in main_double-shear-layer.cpp:389
+int REF_PREFIX(run_threads)(int nx, int ny, int nz, const uint8_t *solid, int col, double tau, double tau_nh,
+                            const double *f_in, int n_steps, int inlet_x, double u_in, int outlet_x, double rho_out,
+                            double *f_post_stream, double *f_post_collision, double *energy, int threads)
 {
     RefCase c;
     make_case(c, nx, ny, nz, solid);
@@ -95,6 +108,7 @@ int REF_PREFIX(run)(int nx, int ny, int nz, const uint8_t *solid, int col, doubl
         if (inlet_x >= 0) ZouHeD3Q19_vx_x(inlet_x, u_in, c.geometry, c.lattice);
 #endif
         if (outlet_x >= 0) devnull_rho_x(outlet_x, rho_out, c.geometry, c.lattice);
+#pragma omp parallel for num_threads(threads > 1 ? threads : 1) if (threads > 1)
         for (int pto = 0; pto < c.geometry.fluid; pto++) {
             double *f = c.lattice.inif + pto * nvel;
             colisao_sitio(f, 0., 0., 0., c.lattice, p, col);

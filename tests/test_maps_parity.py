@@ -1,0 +1,91 @@
+"""GPU parity of the batched stability-map path against the CPU oracle.
+
+FP64: labels, decided steps and margins identical to the oracle's roda_ponto restatement.
+FP32-shifted: label agreement with FP64 reported and bounded.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def eg():
+    import erlbm_gb300 as E
+    return E
+
+
+# a spread of map points: corners, middle and the unstable region (i = U0 axis, j = viscosity axis)
+TG_POINTS = [(399, 0), (300, 20), (200, 100), (10, 300), (0, 399), (50, 50), (120, 10), (399, 399), (5, 0),
+             (60, 180), (250, 250), (30, 390)]
+OB_POINTS = [(0, 0), (200, 200), (399, 399), (10, 5), (100, 40), (300, 10), (50, 300), (390, 100)]
+
+
+@pytest.mark.parametrize("op", [3, 4])
+def test_tg_map_fp64_matches_oracle(op):
+    cap = 3000
+    lab, dec, mg = eg().map_run(eg().MAP_TAYLOR_GREEN, TG_POINTS, precision=eg().FP64, op=op, tau_nh=0.65,
+                                max_steps=cap)
+    olab, odec, omg = O.tg_map(TG_POINTS, op=op, tau_nh=0.65, max_steps=cap)
+    assert np.array_equal(lab, olab)
+    assert np.array_equal(dec, odec)
+    assert np.array_equal(mg, omg)
+
+
+def test_tg_map_both_ops_one_launch():
+    cap = 2000
+    lab, dec, mg = eg().map_run(eg().MAP_TAYLOR_GREEN, TG_POINTS, precision=eg().FP64, op=0, max_steps=cap)
+    n = len(TG_POINTS)
+    for k, op in enumerate((3, 4)):
+        olab, odec, _ = O.tg_map(TG_POINTS, op=op, tau_nh=0.65, max_steps=cap)
+        assert np.array_equal(lab[k * n:(k + 1) * n], olab)
+        assert np.array_equal(dec[k * n:(k + 1) * n], odec)
+
+
+def test_obstacle_map_fp64_matches_oracle():
+    cap = 2500
+    lab, dec, mg = eg().map_run(eg().MAP_OBSTACLE, OB_POINTS, precision=eg().FP64, max_steps=cap)
+    olab, odec, omg = O.obstacle_map(OB_POINTS, max_steps=cap)
+    assert np.array_equal(lab, olab)
+    assert np.array_equal(dec, odec)
+    assert np.array_equal(mg, omg)
+
+
+def test_maps_fp32_label_agreement():
+    pts = [(i, j) for i in range(0, 400, 40) for j in range(0, 400, 40)]
+    cap = 3000
+    for kind in (eg().MAP_TAYLOR_GREEN, eg().MAP_OBSTACLE):
+        l64, d64, _ = eg().map_run(kind, pts, precision=eg().FP64, op=4, max_steps=cap)
+        l32, d32, _ = eg().map_run(kind, pts, precision=eg().FP32_SHIFTED, op=4, max_steps=cap)
+        agree = np.mean(l64 == l32)
+        assert agree >= 0.97, (kind, agree)
+
+
+def test_batch_run_aos_init_matches_lattice_runs():
+    """erlbm_batch_run with per-run initial populations equals single-lattice oracle runs."""
+    rng = np.random.default_rng(3)
+    L = 12
+    runs, blocks = [], []
+    for k in range(6):
+        u0 = 0.02 + 0.01 * k
+        f0 = O.init_taylor_green(9, L, u0, 0.6)
+        f0 = f0 + rng.normal(0, 1e-5, f0.size)
+        blocks.append(f0)
+        runs.append(dict(op=[1, 3, 4][k % 3], tau=0.55 + 0.02 * k, tau_nh=0.7, u0=u0, n_steps=50 + 37 * k,
+                         aos_offset=k * f0.size))
+    aos = np.concatenate(blocks)
+    res = eg().batch_run(9, L, L, runs, precision=eg().FP64, init=eg().INIT_AOS, aos=aos, energy_every=10,
+                         energy_factor=2.0)
+    for k, r in enumerate(runs):
+        lat = O.Lattice(9, L, L, 1, None, r["tau"], r["tau_nh"], r["op"])
+        lat.set(blocks[k])
+        e0 = lat.kinetic_energy(0)
+        lat.step(r["n_steps"])
+        assert res[k]["label"] == 0 and res[k]["steps_done"] == r["n_steps"]
+        # the last energy check ran at the last multiple of 10 below n_steps: compare E there
+        last = (r["n_steps"] - 1) // 10 * 10
+        lat2 = O.Lattice(9, L, L, 1, None, r["tau"], r["tau_nh"], r["op"])
+        lat2.set(blocks[k])
+        lat2.step(last)
+        assert res[k]["energy"] == (lat2.kinetic_energy(0) if last > 0 else e0)
