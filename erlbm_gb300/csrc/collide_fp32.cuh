@@ -5,7 +5,12 @@
 //   f* = f_eq + w_1 f1 + w_gt1 (f - f_eq - f1)  =  f + k_d d + k_f f1,   d = f - f_eq,
 // with k_d = w_gt1 - 1, k_f = w_1 - w_gt1 (RLBM: k_d = -1, k_f = w_1; BGK: k_d = -1/tau, k_f = 0).
 // The increment form is what keeps FP32 honest: the update adds a small correction to the stored
-// population instead of rebuilding it from O(1) pieces.
+// population instead of rebuilding it from O(1) pieces.  The viscosity is set by the factor the
+// Hermite part f1 is multiplied by, w_1 = 1 - 1/tau = delta_1 - 1 with delta_1 = 2 - 1/tau, and
+// at the maps' lowest viscosity delta_1 is ~1e-4: as the sum of two O(1) FP32 coefficients it
+// would carry only ~4 significant digits.  So the update is written with delta_1 itself:
+//   f* = f + [delta_1 f1 + k_d (d - f1) - 2 f1]            (E-RLBM, RLBM: k_d = w_gt1 - 1)
+//   f* = f + [delta d - 2 d],  delta = 2 - 1/tau           (BGK)
 //
 // Each opposite pair (i, j) is split into an even part e = (g_i + g_j)/2 and an odd part
 // o = (g_i - g_j)/2 (both exact).  Then
@@ -28,25 +33,47 @@
 namespace erlbm {
 namespace shifted {
 
-// Increment coefficients, formed in FP64 and rounded once.
+// Increment coefficients, formed in FP64 and rounded once: kd = w_gt1 - 1 (unused by BGK) and
+// d1 = 2 - 1/tau (delta_1, or delta for BGK).
 struct Coef {
-    float kd, kf;
+    float kd, d1;
 };
 
 inline Coef make_coef(const Relax &R)
 {
     Coef k;
-    if (R.op == OP_BGK) {
-        k.kd = (float)(-R.inv_tau);
-        k.kf = 0.f;
-    } else if (R.op == OP_REG) {
+    k.d1 = (float)(2.0 - R.inv_tau);
+    if (R.op == OP_BGK)
+        k.kd = 0.f;
+    else if (R.op == OP_REG)
         k.kd = -1.f;
-        k.kf = (float)R.omega_1;
-    } else {
+    else
         k.kd = (float)(R.omega_gt1 - 1.0);
-        k.kf = (float)(R.omega_1 - R.omega_gt1);
-    }
     return k;
+}
+
+// Update of one opposite pair from its even/odd non-equilibrium parts (de, do) and f1.  The
+// increment is formed from the small quantities first and added to the stored population once,
+// so only that last addition rounds at the scale of g.
+template <int OP>
+__device__ __forceinline__ void update_pair(float &gi, float &gj, float de, float dO, float f1, const Coef &k)
+{
+    if (OP == OP_BGK) {
+        const float di = de + dO, dj = de - dO;
+        gi += fmaf(k.d1, di, -2.f * di);
+        gj += fmaf(k.d1, dj, -2.f * dj);
+    } else {
+        const float a = de - f1, t = -2.f * f1;
+        gi += fmaf(k.d1, f1, fmaf(k.kd, a + dO, t));
+        gj += fmaf(k.d1, f1, fmaf(k.kd, a - dO, t));
+    }
+}
+
+template <int OP>
+__device__ __forceinline__ float update_rest(float g0, float de0, float f10, const Coef &k)
+{
+    if (OP == OP_BGK) return g0 + fmaf(k.d1, de0, -2.f * de0);
+    return g0 + fmaf(k.d1, f10, fmaf(k.kd, de0 - f10, -2.f * f10));
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -104,16 +131,11 @@ __device__ __forceinline__ void collide9(float g[9], const Coef &k)
         f1P = fmaf(pxy, 0.25f, t12);
         f1M = fmaf(pxy, -0.25f, t12);
     }
-    const float kd = k.kd, kf = k.kf;
-    g[0] = fmaf(kd, de0, fmaf(kf, f10, g[0]));
-    g[1] = fmaf(kd, deX + doX, fmaf(kf, f1X, g[1]));
-    g[2] = fmaf(kd, deX - doX, fmaf(kf, f1X, g[2]));
-    g[3] = fmaf(kd, deY + doY, fmaf(kf, f1Y, g[3]));
-    g[4] = fmaf(kd, deY - doY, fmaf(kf, f1Y, g[4]));
-    g[5] = fmaf(kd, deP + doP, fmaf(kf, f1P, g[5]));
-    g[6] = fmaf(kd, deP - doP, fmaf(kf, f1P, g[6]));
-    g[7] = fmaf(kd, deM + doM, fmaf(kf, f1M, g[7]));
-    g[8] = fmaf(kd, deM - doM, fmaf(kf, f1M, g[8]));
+    g[0] = update_rest<OP>(g[0], de0, f10, k);
+    update_pair<OP>(g[1], g[2], deX, doX, f1X, k);
+    update_pair<OP>(g[3], g[4], deY, doY, f1Y, k);
+    update_pair<OP>(g[5], g[6], deP, doP, f1P, k);
+    update_pair<OP>(g[7], g[8], deM, doM, f1M, k);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -198,21 +220,16 @@ __device__ __forceinline__ void collide19(float g[19], const Coef &k)
         f1E = fmaf(0.25f, pyz, byz);
         f1F = fmaf(-0.25f, pyz, byz);
     }
-    const float kd = k.kd, kf = k.kf;
-    g[0] = fmaf(kd, de0, fmaf(kf, f10, g[0]));
-#define ERLBM_PAIR(I, J, DE, DO, F1)                  \
-    g[I] = fmaf(kd, DE + DO, fmaf(kf, F1, g[I]));     \
-    g[J] = fmaf(kd, DE - DO, fmaf(kf, F1, g[J]));
-    ERLBM_PAIR(1, 2, deX, doX, f1X)
-    ERLBM_PAIR(3, 4, deY, doY, f1Y)
-    ERLBM_PAIR(5, 6, deZ, doZ, f1Z)
-    ERLBM_PAIR(7, 8, deA, doA, f1A)
-    ERLBM_PAIR(9, 10, deB, doB, f1B)
-    ERLBM_PAIR(11, 12, deC, doC, f1C)
-    ERLBM_PAIR(13, 14, deD, doD, f1D)
-    ERLBM_PAIR(16, 15, deE, doE, f1E)
-    ERLBM_PAIR(17, 18, deF, doF, f1F)
-#undef ERLBM_PAIR
+    g[0] = update_rest<OP>(g[0], de0, f10, k);
+    update_pair<OP>(g[1], g[2], deX, doX, f1X, k);
+    update_pair<OP>(g[3], g[4], deY, doY, f1Y, k);
+    update_pair<OP>(g[5], g[6], deZ, doZ, f1Z, k);
+    update_pair<OP>(g[7], g[8], deA, doA, f1A, k);
+    update_pair<OP>(g[9], g[10], deB, doB, f1B, k);
+    update_pair<OP>(g[11], g[12], deC, doC, f1C, k);
+    update_pair<OP>(g[13], g[14], deD, doD, f1D, k);
+    update_pair<OP>(g[16], g[15], deE, doE, f1E, k);
+    update_pair<OP>(g[17], g[18], deF, doF, f1F, k);
 }
 
 template <int Q, int OP>

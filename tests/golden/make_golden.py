@@ -1,0 +1,181 @@
+"""Generates the golden fixtures in this folder.  Run where the reference tree is present:
+
+    python tests/golden/make_golden.py [--reference /root/reference]
+
+It reads the reference's published tables (data/*.csv, data/*.vtk) and runs the reference's own
+library and program functions, compiled from their sources by oracle/Makefile (target `ref`), to
+produce:
+
+  published.json          Fig. 3 / feq-init / kappa_4 / Fig. 4 tables (numbers as published), the
+                          unstable-point counts of the three published 400 x 400 maps, and their
+                          20 x 20 subsamples at the README's indices (README "Previous version of
+                          the code": TG i' = 20(i+1)-1, j' = 20 j; obstacle i' = 20 i, j' = 20 j).
+  reference_maps_20x20.json
+                          the same 20 x 20 subsamples computed by the reference's roda_ponto
+                          (main_stability-map_taylor-green.cpp:41-104, main_stability-map_obstacle.cpp:75-123).
+  reference_vectors.npz   inputs and outputs of short runs of the reference library (colisao_sitio +
+                          propag_site loop with its boundary functions): small D2Q9 / D3Q19 lattices,
+                          the obstacle channel, the Taylor-Green and double-shear-layer initial fields.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+
+def read_csv(path):
+    lines = [l.strip() for l in open(path) if l.strip()]
+    head = lines[0].split(",")
+    rows = []
+    for l in lines[1:]:
+        vals = l.split(",")
+        row = {}
+        for h, v in zip(head, vals):
+            try:
+                row[h] = float(v) if any(c in v for c in ".e") or v.lstrip("-").isdigit() else v
+            except ValueError:
+                row[h] = v
+        rows.append(row)
+    return rows
+
+
+def read_map(path):
+    lines = open(path).read().split("\n")
+    nx, ny = [int(v) for v in next(l for l in lines if l.startswith("DIMENSIONS")).split()[1:3]]
+    k = next(n for n, l in enumerate(lines) if l.startswith("LOOKUP_TABLE"))
+    vals = np.array(" ".join(lines[k + 1:]).split(), dtype=float)
+    return vals[: nx * ny].reshape(ny, nx).astype(int)
+
+
+TG_SUB = [(20 * (i + 1) - 1, 20 * j) for j in range(20) for i in range(20)]
+OB_SUB = [(20 * i, 20 * j) for j in range(20) for i in range(20)]
+
+
+def _worker_init():
+    # the reference's boundary functions carry "omp parallel for" pragmas that its map programs
+    # serialise with omp_set_max_active_levels(1) (main_stability-map_obstacle.cpp:137); one thread
+    # per worker process does the same here
+    os.environ["OMP_NUM_THREADS"] = "1"
+
+
+def _ref_tg_point(args):
+    i, j, op, tau_nh, n = args
+    from oracle import oracle as O
+    lib = O.load_ref(19)
+    u0, tau, tnh = O.tg_map_params(i, j, n, n, op, tau_nh)
+    return int(lib.ref19_tg_map_point(16, op, tau, tnh, u0))
+
+
+def _ref_ob_point(args):
+    i, j, n = args
+    from oracle import oracle as O
+    lib = O.load_ref(19)
+    u, tau, tnh = O.obstacle_map_params(i, j, n, n, 0.1)
+    return int(lib.ref19_obstacle_map_point(tau, tnh, u))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
+    a = ap.parse_args()
+    ref = a.reference
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all", "ref", f"REFERENCE={ref}"], check=True)
+    from oracle import oracle as O
+
+    # ---- published tables and maps -------------------------------------------------------------
+    pub = {
+        "fig3_taylor_green_Re50": read_csv(os.path.join(ref, "data", "fig3_taylor_green_Re50.csv")),
+        "fig3_taylor_green_Re50_feq_init": read_csv(os.path.join(ref, "data", "fig3_taylor_green_Re50_feq_init.csv")),
+        "kappa4_check_L64": read_csv(os.path.join(ref, "data", "kappa4_check_L64.csv")),
+        "fig4_double_shear_Re80000": read_csv(os.path.join(ref, "data", "fig4_double_shear_Re80000.csv")),
+        "maps": {},
+    }
+    for name, sub in (("fig1_map_reg", TG_SUB), ("fig1_map_erlbm065", TG_SUB), ("fig2_map_obstacle", OB_SUB)):
+        m = read_map(os.path.join(ref, "data", name + ".vtk"))
+        pub["maps"][name] = {"unstable": int(m.sum()), "points": 160000,
+                             "subsample_20x20": [int(m[j, i]) for (i, j) in sub]}
+    with open(os.path.join(HERE, "published.json"), "w") as f:
+        json.dump(pub, f, indent=0)
+
+    # ---- reference maps on the 20 x 20 subsample --------------------------------------------------
+    ctx = mp.get_context("spawn")
+    # grid400: the 400 x 400 map's own parameters at the subsampled indices;
+    # grid20:  a 20 x 20 run (--n-ma 20 --n-nu 20, --n-tau 20), the README's quick-test protocol, whose
+    #          axis values land on the same points up to the rounding of the axis formulas
+    g20 = [(i, j) for j in range(20) for i in range(20)]
+    with ctx.Pool(a.jobs, initializer=_worker_init) as pool:
+        reg = pool.map(_ref_tg_point, [(i, j, O.OP_REG, 1.0, 400) for (i, j) in TG_SUB])
+        erl = pool.map(_ref_tg_point, [(i, j, O.OP_EXTREG, 0.65, 400) for (i, j) in TG_SUB])
+        obs = pool.map(_ref_ob_point, [(i, j, 400) for (i, j) in OB_SUB])
+        reg20 = pool.map(_ref_tg_point, [(i, j, O.OP_REG, 1.0, 20) for (i, j) in g20])
+        erl20 = pool.map(_ref_tg_point, [(i, j, O.OP_EXTREG, 0.65, 20) for (i, j) in g20])
+        obs20 = pool.map(_ref_ob_point, [(i, j, 20) for (i, j) in g20])
+    maps = {"tg_points": TG_SUB, "obstacle_points": OB_SUB, "tg_reg": reg, "tg_erlbm065": erl, "obstacle": obs,
+            "grid20_points": g20, "grid20_tg_reg": reg20, "grid20_tg_erlbm065": erl20, "grid20_obstacle": obs20}
+    with open(os.path.join(HERE, "reference_maps_20x20.json"), "w") as f:
+        json.dump(maps, f)
+    for name, lab, lab20 in (("fig1_map_reg", reg, reg20), ("fig1_map_erlbm065", erl, erl20),
+                             ("fig2_map_obstacle", obs, obs20)):
+        pubsub = np.array(pub["maps"][name]["subsample_20x20"])
+        print(f"{name}: reference vs published subsample differ at {int(np.sum(np.array(lab) != pubsub))} "
+              f"(400-grid parameters) and {int(np.sum(np.array(lab20) != pubsub))} (20 x 20 run) of 400 points")
+
+    # ---- short reference runs -----------------------------------------------------------------------
+    rng = np.random.default_rng(20261203)
+    vec = {}
+
+    def near_eq(q, n, amp=0.05, noise=1e-3):
+        fs = []
+        for _ in range(n):
+            u = rng.normal(0, amp, 3)
+            if q == 9:
+                u[2] = 0.0
+            fs.append(O.equilibrium(q, u[0], u[1], u[2], 1 + rng.normal(0, 0.01)))
+        f = np.concatenate(fs)
+        return f + rng.normal(0, noise, f.size)
+
+    for q, (nx, ny, nz), steps in ((9, (7, 5, 1), 13), (19, (6, 5, 3), 9)):
+        f0 = near_eq(q, nx * ny * nz)
+        for op, tnh in ((1, 0.57), (3, 1.0), (4, 0.65)):
+            ps, pc, e = O.ref_run(q, nx, ny, nz, None, op, 0.57, tnh, f0, steps)
+            key = f"periodic_q{q}_op{op}"
+            vec[key + "_in"] = f0
+            vec[key + "_post_stream"] = ps
+            vec[key + "_post_collision"] = pc
+            vec[key + "_energy"] = np.array([e])
+            vec[key + "_meta"] = np.array([nx, ny, nz, steps, op, 0.57, tnh])
+    nx, ny, solid = O.obstacle_geometry()
+    n_fluid = int((solid == 0).sum())
+    f0 = np.tile(O.equilibrium(19, 0, 0, 0, 1.0), n_fluid)
+    u = 0.1 / np.sqrt(3.0)
+    ps, pc, e = O.ref_run(19, nx, ny, 1, solid, 4, 0.52, 0.7, f0, 300, 1, u, nx - 2, 1.0)
+    vec["obstacle_in"] = f0
+    vec["obstacle_post_stream"] = ps
+    vec["obstacle_post_collision"] = pc
+    vec["obstacle_meta"] = np.array([nx, ny, 300, 0.52, 0.7, u])
+    f_tg = np.empty(16 * 16 * 9)
+    O.load_ref(9).ref9_init_taylor_green(16, 2 / 16, 0.62, 1, 1, f_tg)
+    vec["tg16_init"] = f_tg
+    ps, pc, e = O.ref_run(9, 16, 16, 1, None, 4, 0.62, 0.65, f_tg, 40)
+    vec["tg16_erlbm_40_post_collision"] = pc
+    f_dsl = np.empty(32 * 32 * 9)
+    O.load_ref(9).ref9_init_double_shear(32, 1.0, f_dsl)
+    vec["dsl32_init"] = f_dsl
+    np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
+    print("wrote", sorted(os.listdir(HERE)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,117 @@
+"""Host-side logic of the library that runs without a GPU: the C ABI's exported symbols and its
+argument checks, the program inputs (initial fields, geometries, map axes) against the oracle, and
+the sharding of map points over ranks (gloo, world size 2)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def E():
+    import erlbm_gb300 as m
+    return m
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "erlbm_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(erlbm_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_function():
+    lib = E().lib()
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_argument_checks_before_any_device_work():
+    m = E()
+    with pytest.raises(m.ErlbmError) as ei:
+        m.Lattice(7, 4, 4)
+    assert ei.value.code == -1
+    with pytest.raises(m.ErlbmError) as ei:
+        m.Lattice(9, 4, 4, 2)  # D2Q9 needs nz = 1
+    assert ei.value.code == -1
+    with pytest.raises(m.ErlbmError) as ei:
+        m.Lattice(9, 4, 4, 1, op=m.OP_MRT)
+    assert ei.value.code == -6
+    with pytest.raises(ValueError):
+        m.operator_from_name("trt")
+    assert [m.operator_from_name(n) for n in ("bgk", "mrt", "reg", "erlbm")] == [1, 2, 3, 4]
+
+
+def test_program_inputs_equal_oracle():
+    m = E()
+    for q in (9, 19):
+        for variant in (0, 1):
+            for neq in (True, False):
+                a = m.init_taylor_green(q, 24, 0.05, 0.6, neq=neq, variant=variant)
+                b = O.init_taylor_green(q, 24, 0.05, 0.6, neq=neq, variant=variant)
+                assert np.array_equal(a, b)
+    assert np.array_equal(m.init_double_shear(64), O.init_double_shear(64))
+    assert np.array_equal(m.equilibrium(19, 0.1, -0.05, 0.02, 1.01), O.equilibrium(19, 0.1, -0.05, 0.02, 1.01))
+    for sx, sy in ((1, 1), (2, 3), (4, 4)):
+        a, b = m.obstacle_geometry(sx, sy), O.obstacle_geometry(sx, sy)
+        assert a[:2] == b[:2] and np.array_equal(a[2], b[2])
+    nx, ny, solid = m.obstacle_geometry()
+    assert (nx, ny, int((solid == 0).sum())) == (22, 12, 232)
+    for (i, j) in ((0, 0), (399, 399), (17, 233)):
+        assert m.tg_map_params(i, j, 400, 400, 4, 0.65) == O.tg_map_params(i, j, 400, 400, 4, 0.65)
+        assert m.tg_map_params(i, j, 400, 400, 3, 0.65)[2] == 1.0
+        assert m.obstacle_map_params(i, j) == O.obstacle_map_params(i, j, 400, 400, 0.1)
+    f = O.init_taylor_green(9, 32, 2 / 32, 0.62)
+    assert np.array_equal(m.taylor_green_error(9, 32, f, 2 / 32, 0.04, 7), O.taylor_green_error(9, 32, f, 2 / 32,
+                                                                                                 0.04, 7))
+
+
+def test_shard_unshard_roundtrip():
+    from erlbm_gb300.sharding import shard, unshard
+    pts = [(i, j) for i in range(7) for j in range(5)]
+    for world in (1, 2, 3, 8):
+        parts = [np.array([p[0] * 100 + p[1] for p in shard(pts, r, world)]) for r in range(world)]
+        assert list(unshard(parts, len(pts), world)) == [p[0] * 100 + p[1] for p in pts]
+
+
+def _gloo_worker(rank, world, port, out):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from erlbm_gb300.sharding import run_sharded
+    pts = [(i, j) for i in range(0, 400, 57) for j in range(0, 400, 91)]
+
+    def runner(mine):  # the oracle stands in for this rank's GPU map run
+        lab, dec, mg = O.tg_map(mine, op=O.OP_EXTREG, tau_nh=0.65, max_steps=1500, threads=1)
+        return lab, dec, mg
+
+    lab, dec, mg = run_sharded(pts, runner)
+    if rank == 0:
+        ref = O.tg_map(pts, op=O.OP_EXTREG, tau_nh=0.65, max_steps=1500, threads=1)
+        out.put((np.array_equal(lab, ref[0]), np.array_equal(dec, ref[1]), np.array_equal(mg, ref[2])))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_sharded_map_gloo_world2():
+    import multiprocessing as mp
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_gloo_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = q.get(timeout=240)
+    for p in ps:
+        p.join(timeout=60)
+    assert res == (True, True, True)

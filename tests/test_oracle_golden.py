@@ -1,0 +1,134 @@
+"""The CPU oracle pinned against the reference: its published tables and golden vectors produced by
+the reference library compiled from its own sources (tests/golden/make_golden.py).  CPU only."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def published():
+    with open(os.path.join(GOLD, "published.json")) as f:
+        return json.load(f)
+
+
+def sig6(x):
+    return float(f"{x:.6g}")
+
+
+OPS = {"BGK": (O.OP_BGK, 0.0), "REG": (O.OP_REG, 1.0), "ERLBM065": (O.OP_EXTREG, 0.65)}
+
+
+@pytest.mark.parametrize("L", [32, 64])
+def test_fig3_rows(L):
+    """data/fig3_taylor_green_Re50.csv: E_vector and E_magnitude to the 6 printed digits."""
+    rows = [r for r in published()["fig3_taylor_green_Re50"] if int(r["L"]) == L]
+    assert len(rows) == 3
+    for r in rows:
+        op, tnh = OPS[r["model"]]
+        out = O.taylor_green_program(L, op, tnh)
+        assert sig6(out["e_vec"]) == r["E_vector"] and sig6(out["e_mag"]) == r["E_magnitude"], (r, out)
+
+
+def test_fig3_feq_init_rows():
+    rows = [r for r in published()["fig3_taylor_green_Re50_feq_init"] if int(r["L"]) == 32]
+    for r in rows:
+        op, tnh = OPS[r["model"]]
+        out = O.taylor_green_program(32, op, tnh, neq=False)
+        assert sig6(out["e_vec"]) == r["E_vector"] and sig6(out["e_mag"]) == r["E_magnitude"], (r, out)
+
+
+@pytest.mark.parametrize("tau", [1.0, 1.1, 1.2])
+def test_kappa4_rows(tau):
+    """data/kappa4_check_L64.csv (tau mode, U0 = 1e-3): steps, E_vector, E_magnitude, nu_ef/nu - 1."""
+    rows = [r for r in published()["kappa4_check_L64"] if abs(r["tau"] - tau) < 1e-12]
+    assert len(rows) == 6
+    for r in rows:
+        op = OPS[r["model"]][0]
+        out = O.taylor_green_program(64, op, r["tau_nh"], u0=1e-3, tau=tau, neq=r["init"] == "neq")
+        assert out["steps"] == int(r["steps"])
+        for k, col in (("e_vec", "E_vector"), ("e_mag", "E_magnitude"), ("nu_rel", "rel_visc_error")):
+            assert sig6(out[k]) == r[col], (r, out)
+
+
+def vectors():
+    path = os.path.join(GOLD, "reference_vectors.npz")
+    if not os.path.exists(path):
+        pytest.skip("reference vectors not generated")
+    return np.load(path)
+
+
+@pytest.mark.parametrize("q", [9, 19])
+@pytest.mark.parametrize("op", [1, 3, 4])
+def test_periodic_vectors(q, op):
+    v = vectors()
+    key = f"periodic_q{q}_op{op}"
+    nx, ny, nz, steps, _, tau, tnh = v[key + "_meta"]
+    lat = O.Lattice(q, int(nx), int(ny), int(nz), None, tau, tnh, op)
+    lat.set(v[key + "_in"])
+    lat.step(int(steps))
+    np.testing.assert_allclose(lat.get(0), v[key + "_post_stream"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(lat.get(1), v[key + "_post_collision"], rtol=1e-13, atol=0)
+    assert lat.kinetic_energy(0) == pytest.approx(float(v[key + "_energy"][0]), rel=1e-13)
+
+
+def test_obstacle_vectors():
+    v = vectors()
+    nx, ny, steps, tau, tnh, u = v["obstacle_meta"]
+    nx, ny, solid = O.obstacle_geometry()
+    lat = O.Lattice(19, nx, ny, 1, solid, tau, tnh, 4)
+    lat.set(v["obstacle_in"])
+    lat.step(int(steps), dict(inlet_x=1, u_in=u, outlet_x=nx - 2, rho_out=1.0))
+    np.testing.assert_allclose(lat.get(0), v["obstacle_post_stream"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(lat.get(1), v["obstacle_post_collision"], rtol=1e-13, atol=0)
+
+
+def test_program_inits():
+    v = vectors()
+    np.testing.assert_allclose(O.init_taylor_green(9, 16, 2 / 16, 0.62), v["tg16_init"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(O.init_double_shear(32), v["dsl32_init"], rtol=1e-14, atol=0)
+    lat = O.Lattice(9, 16, 16, 1, None, 0.62, 0.65, 4)
+    lat.set(v["tg16_init"])
+    lat.step(40)
+    np.testing.assert_allclose(lat.get(1), v["tg16_erlbm_40_post_collision"], rtol=1e-13, atol=0)
+
+
+def ref_maps():
+    path = os.path.join(GOLD, "reference_maps_20x20.json")
+    if not os.path.exists(path):
+        pytest.skip("reference maps not generated")
+    with open(path) as f:
+        return json.load(f)
+
+
+def test_reference_maps_vs_published():
+    """The README's regression protocol (a 20 x 20 subsample of each published 400 x 400 map) run on
+    the reference compiled here: with the 400-grid parameters at the subsampled indices the current
+    code differs from the published maps at 1 (RLBM), 0 (E-RLBM) and 0 (obstacle) points; as true
+    20 x 20 runs (axes computed with n = 20) at none.  The published unstable counts are pinned too."""
+    m, p = ref_maps(), published()["maps"]
+    pairs = (("tg_reg", "fig1_map_reg"), ("tg_erlbm065", "fig1_map_erlbm065"), ("obstacle", "fig2_map_obstacle"))
+    diffs = [int(np.sum(np.array(m[a]) != np.array(p[b]["subsample_20x20"]))) for a, b in pairs]
+    diffs20 = [int(np.sum(np.array(m["grid20_" + a]) != np.array(p[b]["subsample_20x20"]))) for a, b in pairs]
+    assert diffs == [1, 0, 0]
+    assert diffs20 == [0, 0, 0]
+    assert (p["fig1_map_reg"]["unstable"], p["fig1_map_erlbm065"]["unstable"], p["fig2_map_obstacle"]["unstable"]) \
+        == (101829, 84190, 86407)
+
+
+def test_oracle_maps_vs_reference_fast_points():
+    """Labels of the oracle's roda_ponto restatement equal the reference's on the subsample points
+    that the reference decides within 1500 steps (cheap to run here) -- plus a handful of stable ones."""
+    m = ref_maps()
+    pts = [tuple(p) for p in m["tg_points"]]
+    sel = list(range(0, 400, 23))
+    lab, dec, _ = O.tg_map([pts[k] for k in sel], op=O.OP_EXTREG, tau_nh=0.65)
+    assert list(lab) == [m["tg_erlbm065"][k] for k in sel]
+    opts = [tuple(p) for p in m["obstacle_points"]]
+    sel = list(range(0, 400, 41))
+    lab, dec, _ = O.obstacle_map([opts[k] for k in sel])
+    assert list(lab) == [m["obstacle"][k] for k in sel]
