@@ -14,13 +14,14 @@ import numpy as np
 
 from . import _lib
 from ._lib import (FP32_SHIFTED, FP64, INIT_AOS, INIT_REST, INIT_TG_MAP, MAP_OBSTACLE, MAP_TAYLOR_GREEN, OP_BGK,
-                   OP_EXTREG, OP_MRT, OP_REG, STAGE_POST_COLLISION, STAGE_POST_STREAM, ErlbmError, check, lib)
+                   OP_EXTREG, OP_MRT, OP_REG, REQ_OBSTACLE, REQ_TG2D, REQ_TG3D, REQ_TG_MAP_POINT, STAGE_POST_COLLISION,
+                   STAGE_POST_STREAM, ErlbmError, check, lib)
 
 __all__ = ["Lattice", "ErlbmError", "lib", "OP_BGK", "OP_MRT", "OP_REG", "OP_EXTREG", "FP64", "FP32_SHIFTED",
            "STAGE_POST_STREAM", "STAGE_POST_COLLISION", "MAP_TAYLOR_GREEN", "MAP_OBSTACLE", "init_taylor_green",
            "init_double_shear", "equilibrium", "obstacle_geometry", "taylor_green_error", "tg_map_params",
            "obstacle_map_params", "operator_from_name", "map_run", "batch_run", "INIT_REST", "INIT_TG_MAP",
-           "INIT_AOS"]
+           "INIT_AOS", "Server", "REQ_TG2D", "REQ_TG_MAP_POINT", "REQ_OBSTACLE", "REQ_TG3D"]
 
 _OPS = {"bgk": OP_BGK, "mrt": OP_MRT, "reg": OP_REG, "erlbm": OP_EXTREG}
 
@@ -250,3 +251,56 @@ def batch_run(q: int, nx: int, ny: int, runs, precision: int = FP64, solid=None,
                                 0 if a is None else a.size, out), "erlbm_batch_run")
     return [dict(label=o.label, decided_step=o.decided_step, steps_done=o.steps_done, status=o.status,
                  margin=o.margin, energy=o.energy) for o in out[:len(runs)]]
+
+
+# ---- request server ---------------------------------------------------------------------------------
+
+class Server:
+    """Continuous-batching server (erlbm_server_*): submit runs while others are on the GPU."""
+
+    def __init__(self, hbm_budget_bytes: int = 8 << 30, slot_ctas: int = 0, max_streams: int = 16,
+                 queue_capacity: int = 0):
+        d = _lib.ServerDesc(int(hbm_budget_bytes), int(slot_ctas), int(max_streams), int(queue_capacity))
+        h = C.c_void_p()
+        check(lib().erlbm_server_start(C.byref(d), C.byref(h)), "erlbm_server_start")
+        self._h = h
+
+    def submit(self, kind: int, precision: int = FP64, op: int = OP_EXTREG, L: int = 16, sx: int = 1, sy: int = 1,
+               tau: float = 0.6, tau_nh: float = 0.65, u0: float = 0.05, n_steps: int = 100) -> int:
+        q = _lib.Request(kind, precision, op, L, sx, sy, tau, tau_nh, u0, n_steps)
+        t = C.c_int64()
+        check(lib().erlbm_server_submit(self._h, C.byref(q), C.byref(t)), "erlbm_server_submit")
+        return t.value
+
+    @staticmethod
+    def _res(r):
+        return dict(status=r.status, label=r.label, steps_done=r.steps_done, decided_step=r.decided_step,
+                    energy=r.energy, margin=r.margin, t_submit=r.t_submit, t_admit=r.t_admit, t_done=r.t_done,
+                    lane=r.lane)
+
+    def poll(self, ticket: int):
+        r = _lib.Result()
+        rc = lib().erlbm_server_poll(self._h, ticket, C.byref(r))
+        if rc == 1:
+            return None
+        check(rc, "erlbm_server_poll")
+        return self._res(r)
+
+    def wait(self, ticket: int, timeout: float = 600.0):
+        r = _lib.Result()
+        check(lib().erlbm_server_wait(self._h, ticket, C.byref(r), timeout), "erlbm_server_wait")
+        return self._res(r)
+
+    def clock(self) -> float:
+        return lib().erlbm_server_clock(self._h)
+
+    def stop(self):
+        if getattr(self, "_h", None):
+            check(lib().erlbm_server_stop(self._h), "erlbm_server_stop")
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.stop()

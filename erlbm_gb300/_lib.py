@@ -18,6 +18,7 @@ FP64, FP32_SHIFTED = 0, 1
 STAGE_POST_STREAM, STAGE_POST_COLLISION = 0, 1
 MAP_TAYLOR_GREEN, MAP_OBSTACLE = 1, 2
 INIT_REST, INIT_TG_MAP, INIT_AOS = 0, 1, 2
+REQ_TG2D, REQ_TG_MAP_POINT, REQ_OBSTACLE, REQ_TG3D = 1, 2, 3, 4
 
 
 class ErlbmError(RuntimeError):
@@ -73,9 +74,9 @@ class ServerDesc(C.Structure):
 
 
 class Request(C.Structure):
-    _fields_ = [("kind", C.c_int), ("precision", C.c_int), ("op", C.c_int), ("L", C.c_int), ("nz", C.c_int),
-                ("sx", C.c_int), ("sy", C.c_int), ("tau", C.c_double), ("tau_nh", C.c_double), ("u0", C.c_double),
-                ("n_steps", C.c_int), ("check", C.c_int)]
+    _fields_ = [("kind", C.c_int), ("precision", C.c_int), ("op", C.c_int), ("L", C.c_int), ("sx", C.c_int),
+                ("sy", C.c_int), ("tau", C.c_double), ("tau_nh", C.c_double), ("u0", C.c_double),
+                ("n_steps", C.c_int)]
 
 
 class Result(C.Structure):
@@ -107,6 +108,12 @@ _SIGS = {
     "erlbm_batch_run": (C.c_int, [C.POINTER(BatchDesc), C.c_int, C.POINTER(RunSpec), C.c_void_p, C.c_size_t,
                                   C.POINTER(BatchResult)]),
     "erlbm_map_run": (C.c_int, [C.POINTER(MapDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "erlbm_server_start": (C.c_int, [C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),
+    "erlbm_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),
+    "erlbm_server_poll": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(Result)]),
+    "erlbm_server_wait": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(Result), C.c_double]),
+    "erlbm_server_clock": (C.c_double, [C.c_void_p]),
+    "erlbm_server_stop": (C.c_int, [C.c_void_p]),
 }
 
 

@@ -166,25 +166,34 @@ struct BatchBounds {
     static constexpr int MINB = NPT == 1 ? (BYTES == 8 ? 2 : 3) : 1;
 };
 
+// Shared-memory carve-up of a batched CTA (sizes from batch_smem_bytes).
+template <class P, int Q>
+struct BatchSmem {
+    typename P::T *buf;
+    double *red;
+    uint8_t *solid;
+    __device__ BatchSmem(unsigned char *raw, int nb)
+    {
+        buf = reinterpret_cast<typename P::T *>(raw);
+        red = reinterpret_cast<double *>(raw + ((size_t)Q * nb * sizeof(typename P::T) + 15) / 16 * 16);
+        solid = reinterpret_cast<uint8_t *>(red + blockDim.x + 1);
+    }
+};
+
+// One run of one lattice by the whole CTA.  sm.solid must hold the geometry's mask.  The result is
+// returned to every thread.
 template <class P, int Q, int NPT>
-__global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
-                                  BatchBounds<NPT, sizeof(typename P::T)>::MINB) k_batch(BatchGeo g, const BatchRun *__restrict__ runs, int n_runs,
-                                               int *__restrict__ counter, BatchResult *__restrict__ res,
-                                               const double *__restrict__ aos)
+__device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const BatchSmem<P, Q> &sm,
+                                     const double *__restrict__ aos)
 {
     using T = typename P::T;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int NB = g.nb;
-    T *buf = reinterpret_cast<T *>(smem_raw);
-    double *red = reinterpret_cast<double *>(smem_raw + ((size_t)Q * NB * sizeof(T) + 15) / 16 * 16);
-    uint8_t *solid = reinterpret_cast<uint8_t *>(red + blockDim.x + 1);
-    __shared__ int s_run;
+    T *buf = sm.buf;
+    double *red = sm.red;
+    const uint8_t *solid = sm.solid;
     const int tid = threadIdx.x;
-
-    for (int k = tid; k < NB; k += blockDim.x) solid[k] = g.solid ? g.solid[k] : 0;
     const bool any_solid = g.solid != nullptr;
 
-    // per-thread node slots
     int node[NPT], nx_[NPT], ny_[NPT];
     bool fluid[NPT];
 #pragma unroll
@@ -192,11 +201,165 @@ __global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
         node[s] = tid + s * blockDim.x;
         nx_[s] = node[s] % g.nx;
         ny_[s] = node[s] / g.nx;
+        fluid[s] = node[s] < NB && !solid[node[s]];
+    }
+
+    // ---- initial populations (post-stream state of step 0) ----
+    T f[NPT][Q];
+#pragma unroll
+    for (int s = 0; s < NPT; s++) {
+        if (!fluid[s]) continue;
+        if (g.init == INIT_TG_MAP) {
+            tg_map_init<P, Q>(f[s], nx_[s], ny_[s], r.u0, g);
+        } else if (g.init == INIT_AOS) {
+            // fluid index of this node: count of fluid nodes before it (solid masks are small)
+            int p = 0;
+            for (int k = 0; k < node[s]; k++) p += !solid[k];
+            const double *src = aos + r.aos_off + (long long)p * Q;
+#pragma unroll
+            for (int i = 0; i < Q; i++) f[s][i] = P::template from_f<Q>(src[i], i);
+        } else {
+#pragma unroll
+            for (int i = 0; i < Q; i++) f[s][i] = P::template from_f<Q>(Lat<Q>::w(i) * g.rho0, i);
+        }
+#pragma unroll
+        for (int i = 0; i < Q; i++) buf[i * NB + node[s]] = f[s][i];
     }
     __syncthreads();
-#pragma unroll
-    for (int s = 0; s < NPT; s++) fluid[s] = node[s] < NB && !solid[node[s]];
 
+    double E0 = 0.0, E = 0.0, margin = 0.0, max_rho = 0.0;
+    int label = 0, decided = r.n_steps, status = 0, steps_done = r.n_steps;
+    constexpr bool SERIAL = NPT == 1 && sizeof(T) == 8;
+    if (g.energy_every > 0) {
+        double e = 0.0;
+#pragma unroll
+        for (int s = 0; s < NPT; s++)
+            if (fluid[s]) e += P::template energy<Q>(f[s]);
+        E0 = block_sum<SERIAL>(e, red, NB);
+        E = E0;
+    }
+
+    for (int step = 0; step < r.n_steps; step++) {
+        // ---- stream: post-stream populations of this step ----
+        if (step > 0) {
+#pragma unroll
+            for (int s = 0; s < NPT; s++) {
+                if (!fluid[s]) continue;
+                int x = nx_[s];
+                const int y = ny_[s];
+                int me = node[s];
+                if (x == g.outlet_x) {  // the outlet copies its inner neighbour (devnull_rho_x)
+                    x += (g.outlet_x < g.nx / 2) ? 1 : -1;
+                    me = node[s] + (x - nx_[s]);
+                }
+#pragma unroll
+                for (int i = 0; i < Q; i++) {
+                    const int xs = wrap1(x - Lat<Q>::cx(i), g.nx);
+                    const int ys = wrap1(y - Lat<Q>::cy(i), g.ny);
+                    const int src = xs + g.nx * ys;
+                    f[s][i] = (any_solid && solid[src]) ? buf[Lat<Q>::opp(i) * NB + me] : buf[i * NB + src];
+                }
+            }
+        } else if (g.outlet_x >= 0) {
+#pragma unroll
+            for (int s = 0; s < NPT; s++) {
+                if (!fluid[s] || nx_[s] != g.outlet_x) continue;
+                const int me = node[s] + ((g.outlet_x < g.nx / 2) ? 1 : -1);
+#pragma unroll
+                for (int i = 0; i < Q; i++) f[s][i] = buf[i * NB + me];
+            }
+        }
+        __syncthreads();
+
+        // ---- energy check on the post-stream populations ----
+        if (g.energy_every > 0 && step > 0 && step % g.energy_every == 0) {
+            double e = 0.0;
+#pragma unroll
+            for (int s = 0; s < NPT; s++)
+                if (fluid[s]) e += P::template energy<Q>(f[s]);
+            E = block_sum<SERIAL>(e, red, NB);
+            const double lim = g.energy_factor * E0;
+            const double rr = isfinite(E) ? E / lim : INFINITY;
+            margin = fmax(margin, rr);
+            if (E > lim || !isfinite(E)) {
+                label = 1;
+                decided = step;
+                steps_done = step;
+                status |= 4;
+                break;
+            }
+        }
+
+        // ---- boundary planes, collision, density check, store ----
+        int flag = 0;
+#pragma unroll
+        for (int s = 0; s < NPT; s++) {
+            if (!fluid[s]) continue;
+            const int x = nx_[s];
+            if (x == g.outlet_x) {
+                const int xn = x + ((g.outlet_x < g.nx / 2) ? 1 : -1);
+                if (Q == 19 && xn == g.inlet_x) P::zou_he(f[s], r.u0, g.inlet_x < g.nx / 2);
+                if (any_solid && solid[node[s] + (xn - x)])
+                    P::template rest<Q>(f[s], g.rho0);
+                else
+                    P::template outlet<Q>(f[s], g.rho0);
+            } else if (Q == 19 && x == g.inlet_x) {
+                P::zou_he(f[s], r.u0, g.inlet_x < g.nx / 2);
+            }
+            batch_collide<P, Q>(f[s], r);
+            if (g.density_check) {
+                const double rho = P::template density<Q>(f[s]);
+                if (!isfinite(rho)) {
+                    flag |= 2;
+                } else {
+                    const double a = fabs(rho);
+                    max_rho = fmax(max_rho, a);
+                    if (a > g.density_limit) flag |= 1;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < Q; i++) buf[i * NB + node[s]] = f[s][i];
+        }
+        if (g.density_check) {
+            // finish the step everywhere, then stop if any node failed
+            const int any = __syncthreads_or(flag);
+            if (any) {
+                label = 1;
+                decided = step;
+                steps_done = step + 1;
+                status |= __syncthreads_or(flag & 2) ? 3 : 1;
+                break;
+            }
+        } else {
+            __syncthreads();
+        }
+    }
+    if (g.density_check) {
+        max_rho = block_max(max_rho, red);
+        margin = (status & 2) ? INFINITY : max_rho / g.density_limit;
+    }
+    BatchResult o;
+    o.label = label;
+    o.decided_step = decided;
+    o.steps_done = steps_done;
+    o.status = status;
+    o.margin = margin;
+    o.energy = E;
+    __syncthreads();
+    return o;
+}
+
+template <class P, int Q, int NPT>
+__global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
+                                  BatchBounds<NPT, sizeof(typename P::T)>::MINB)
+    k_batch(BatchGeo g, const BatchRun *__restrict__ runs, int n_runs, int *__restrict__ counter,
+            BatchResult *__restrict__ res, const double *__restrict__ aos)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const BatchSmem<P, Q> sm(smem_raw, g.nb);
+    __shared__ int s_run;
+    const int tid = threadIdx.x;
+    for (int k = tid; k < g.nb; k += blockDim.x) sm.solid[k] = g.solid ? g.solid[k] : 0;
     for (;;) {
         __syncthreads();
         if (tid == 0) s_run = atomicAdd(counter, 1);
@@ -204,149 +367,118 @@ __global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
         const int ri = s_run;
         if (ri >= n_runs) break;
         const BatchRun r = runs[ri];
+        const BatchResult o = batch_one_run<P, Q, NPT>(g, r, sm, aos);
+        if (tid == 0) res[r.out] = o;
+    }
+}
 
-        // ---- initial populations (post-stream state of step 0) ----
-        T f[NPT][Q];
-#pragma unroll
-        for (int s = 0; s < NPT; s++) {
-            if (!fluid[s]) continue;
-            if (g.init == INIT_TG_MAP) {
-                tg_map_init<P, Q>(f[s], nx_[s], ny_[s], r.u0, g);
-            } else if (g.init == INIT_AOS) {
-                // fluid index of this node: count of fluid nodes before it (solid masks are small)
-                int p = 0;
-                for (int k = 0; k < node[s]; k++) p += !solid[k];
-                const double *src = aos + r.aos_off + (long long)p * Q;
-#pragma unroll
-                for (int i = 0; i < Q; i++) f[s][i] = P::template from_f<Q>(src[i], i);
-            } else {
-#pragma unroll
-                for (int i = 0; i < Q; i++) f[s][i] = P::template from_f<Q>(Lat<Q>::w(i) * g.rho0, i);
+// ------------------------------------------------------------------------------------------------
+// Device-resident request loop (serving): CTAs claim requests that the host publishes in a ring
+// in mapped pinned memory, run them to completion and publish the results.  Every wait is bounded.
+// ------------------------------------------------------------------------------------------------
+
+struct SlotEntry {        // written by the host before it publishes the ring tail
+    BatchRun run;
+    int geo;              // index into the launch's geometry table
+    int pad[3];
+};
+
+struct SlotDone {         // written by the device; seq is published last
+    BatchResult res;
+    int seq;              // ring index + 1 once res is valid
+    int lane_exit;        // unused by runs
+    int pad[2];
+};
+
+struct SlotRing {
+    const int *tail;             // host-mapped: number of entries published
+    const SlotEntry *entries;    // host-mapped ring of `capacity` entries
+    SlotDone *done;              // host-mapped ring of results
+    const int *stop;             // host-mapped: 1 = stop after the current run
+    int *head;                   // device: next entry to claim
+    int *exits;                  // device: [0] CTAs that left idle-timed-out, [1] stopped
+    int capacity;
+    long long idle_polls;        // bounded wait: polls of the tail before a CTA gives up
+    const BatchGeo *geos;        // device table of geometries
+    int n_geos;
+};
+
+__device__ __forceinline__ int ld_acquire_sys(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.sys.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_sys(int *p, int v)
+{
+    asm volatile("st.release.sys.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <class P, int Q, int NPT>
+__global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
+                                  BatchBounds<NPT, sizeof(typename P::T)>::MINB)
+    k_slot_server(SlotRing ring, int max_nb)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const BatchSmem<P, Q> sm(smem_raw, max_nb);
+    __shared__ int s_idx;
+    __shared__ SlotEntry s_entry;
+    const int tid = threadIdx.x;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            int idx = -1;
+            for (long long polls = 0;; polls++) {
+                if (ld_acquire_sys(ring.stop)) {
+                    idx = -2;
+                    break;
+                }
+                const int t = ld_acquire_sys(ring.tail);
+                const int h = *(volatile int *)ring.head;
+                if (h < t) {
+                    if (atomicCAS(ring.head, h, h + 1) == h) {
+                        idx = h;
+                        break;
+                    }
+                    continue;
+                }
+                if (polls >= ring.idle_polls) {
+                    idx = -3;
+                    break;
+                }
+                __nanosleep(2000);
             }
-#pragma unroll
-            for (int i = 0; i < Q; i++) buf[i * NB + node[s]] = f[s][i];
+            if (idx >= 0) s_entry = ring.entries[idx % ring.capacity];
+            s_idx = idx;
         }
         __syncthreads();
-
-        double E0 = 0.0, E = 0.0, margin = 0.0, max_rho = 0.0;
-        int label = 0, decided = r.n_steps, status = 0, steps_done = r.n_steps;
-        if (g.energy_every > 0) {
-            double e = 0.0;
-#pragma unroll
-            for (int s = 0; s < NPT; s++)
-                if (fluid[s]) e += P::template energy<Q>(f[s]);
-            E0 = block_sum<NPT == 1 && sizeof(T) == 8>(e, red, NB);
-            E = E0;
+        const int idx = s_idx;
+        if (idx < 0) {
+            if (tid == 0) atomicAdd(&ring.exits[idx == -3 ? 0 : 1], 1);
+            return;
         }
-
-        for (int step = 0; step < r.n_steps; step++) {
-            // ---- stream: post-stream populations of this step ----
-            if (step > 0) {
-#pragma unroll
-                for (int s = 0; s < NPT; s++) {
-                    if (!fluid[s]) continue;
-                    int x = nx_[s];
-                    const int y = ny_[s];
-                    int me = node[s];
-                    if (x == g.outlet_x) {  // the outlet copies its inner neighbour (devnull_rho_x)
-                        x += (g.outlet_x < g.nx / 2) ? 1 : -1;
-                        me = node[s] + (x - nx_[s]);
-                    }
-#pragma unroll
-                    for (int i = 0; i < Q; i++) {
-                        const int xs = wrap1(x - Lat<Q>::cx(i), g.nx);
-                        const int ys = wrap1(y - Lat<Q>::cy(i), g.ny);
-                        const int src = xs + g.nx * ys;
-                        f[s][i] = (any_solid && solid[src]) ? buf[Lat<Q>::opp(i) * NB + me] : buf[i * NB + src];
-                    }
-                }
-            } else if (g.outlet_x >= 0) {
-#pragma unroll
-                for (int s = 0; s < NPT; s++) {
-                    if (!fluid[s] || nx_[s] != g.outlet_x) continue;
-                    const int me = node[s] + ((g.outlet_x < g.nx / 2) ? 1 : -1);
-#pragma unroll
-                    for (int i = 0; i < Q; i++) f[s][i] = buf[i * NB + me];
-                }
-            }
-            __syncthreads();
-
-            // ---- energy check on the post-stream populations ----
-            if (g.energy_every > 0 && step > 0 && step % g.energy_every == 0) {
-                double e = 0.0;
-#pragma unroll
-                for (int s = 0; s < NPT; s++)
-                    if (fluid[s]) e += P::template energy<Q>(f[s]);
-                E = block_sum<NPT == 1 && sizeof(T) == 8>(e, red, NB);
-                const double lim = g.energy_factor * E0;
-                const double rr = isfinite(E) ? E / lim : INFINITY;
-                margin = fmax(margin, rr);
-                if (E > lim || !isfinite(E)) {
-                    label = 1;
-                    decided = step;
-                    steps_done = step;
-                    status |= 4;
-                    break;
-                }
-            }
-
-            // ---- boundary planes, collision, density check, store ----
-            int flag = 0;
-#pragma unroll
-            for (int s = 0; s < NPT; s++) {
-                if (!fluid[s]) continue;
-                const int x = nx_[s];
-                if (x == g.outlet_x) {
-                    const int xn = x + ((g.outlet_x < g.nx / 2) ? 1 : -1);
-                    if (Q == 19 && xn == g.inlet_x) P::zou_he(f[s], r.u0, g.inlet_x < g.nx / 2);
-                    if (any_solid && solid[node[s] + (xn - x)])
-                        P::template rest<Q>(f[s], g.rho0);
-                    else
-                        P::template outlet<Q>(f[s], g.rho0);
-                } else if (Q == 19 && x == g.inlet_x) {
-                    P::zou_he(f[s], r.u0, g.inlet_x < g.nx / 2);
-                }
-                batch_collide<P, Q>(f[s], r);
-                if (g.density_check) {
-                    const double rho = P::template density<Q>(f[s]);
-                    if (!isfinite(rho)) {
-                        flag |= 2;
-                    } else {
-                        const double a = fabs(rho);
-                        max_rho = fmax(max_rho, a);
-                        if (a > g.density_limit) flag |= 1;
-                    }
-                }
-#pragma unroll
-                for (int i = 0; i < Q; i++) buf[i * NB + node[s]] = f[s][i];
-            }
-            if (g.density_check) {
-                // finish the step everywhere, then stop if any node failed
-                const int any = __syncthreads_or(flag);
-                if (any) {
-                    label = 1;
-                    decided = step;
-                    steps_done = step + 1;
-                    status |= __syncthreads_or(flag & 2) ? 3 : 1;
-                    break;
-                }
-            } else {
-                __syncthreads();
-            }
-        }
-        if (g.density_check) {
-            max_rho = block_max(max_rho, red);
-            margin = (status & 2) ? INFINITY : max_rho / g.density_limit;
+        const SlotEntry e = s_entry;
+        const int gi = (e.geo >= 0 && e.geo < ring.n_geos) ? e.geo : 0;
+        const BatchGeo g = ring.geos[gi];
+        // the launch's shared memory is sized for max_nb nodes; a smaller lattice uses its prefix
+        for (int k = tid; k < g.nb && k < max_nb; k += blockDim.x) sm.solid[k] = g.solid ? g.solid[k] : 0;
+        __syncthreads();
+        BatchResult o;
+        if (g.nb > max_nb || g.nb > NPT * (int)blockDim.x) {
+            o.label = 0;
+            o.decided_step = 0;
+            o.steps_done = 0;
+            o.status = 8;  // rejected: lattice does not fit this lane
+            o.margin = 0;
+            o.energy = 0;
+        } else {
+            o = batch_one_run<P, Q, NPT>(g, e.run, sm, nullptr);
         }
         if (tid == 0) {
-            BatchResult o;
-            o.label = label;
-            o.decided_step = decided;
-            o.steps_done = steps_done;
-            o.status = status;
-            o.margin = margin;
-            o.energy = E;
-            res[r.out] = o;
+            SlotDone *d = ring.done + (idx % ring.capacity);
+            d->res = o;
+            st_release_sys(&d->seq, idx + 1);
         }
     }
 }

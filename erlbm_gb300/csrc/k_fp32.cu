@@ -147,4 +147,13 @@ int launch_node_fields_fp32(int q, const Geo &g, long long n, const int *nof, co
     return node_fields_any<PrecShifted32>(q, g, n, nof, buf, e, rho, u, s);
 }
 
+
+// Initial fields on the device (lattice_kernels.cuh): kind 1 = D2Q9 Taylor-Green program init,
+// 4 = D3Q19 3-D Taylor-Green equilibrium, 0 = rest equilibrium.
+int launch_init_fp32(int kind, int q, const Geo &g, float *buf, const double *tab, double u0, double tau, double k,
+                     double rho, cudaStream_t s)
+{
+    return init_any<PrecShifted32>(kind, q, g, buf, tab, u0, tau, k, rho, s);
+}
+
 }  // namespace erlbm

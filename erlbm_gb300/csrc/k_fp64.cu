@@ -140,4 +140,13 @@ int launch_maxabs(const double *x, long long n, double *scratch, double *out, cu
     return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
+
+// Initial fields on the device (lattice_kernels.cuh): kind 1 = D2Q9 Taylor-Green program init,
+// 4 = D3Q19 3-D Taylor-Green equilibrium, 0 = rest equilibrium.
+int launch_init_fp64(int kind, int q, const Geo &g, double *buf, const double *tab, double u0, double tau, double k,
+                     double rho, cudaStream_t s)
+{
+    return init_any<PrecExact64>(kind, q, g, buf, tab, u0, tau, k, rho, s);
+}
+
 }  // namespace erlbm

@@ -75,4 +75,29 @@ size_t batch_smem(int prec, int q, int nb, int block)
     return q == 9 ? batch_smem_bytes<PrecShifted32, 9>(nb, block) : batch_smem_bytes<PrecShifted32, 19>(nb, block);
 }
 
+
+int launch_slot_server_fp32(const SlotRing &ring, int max_nb, int grid, int block, size_t smem, cudaStream_t s)
+{
+    auto k = k_slot_server<PrecShifted32, 19, 1>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return -3;
+    k<<<grid, block, smem, s>>>(ring, max_nb);
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+int slot_server_occupancy_fp32(int block, size_t smem)
+{
+    auto k = k_slot_server<PrecShifted32, 19, 1>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
 }  // namespace erlbm

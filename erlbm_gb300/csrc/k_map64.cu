@@ -57,4 +57,29 @@ int batch_occupancy_fp64(int q, int npt, int block, size_t smem)
     return 0;
 }
 
+
+int launch_slot_server_fp64(const SlotRing &ring, int max_nb, int grid, int block, size_t smem, cudaStream_t s)
+{
+    auto k = k_slot_server<PrecExact64, 19, 1>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return -3;
+    k<<<grid, block, smem, s>>>(ring, max_nb);
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+int slot_server_occupancy_fp64(int block, size_t smem)
+{
+    auto k = k_slot_server<PrecExact64, 19, 1>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
 }  // namespace erlbm

@@ -100,3 +100,26 @@ int batch_occupancy(int prec, int q, int npt, int block, size_t smem);
 size_t batch_smem(int prec, int q, int nb, int block);
 
 }  // namespace erlbm
+
+namespace erlbm {
+
+struct SlotRing;
+
+// Device-resident request loop for D3Q19 lattices of <= 288 nodes (batch_kernels.cuh).
+int launch_slot_server_fp64(const SlotRing &ring, int max_nb, int grid, int block, size_t smem, cudaStream_t s);
+int launch_slot_server_fp32(const SlotRing &ring, int max_nb, int grid, int block, size_t smem, cudaStream_t s);
+int slot_server_occupancy_fp64(int block, size_t smem);
+int slot_server_occupancy_fp32(int block, size_t smem);
+
+}  // namespace erlbm
+
+namespace erlbm {
+
+// Initial populations on the device: kind 1 = D2Q9 Taylor-Green program (tab = 4 L doubles),
+// 4 = D3Q19 3-D Taylor-Green (tab = 2 L doubles), 0 = rest equilibrium with density rho.
+int launch_init_fp64(int kind, int q, const Geo &g, double *buf, const double *tab, double u0, double tau, double k,
+                     double rho, cudaStream_t s);
+int launch_init_fp32(int kind, int q, const Geo &g, float *buf, const double *tab, double u0, double tau, double k,
+                     double rho, cudaStream_t s);
+
+}  // namespace erlbm

@@ -410,3 +410,91 @@ int node_fields_any(int q, const Geo &g, long long n, const int *nof, const type
 }
 
 }  // namespace erlbm
+
+namespace erlbm {
+
+// ------------------------------------------------------------------------------------------------
+// Initial populations written directly into a device SoA buffer (post-stream state of step 0).
+// Trig values come from host tables so that the FP64 path reproduces the host programs bit for bit.
+// ------------------------------------------------------------------------------------------------
+
+// inicializa_taylor_green (main_taylor-green.cpp:57-100), D2Q9, Poisson density and f_eq + f1.
+// tab: [s2 | c2 | c4 | ck] of L doubles each: sin(2 pi x / L), cos(2 pi x / L), cos(4 pi x / L),
+// cos(k x) with k = 2 pi / L, evaluated as the reference writes them.
+template <class P>
+__global__ void __launch_bounds__(256) k_init_tg2d(typename P::T *buf, Geo g, const double *__restrict__ tab,
+                                                   double u0, double tau, double k)
+{
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int L = g.nx;
+    if (node >= g.nbox) return;
+    const int x = (int)(node % L), y = (int)(node / L);
+    const double *s2 = tab, *c2 = tab + L, *c4 = tab + 2 * L, *ck = tab + 3 * L;
+    const double cs2 = 1. / 3.;
+    const double rho = 1.0 + 0.75 * u0 * u0 * (c4[x] + c4[y]);
+    const double ux = u0 * s2[x] * c2[y];
+    const double uy = -u0 * c2[x] * s2[y];
+    double f[9];
+    exact::equilibrium9(rho, ux, uy, f);
+    const double Sxx = 2. * u0 * k * ck[x] * ck[y];
+    const double Pxx = -rho * cs2 * tau * Sxx;
+    const double Pyy = -Pxx;
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+        const double cx = Lat<9>::cx(i), cy = Lat<9>::cy(i);
+        f[i] += Lat<9>::w(i) / (2. * cs2 * cs2) * ((cx * cx - cs2) * Pxx + (cy * cy - cs2) * Pyy);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; i++) buf[(long long)i * g.plane + node] = P::template from_f<9>(f[i], i);
+}
+
+// Three-dimensional Taylor-Green equilibrium (no driver in the reference; defined here):
+// rho = 1, u = U0 (sin kx cos ky cos kz, -cos kx sin ky cos kz, 0).  tab: [s | c] of L doubles.
+template <class P>
+__global__ void __launch_bounds__(256) k_init_tg3d(typename P::T *buf, Geo g, const double *__restrict__ tab,
+                                                   double u0)
+{
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= g.nbox) return;
+    const int L = g.nx;
+    const int x = (int)(node % L);
+    const long long r = node / L;
+    const int y = (int)(r % g.ny), z = (int)(r / g.ny);
+    const double *s = tab, *c = tab + L;
+    const double ux = u0 * s[x] * c[y] * c[z];
+    const double uy = -u0 * c[x] * s[y] * c[z];
+    double f[19];
+    exact::equilibrium19(1.0, ux, uy, 0.0, f);
+#pragma unroll
+    for (int i = 0; i < 19; i++) buf[(long long)i * g.plane + node] = P::template from_f<19>(f[i], i);
+}
+
+// Rest equilibrium f_i = w_i rho on every fluid node (main_stability-map_obstacle.cpp:81-82).
+template <class P, int Q>
+__global__ void __launch_bounds__(256) k_init_rest(typename P::T *buf, Geo g, double rho)
+{
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= g.nbox) return;
+#pragma unroll
+    for (int i = 0; i < Q; i++) buf[(long long)i * g.plane + node] = P::template from_f<Q>(Lat<Q>::w(i) * rho, i);
+}
+
+template <class P>
+int init_any(int kind, int q, const Geo &g, typename P::T *buf, const double *tab, double u0, double tau, double k,
+             double rho, cudaStream_t s)
+{
+    const unsigned nb = blocks_for(g.nbox, 256);
+    if (kind == 1 && q == 9)
+        k_init_tg2d<P><<<nb, 256, 0, s>>>(buf, g, tab, u0, tau, k);
+    else if (kind == 4 && q == 19)
+        k_init_tg3d<P><<<nb, 256, 0, s>>>(buf, g, tab, u0);
+    else if (kind == 0 && q == 9)
+        k_init_rest<P, 9><<<nb, 256, 0, s>>>(buf, g, rho);
+    else if (kind == 0 && q == 19)
+        k_init_rest<P, 19><<<nb, 256, 0, s>>>(buf, g, rho);
+    else
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+}  // namespace erlbm

@@ -197,6 +197,58 @@ typedef struct erlbm_map_desc {
 /* labels (and optionally decided steps and margins) of n_points (x 2 when op = 0) runs */
 int erlbm_map_run(const erlbm_map_desc *d, int32_t *labels, int32_t *decided_step, double *margins);
 
+/* ---- request server (continuous batching) ---------------------------------------------------- */
+/* No counterpart in the reference, which runs one program per invocation.  A server owns a fixed
+ * slice of device memory and a scheduler thread; requests are admitted while others run:
+ *  - D3Q19 lattices of <= 288 nodes (Taylor-Green map points, the obstacle channel at scale 1) go to
+ *    a device-resident loop whose CTAs claim them from a ring as soon as they are published;
+ *  - larger lattices are admitted by memory footprint and advanced on their own CUDA streams.
+ * The lane a request takes depends only on the request, so its result does not depend on the mix.
+ * While a server runs, avoid calls that synchronise the whole device (erlbm_destroy frees memory)
+ * on the same GPU: they wait until the resident loop idles out (about a second). */
+#define ERLBM_REQ_TG2D 1          /* D2Q9 Taylor-Green L x L, inicializa_taylor_green init (main_taylor-green.cpp:57-100) */
+#define ERLBM_REQ_TG_MAP_POINT 2  /* D3Q19 16 x 16 x 1 map point, energy checks every 100 steps (TG map roda_ponto) */
+#define ERLBM_REQ_OBSTACLE 3      /* D3Q19 obstacle channel scaled (sx, sy), Zou-He inlet with u0, density checks */
+#define ERLBM_REQ_TG3D 4          /* D3Q19 L^3 periodic Taylor-Green equilibrium, rho = 1,
+                                     u = u0 (sin kx cos ky cos kz, -cos kx sin ky cos kz, 0) */
+
+typedef struct erlbm_server erlbm_server;
+
+typedef struct erlbm_server_desc {
+    int64_t hbm_budget_bytes;   /* device memory for admitted lattices (default 8 GiB) */
+    int slot_ctas;              /* CTAs of each resident loop (one per precision); 0 = SMs / 2 */
+    int max_streams;            /* concurrent stream-lane runs; 0 = 16 */
+    int queue_capacity;         /* ring entries per resident loop; 0 = 65536 */
+} erlbm_server_desc;
+
+typedef struct erlbm_request {
+    int kind;                   /* ERLBM_REQ_* */
+    int precision, op;
+    int L;                      /* TG2D / TG3D side */
+    int sx, sy;                 /* obstacle scale */
+    double tau, tau_nh, u0;
+    int n_steps;                /* step budget */
+} erlbm_request;
+
+typedef struct erlbm_result {
+    int status;                 /* ERLBM_OK or an error code */
+    int label, steps_done, decided_step;
+    double energy;              /* kinetic energy: post-stream state after the run (stream lane) or at
+                                   the last energy check (map points) */
+    double margin;
+    double t_submit, t_admit, t_done; /* seconds on the server clock (t_admit < 0: resident loop) */
+    int lane;                   /* 0 resident loop, 1 stream lane */
+} erlbm_result;
+
+int erlbm_server_start(const erlbm_server_desc *d, erlbm_server **s);
+int erlbm_server_submit(erlbm_server *s, const erlbm_request *req, int64_t *ticket);
+/* ERLBM_OK and *res filled when the request is done, 1 while it is pending */
+int erlbm_server_poll(erlbm_server *s, int64_t ticket, erlbm_result *res);
+int erlbm_server_wait(erlbm_server *s, int64_t ticket, erlbm_result *res, double timeout_s);
+double erlbm_server_clock(erlbm_server *s);
+/* finishes every accepted request, then stops */
+int erlbm_server_stop(erlbm_server *s);
+
 /* ---- program inputs (host functions; what the reference's drivers build around their loops) --- */
 /* inicializa_taylor_green (main_taylor-green.cpp:57-100) on an L x L (x nz) periodic box, AoS in
  * fluid-index order.  variant 1 is the same vortex translated by (L/4, L/4):
