@@ -1,0 +1,98 @@
+"""Request server: continuous batching, admission while others run, and results independent of the
+mix (the same request alone and among others gives the same result, bit for bit)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def E():
+    import erlbm_gb300 as m
+    return m
+
+
+def mix(m, rng, n):
+    reqs = []
+    for k in range(n):
+        kind = [m.REQ_TG2D, m.REQ_TG_MAP_POINT, m.REQ_OBSTACLE, m.REQ_TG3D][k % 4]
+        prec = [m.FP64, m.FP32_SHIFTED][(k // 4) % 2]
+        steps = int(rng.integers(1, 300))
+        if kind == m.REQ_TG2D:
+            L = int(rng.choice([32, 64, 128]))
+            u0 = 2.0 / L
+            tau = 0.5 + 3 * u0 * L / 50.0
+            reqs.append(dict(kind=kind, precision=prec, op=m.OP_EXTREG, L=L, tau=tau, tau_nh=0.65, u0=u0,
+                             n_steps=steps))
+        elif kind == m.REQ_TG_MAP_POINT:
+            u0, tau, tnh = m.tg_map_params(int(rng.integers(0, 400)), int(rng.integers(0, 400)))
+            reqs.append(dict(kind=kind, precision=prec, op=m.OP_EXTREG, tau=tau, tau_nh=tnh, u0=u0,
+                             n_steps=steps * 10))
+        elif kind == m.REQ_OBSTACLE:
+            u, tau, tnh = m.obstacle_map_params(int(rng.integers(0, 400)), int(rng.integers(0, 400)))
+            s = int(rng.integers(1, 3))
+            reqs.append(dict(kind=kind, precision=prec, op=m.OP_EXTREG, sx=s, sy=s, tau=tau, tau_nh=tnh, u0=u,
+                             n_steps=steps * 5))
+        else:
+            reqs.append(dict(kind=kind, precision=prec, op=m.OP_EXTREG, L=32, tau=0.55, tau_nh=0.65, u0=0.05,
+                             n_steps=steps))
+    return reqs
+
+
+KEYS = ("status", "label", "steps_done", "decided_step", "energy", "margin", "lane")
+
+
+def test_results_same_alone_and_in_mix():
+    m = E()
+    reqs = mix(m, np.random.default_rng(11), 24)
+    with m.Server(hbm_budget_bytes=2 << 30) as srv:
+        alone = []
+        for r in reqs:
+            alone.append(srv.wait(srv.submit(**r)))
+        tickets = [srv.submit(**r) for r in reqs]
+        together = [srv.wait(t) for t in tickets]
+    for a, b, r in zip(alone, together, reqs):
+        assert a["status"] == 0, (a, r)
+        assert all(a[k] == b[k] or (np.isnan(a[k]) and np.isnan(b[k])) for k in KEYS), (a, b, r)
+
+
+def test_continuous_admission():
+    """Short requests submitted after a long one start and finish while the long one still runs."""
+    m = E()
+    with m.Server(hbm_budget_bytes=2 << 30) as srv:
+        long_t = srv.submit(m.REQ_TG2D, m.FP64, L=512, tau=0.5 + 3 * (2 / 512) * 512 / 50, u0=2 / 512,
+                            n_steps=3000)
+        shorts = [srv.submit(m.REQ_TG_MAP_POINT, m.FP32_SHIFTED, tau=0.51, tau_nh=0.65, u0=0.1, n_steps=200)
+                  for _ in range(50)]
+        shorts += [srv.submit(m.REQ_TG2D, m.FP32_SHIFTED, L=64, tau=0.62, u0=2 / 64, n_steps=50) for _ in range(8)]
+        rs = [srv.wait(t) for t in shorts]
+        lr = srv.wait(long_t)
+    assert all(r["status"] == 0 for r in rs)
+    assert max(r["t_done"] for r in rs) < lr["t_done"]
+    assert lr["steps_done"] == 3000
+
+
+def test_server_results_match_oracle():
+    m = E()
+    with m.Server(hbm_budget_bytes=1 << 30) as srv:
+        L, u0 = 32, 2 / 32
+        tau = 0.5 + 3 * u0 * L / 50
+        t = srv.submit(m.REQ_TG2D, m.FP64, op=m.OP_EXTREG, L=L, tau=tau, tau_nh=0.65, u0=u0, n_steps=77)
+        r = srv.wait(t)
+        lat = O.Lattice(9, L, L, 1, None, tau, 0.65, O.OP_EXTREG)
+        lat.set(O.init_taylor_green(9, L, u0, tau))
+        lat.step(77)
+        assert r["energy"] == lat.kinetic_energy(0)
+        # a map point through the resident loop equals the batched map kernel's result
+        u0, tau, tnh = m.tg_map_params(300, 20)
+        r = srv.wait(srv.submit(m.REQ_TG_MAP_POINT, m.FP64, tau=tau, tau_nh=tnh, u0=u0, n_steps=3623))
+        lab, dec, mg = O.tg_map_point(16, O.OP_EXTREG, tau, tnh, u0)
+        assert (r["label"], r["decided_step"], r["margin"]) == (lab, dec, mg)
+        u, tau, tnh = m.obstacle_map_params(0, 0)
+        r = srv.wait(srv.submit(m.REQ_OBSTACLE, m.FP64, sx=1, sy=1, tau=tau, tau_nh=tnh, u0=u, n_steps=2000))
+        lab, dec, mg = O.obstacle_map_point(tau, tnh, u, max_steps=2000)
+        assert (r["label"], r["decided_step"], r["margin"]) == (lab, dec, mg)
+        r = srv.wait(srv.submit(m.REQ_OBSTACLE, m.FP64, sx=2, sy=2, tau=tau, tau_nh=tnh, u0=u, n_steps=500))
+        lab, dec, mg = O.obstacle_map_point(tau, tnh, u, sx=2, sy=2, max_steps=500)
+        assert (r["label"], r["decided_step"]) == (lab, dec)
