@@ -3,7 +3,7 @@
     python -m erlbm_gb300.build            # or erlbm_gb300.build.build()
 
 Each .cu file is compiled in parallel into erlbm_gb300/_build/ and linked into
-erlbm_gb300/liberlbm_gb300.so.  The FP64 kernels (k_fp64.cu, k_map64.cu) are compiled with
+erlbm_gb300/liberlbm_gb300.so.  The FP64 kernels (k_fp64.cu, k_map64.cu) and noalloc.cu are compiled with
 --fmad=false: the reference's GCC -std=c++17 build never fuses a multiply and an add, and the
 plain FP64 path reproduces its results bit for bit only with the same rounding.
 """
@@ -24,7 +24,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off",
           f"-I{CSRC}", f"-I{INCLUDE}"]
-NO_FMA = {"k_fp64.cu", "k_map64.cu"}
+NO_FMA = {"k_fp64.cu", "k_map64.cu", "noalloc.cu"}
 
 
 def nvcc() -> str:

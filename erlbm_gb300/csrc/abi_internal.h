@@ -3,7 +3,12 @@
 
 #include <cuda_runtime.h>
 
+struct erlbm_batch_desc;
+
 namespace erlbm {
+
+// Validates a batch description (batch_abi.cu).
+int check_desc(const erlbm_batch_desc *d);
 
 // Records the message returned by erlbm_last_error() for this host thread (two %s arguments).
 void set_error(const char *fmt, const char *a, const char *b);

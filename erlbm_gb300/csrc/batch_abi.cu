@@ -57,10 +57,9 @@ struct Scratch {
     }
 };
 
-struct LaunchShape {
-    int npt, block, grid;
-    size_t smem;
-};
+}  // namespace
+
+namespace erlbm {
 
 int pick_shape(int prec, int q, int nb, int slots, int n_runs, LaunchShape *out)
 {
@@ -108,10 +107,6 @@ int check_desc(const erlbm_batch_desc *d)
     if (d->init != ERLBM_INIT_REST && d->init != ERLBM_INIT_TG_MAP && d->init != ERLBM_INIT_AOS) return ERLBM_E_INVAL;
     return ERLBM_OK;
 }
-
-}  // namespace
-
-namespace erlbm {
 
 // Shared by erlbm_batch_run and the server: run a prepared batch on `stream` (synchronous).
 int run_batch(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec *runs, const double *aos, size_t n_aos,

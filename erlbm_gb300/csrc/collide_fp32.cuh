@@ -39,7 +39,7 @@ struct Coef {
     float kd, d1;
 };
 
-inline Coef make_coef(const Relax &R)
+__host__ __device__ inline Coef make_coef(const Relax &R)
 {
     Coef k;
     k.d1 = (float)(2.0 - R.inv_tau);

@@ -95,6 +95,13 @@ int launch_batch_fp64(int q, int npt, const BatchGeo &g, const BatchRun *runs, i
                       BatchResult *res, const double *aos, int grid, int block, size_t smem, cudaStream_t s);
 int launch_batch_fp32(int q, int npt, const BatchGeo &g, const BatchRun *runs, int n_runs, int *counter,
                       BatchResult *res, const double *aos, int grid, int block, size_t smem, cudaStream_t s);
+// Launch shape of a batch: nodes per thread, threads per CTA, CTAs, dynamic shared bytes.
+struct LaunchShape {
+    int npt, block, grid;
+    size_t smem;
+};
+int pick_shape(int prec, int q, int nb, int slots, int n_runs, LaunchShape *out);
+
 // Resident CTAs per SM for a configuration (0 if it cannot run).
 int batch_occupancy(int prec, int q, int npt, int block, size_t smem);
 size_t batch_smem(int prec, int q, int nb, int block);

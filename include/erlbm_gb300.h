@@ -174,6 +174,23 @@ typedef struct erlbm_batch_result {
 int erlbm_batch_run(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec *runs, const double *aos,
                     size_t n_aos, erlbm_batch_result *out);
 
+/* Batched runs without any allocation.  No counterpart in the reference.  For callers that cannot
+ * let a library allocate GPU memory (their own allocator owns the device, or their loop may not pay
+ * for cudaMalloc / cudaFree and the synchronisation cudaFree implies): the per-call scratch that
+ * erlbm_batch_run allocates lives here in one static device array of about 1.2 MB per GPU, held
+ * until the process exits, and nothing is allocated.  runs and out are DEVICE arrays of n_runs
+ * entries owned by the caller; d->solid, when set, is a DEVICE pointer; d->init must be
+ * ERLBM_INIT_REST or ERLBM_INIT_TG_MAP.  At most ERLBM_NOALLOC_MAX_RUNS runs per call (more is
+ * ERLBM_E_INVAL).  The work is queued on `stream` (a cudaStream_t; NULL = the default stream) and
+ * the call returns without waiting; results follow the stream's order.  Runs are taken in the
+ * caller's order (erlbm_batch_run starts the longest first); results are the same.  The first call
+ * on a device looks up the array's device address: make that first call before any stream capture.
+ * Every call shares the one array, so calls that overlap on the GPU (different streams, or several
+ * host threads) race: order them on one stream. */
+#define ERLBM_NOALLOC_MAX_RUNS 16384
+int erlbm_batch_run_noalloc(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec *runs,
+                            erlbm_batch_result *out, void *stream);
+
 /* The reference's stability maps with their axes (main_stability-map_taylor-green.cpp:134-166,
  * main_stability-map_obstacle.cpp:147-175). */
 #define ERLBM_MAP_TAYLOR_GREEN 1
