@@ -176,6 +176,7 @@ int run_batch(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec *runs,
     g.density_check = d->density_check;
     g.density_limit = d->density_limit;
     g.init = d->init;
+    density_bounds(g);
     std::vector<double> tab;
     if (d->init == ERLBM_INIT_TG_MAP) {
         // sin(2 pi x / L) and cos(2 pi x / L) as main_stability-map_taylor-green.cpp:55-57 evaluates them

@@ -42,7 +42,22 @@ struct BatchGeo {
     double density_limit;
     int init;                     // BatchInit
     const double *sinx, *cosx;    // INIT_TG_MAP: sin(2 pi x / L), cos(2 pi x / L) for x < nx
+    // FP32 path: |1 + drho| > density_limit  <=>  drho > drho_hi || drho < drho_lo for a float drho
+    // (bounds limit - 1 and -limit - 1 rounded outward to float on the host; see density_bounds)
+    float drho_hi, drho_lo;
 };
+
+// Float bounds equivalent to the FP64 test |1 + (double)d| > limit for every float d: 1 + d is exact
+// in FP64 near the thresholds, and "d > x" for a double x equals "d > x rounded down to float".
+inline void density_bounds(BatchGeo &g)
+{
+    const double hi = g.density_limit - 1.0, lo = -g.density_limit - 1.0;
+    float fh = (float)hi, fl = (float)lo;
+    if ((double)fh > hi) fh = nextafterf(fh, -INFINITY);
+    if ((double)fl < lo) fl = nextafterf(fl, INFINITY);
+    g.drho_hi = fh;
+    g.drho_lo = fl;
+}
 
 // One run, prepared on the host.
 struct BatchRun {
@@ -228,6 +243,7 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
     __syncthreads();
 
     double E0 = 0.0, E = 0.0, margin = 0.0, max_rho = 0.0;
+    float dmax = -INFINITY, dmin = INFINITY;  // FP32 path: extreme drho seen by this thread
     int label = 0, decided = r.n_steps, status = 0, steps_done = r.n_steps;
     constexpr bool SERIAL = NPT == 1 && sizeof(T) == 8;
     if (g.energy_every > 0) {
@@ -308,13 +324,24 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
             }
             batch_collide<P, Q>(f[s], r);
             if (g.density_check) {
-                const double rho = P::template density<Q>(f[s]);
-                if (!isfinite(rho)) {
-                    flag |= 2;
+                if constexpr (sizeof(T) == 4) {
+                    const float d = shifted::node_drho<Q>(f[s]);
+                    if (!isfinite(d)) {
+                        flag |= 2;
+                    } else {
+                        dmax = fmaxf(dmax, d);
+                        dmin = fminf(dmin, d);
+                        if (d > g.drho_hi || d < g.drho_lo) flag |= 1;
+                    }
                 } else {
-                    const double a = fabs(rho);
-                    max_rho = fmax(max_rho, a);
-                    if (a > g.density_limit) flag |= 1;
+                    const double rho = P::template density<Q>(f[s]);
+                    if (!isfinite(rho)) {
+                        flag |= 2;
+                    } else {
+                        const double a = fabs(rho);
+                        max_rho = fmax(max_rho, a);
+                        if (a > g.density_limit) flag |= 1;
+                    }
                 }
             }
 #pragma unroll
@@ -335,6 +362,9 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
         }
     }
     if (g.density_check) {
+        if constexpr (sizeof(T) == 4) {
+            if (dmax >= dmin) max_rho = fmax(fabs(1.0 + (double)dmax), fabs(1.0 + (double)dmin));
+        }
         max_rho = block_max(max_rho, red);
         margin = (status & 2) ? INFINITY : max_rho / g.density_limit;
     }

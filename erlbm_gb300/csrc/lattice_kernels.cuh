@@ -118,15 +118,15 @@ struct PrecShifted32 {
         uz = fz;
     }
     __device__ static __forceinline__ void zou_he(T *f, double vx, bool left) { shifted::zou_he(f, vx, left); }
+    // devnull_rho_x on shifted populations: f = f_adj * (rho / rho_adj) becomes
+    // g = g_adj s + w (s - 1), s = rho / rho_adj; s and s - 1 are formed in FP64, the update in FP32.
     template <int Q>
     __device__ static __forceinline__ void outlet(T *f, double rho)
     {
-        double r = 1.0;
+        const double r = 1.0 + (double)shifted::node_drho<Q>(f);
+        const float s = (float)(rho / r), sm1 = (float)((rho - r) / r);
 #pragma unroll
-        for (int i = 0; i < Q; i++) r += (double)f[i];
-        const double s = rho / r;
-#pragma unroll
-        for (int i = 0; i < Q; i++) f[i] = (float)(((double)f[i] + Lat<Q>::w(i)) * s - Lat<Q>::w(i));
+        for (int i = 0; i < Q; i++) f[i] = fmaf(f[i], s, (float)Lat<Q>::w(i) * sm1);
     }
     template <int Q>
     __device__ static __forceinline__ void rest(T *f, double rho)

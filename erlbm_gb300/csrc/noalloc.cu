@@ -131,6 +131,7 @@ extern "C" int erlbm_batch_run_noalloc(const erlbm_batch_desc *d, int n_runs, co
     g.density_check = d->density_check;
     g.density_limit = d->density_limit;
     g.init = d->init;
+    density_bounds(g);
     cudaError_t e;
     if (d->init == ERLBM_INIT_TG_MAP) {
         // the same tables erlbm_batch_run builds, staged from a stack buffer

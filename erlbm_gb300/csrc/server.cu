@@ -745,6 +745,7 @@ int erlbm_server_start(const erlbm_server_desc *d, erlbm_server **out)
     tg.energy_every = 100;
     tg.energy_factor = 2.0;
     tg.init = INIT_TG_MAP;
+    density_bounds(tg);
     tg.sinx = s->d_tg_tab;
     tg.cosx = s->d_tg_tab + 16;
     BatchGeo &ob = s->geos_host[1];
@@ -759,6 +760,7 @@ int erlbm_server_start(const erlbm_server_desc *d, erlbm_server **out)
     ob.density_check = 1;
     ob.density_limit = 10.0;
     ob.init = INIT_REST;
+    density_bounds(ob);
     if ((rc = lane_setup(s.get(), s->lane[0], ERLBM_FP64))) return rc;
     if ((rc = lane_setup(s.get(), s->lane[1], ERLBM_FP32_SHIFTED))) return rc;
     for (int k = 0; k < s->desc.max_streams; k++) {
