@@ -18,6 +18,16 @@ reference's own CPU code when it could be compiled from its sources here (oracle
 that same restatement, and prints the same JSON line with "impl": "reference".
 
 Multi-GPU: one lattice does not shard, so N GPUs run N independent replicas (weak scaling).
+
+Other workloads (--workload; the default is the one above):
+  tg-map, obstacle-map   stability maps (main_stability-map_*.cpp) on an evenly spaced P x P subset
+                         of the 400 x 400 grid; one bench step = one batched map launch; runs/s.
+                         The Taylor-Green map runs every point with RLBM and with E-RLBM.
+  serve                  a seeded Poisson stream of mixed requests (Taylor-Green D2Q9 L = 32..512,
+                         map points, obstacle channels scaled 1-4x, 3-D Taylor-Green 32^3 / 64^3;
+                         FP32 or FP64; budgets 1..10000 steps) through the request server; runs/s
+                         with p50 / p99 latency, beside the plain path (one run at a time, FP64,
+                         one launch per step) on a prefix of the same stream.
 """
 from __future__ import annotations
 
@@ -49,6 +59,12 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extras", action="store_true")
+    p.add_argument("--workload", default="dsl", choices=["dsl", "tg-map", "obstacle-map", "serve"])
+    p.add_argument("--map-points", type=int, default=100, help="P: P x P map points per bench step")
+    p.add_argument("--max-steps", type=int, default=0, help="cap on map run budgets (0 = the reference's)")
+    p.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
+    p.add_argument("--rate", type=float, default=2000.0, help="serve: mean arrivals per second")
+    p.add_argument("--plain-requests", type=int, default=24, help="serve: stream prefix run on the plain path")
     return p.parse_args()
 
 
@@ -355,10 +371,175 @@ def gpu_extras(E, torch, L, f0, tau, prec):
     return out
 
 
+def map_points(P):
+    step = 400 / P
+    return [(int(i * step), int(j * step)) for j in range(P) for i in range(P)]
+
+
+def run_map(args):
+    import numpy as np
+    import torch
+    import erlbm_gb300 as E
+    torch.cuda.set_device(0)
+    kind = E.MAP_TAYLOR_GREEN if args.workload == "tg-map" else E.MAP_OBSTACLE
+    prec = E.FP32_SHIFTED if args.precision == "fp32" else E.FP64
+    pts = map_points(args.map_points)
+    op = 0 if kind == E.MAP_TAYLOR_GREEN else E.OP_EXTREG
+    nodes = 256 if kind == E.MAP_TAYLOR_GREEN else 232
+    for _ in range(args.warmup):
+        E.map_run(kind, pts[: max(1, len(pts) // 8)], precision=prec, op=op, max_steps=args.max_steps)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    runs, lus = 0, 0
+    for _ in range(args.steps):
+        lab, dec, _ = E.map_run(kind, pts, precision=prec, op=op, max_steps=args.max_steps)
+        runs += len(lab)
+        lus += int(np.sum(dec.astype(np.int64))) * nodes
+    dt = time.perf_counter() - t0
+    clk = clocks.stop()
+    value = runs / dt
+    line = {"metric": "map runs/s", "value": value, "unit": "runs/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec else "f64",
+            "data": "synthetic (the reference's map axes)",
+            "config": {"workload": f"{args.workload} D3Q19, {args.map_points}x{args.map_points} points of the 400x400 "
+                                   f"grid{' x {RLBM, E-RLBM}' if op == 0 else ''}, max_steps={args.max_steps}",
+                       "precision": args.precision},
+            "lattice_updates_per_s": lus / dt, "roofline": None,
+            "e2e": {"value": value, "unit": "runs/s", "h2d_bytes_per_step": len(pts) * 48,
+                    "d2h_bytes_per_step": len(pts) * 32},
+            "gpu_launches": args.steps, "clocks": clk}
+    if not args.no_cpu:
+        from oracle import oracle as O
+        few = pts[:: max(1, len(pts) // 16)]
+        t = time.perf_counter()
+        if kind == E.MAP_TAYLOR_GREEN:
+            O.tg_map(few, op=O.OP_EXTREG, tau_nh=0.65, max_steps=args.max_steps)
+        else:
+            O.obstacle_map(few, max_steps=args.max_steps)
+        ct = time.perf_counter() - t
+        line["cpu_baseline"] = {"value": len(few) / ct, "unit": "runs/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{len(few)} of the same points, OpenMP over points"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def serve_stream(E, n, rate, seed=20261203):
+    """Config-5 request mix: (arrival time, request kwargs) in arrival order."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    out = []
+    for k in range(n):
+        kind = int(rng.integers(0, 4))
+        prec = [E.FP32_SHIFTED, E.FP64][int(rng.integers(0, 2))]
+        steps = int(rng.integers(1, 10001))
+        if kind == 0:
+            L = int(rng.choice([32, 64, 128, 256, 512]))
+            u0 = 2.0 / L
+            r = dict(kind=E.REQ_TG2D, precision=prec, op=E.OP_EXTREG, L=L, tau=0.5 + 3 * u0 * L / 50.0, tau_nh=0.65,
+                     u0=u0, n_steps=steps)
+        elif kind == 1:
+            op = [E.OP_REG, E.OP_EXTREG][int(rng.integers(0, 2))]
+            u0, tau, tnh = E.tg_map_params(int(rng.integers(0, 400)), int(rng.integers(0, 400)), op=op)
+            r = dict(kind=E.REQ_TG_MAP_POINT, precision=prec, op=op, tau=tau, tau_nh=tnh, u0=u0, n_steps=steps)
+        elif kind == 2:
+            u, tau, tnh = E.obstacle_map_params(int(rng.integers(0, 400)), int(rng.integers(0, 400)))
+            r = dict(kind=E.REQ_OBSTACLE, precision=prec, op=E.OP_EXTREG, sx=int(rng.integers(1, 5)),
+                     sy=int(rng.integers(1, 5)), tau=tau, tau_nh=tnh, u0=u, n_steps=steps)
+        else:
+            r = dict(kind=E.REQ_TG3D, precision=prec, op=E.OP_EXTREG, L=int(rng.choice([32, 64])), tau=0.55,
+                     tau_nh=0.65, u0=0.05, n_steps=steps)
+        out.append((float(t[k]), r))
+    return out
+
+
+def plain_run(E, r):
+    """One request on the plain single-lattice path: FP64, one launch per step, one run at a time."""
+    import numpy as np
+    k = r["kind"]
+    if k == E.REQ_TG2D:
+        L = r["L"]
+        with E.Lattice(9, L, L, 1, None, r["tau"], r["tau_nh"], r["op"], E.FP64) as lat:
+            lat.set_populations(E.init_taylor_green(9, L, r["u0"], r["tau"]))
+            lat.step(r["n_steps"])
+            return lat.kinetic_energy()
+    if k == E.REQ_TG_MAP_POINT:
+        with E.Lattice(19, 16, 16, 1, None, r["tau"], r["tau_nh"], r["op"], E.FP64) as lat:
+            lat.set_populations(E.init_taylor_green(19, 16, r["u0"], r["tau"], poisson=False, neq=False))
+            return lat.run(r["n_steps"], None, energy_every=100, energy_factor=2.0)["label"]
+    if k == E.REQ_OBSTACLE:
+        nx, ny, solid = E.obstacle_geometry(r["sx"], r["sy"])
+        with E.Lattice(19, nx, ny, 1, solid, r["tau"], r["tau_nh"], r["op"], E.FP64) as lat:
+            lat.set_populations(np.tile(E.equilibrium(19, 0, 0, 0, 1.0), lat.n_fluid))
+            return lat.run(r["n_steps"], dict(inlet_x=1, u_in=r["u0"], outlet_x=nx - 2, rho_out=1.0),
+                           density_check=True)["label"]
+    L = r["L"]
+    with E.Lattice(19, L, L, L, None, r["tau"], r["tau_nh"], r["op"], E.FP64) as lat:
+        lat.set_populations(np.concatenate([E.init_taylor_green(19, L, r["u0"], r["tau"], poisson=False, neq=False,
+                                                                nz=1)] * L))
+        lat.step(r["n_steps"])
+        return lat.kinetic_energy()
+
+
+def run_serve(args):
+    import numpy as np
+    import torch
+    import erlbm_gb300 as E
+    torch.cuda.set_device(0)
+    stream = serve_stream(E, args.requests, args.rate)
+    with E.Server(hbm_budget_bytes=16 << 30) as srv:
+        # warm-up: one request of each kind
+        for _, r in stream[:8]:
+            srv.wait(srv.submit(**dict(r, n_steps=min(r["n_steps"], 10))))
+        clocks = Clocks(0)
+        clocks.start()
+        t0 = time.perf_counter()
+        tickets = []
+        for at, r in stream:
+            now = time.perf_counter() - t0
+            if at > now:
+                time.sleep(at - now)
+            tickets.append(srv.submit(**r))
+        res = [srv.wait(t, 3600.0) for t in tickets]
+        clk = clocks.stop()
+    ok = [x for x in res if x["status"] == 0]
+    lat = np.array([x["t_done"] - x["t_submit"] for x in ok])
+    span = max(x["t_done"] for x in ok) - min(x["t_submit"] for x in ok)
+    value = len(ok) / span
+    # the plain path on a prefix of the same stream, one run after another
+    t = time.perf_counter()
+    m = min(args.plain_requests, len(stream))
+    for _, r in stream[:m]:
+        plain_run(E, r)
+    plain = m / (time.perf_counter() - t)
+    line = {"metric": "served runs/s", "value": value, "unit": "runs/s", "n_gpus": 1, "steps": len(ok),
+            "warmup": 8, "ms_per_step": span / max(1, len(ok)) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded Poisson stream of config-5 requests)",
+            "config": {"workload": f"serve {args.requests} requests, Poisson {args.rate:.0f}/s, mixed kinds",
+                       "requests": args.requests},
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(lat.max())},
+            "failed": len(res) - len(ok), "lanes": {"resident": sum(1 for x in ok if x["lane"] == 0),
+                                                    "stream": sum(1 for x in ok if x["lane"] == 1)},
+            "plain_fp64_one_run_at_a_time": {"value": plain, "unit": "runs/s", "requests": m},
+            "roofline": None, "e2e": {"value": value, "unit": "runs/s", "h2d_bytes_per_step": 64,
+                                      "d2h_bytes_per_step": 64},
+            "gpu_launches": None, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload in ("tg-map", "obstacle-map"):
+        return run_map(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 
