@@ -102,6 +102,10 @@ class Lattice:
         check(lib().erlbm_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None),
               "erlbm_set_stream")
 
+    def set_launch(self, block_threads: int = 0, streaming_stores: bool = False) -> None:
+        """Launch shape of the fused periodic D2Q9 FP32 kernel (see erlbm_gb300.autotune)."""
+        check(lib().erlbm_set_launch(self._h, int(block_threads), 1 if streaming_stores else 0), "erlbm_set_launch")
+
     def kinetic_energy(self, stage: int = STAGE_POST_STREAM) -> float:
         e = C.c_double()
         check(lib().erlbm_kinetic_energy(self._h, stage, C.byref(e)), "erlbm_kinetic_energy")
@@ -206,8 +210,12 @@ def map_run(kind: int, points=None, precision: int = FP64, op: int = OP_EXTREG, 
     kind: MAP_TAYLOR_GREEN (main_stability-map_taylor-green.cpp) or MAP_OBSTACLE
     (main_stability-map_obstacle.cpp).  points: list of (i, j) map indices, or None for the whole
     n_i x n_j grid (i fastest).  op = 0 on the Taylor-Green map runs every point with RLBM and with
-    E-RLBM (results concatenated, RLBM first).  Returns (labels, decided_step, margins) arrays.
+    E-RLBM (results concatenated, RLBM first).  slots: resident lattices per SM, 0 = as many as fit,
+    -1 = the autotuner's cached choice.  Returns (labels, decided_step, margins) arrays.
     """
+    if slots < 0:
+        from . import autotune
+        slots = autotune.best_slots(kind, precision)
     if points is None:
         n, pi, pj = n_i * n_j, None, None
     else:

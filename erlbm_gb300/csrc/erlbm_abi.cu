@@ -79,6 +79,7 @@ struct erlbm_handle {
     RunStatus *d_status = nullptr;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the stream created at erlbm_create
+    int shape = 0;                      // launch shape of the fused periodic kernel (erlbm_set_launch)
     size_t elem() const { return prec == ERLBM_FP64 ? sizeof(double) : sizeof(float); }
 };
 
@@ -220,7 +221,8 @@ int enqueue_step(erlbm_handle *h, const BCp &bc, int check_density, double densi
     void *src = h->d_buf[h->cur], *dst = h->d_buf[h->cur ^ 1];
     const bool plain = bc.inlet_x < 0 && bc.outlet_x < 0 && !check_density && !stop_on_flag && a.mode == 0;
     if (h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && plain && periodic_d2q9_fp32_ok(h->g)) {
-        CKL(launch_periodic_d2q9_fp32(h->op, h->g, h->R, (const float *)src, (float *)dst, h->stream), "periodic_d2q9");
+        CKL(launch_periodic_d2q9_fp32(h->op, h->g, h->R, (const float *)src, (float *)dst, h->stream, h->shape),
+            "periodic_d2q9");
     } else if (h->prec == ERLBM_FP64) {
         CKL(launch_step_fp64(h->q, h->op, h->g, bc, h->R, a, (const double *)src, (double *)dst, h->stream), "step");
     } else {
@@ -454,6 +456,19 @@ int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc)
     if ((rc = validate_bc(h, bc, &b))) return rc;
     for (int s = 0; s < n_steps; s++)
         if ((rc = enqueue_step(h, b, 0, 0.0, false))) return rc;
+    return ERLBM_OK;
+}
+
+int erlbm_set_launch(erlbm_handle *h, int block_threads, int flags)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (block_threads != 0 && block_threads != 128 && block_threads != 256 && block_threads != 512) {
+        set_error("block_threads must be 0, 128, 256 or 512%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    if (flags & ~ERLBM_LAUNCH_STREAMING_STORES) return ERLBM_E_INVAL;
+    h->shape = block_threads | ((flags & ERLBM_LAUNCH_STREAMING_STORES) ? 0x1000 : 0);
     return ERLBM_OK;
 }
 

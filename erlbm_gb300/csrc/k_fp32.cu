@@ -48,9 +48,21 @@ __device__ __forceinline__ void setc(float4 &v, int k, float x)
         v.w = x;
 }
 
-template <int OP>
-__global__ void __launch_bounds__(256) k_periodic_d2q9(const float *__restrict__ src, float *__restrict__ dst, int nx,
-                                                        int ny, long long plane, shifted::Coef k)
+// Store of one direction plane's four nodes: plain, or streaming (evict-first: the next launch
+// reads these lines back, but the lattice is larger than L2, so keeping them there only displaces
+// lines still to be read in this launch).
+template <bool STREAMING>
+__device__ __forceinline__ void store4(float *p, const float4 &v)
+{
+    if (STREAMING)
+        __stcs(reinterpret_cast<float4 *>(p), v);
+    else
+        *reinterpret_cast<float4 *>(p) = v;
+}
+
+template <int OP, int BLOCK, bool STREAMING>
+__global__ void __launch_bounds__(BLOCK) k_periodic_d2q9(const float *__restrict__ src, float *__restrict__ dst, int nx,
+                                                          int ny, long long plane, shifted::Coef k)
 {
     const int lane = threadIdx.x & 31;
     const int wpr = nx >> 7;  // warps per row
@@ -86,7 +98,7 @@ __global__ void __launch_bounds__(256) k_periodic_d2q9(const float *__restrict__
         for (int i = 0; i < 9; i++) setc(v[i], c, g[i]);
     }
 #pragma unroll
-    for (int i = 0; i < 9; i++) *reinterpret_cast<float4 *>(dst + i * plane + ry + x0) = v[i];
+    for (int i = 0; i < 9; i++) store4<STREAMING>(dst + i * plane + ry + x0, v[i]);
 }
 
 }  // namespace
@@ -96,25 +108,55 @@ bool periodic_d2q9_fp32_ok(const Geo &g)
     return g.solid == nullptr && g.nz == 1 && g.nx % 128 == 0 && g.ny >= 2 && g.plane % 4 == 0;
 }
 
-int launch_periodic_d2q9_fp32(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s)
+namespace {
+
+template <int OP, int BLOCK, bool ST>
+void go_periodic(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
+{
+    const long long warps = (long long)(g.nx / 128) * g.ny;
+    const unsigned nb = (unsigned)((warps * 32 + BLOCK - 1) / BLOCK);
+    k_periodic_d2q9<OP, BLOCK, ST><<<nb, BLOCK, 0, s>>>(src, dst, g.nx, g.ny, g.plane, k);
+}
+
+template <int OP>
+int periodic_shape(int block, bool st, const Geo &g, const shifted::Coef &k, const float *src, float *dst,
+                   cudaStream_t s)
+{
+    if (block == 128 && !st) go_periodic<OP, 128, false>(g, k, src, dst, s);
+    else if (block == 128 && st) go_periodic<OP, 128, true>(g, k, src, dst, s);
+    else if (block == 256 && !st) go_periodic<OP, 256, false>(g, k, src, dst, s);
+    else if (block == 256 && st) go_periodic<OP, 256, true>(g, k, src, dst, s);
+    else if (block == 512 && !st) go_periodic<OP, 512, false>(g, k, src, dst, s);
+    else if (block == 512 && st) go_periodic<OP, 512, true>(g, k, src, dst, s);
+    else return -1;
+    return 0;
+}
+
+}  // namespace
+
+// shape: threads per block (128, 256 or 512; 0 = 256) and bit 0x1000 for streaming stores.
+int launch_periodic_d2q9_fp32(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s,
+                              int shape)
 {
     if (!periodic_d2q9_fp32_ok(g)) return -1;
     const shifted::Coef k = shifted::make_coef(R);
-    const long long warps = (long long)(g.nx / 128) * g.ny;
-    const unsigned nb = (unsigned)((warps * 32 + 255) / 256);
+    const int block = (shape & 0xfff) ? (shape & 0xfff) : 256;
+    const bool st = (shape & 0x1000) != 0;
+    int rc;
     switch (op) {
     case OP_BGK:
-        k_periodic_d2q9<OP_BGK><<<nb, 256, 0, s>>>(src, dst, g.nx, g.ny, g.plane, k);
+        rc = periodic_shape<OP_BGK>(block, st, g, k, src, dst, s);
         break;
     case OP_REG:
-        k_periodic_d2q9<OP_REG><<<nb, 256, 0, s>>>(src, dst, g.nx, g.ny, g.plane, k);
+        rc = periodic_shape<OP_REG>(block, st, g, k, src, dst, s);
         break;
     case OP_EXTREG:
-        k_periodic_d2q9<OP_EXTREG><<<nb, 256, 0, s>>>(src, dst, g.nx, g.ny, g.plane, k);
+        rc = periodic_shape<OP_EXTREG>(block, st, g, k, src, dst, s);
         break;
     default:
         return -1;
     }
+    if (rc) return rc;
     return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

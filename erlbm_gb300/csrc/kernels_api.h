@@ -49,8 +49,10 @@ int launch_step_fp64(int q, int op, const Geo &g, const BCp &bc, const Relax &R,
 int launch_step_fp32(int q, int op, const Geo &g, const BCp &bc, const Relax &R, const StepArgs &a, const float *src,
                      float *dst, cudaStream_t s);
 
-// Fused periodic D2Q9 FP32 kernel (nx % 128 == 0, no solids, no boundary planes).
-int launch_periodic_d2q9_fp32(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s);
+// Fused periodic D2Q9 FP32 kernel (nx % 128 == 0, no solids, no boundary planes).  shape: threads
+// per block (128, 256, 512; 0 = 256), plus 0x1000 for streaming (evict-first) stores.
+int launch_periodic_d2q9_fp32(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s,
+                              int shape = 0);
 bool periodic_d2q9_fp32_ok(const Geo &g);
 
 // Stream only: dst = post-stream populations of the post-collision state src (no BC, no collision).

@@ -125,6 +125,11 @@ int erlbm_macroscopic(erlbm_handle *h, int stage, double *rho, double *u);
 int erlbm_run(erlbm_handle *h, int n_steps, const erlbm_bc *bc, const erlbm_checks *chk, erlbm_run_result *res);
 /* wait for the handle's queued work */
 int erlbm_sync(erlbm_handle *h);
+/* launch shape of the fused periodic D2Q9 FP32 kernel (the double-shear-layer lattices): threads per
+ * block (128, 256, 512; 0 = default 256) and flags (ERLBM_LAUNCH_STREAMING_STORES: evict-first
+ * stores).  Chosen by erlbm_gb300.autotune; no counterpart in the reference. */
+#define ERLBM_LAUNCH_STREAMING_STORES 1
+int erlbm_set_launch(erlbm_handle *h, int block_threads, int flags);
 /* run the handle's work on the caller's CUDA stream (a cudaStream_t; NULL = the handle's own
  * stream).  Waits for the work queued so far first.  No counterpart in the reference, whose loops
  * are synchronous; it lets a caller order the engine with its own GPU work and time it with events. */

@@ -178,3 +178,26 @@ def test_run_energy_check_matches_oracle():
             r = lat.run(n_steps, None, energy_every=100, energy_factor=2.0)
         assert (r["label"], r["decided_step"]) == (lab, ds)
         assert r["margin"] == mg
+
+
+def test_fused_kernel_launch_shapes_identical_and_tuned(tmp_path, monkeypatch):
+    """Every launch shape of the fused D2Q9 kernel computes the same bits; the autotuner picks one."""
+    monkeypatch.setenv("ERLBM_TUNE_CACHE", str(tmp_path / "tune.json"))
+    from erlbm_gb300 import autotune
+    L = 256
+    f0 = eg().init_double_shear(L)
+    tau = 0.5 + 3 * (1 / 32) * L / 80000
+    outs = []
+    for block, st in autotune.PERIODIC_CANDIDATES:
+        with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
+            lat.set_launch(block, st)
+            lat.set_populations(f0)
+            lat.step(30)
+            outs.append(lat.get_populations(1))
+    assert all(np.array_equal(o, outs[0]) for o in outs[1:])
+    best = autotune.tune_periodic(L, steps=50)
+    assert (best["block_threads"], best["streaming_stores"]) in autotune.PERIODIC_CANDIDATES
+    assert autotune.tune_periodic(L)["mlups"] == best["mlups"]  # served from the cache
+    with pytest.raises(eg().ErlbmError):
+        with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
+            lat.set_launch(100)
