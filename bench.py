@@ -47,6 +47,12 @@ sys.path.insert(0, ROOT)
 BYTES_PER_LU = {"fp32": 2 * 9 * 4, "fp64": 2 * 9 * 8}
 
 
+# DSL operators as main_double-shear-layer.cpp takes them (--collision; tau_nh = 1 for reg, :89):
+# name -> (op code, tau_nh, label)
+DSL_OPS = {"erlbm": (4, 0.65, "E-RLBM tau_nh=0.65"), "reg": (3, 1.0, "RLBM"), "bgk": (1, 0.65, "BGK"),
+           "mrt": (2, 0.65, "MRT")}
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -55,11 +61,15 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--L", type=int, default=2048)
     p.add_argument("--inner", type=int, default=1000, help="LBM steps per bench step")
-    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "refined"],
+                   help="refined (map workloads): the whole map-points x map-points grid screened in FP32 with "
+                        "the boundary points re-run in FP64")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extras", action="store_true")
     p.add_argument("--workload", default="dsl", choices=["dsl", "tg-map", "obstacle-map", "serve"])
+    p.add_argument("--op", default="erlbm", choices=list(DSL_OPS),
+                   help="dsl: collision operator (main_double-shear-layer.cpp --collision)")
     p.add_argument("--map-points", type=int, default=100, help="P: P x P map points per bench step")
     p.add_argument("--max-steps", type=int, default=0, help="cap on map run budgets (0 = the reference's)")
     p.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
@@ -150,13 +160,14 @@ class Clocks:
 # CPU legs (the only places bench.py executes oracle/)
 # ------------------------------------------------------------------------------------------------
 
-def cpu_sample(L: int, seconds: float, prefer_reference: bool):
+def cpu_sample(L: int, seconds: float, prefer_reference: bool, op_name: str = "erlbm"):
     """Time the reference's CPU algorithm on this host's cores: the reference library compiled from
     its sources (oracle/_ref, only where it was built) or the oracle's restatement of it."""
     import numpy as np
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     tau = tau_of(L)
+    op, tnh, label = DSL_OPS[op_name]
     f0 = O.init_double_shear(L)
     kind = "port"
     if prefer_reference and O.ref_available(9):
@@ -169,11 +180,11 @@ def cpu_sample(L: int, seconds: float, prefer_reference: bool):
 
         def run(n):
             t = time.perf_counter()
-            fn(L, L, 1, None, 4, tau, 0.65, f0.ctypes.data, n, -1, 0.0, -1, 1.0, None, None, None, threads)
+            fn(L, L, 1, None, op, tau, tnh, f0.ctypes.data, n, -1, 0.0, -1, 1.0, None, None, None, threads)
             return time.perf_counter() - t
         kind = "reference"
     else:
-        lat = O.Lattice(9, L, L, 1, None, tau, 0.65, O.OP_EXTREG)
+        lat = O.Lattice(9, L, L, 1, None, tau, tnh, op)
         lat.set(f0)
 
         def run(n):
@@ -187,7 +198,7 @@ def cpu_sample(L: int, seconds: float, prefer_reference: bool):
         dt = max(dt - run(1) + t1, 1e-9)
     mlups = L * L * n / dt / 1e6
     return {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": kind,
-            "sample": f"double shear layer D2Q9 E-RLBM FP64, L={L}, {n} steps, {threads} OpenMP threads"}
+            "sample": f"double shear layer D2Q9 {label} FP64, L={L}, {n} steps, {threads} OpenMP threads"}
 
 
 def run_reference(args):
@@ -198,8 +209,8 @@ def run_reference(args):
     # each bench step is a bounded sample; warm-up samples are shorter
     per = max(1.0, min(8.0, 120.0 / max(1, K + W)))
     for _ in range(W):
-        cpu_sample(args.L, per / 4, True)
-    vals = [cpu_sample(args.L, per, True) for _ in range(K)]
+        cpu_sample(args.L, per / 4, True, args.op)
+    vals = [cpu_sample(args.L, per, True, args.op) for _ in range(K)]
     v = statistics.median(x["value"] for x in vals)
     cb = dict(vals[-1])
     cb["value"] = v
@@ -207,7 +218,7 @@ def run_reference(args):
     line = {"metric": "MLUPS", "value": v, "unit": "MLUPS", "n_gpus": args.gpus, "steps": K, "warmup": W,
             "ms_per_step": L * L * args.inner / (v * 1e6) * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (double shear layer initial condition)",
-            "config": {"workload": f"double shear layer D2Q9 E-RLBM tau_nh=0.65 Re=80000 L={L}", "L": L,
+            "config": {"workload": f"double shear layer D2Q9 {DSL_OPS[args.op][2]} Re=80000 L={L}", "L": L,
                        "lbm_steps_per_step": args.inner, "precision": "fp64 (reference CPU path)"},
             "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -241,7 +252,8 @@ def run_ours(args):
     tau = tau_of(L)
     f0 = E.init_double_shear(L)
     stream = torch.cuda.Stream()
-    lat = E.Lattice(9, L, L, 1, None, tau, 0.65, E.OP_EXTREG, prec)
+    op, tnh, op_label = DSL_OPS[args.op]
+    lat = E.Lattice(9, L, L, 1, None, tau, tnh, op, prec)
     shape = None
     if args.precision == "fp32" and L % 128 == 0:
         from erlbm_gb300 import autotune  # launch shape chosen by measurement (cached), outside the timed region
@@ -306,7 +318,7 @@ def run_ours(args):
 
     extras = {}
     if not args.no_extras and rank == 0:
-        extras = gpu_extras(E, torch, L, f0, tau, prec)
+        extras = gpu_extras(E, torch, L, f0, tau, op, tnh)
     lat.close()
 
     if rank != 0:
@@ -315,13 +327,13 @@ def run_ours(args):
         return 0
     cpu = None
     if world == 1 and not args.no_cpu:
-        cpu = cpu_sample(L, args.cpu_seconds, False)
+        cpu = cpu_sample(L, args.cpu_seconds, False, args.op)
     line = {
         "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.precision == "fp32" else "f64",
         "data": "synthetic (double shear layer initial condition, main_double-shear-layer.cpp:48-66)",
-        "config": {"workload": f"double shear layer D2Q9 E-RLBM tau_nh=0.65 Re=80000 L={L}, "
+        "config": {"workload": f"double shear layer D2Q9 {op_label} Re=80000 L={L}, "
                                f"{'FP32-shifted' if args.precision == 'fp32' else 'FP64 plain'}",
                    "L": L, "lbm_steps_per_step": inner, "parallelism": f"replicas x{world}",
                    "l2": f"working set {2 * BYTES_PER_LU[args.precision] // 2 * L * L / 1e6:.0f} MB > 129 MB L2, "
@@ -329,9 +341,9 @@ def run_ours(args):
                    "launch_shape": None if shape is None else {"block_threads": shape["block_threads"],
                                                                "streaming_stores": shape["streaming_stores"]}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": ncu_traffic(L, args.precision),
+                     "peak_kind": peak_kind, "traffic": ncu_traffic(L, args.precision) if args.op == "erlbm" else None,
                      "algorithmic_bytes_per_launch": algo_bytes, "launch_us": launch_ms * 1e3,
-                     "kernel": "k_periodic_d2q9" if args.precision == "fp32" else "k_step<PrecExact64,9,EXTREG>"},
+                     "kernel": f"k_periodic_d2q9<{op}>" if args.precision == "fp32" else f"k_step<PrecExact64,9,{op}>"},
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
@@ -346,14 +358,14 @@ def run_ours(args):
     return 0
 
 
-def gpu_extras(E, torch, L, f0, tau, prec):
+def gpu_extras(E, torch, L, f0, tau, op, tnh):
     """Secondary figures of the metric line: the plain FP64 path on the same lattice and the
     FP32-shifted velocity error against it after a short common run."""
     import numpy as np
     out = {}
     n64 = 200
     s = torch.cuda.Stream()
-    with E.Lattice(9, L, L, 1, None, tau, 0.65, E.OP_EXTREG, E.FP64) as l64:
+    with E.Lattice(9, L, L, 1, None, tau, tnh, op, E.FP64) as l64:
         l64.set_stream(s.cuda_stream)
         l64.set_populations(f0)
         l64.step(1 + 10)
@@ -368,7 +380,7 @@ def gpu_extras(E, torch, L, f0, tau, prec):
         out["fp64_plain_launch_us"] = ms / n64 * 1e3
         # velocity error of FP32-shifted vs FP64 after the same 1 + 10 + n64 steps
         _, u64 = l64.macroscopic(E.STAGE_POST_COLLISION)
-    with E.Lattice(9, L, L, 1, None, tau, 0.65, E.OP_EXTREG, E.FP32_SHIFTED) as l32:
+    with E.Lattice(9, L, L, 1, None, tau, tnh, op, E.FP32_SHIFTED) as l32:
         l32.set_populations(f0)
         l32.step(1 + 10 + n64)
         _, u32 = l32.macroscopic(E.STAGE_POST_COLLISION)
@@ -388,37 +400,53 @@ def run_map(args):
     import erlbm_gb300 as E
     torch.cuda.set_device(0)
     kind = E.MAP_TAYLOR_GREEN if args.workload == "tg-map" else E.MAP_OBSTACLE
-    prec = E.FP32_SHIFTED if args.precision == "fp32" else E.FP64
+    refined = args.precision == "refined"
+    prec = E.FP64 if args.precision == "fp64" else E.FP32_SHIFTED
     pts = map_points(args.map_points)
+    P = args.map_points
+
+    def one_map(points):
+        if refined:  # the whole P x P grid of the map's axes; refinement needs neighbours
+            lab, dec, _, ref = E.map_run_refined(kind, op=op, n_i=P, n_j=P, max_steps=args.max_steps, slots=-1)
+            return lab, dec, int(ref.sum())
+        lab, dec, _ = E.map_run(kind, points, precision=prec, op=op, max_steps=args.max_steps, slots=-1)
+        return lab, dec, 0
+
     op = 0 if kind == E.MAP_TAYLOR_GREEN else E.OP_EXTREG
     nodes = 256 if kind == E.MAP_TAYLOR_GREEN else 232
     from erlbm_gb300 import autotune
     tuned = autotune.tune_map(kind, prec)  # cached after the first run; outside the timed region
     for _ in range(args.warmup):
         E.map_run(kind, pts[: max(1, len(pts) // 8)], precision=prec, op=op, max_steps=args.max_steps, slots=-1)
+    if refined:
+        autotune.tune_map(kind, E.FP64)
     torch.cuda.synchronize()
     clocks = Clocks(0)
     clocks.start()
     t0 = time.perf_counter()
-    runs, lus = 0, 0
+    runs, lus, n_ref = 0, 0, 0
     for _ in range(args.steps):
-        lab, dec, _ = E.map_run(kind, pts, precision=prec, op=op, max_steps=args.max_steps, slots=-1)
+        lab, dec, nr = one_map(pts)
         runs += len(lab)
+        n_ref += nr
         lus += int(np.sum(dec.astype(np.int64))) * nodes
     dt = time.perf_counter() - t0
     clk = clocks.stop()
     value = runs / dt
     line = {"metric": "map runs/s", "value": value, "unit": "runs/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec else "f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if refined else ("f32" if prec else "f64"),
             "data": "synthetic (the reference's map axes)",
-            "config": {"workload": f"{args.workload} D3Q19, {args.map_points}x{args.map_points} points of the 400x400 "
-                                   f"grid{' x {RLBM, E-RLBM}' if op == 0 else ''}, max_steps={args.max_steps}",
+            "config": {"workload": f"{args.workload} D3Q19, "
+                                   + (f"whole {P}x{P} grid" if refined else f"{P}x{P} points of the 400x400 grid")
+                                   + f"{' x {RLBM, E-RLBM}' if op == 0 else ''}, max_steps={args.max_steps}",
                        "precision": args.precision, "slots_per_sm": tuned["slots"]},
             "lattice_updates_per_s": lus / dt, "roofline": None,
             "e2e": {"value": value, "unit": "runs/s", "h2d_bytes_per_step": len(pts) * 48,
                     "d2h_bytes_per_step": len(pts) * 32},
-            "gpu_launches": args.steps, "clocks": clk}
+            "gpu_launches": args.steps * (2 if refined else 1), "clocks": clk}
+    if refined:
+        line["refined_fraction"] = n_ref / runs
     if not args.no_cpu:
         from oracle import oracle as O
         few = pts[:: max(1, len(pts) // 16)]

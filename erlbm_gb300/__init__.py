@@ -20,8 +20,8 @@ from ._lib import (FP32_SHIFTED, FP64, INIT_AOS, INIT_REST, INIT_TG_MAP, MAP_OBS
 __all__ = ["Lattice", "ErlbmError", "lib", "OP_BGK", "OP_MRT", "OP_REG", "OP_EXTREG", "FP64", "FP32_SHIFTED",
            "STAGE_POST_STREAM", "STAGE_POST_COLLISION", "MAP_TAYLOR_GREEN", "MAP_OBSTACLE", "init_taylor_green",
            "init_double_shear", "equilibrium", "obstacle_geometry", "taylor_green_error", "tg_map_params",
-           "obstacle_map_params", "operator_from_name", "map_run", "batch_run", "INIT_REST", "INIT_TG_MAP",
-           "INIT_AOS", "Server", "REQ_TG2D", "REQ_TG_MAP_POINT", "REQ_OBSTACLE", "REQ_TG3D"]
+           "obstacle_map_params", "operator_from_name", "map_run", "map_run_refined", "batch_run", "INIT_REST",
+           "INIT_TG_MAP", "INIT_AOS", "Server", "REQ_TG2D", "REQ_TG_MAP_POINT", "REQ_OBSTACLE", "REQ_TG3D"]
 
 _OPS = {"bgk": OP_BGK, "mrt": OP_MRT, "reg": OP_REG, "erlbm": OP_EXTREG}
 
@@ -230,6 +230,26 @@ def map_run(kind: int, points=None, precision: int = FP64, op: int = OP_EXTREG, 
     mg = np.zeros(m, np.float64)
     check(lib().erlbm_map_run(C.byref(d), _dptr(labels), _dptr(dec), _dptr(mg)), "erlbm_map_run")
     return labels, dec, mg
+
+
+def map_run_refined(kind: int, op: int = OP_EXTREG, tau_nh: float = 0.65, L: int = 16, ma: float = 0.1,
+                    n_i: int = 400, n_j: int = 400, max_steps: int = 0, slots: int = 0, radius: int = 2,
+                    late_fraction: float = 0.3):
+    """A whole stability map screened in FP32-shifted, with the boundary points refined in FP64.
+
+    Points whose FP32 label differs from a neighbour within `radius` map steps, or whose FP32 run
+    turned unstable after `late_fraction` of its budget, are run again in FP64 (the reference's
+    results).  Returns (labels, decided_step, margins, refined) with refined a boolean mask.
+    """
+    d = _lib.MapDesc(kind, FP32_SHIFTED, op, tau_nh, L, ma, n_i, n_j, 0, None, None, max_steps, slots)
+    m = n_i * n_j * (2 if (kind == MAP_TAYLOR_GREEN and op == 0) else 1)
+    labels = np.zeros(m, np.int32)
+    dec = np.zeros(m, np.int32)
+    mg = np.zeros(m, np.float64)
+    ref = np.zeros(m, np.uint8)
+    check(lib().erlbm_map_run_refined(C.byref(d), radius, late_fraction, _dptr(labels), _dptr(dec), _dptr(mg),
+                                      _dptr(ref)), "erlbm_map_run_refined")
+    return labels, dec, mg, ref.astype(bool)
 
 
 def batch_run(q: int, nx: int, ny: int, runs, precision: int = FP64, solid=None, inlet_x: int = -1,

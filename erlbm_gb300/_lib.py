@@ -109,6 +109,8 @@ _SIGS = {
     "erlbm_batch_run": (C.c_int, [C.POINTER(BatchDesc), C.c_int, C.POINTER(RunSpec), C.c_void_p, C.c_size_t,
                                   C.POINTER(BatchResult)]),
     "erlbm_map_run": (C.c_int, [C.POINTER(MapDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "erlbm_map_run_refined": (C.c_int, [C.POINTER(MapDesc), C.c_int, C.c_double, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]),
     "erlbm_server_start": (C.c_int, [C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),
     "erlbm_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),
     "erlbm_server_poll": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(Result)]),

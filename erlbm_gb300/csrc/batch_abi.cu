@@ -129,8 +129,9 @@ int run_batch(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec *runs,
     }
     for (int k = 0; k < n_runs; k++) {
         const erlbm_run_spec &s = runs[order[k]];
-        if (s.op != ERLBM_OP_BGK && s.op != ERLBM_OP_REG && s.op != ERLBM_OP_EXTREG) {
-            set_error("run %s: unknown or unsupported collision operator%s", std::to_string(order[k]).c_str(), "");
+        if (s.op != ERLBM_OP_BGK && s.op != ERLBM_OP_REG && s.op != ERLBM_OP_EXTREG &&
+            !(s.op == ERLBM_OP_MRT && d->q == 9)) {
+            set_error("run %s: unknown collision operator, or MRT on D3Q19%s", std::to_string(order[k]).c_str(), "");
             return s.op == ERLBM_OP_MRT ? ERLBM_E_UNSUPPORTED : ERLBM_E_INVAL;
         }
         if (!(s.tau > 0) || !std::isfinite(s.tau) || !std::isfinite(s.tau_nh) || s.tau_nh == 0 || s.n_steps < 0)
@@ -234,6 +235,88 @@ int run_batch(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec *runs,
 
 }  // namespace erlbm
 
+// The run table of a stability map: one erlbm_run_spec per point (per operator, RLBM first when
+// op = 0), the batch descriptor, and the obstacle's solid mask (bd->solid points into it).
+static int build_map_runs(const erlbm_map_desc *d, erlbm_batch_desc *bd, std::vector<erlbm_run_spec> *runs,
+                          std::vector<uint8_t> *solid, int *n_ops)
+{
+    if (d->n_i < 1 || d->n_j < 1) return ERLBM_E_INVAL;
+    const int npts = d->n_points > 0 ? d->n_points : d->n_i * d->n_j;
+    if (d->n_points > 0 && (!d->pi || !d->pj)) return ERLBM_E_INVAL;
+    std::vector<int> ops;
+    if (d->kind == ERLBM_MAP_TAYLOR_GREEN) {
+        if (d->op == 0) ops = {ERLBM_OP_REG, ERLBM_OP_EXTREG};
+        else if (d->op == ERLBM_OP_REG || d->op == ERLBM_OP_EXTREG || d->op == ERLBM_OP_BGK) ops = {d->op};
+        else return d->op == ERLBM_OP_MRT ? ERLBM_E_UNSUPPORTED : ERLBM_E_INVAL;
+    } else if (d->kind == ERLBM_MAP_OBSTACLE) {
+        ops = {ERLBM_OP_EXTREG};  // the obstacle program always uses coll_Ext_Reg (:102)
+    } else {
+        return ERLBM_E_INVAL;
+    }
+    *n_ops = (int)ops.size();
+    const int n_runs = npts * (int)ops.size();
+    runs->assign(n_runs, erlbm_run_spec{});
+    memset(bd, 0, sizeof(*bd));
+    bd->precision = d->precision;
+    bd->slots = d->slots;
+    if (d->kind == ERLBM_MAP_TAYLOR_GREEN) {
+        const int L = d->L > 0 ? d->L : 16;
+        bd->q = 19;
+        bd->nx = bd->ny = L;
+        bd->inlet_x = bd->outlet_x = -1;
+        bd->rho0 = 1.0;
+        bd->energy_every = 100;    // :71
+        bd->energy_factor = 2.0;   // :75
+        bd->init = ERLBM_INIT_TG_MAP;
+        for (size_t o = 0; o < ops.size(); o++)
+            for (int k = 0; k < npts; k++) {
+                const int i = d->n_points > 0 ? d->pi[k] : k % d->n_i;
+                const int j = d->n_points > 0 ? d->pj[k] : k / d->n_i;
+                double u0, tau, tau_nh;
+                erlbm_tg_map_params(i, j, d->n_i, d->n_j, ops[o], d->tau_nh, &u0, &tau, &tau_nh);
+                erlbm_run_spec &r = (*runs)[o * npts + k];
+                r.op = ops[o];
+                r.tau = tau;
+                r.tau_nh = tau_nh;
+                r.u0 = u0;
+                r.n_steps = (int)((double)(100 * L) / u0);  // :63, 100 T
+                if (d->max_steps > 0 && r.n_steps > d->max_steps) r.n_steps = d->max_steps;
+                r.aos_offset = 0;
+            }
+    } else {
+        int nx, ny;
+        erlbm_obstacle_geometry(1, 1, &nx, &ny, nullptr);
+        solid->resize((size_t)nx * ny);
+        erlbm_obstacle_geometry(1, 1, &nx, &ny, solid->data());
+        bd->q = 19;
+        bd->nx = nx;
+        bd->ny = ny;
+        bd->solid = solid->data();
+        bd->inlet_x = 1;            // :92
+        bd->outlet_x = nx - 2;      // :94
+        bd->rho0 = 1.0;
+        bd->density_check = 1;      // :104-106
+        bd->density_limit = 10.0;
+        bd->init = ERLBM_INIT_REST; // :81-82
+        const double ma = d->ma > 0 ? d->ma : 0.1;
+        for (int k = 0; k < npts; k++) {
+            const int i = d->n_points > 0 ? d->pi[k] : k % d->n_i;
+            const int j = d->n_points > 0 ? d->pj[k] : k / d->n_i;
+            double u_imp, tau, tau_nh;
+            erlbm_obstacle_map_params(i, j, d->n_i, d->n_j, ma, &u_imp, &tau, &tau_nh);
+            erlbm_run_spec &r = (*runs)[k];
+            r.op = ERLBM_OP_EXTREG;
+            r.tau = tau;
+            r.tau_nh = tau_nh;
+            r.u0 = u_imp;
+            r.n_steps = (int)((double)(200 * ny) / u_imp);  // :84
+            if (d->max_steps > 0 && r.n_steps > d->max_steps) r.n_steps = d->max_steps;
+            r.aos_offset = 0;
+        }
+    }
+    return ERLBM_OK;
+}
+
 extern "C" {
 
 int erlbm_batch_run(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec *runs, const double *aos,
@@ -249,84 +332,81 @@ int erlbm_batch_run(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec 
 int erlbm_map_run(const erlbm_map_desc *d, int32_t *labels, int32_t *decided_step, double *margins)
 {
     if (!d || !labels) return ERLBM_E_INVAL;
-    if (d->n_i < 1 || d->n_j < 1) return ERLBM_E_INVAL;
-    const int npts = d->n_points > 0 ? d->n_points : d->n_i * d->n_j;
-    if (d->n_points > 0 && (!d->pi || !d->pj)) return ERLBM_E_INVAL;
-    std::vector<int> ops;
-    if (d->kind == ERLBM_MAP_TAYLOR_GREEN) {
-        if (d->op == 0) ops = {ERLBM_OP_REG, ERLBM_OP_EXTREG};
-        else if (d->op == ERLBM_OP_REG || d->op == ERLBM_OP_EXTREG || d->op == ERLBM_OP_BGK) ops = {d->op};
-        else return d->op == ERLBM_OP_MRT ? ERLBM_E_UNSUPPORTED : ERLBM_E_INVAL;
-    } else if (d->kind == ERLBM_MAP_OBSTACLE) {
-        ops = {ERLBM_OP_EXTREG};  // the obstacle program always uses coll_Ext_Reg (:102)
-    } else {
+    erlbm_batch_desc bd;
+    std::vector<erlbm_run_spec> runs;
+    std::vector<uint8_t> solid;
+    int n_ops = 0;
+    int rc = build_map_runs(d, &bd, &runs, &solid, &n_ops);
+    if (rc) return rc;
+    const int n_runs = (int)runs.size();
+    std::vector<erlbm_batch_result> res(n_runs);
+    rc = erlbm_batch_run(&bd, n_runs, runs.data(), nullptr, 0, res.data());
+    if (rc) return rc;
+    for (int k = 0; k < n_runs; k++) {
+        labels[k] = res[k].label;
+        if (decided_step) decided_step[k] = res[k].decided_step;
+        if (margins) margins[k] = res[k].margin;
+    }
+    return ERLBM_OK;
+}
+
+int erlbm_map_run_refined(const erlbm_map_desc *d, int radius, double late_fraction, int32_t *labels,
+                          int32_t *decided_step, double *margins, uint8_t *refined)
+{
+    if (!d || !labels) return ERLBM_E_INVAL;
+    if (d->n_points != 0) {
+        set_error("a refined map needs the whole n_i x n_j grid (n_points = 0)%s%s", "", "");
         return ERLBM_E_INVAL;
     }
-    const int n_runs = npts * (int)ops.size();
-    std::vector<erlbm_run_spec> runs(n_runs);
-    erlbm_batch_desc bd;
-    memset(&bd, 0, sizeof(bd));
-    bd.precision = d->precision;
-    bd.slots = d->slots;
-    std::vector<uint8_t> solid;
-    if (d->kind == ERLBM_MAP_TAYLOR_GREEN) {
-        const int L = d->L > 0 ? d->L : 16;
-        bd.q = 19;
-        bd.nx = bd.ny = L;
-        bd.inlet_x = bd.outlet_x = -1;
-        bd.rho0 = 1.0;
-        bd.energy_every = 100;    // :71
-        bd.energy_factor = 2.0;   // :75
-        bd.init = ERLBM_INIT_TG_MAP;
-        for (size_t o = 0; o < ops.size(); o++)
-            for (int k = 0; k < npts; k++) {
-                const int i = d->n_points > 0 ? d->pi[k] : k % d->n_i;
-                const int j = d->n_points > 0 ? d->pj[k] : k / d->n_i;
-                double u0, tau, tau_nh;
-                erlbm_tg_map_params(i, j, d->n_i, d->n_j, ops[o], d->tau_nh, &u0, &tau, &tau_nh);
-                erlbm_run_spec &r = runs[o * npts + k];
-                r.op = ops[o];
-                r.tau = tau;
-                r.tau_nh = tau_nh;
-                r.u0 = u0;
-                r.n_steps = (int)((double)(100 * L) / u0);  // :63, 100 T
-                if (d->max_steps > 0 && r.n_steps > d->max_steps) r.n_steps = d->max_steps;
-                r.aos_offset = 0;
-            }
-    } else {
-        int nx, ny;
-        erlbm_obstacle_geometry(1, 1, &nx, &ny, nullptr);
-        solid.resize((size_t)nx * ny);
-        erlbm_obstacle_geometry(1, 1, &nx, &ny, solid.data());
-        bd.q = 19;
-        bd.nx = nx;
-        bd.ny = ny;
-        bd.solid = solid.data();
-        bd.inlet_x = 1;            // :92
-        bd.outlet_x = nx - 2;      // :94
-        bd.rho0 = 1.0;
-        bd.density_check = 1;      // :104-106
-        bd.density_limit = 10.0;
-        bd.init = ERLBM_INIT_REST; // :81-82
-        const double ma = d->ma > 0 ? d->ma : 0.1;
-        for (int k = 0; k < npts; k++) {
-            const int i = d->n_points > 0 ? d->pi[k] : k % d->n_i;
-            const int j = d->n_points > 0 ? d->pj[k] : k / d->n_i;
-            double u_imp, tau, tau_nh;
-            erlbm_obstacle_map_params(i, j, d->n_i, d->n_j, ma, &u_imp, &tau, &tau_nh);
-            erlbm_run_spec &r = runs[k];
-            r.op = ERLBM_OP_EXTREG;
-            r.tau = tau;
-            r.tau_nh = tau_nh;
-            r.u0 = u_imp;
-            r.n_steps = (int)((double)(200 * ny) / u_imp);  // :84
-            if (d->max_steps > 0 && r.n_steps > d->max_steps) r.n_steps = d->max_steps;
-            r.aos_offset = 0;
-        }
+    if (radius < 0 || radius > 64 || !(late_fraction <= 1.0)) {
+        set_error("refine radius must lie in [0, 64] and late_fraction be at most 1%s%s", "", "");
+        return ERLBM_E_INVAL;
     }
-    std::vector<erlbm_batch_result> res(n_runs);
-    const int rc = erlbm_batch_run(&bd, n_runs, runs.data(), nullptr, 0, res.data());
+    erlbm_batch_desc bd;
+    std::vector<erlbm_run_spec> runs;
+    std::vector<uint8_t> solid;
+    int n_ops = 0;
+    int rc = build_map_runs(d, &bd, &runs, &solid, &n_ops);
     if (rc) return rc;
+    const int ni = d->n_i, nj = d->n_j, n_runs = (int)runs.size();
+    // pass 1: every point in FP32-shifted
+    std::vector<erlbm_batch_result> res(n_runs);
+    bd.precision = ERLBM_FP32_SHIFTED;
+    rc = erlbm_batch_run(&bd, n_runs, runs.data(), nullptr, 0, res.data());
+    if (rc) return rc;
+    // selection, per operator plane: a label differs inside the (2r+1)^2 window of map neighbours
+    // (the stability boundary), or an FP32 instability was found after late_fraction of the budget
+    std::vector<int> pick;
+    for (int o = 0; o < n_ops; o++) {
+        const erlbm_batch_result *plane = res.data() + (size_t)o * ni * nj;
+        for (int j = 0; j < nj; j++)
+            for (int i = 0; i < ni; i++) {
+                const int k = j * ni + i, lab = plane[k].label;
+                bool sel = late_fraction > 0.0 && lab == 1 &&
+                           plane[k].decided_step > late_fraction * runs[(size_t)o * ni * nj + k].n_steps;
+                for (int jj = std::max(0, j - radius); !sel && jj <= std::min(nj - 1, j + radius); jj++)
+                    for (int ii = std::max(0, i - radius); ii <= std::min(ni - 1, i + radius); ii++)
+                        if (plane[jj * ni + ii].label != lab) {
+                            sel = true;
+                            break;
+                        }
+                if (sel) pick.push_back(o * ni * nj + k);
+            }
+    }
+    // pass 2: the selected runs again in FP64, whose results are the reference's
+    if (!pick.empty()) {
+        std::vector<erlbm_run_spec> sub(pick.size());
+        for (size_t m = 0; m < pick.size(); m++) sub[m] = runs[pick[m]];
+        std::vector<erlbm_batch_result> r64(pick.size());
+        bd.precision = ERLBM_FP64;
+        rc = erlbm_batch_run(&bd, (int)sub.size(), sub.data(), nullptr, 0, r64.data());
+        if (rc) return rc;
+        for (size_t m = 0; m < pick.size(); m++) res[pick[m]] = r64[m];
+    }
+    if (refined) {
+        memset(refined, 0, (size_t)n_runs);
+        for (int k : pick) refined[k] = 1;
+    }
     for (int k = 0; k < n_runs; k++) {
         labels[k] = res[k].label;
         if (decided_step) decided_step[k] = res[k].decided_step;

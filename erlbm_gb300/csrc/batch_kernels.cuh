@@ -86,6 +86,12 @@ __device__ __forceinline__ void batch_collide(typename P::T *f, const BatchRun &
     CollParams prm;
     prm.R = r.R;
     prm.k = r.k;
+    if constexpr (Q == 9) {
+        if (r.op == OP_MRT) {
+            P::template collide<Q, OP_MRT>(f, prm);
+            return;
+        }
+    }
     if (r.op == OP_BGK)
         P::template collide<Q, OP_BGK>(f, prm);
     else if (r.op == OP_REG)

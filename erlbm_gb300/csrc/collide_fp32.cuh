@@ -43,7 +43,7 @@ __host__ __device__ inline Coef make_coef(const Relax &R)
 {
     Coef k;
     k.d1 = (float)(2.0 - R.inv_tau);
-    if (R.op == OP_BGK)
+    if (R.op == OP_BGK || R.op == OP_MRT)
         k.kd = 0.f;
     else if (R.op == OP_REG)
         k.kd = -1.f;
@@ -118,6 +118,33 @@ __device__ __forceinline__ void collide9(float g[9], const Coef &k)
     const float doM = fmaf(-3.f * W2, cmM, oM);
     const float doX = -(doP + doM);
     const float doY = -(doP - doM);
+    if constexpr (OP == OP_MRT) {
+        // coll_MRT (Collision_operators.cpp:583-699) as an increment on the non-equilibrium part n:
+        // f* = f - M^-1 S M n.  With A = deX + deY, B = deP + deM and the closed parts substituted,
+        // the relaxed moments of n are e = 6A + 12B, eps = -12A - 6B, qx = 6 (doP + doM),
+        // qy = 6 (doP - doM), pxx = 2 (deX - deY), pxy = 2 (deP - deM); back through M^-1 the odd
+        // parts relax with s_q alone, and the even parts take hE = s_e e / 36, hP = s_eps eps / 36 and
+        // the shear part, written with delta = 2 - 1/tau as s_nu x / 2 = x - delta x / 2.
+        const float A = deX + deY, B = deP + deM;
+        const float hE = (float)(MRT9_SE / 6.0) * fmaf(2.f, B, A);
+        const float hP = (float)(MRT9_SEPS / 6.0) * fmaf(-2.f, A, -B);
+        const float sX = deX - deY, sP = deP - deM;
+        const float vX = fmaf(-0.5f * k.d1, sX, sX), vP = fmaf(-0.5f * k.d1, sP, sP);
+        const float ax = fmaf(2.f, hP, hE), ap = -fmaf(2.f, hE, hP);
+        const float eX = ax - vX, eY = ax + vX, eP = ap - vP, eM = ap + vP;
+        const float oP = (float)-MRT9_SQ * doP, oM = (float)-MRT9_SQ * doM;
+        const float oX = -(oP + oM), oY = -(oP - oM);
+        g[0] += -2.f * ((eX + eY) + (eP + eM));
+        g[1] += eX + oX;
+        g[2] += eX - oX;
+        g[3] += eY + oY;
+        g[4] += eY - oY;
+        g[5] += eP + oP;
+        g[6] += eP - oP;
+        g[7] += eM + oM;
+        g[8] += eM - oM;
+        return;
+    }
     float f10 = 0.f, f1X = 0.f, f1Y = 0.f, f1P = 0.f, f1M = 0.f;
     if (OP != OP_BGK) {
         const float pxx = 2.f * (deX + (deP + deM));
@@ -235,6 +262,7 @@ __device__ __forceinline__ void collide19(float g[19], const Coef &k)
 template <int Q, int OP>
 __device__ __forceinline__ void collide(float *g, const Coef &k)
 {
+    static_assert(Q == 9 || OP != OP_MRT, "MRT is a D2Q9 operator");
     if constexpr (Q == 9)
         collide9<OP>(g, k);
     else

@@ -10,6 +10,7 @@
 //        coll_Ext_Reg    Collision_operators.cpp:1182-1307  (Pi accumulation, f1, f_gt1, update)
 //        coll_Reg        Collision_operators.cpp:860-967
 //        coll_BGK        Collision_operators.cpp:12-49
+//        coll_MRT        Collision_operators.cpp:583-699 (D2Q9)
 //  (3) the only operations left out are exact ones: products by the velocity components
 //      c in {-1, 0, +1}, sums with +-0 (the terms whose coefficient is zero), and the source
 //      term S of source() (LBM_functions.cpp:5646-5716), which is +-0 for every finite state
@@ -79,12 +80,83 @@ __device__ __forceinline__ void equilibrium9(double rho, double ux, double uy, d
     feq_pair(ux - uy, wr2, C, feq[7], feq[8]);
 }
 
+// Row ROW of the MRT transform applied to f: the reference sums M[ROW][i] * f[i] from 0.0 in
+// column order.  Terms with M = 0 add +-0 and are left out; products by +-1 are exact.
+template <int ROW>
+__device__ __forceinline__ double mrt9_row(const double f[9])
+{
+    double acc = 0.0;
+    bool first = true;
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+        const int m = mrt9_m(ROW, i);
+        if (m == 0) continue;
+        const double t = m == 1 ? f[i] : (m == -1 ? -f[i] : (double)m * f[i]);
+        acc = first ? t : acc + t;
+        first = false;
+    }
+    return acc;
+}
+
+// Population I from the moments: sum over c of M^-1[I][c] * m[c] from 0.0, M^-1[I][c] =
+// M[c][I] / |row c|^2 (a correctly rounded quotient, the value of the reference's literal).
+template <int I>
+__device__ __forceinline__ double mrt9_back(const double m[9])
+{
+    double acc = 0.0;
+    bool first = true;
+#pragma unroll
+    for (int c = 0; c < 9; c++) {
+        const int a = mrt9_m(c, I);
+        if (a == 0) continue;
+        const double t = ((double)a / (double)mrt9_norm2(c)) * m[c];
+        acc = first ? t : acc + t;
+        first = false;
+    }
+    return acc;
+}
+
+// coll_MRT, D2Q9: moments m = M f and m_eq = M f_eq; m <- m - s (m - m_eq) on the non-conserved
+// rows (the conserved rows have s = 0, and the force moments are those of a zero force); f = M^-1 m.
+__device__ __forceinline__ void collide9_mrt(double f[9], const Relax &R, const double feq[9])
+{
+    double m[9];
+    m[0] = mrt9_row<0>(f);
+    m[3] = mrt9_row<3>(f);
+    m[5] = mrt9_row<5>(f);
+    m[1] = mrt9_row<1>(f);
+    m[1] = m[1] - MRT9_SE * (m[1] - mrt9_row<1>(feq));
+    m[2] = mrt9_row<2>(f);
+    m[2] = m[2] - MRT9_SEPS * (m[2] - mrt9_row<2>(feq));
+    m[4] = mrt9_row<4>(f);
+    m[4] = m[4] - MRT9_SQ * (m[4] - mrt9_row<4>(feq));
+    m[6] = mrt9_row<6>(f);
+    m[6] = m[6] - MRT9_SQ * (m[6] - mrt9_row<6>(feq));
+    m[7] = mrt9_row<7>(f);
+    m[7] = m[7] - R.inv_tau * (m[7] - mrt9_row<7>(feq));
+    m[8] = mrt9_row<8>(f);
+    m[8] = m[8] - R.inv_tau * (m[8] - mrt9_row<8>(feq));
+    f[0] = mrt9_back<0>(m);
+    f[1] = mrt9_back<1>(m);
+    f[2] = mrt9_back<2>(m);
+    f[3] = mrt9_back<3>(m);
+    f[4] = mrt9_back<4>(m);
+    f[5] = mrt9_back<5>(m);
+    f[6] = mrt9_back<6>(m);
+    f[7] = mrt9_back<7>(m);
+    f[8] = mrt9_back<8>(m);
+}
+
 template <int OP>
 __device__ __forceinline__ void collide9(double f[9], const Relax &R)
 {
     double rho, ux, uy, feq[9];
     moments9(f, rho, ux, uy);
     equilibrium9(rho, ux, uy, feq);
+    if constexpr (OP == OP_MRT) {
+        collide9_mrt(f, R, feq);
+        return;
+    }
     if (OP == OP_BGK) {
 #pragma unroll
         for (int i = 0; i < 9; i++) f[i] = f[i] + (feq[i] - f[i]) * R.inv_tau;
@@ -213,6 +285,7 @@ __device__ __forceinline__ void collide19(double f[19], const Relax &R)
 template <int Q, int OP>
 __device__ __forceinline__ void collide(double *f, const Relax &R)
 {
+    static_assert(Q == 9 || OP != OP_MRT, "MRT is a D2Q9 operator");
     if constexpr (Q == 9)
         collide9<OP>(f, R);
     else

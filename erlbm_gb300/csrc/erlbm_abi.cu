@@ -94,14 +94,17 @@ int check_handle(const erlbm_handle *h)
     return ERLBM_OK;
 }
 
-int check_op(int op)
+// MRT exists for D2Q9 only: the reference's dispatch compiles coll_MRT into D2Q9 builds alone
+// (src/erlbm_common.h:74-76), and a D3Q19 build given "mrt" collides nothing.
+int check_op(int op, int q)
 {
     if (op == ERLBM_OP_BGK || op == ERLBM_OP_REG || op == ERLBM_OP_EXTREG) return ERLBM_OK;
     if (op == ERLBM_OP_MRT) {
-        set_error("collision operator MRT is not provided by this library%s%s", "", "");
+        if (q == 9) return ERLBM_OK;
+        set_error("collision operator MRT is a D2Q9 operator%s%s", "", "");
         return ERLBM_E_UNSUPPORTED;
     }
-    set_error("unknown collision operator (use BGK=1, REG=3, EXTREG=4)%s%s", "", "");
+    set_error("unknown collision operator (use BGK=1, MRT=2, REG=3, EXTREG=4)%s%s", "", "");
     return ERLBM_E_INVAL;
 }
 
@@ -293,7 +296,7 @@ int erlbm_create(const erlbm_desc *d, erlbm_handle **out)
         set_error("unknown precision%s%s", "", "");
         return ERLBM_E_INVAL;
     }
-    int rc = check_op(d->op);
+    int rc = check_op(d->op, d->q);
     if (rc) return rc;
     if (!(d->tau > 0) || !std::isfinite(d->tau) || !std::isfinite(d->tau_nh) || d->tau_nh == 0) {
         set_error("tau and tau_nh must be finite and non-zero%s%s", "", "");
@@ -390,7 +393,7 @@ int erlbm_set_params(erlbm_handle *h, double tau, double tau_nh, int op)
 {
     int rc = check_handle(h);
     if (rc) return rc;
-    if ((rc = check_op(op))) return rc;
+    if ((rc = check_op(op, h->q))) return rc;
     if (!(tau > 0) || !std::isfinite(tau) || !std::isfinite(tau_nh) || tau_nh == 0) {
         set_error("tau and tau_nh must be finite and non-zero%s%s", "", "");
         return ERLBM_E_INVAL;

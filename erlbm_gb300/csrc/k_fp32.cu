@@ -147,6 +147,9 @@ int launch_periodic_d2q9_fp32(int op, const Geo &g, const Relax &R, const float 
     case OP_BGK:
         rc = periodic_shape<OP_BGK>(block, st, g, k, src, dst, s);
         break;
+    case OP_MRT:
+        rc = periodic_shape<OP_MRT>(block, st, g, k, src, dst, s);
+        break;
     case OP_REG:
         rc = periodic_shape<OP_REG>(block, st, g, k, src, dst, s);
         break;

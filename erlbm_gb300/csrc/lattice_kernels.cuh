@@ -330,6 +330,13 @@ int step_dispatch(int op, const Geo &g, const BCp &bc, const Relax &R, const Ste
     case OP_BGK:
         k_step<P, Q, OP_BGK><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, a);
         break;
+    case OP_MRT:
+        if constexpr (Q == 9) {
+            k_step<P, Q, OP_MRT><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, a);
+            break;
+        } else {
+            return -1;
+        }
     case OP_REG:
         k_step<P, Q, OP_REG><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, a);
         break;

@@ -65,7 +65,7 @@ int scratch_address(unsigned char **out)
 // Turns the caller's run descriptions (device memory) into the kernel's prepared runs, in the
 // caller's order.  A run with refused parameters becomes an empty run (no steps) and is flagged, so
 // that its result can be marked afterwards (status 8).
-__global__ void k_prepare_runs(const erlbm_run_spec *__restrict__ specs, int n, BatchRun *__restrict__ runs,
+__global__ void k_prepare_runs(const erlbm_run_spec *__restrict__ specs, int n, int q, BatchRun *__restrict__ runs,
                                uint8_t *__restrict__ refused)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -73,7 +73,8 @@ __global__ void k_prepare_runs(const erlbm_run_spec *__restrict__ specs, int n, 
     const erlbm_run_spec s = specs[i];
     BatchRun r;
     memset(&r, 0, sizeof(r));
-    const bool ok = (s.op == ERLBM_OP_BGK || s.op == ERLBM_OP_REG || s.op == ERLBM_OP_EXTREG) && s.tau > 0 &&
+    const bool ok = (s.op == ERLBM_OP_BGK || s.op == ERLBM_OP_REG || s.op == ERLBM_OP_EXTREG ||
+                     (s.op == ERLBM_OP_MRT && q == 9)) && s.tau > 0 &&
                     isfinite(s.tau) && isfinite(s.tau_nh) && s.tau_nh != 0 && s.n_steps >= 0;
     r.R = make_relax(ok ? s.tau : 1.0, ok ? s.tau_nh : 1.0, ok ? s.op : ERLBM_OP_EXTREG);
     r.k = shifted::make_coef(r.R);
@@ -149,7 +150,7 @@ extern "C" int erlbm_batch_run_noalloc(const erlbm_batch_desc *d, int n_runs, co
     }
     // the array keeps the previous call's contents: the work counter must start at zero
     if ((e = cudaMemsetAsync(counter, 0, sizeof(int), s)) != cudaSuccess) return cuda_fail(e, "noalloc counter");
-    k_prepare_runs<<<(n_runs + 255) / 256, 256, 0, s>>>(runs, n_runs, prepared, refused);
+    k_prepare_runs<<<(n_runs + 255) / 256, 256, 0, s>>>(runs, n_runs, d->q, prepared, refused);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc prepare");
     LaunchShape sh;
     if ((rc = pick_shape(d->precision, d->q, g.nb, d->slots, n_runs, &sh))) return rc;

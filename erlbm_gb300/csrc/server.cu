@@ -786,7 +786,8 @@ int erlbm_server_submit(erlbm_server *s, const erlbm_request *q, int64_t *ticket
     if (!s || !q || !ticket) return ERLBM_E_INVAL;
     if (s->stopping.load()) return ERLBM_E_STATE;
     if (q->precision != ERLBM_FP64 && q->precision != ERLBM_FP32_SHIFTED) return ERLBM_E_INVAL;
-    if (q->op != ERLBM_OP_BGK && q->op != ERLBM_OP_REG && q->op != ERLBM_OP_EXTREG)
+    if (q->op != ERLBM_OP_BGK && q->op != ERLBM_OP_REG && q->op != ERLBM_OP_EXTREG &&
+        !(q->op == ERLBM_OP_MRT && q->kind == ERLBM_REQ_TG2D))  // MRT is D2Q9 only
         return q->op == ERLBM_OP_MRT ? ERLBM_E_UNSUPPORTED : ERLBM_E_INVAL;
     if (q->n_steps < 0 || !(q->tau > 0) || !std::isfinite(q->tau) || !std::isfinite(q->tau_nh) || q->tau_nh == 0)
         return ERLBM_E_INVAL;

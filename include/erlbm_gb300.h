@@ -38,7 +38,7 @@ extern "C" {
 
 /* ---- collision operators: same numbers as COLISAO (src/erlbm_common.h:42) ------------------- */
 #define ERLBM_OP_BGK 1    /* coll_BGK     Collision_operators.cpp:12-49 */
-#define ERLBM_OP_MRT 2    /* coll_MRT: not provided (ERLBM_E_UNSUPPORTED) */
+#define ERLBM_OP_MRT 2    /* coll_MRT     Collision_operators.cpp:487-701 (D2Q9 only, as in the reference) */
 #define ERLBM_OP_REG 3    /* coll_Reg     Collision_operators.cpp:860-967 (E-RLBM with tau_nh = 1) */
 #define ERLBM_OP_EXTREG 4 /* coll_Ext_Reg Collision_operators.cpp:1182-1307 */
 
@@ -218,6 +218,17 @@ typedef struct erlbm_map_desc {
 
 /* labels (and optionally decided steps and margins) of n_points (x 2 when op = 0) runs */
 int erlbm_map_run(const erlbm_map_desc *d, int32_t *labels, int32_t *decided_step, double *margins);
+
+/* A stability map screened in FP32-shifted and refined in FP64.  No counterpart in the reference,
+ * whose maps (main_stability-map_*.cpp) run every point in FP64.  Every point runs first in
+ * ERLBM_FP32_SHIFTED (d->precision is ignored); a point is then run again in ERLBM_FP64, whose
+ * results replace the FP32 ones and equal the reference's, when its FP32 label differs from any label
+ * within `radius` map steps in i and j (same operator: the stability boundary), or when its FP32 run
+ * turned unstable after `late_fraction` of its step budget (late_fraction <= 0 turns that rule off).
+ * The whole grid only (d->n_points = 0).  refined (optional, one byte per result) is set to 1 for the
+ * results that came from FP64.  Arrays are laid out as in erlbm_map_run. */
+int erlbm_map_run_refined(const erlbm_map_desc *d, int radius, double late_fraction, int32_t *labels,
+                          int32_t *decided_step, double *margins, uint8_t *refined);
 
 /* ---- request server (continuous batching) ---------------------------------------------------- */
 /* No counterpart in the reference, which runs one program per invocation.  A server owns a fixed

@@ -209,11 +209,85 @@ static inline void hermite_f1(const tables_t *t, const double *f, const double *
     }
 }
 
+/* MRT transform of d'Humieres (D2Q9; moments rho, e, eps, jx, qx, jy, qy, pxx, pxy), as used by
+ * coll_MRT (Collision_operators.cpp:459-470).  Each row of M is a polynomial in c evaluated on the
+ * velocity set; the rows are orthogonal, so M^-1 = M^T diag(1 / |row|^2), every entry a correctly
+ * rounded quotient of two integers, which is what the reference's literals (1./9., -1./36., ...)
+ * evaluate to. */
+static int mrt9_row(int row, int cx, int cy)
+{
+    const int c2 = cx * cx + cy * cy;
+    switch (row) {
+    case 0: return 1;
+    case 1: return 3 * c2 - 4;
+    case 2: return (9 * c2 * c2 - 21 * c2 + 8) / 2;
+    case 3: return cx;
+    case 4: return (3 * c2 - 5) * cx;
+    case 5: return cy;
+    case 6: return (3 * c2 - 5) * cy;
+    case 7: return cx * cx - cy * cy;
+    default: return cx * cy;
+    }
+}
+
+static double MRT9_M[9][9], MRT9_MINV[9][9];
+static int mrt9_ready = 0;
+
+static void mrt9_tables(void)
+{
+    if (mrt9_ready) return;
+    for (int r = 0; r < 9; r++) {
+        int n2 = 0;
+        for (int i = 0; i < 9; i++) {
+            const int m = mrt9_row(r, D2Q9_C[i][0], D2Q9_C[i][1]);
+            MRT9_M[r][i] = (double)m;
+            n2 += m * m;
+        }
+        for (int i = 0; i < 9; i++) MRT9_MINV[i][r] = MRT9_M[r][i] / (double)n2;
+    }
+    mrt9_ready = 1;
+}
+
+/* coll_MRT, D2Q9 branch (Collision_operators.cpp:583-699): moments of f and f_eq by M (sums from
+ * 0.0 in column order), relaxation m - s (m - m_eq) + (1 - s/2) F_m with the rates of :586-594,
+ * back-transform by M^-1.  F_m is the transform of a zero force term. */
+static void collide_mrt9(const tables_t *t, double *f, double tau)
+{
+    const double s[9] = {0.0, 1.6, 1.8, 0.0, 1.9, 0.0, 1.9, 1. / tau, 1. / tau};
+    double u[3], rho, feq[9];
+    mrt9_tables();
+    moments(t, f, u, &rho);
+    equilibrium(t, u, rho, feq);
+    double m[9], meq[9], fm[9];
+    const double Sf[9] = {0.0};
+    for (int r = 0; r < 9; r++) {
+        m[r] = 0.0;
+        meq[r] = 0.0;
+        fm[r] = 0.0;
+        for (int c = 0; c < 9; c++) {
+            m[r] = m[r] + MRT9_M[r][c] * f[c];
+            meq[r] = meq[r] + MRT9_M[r][c] * feq[c];
+            fm[r] = fm[r] + MRT9_M[r][c] * Sf[c];
+        }
+    }
+    for (int r = 0; r < 9; r++) m[r] = m[r] - s[r] * (m[r] - meq[r]) + (1.0 - 0.5 * s[r]) * fm[r];
+    for (int i = 0; i < 9; i++) {
+        f[i] = 0.0;
+        for (int c = 0; c < 9; c++) f[i] = f[i] + MRT9_MINV[i][c] * m[c];
+    }
+}
+
 /* One node's collision, in place.  op: ORC_OP_BGK (coll_BGK, Collision_operators.cpp:12-49),
- * ORC_OP_REG (coll_Reg, :860-967), ORC_OP_EXTREG (coll_Ext_Reg, :1182-1307). */
+ * ORC_OP_MRT (coll_MRT, :487-701), ORC_OP_REG (coll_Reg, :860-967), ORC_OP_EXTREG (coll_Ext_Reg,
+ * :1182-1307).  The reference's dispatch (src/erlbm_common.h:69-80) compiles coll_MRT only into
+ * D2Q9 builds; in a D3Q19 build it matches no case and the site is not collided, as here. */
 static void collide_site(const tables_t *t, double *f, int op, double tau, double tau_nh)
 {
     double feq[19], S[19];
+    if (op == ORC_OP_MRT) {
+        if (t->q == 9) collide_mrt9(t, f, tau);
+        return;
+    }
     collide_front(t, f, tau, feq, S);
     if (op == ORC_OP_BGK) {
         const double one_over_tau = 1.0 / tau;

@@ -14,6 +14,7 @@ extern "C" {
 
 /* operator numbers of COLISAO (src/erlbm_common.h:42) */
 #define ORC_OP_BGK 1
+#define ORC_OP_MRT 2
 #define ORC_OP_REG 3
 #define ORC_OP_EXTREG 4
 

@@ -14,7 +14,7 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-OP_BGK, OP_REG, OP_EXTREG = 1, 3, 4
+OP_BGK, OP_MRT, OP_REG, OP_EXTREG = 1, 2, 3, 4
 
 _lib = None
 _ref = {}

@@ -14,8 +14,10 @@ produce:
                           the same 20 x 20 subsamples computed by the reference's roda_ponto
                           (main_stability-map_taylor-green.cpp:41-104, main_stability-map_obstacle.cpp:75-123).
   reference_vectors.npz   inputs and outputs of short runs of the reference library (colisao_sitio +
-                          propag_site loop with its boundary functions): small D2Q9 / D3Q19 lattices,
-                          the obstacle channel, the Taylor-Green and double-shear-layer initial fields.
+                          propag_site loop with its boundary functions): small D2Q9 / D3Q19 lattices
+                          under BGK, MRT (D2Q9), RLBM and E-RLBM, the obstacle channel, the
+                          Taylor-Green and double-shear-layer initial fields.  --vectors-only rewrites
+                          this file alone.
 """
 from __future__ import annotations
 
@@ -89,9 +91,17 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
+    ap.add_argument("--vectors-only", action="store_true", help="rewrite reference_vectors.npz only")
     a = ap.parse_args()
     ref = a.reference
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all", "ref", f"REFERENCE={ref}"], check=True)
+    if not a.vectors_only:
+        tables_and_maps(a)
+    vectors()
+
+
+def tables_and_maps(a):
+    ref = a.reference
     from oracle import oracle as O
 
     # ---- published tables and maps -------------------------------------------------------------
@@ -132,7 +142,11 @@ def main():
         print(f"{name}: reference vs published subsample differ at {int(np.sum(np.array(lab) != pubsub))} "
               f"(400-grid parameters) and {int(np.sum(np.array(lab20) != pubsub))} (20 x 20 run) of 400 points")
 
-    # ---- short reference runs -----------------------------------------------------------------------
+
+
+def vectors():
+    """Short runs of the reference library (colisao_sitio + propag_site loop with its boundary functions)."""
+    from oracle import oracle as O
     rng = np.random.default_rng(20261203)
     vec = {}
 
@@ -148,7 +162,8 @@ def main():
 
     for q, (nx, ny, nz), steps in ((9, (7, 5, 1), 13), (19, (6, 5, 3), 9)):
         f0 = near_eq(q, nx * ny * nz)
-        for op, tnh in ((1, 0.57), (3, 1.0), (4, 0.65)):
+        # coll_MRT (op 2) exists for D2Q9 only (src/erlbm_common.h:74-76)
+        for op, tnh in ((1, 0.57), (2, 0.57), (3, 1.0), (4, 0.65)) if q == 9 else ((1, 0.57), (3, 1.0), (4, 0.65)):
             ps, pc, e = O.ref_run(q, nx, ny, nz, None, op, 0.57, tnh, f0, steps)
             key = f"periodic_q{q}_op{op}"
             vec[key + "_in"] = f0
@@ -170,6 +185,8 @@ def main():
     vec["tg16_init"] = f_tg
     ps, pc, e = O.ref_run(9, 16, 16, 1, None, 4, 0.62, 0.65, f_tg, 40)
     vec["tg16_erlbm_40_post_collision"] = pc
+    ps, pc, e = O.ref_run(9, 16, 16, 1, None, 2, 0.62, 0.62, f_tg, 40)
+    vec["tg16_mrt_40_post_collision"] = pc
     f_dsl = np.empty(32 * 32 * 9)
     O.load_ref(9).ref9_init_double_shear(32, 1.0, f_dsl)
     vec["dsl32_init"] = f_dsl

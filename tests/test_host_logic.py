@@ -41,11 +41,15 @@ def test_argument_checks_before_any_device_work():
         m.Lattice(9, 4, 4, 2)  # D2Q9 needs nz = 1
     assert ei.value.code == -1
     with pytest.raises(m.ErlbmError) as ei:
-        m.Lattice(9, 4, 4, 1, op=m.OP_MRT)
+        m.Lattice(19, 4, 4, 1, op=m.OP_MRT)  # coll_MRT is a D2Q9 operator
     assert ei.value.code == -6
     with pytest.raises(ValueError):
         m.operator_from_name("trt")
     assert [m.operator_from_name(n) for n in ("bgk", "mrt", "reg", "erlbm")] == [1, 2, 3, 4]
+    for kw in (dict(radius=-1), dict(late_fraction=1.5)):
+        with pytest.raises(m.ErlbmError) as ei:
+            m.map_run_refined(m.MAP_OBSTACLE, n_i=4, n_j=4, **kw)
+        assert ei.value.code == -1
 
 
 def test_program_inputs_equal_oracle():
