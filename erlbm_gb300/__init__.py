@@ -9,19 +9,23 @@ vocabulary: a ``Lattice`` is what define_rede + aloca_populacoes build (src/erlb
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
 from . import _lib
-from ._lib import (FP32_SHIFTED, FP64, INIT_AOS, INIT_REST, INIT_TG_MAP, MAP_OBSTACLE, MAP_TAYLOR_GREEN, OP_BGK,
-                   OP_EXTREG, OP_MRT, OP_REG, REQ_OBSTACLE, REQ_TG2D, REQ_TG3D, REQ_TG_MAP_POINT, STAGE_POST_COLLISION,
-                   STAGE_POST_STREAM, ErlbmError, check, lib)
+from ._lib import (FIELD_DENSITY, FIELD_VELOCITY, FIELD_VORTICITY, FP32_SHIFTED, FP64, INIT_AOS, INIT_REST,
+                   INIT_TG_MAP, MAP_OBSTACLE, MAP_TAYLOR_GREEN, OP_BGK, OP_EXTREG, OP_MRT, OP_REG, REQ_OBSTACLE,
+                   REQ_TG2D, REQ_TG3D, REQ_TG_MAP_POINT, STAGE_POST_COLLISION, STAGE_POST_STREAM, VTK_ASCII,
+                   VTK_BINARY_DOUBLE, VTK_BINARY_FLOAT, ErlbmError, check, lib)
 
 __all__ = ["Lattice", "ErlbmError", "lib", "OP_BGK", "OP_MRT", "OP_REG", "OP_EXTREG", "FP64", "FP32_SHIFTED",
            "STAGE_POST_STREAM", "STAGE_POST_COLLISION", "MAP_TAYLOR_GREEN", "MAP_OBSTACLE", "init_taylor_green",
            "init_double_shear", "equilibrium", "obstacle_geometry", "taylor_green_error", "tg_map_params",
            "obstacle_map_params", "operator_from_name", "map_run", "map_run_refined", "batch_run", "INIT_REST",
-           "INIT_TG_MAP", "INIT_AOS", "Server", "REQ_TG2D", "REQ_TG_MAP_POINT", "REQ_OBSTACLE", "REQ_TG3D"]
+           "INIT_TG_MAP", "INIT_AOS", "Server", "REQ_TG2D", "REQ_TG_MAP_POINT", "REQ_OBSTACLE", "REQ_TG3D",
+           "FIELD_VELOCITY", "FIELD_VORTICITY", "FIELD_DENSITY", "VTK_ASCII", "VTK_BINARY_FLOAT",
+           "VTK_BINARY_DOUBLE", "velocity_error"]
 
 _OPS = {"bgk": OP_BGK, "mrt": OP_MRT, "reg": OP_REG, "erlbm": OP_EXTREG}
 
@@ -122,6 +126,20 @@ class Lattice:
         check(lib().erlbm_macroscopic(self._h, stage, _dptr(rho), _dptr(u)), "erlbm_macroscopic")
         return rho, u
 
+    def field(self, kind: int = FIELD_VELOCITY, stage: int = STAGE_POST_COLLISION) -> np.ndarray:
+        """A field of the reference's writers at every box node (x fastest, solid nodes 0), computed on
+        the device: velocity or vorticity as (n, 3), density as (n,)."""
+        n = self.nx * self.ny * self.nz
+        out = np.empty(n if kind == FIELD_DENSITY else (n, 3))
+        check(lib().erlbm_field(self._h, stage, kind, _dptr(out), out.size), "erlbm_field")
+        return out
+
+    def write_vtk(self, path: str, kind: int = FIELD_VELOCITY, fmt: int = VTK_ASCII,
+                  stage: int = STAGE_POST_COLLISION) -> None:
+        """The field as a legacy VTK file, byte for byte what rec_velocity / rec_vorticity / rec_density
+        (fmt VTK_ASCII) or their _bin variants (VTK_BINARY_FLOAT / _DOUBLE) write."""
+        check(lib().erlbm_write_vtk(self._h, stage, kind, fmt, os.fsencode(path)), "erlbm_write_vtk")
+
     def run(self, n_steps: int, bc: dict | None = None, energy_every: int = 0, energy_factor: float = 2.0,
             density_check: bool = False, density_limit: float = 10.0) -> dict:
         b = _bc(bc)
@@ -130,6 +148,17 @@ class Lattice:
         check(lib().erlbm_run(self._h, int(n_steps), C.byref(b) if b is not None else None, C.byref(c), C.byref(r)),
               "erlbm_run")
         return dict(label=r.label, decided_step=r.decided_step, steps_done=r.steps_done, margin=r.margin)
+
+
+def velocity_error(sim: Lattice, ref: Lattice, text_digits: int = 0, sim_stage: int = STAGE_POST_COLLISION,
+                   ref_stage: int = STAGE_POST_COLLISION):
+    """tools/error_calculator.cpp between two lattices on the GPU: (E_vec, E_mod) of sim's velocity
+    against ref's sampled at the same physical points.  text_digits = 6 reproduces the tool, which
+    reads 6-significant-digit ASCII files; 0 uses the full-precision fields."""
+    ev, em = C.c_double(), C.c_double()
+    check(lib().erlbm_velocity_error(sim._h, sim_stage, ref._h, ref_stage, int(text_digits), C.byref(ev), C.byref(em)),
+          "erlbm_velocity_error")
+    return ev.value, em.value
 
 
 def _bc(bc: dict | None):

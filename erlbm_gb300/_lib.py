@@ -19,6 +19,8 @@ STAGE_POST_STREAM, STAGE_POST_COLLISION = 0, 1
 MAP_TAYLOR_GREEN, MAP_OBSTACLE = 1, 2
 INIT_REST, INIT_TG_MAP, INIT_AOS = 0, 1, 2
 REQ_TG2D, REQ_TG_MAP_POINT, REQ_OBSTACLE, REQ_TG3D = 1, 2, 3, 4
+FIELD_VELOCITY, FIELD_VORTICITY, FIELD_DENSITY = 1, 2, 3
+VTK_ASCII, VTK_BINARY_FLOAT, VTK_BINARY_DOUBLE = 0, 1, 2
 
 
 class ErlbmError(RuntimeError):
@@ -102,6 +104,10 @@ _SIGS = {
     "erlbm_kinetic_energy": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "erlbm_max_abs_density": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "erlbm_macroscopic": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "erlbm_field": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
+    "erlbm_write_vtk": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_char_p]),
+    "erlbm_velocity_error": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]),
     "erlbm_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(BC), C.POINTER(Checks), C.POINTER(RunResult)]),
     "erlbm_sync": (C.c_int, [C.c_void_p]),
     "erlbm_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -614,3 +614,154 @@ int erlbm_run(erlbm_handle *h, int n_steps, const erlbm_bc *bc, const erlbm_chec
 }
 
 }  // extern "C"
+
+// ---- fields, VTK output, error calculator --------------------------------------------------------
+
+namespace {
+
+// A device buffer allocated and freed in the order of one stream (no device-wide synchronisation).
+struct StreamBuf {
+    void *p = nullptr;
+    cudaStream_t s = nullptr;
+    ~StreamBuf()
+    {
+        if (p) cudaFreeAsync(p, s);
+    }
+    int alloc(size_t bytes, cudaStream_t stream)
+    {
+        s = stream;
+        if (cudaMallocAsync(&p, bytes ? bytes : 16, stream) != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            set_error("out of device memory for a field buffer%s%s", "", "");
+            return ERLBM_E_OOM;
+        }
+        return ERLBM_OK;
+    }
+};
+
+size_t field_values(const erlbm_handle *h, int field) { return (size_t)h->g.nbox * (field == 3 ? 1 : 3); }
+
+// The field of the chosen stage at every box node into out (device, field_values doubles).
+int field_on_device(erlbm_handle *h, int stage, int field, double *out)
+{
+    if (field < 1 || field > 3) {
+        set_error("unknown field (1 velocity, 2 vorticity, 3 density)%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    const void *buf;
+    int rc = stage_buffer(h, stage, &buf);
+    if (rc) return rc;
+    StreamBuf vel;
+    double *target = out;
+    if (field == 2) {
+        if ((rc = vel.alloc(field_values(h, 1) * sizeof(double), h->stream))) return rc;
+        target = (double *)vel.p;
+    }
+    const int kind = field == 3 ? 3 : 1;
+    if (h->prec == ERLBM_FP64)
+        CKL(launch_box_field_fp64(h->q, h->g, (const double *)buf, kind, target, h->stream), "box_field");
+    else
+        CKL(launch_box_field_fp32(h->q, h->g, (const float *)buf, kind, target, h->stream), "box_field");
+    if (field == 2) CKL(launch_vorticity(h->g, target, out, h->stream), "vorticity");
+    return ERLBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int erlbm_field(erlbm_handle *h, int stage, int field, double *out, size_t n)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!out || field < 1 || field > 3 || n != field_values(h, field)) {
+        set_error("field: out must hold nx*ny*nz (density) or 3*nx*ny*nz (velocity, vorticity) doubles%s%s", "",
+                  "");
+        return ERLBM_E_INVAL;
+    }
+    StreamBuf d;
+    if ((rc = d.alloc(n * sizeof(double), h->stream))) return rc;
+    if ((rc = field_on_device(h, stage, field, (double *)d.p))) return rc;
+    CK(cudaMemcpyAsync(out, d.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return ERLBM_OK;
+}
+
+int erlbm_write_vtk(erlbm_handle *h, int stage, int field, int format, const char *path)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!path || field < 1 || field > 3 || format < ERLBM_VTK_ASCII || format > ERLBM_VTK_BINARY_DOUBLE) {
+        set_error("write_vtk: bad field, format or path%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    const size_t n = field_values(h, field);
+    StreamBuf d, enc;
+    if ((rc = d.alloc(n * sizeof(double), h->stream))) return rc;
+    if ((rc = field_on_device(h, stage, field, (double *)d.p))) return rc;
+    std::vector<double> vals;
+    std::vector<unsigned char> bytes;
+    if (format == ERLBM_VTK_ASCII) {
+        vals.resize(n);
+        CK(cudaMemcpyAsync(vals.data(), d.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    } else {
+        const size_t w = format == ERLBM_VTK_BINARY_DOUBLE ? 8 : 4;
+        if ((rc = enc.alloc(n * w, h->stream))) return rc;
+        CKL(launch_encode_be((const double *)d.p, (long long)n, w == 8, (unsigned char *)enc.p, h->stream), "encode");
+        bytes.resize(n * w);
+        CK(cudaMemcpyAsync(bytes.data(), enc.p, n * w, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    if (write_vtk_file(path, field, format, h->g.nx, h->g.ny, h->g.nz, vals.data(), bytes.data(), bytes.size())) {
+        set_error("cannot write %s%s", path, "");
+        return ERLBM_E_INVAL;
+    }
+    return ERLBM_OK;
+}
+
+int erlbm_velocity_error(erlbm_handle *sim, int sim_stage, erlbm_handle *ref, int ref_stage, int text_digits,
+                         double *e_vec, double *e_mod)
+{
+    int rc = check_handle(sim);
+    if (rc || (rc = check_handle(ref))) return rc;
+    if (!e_vec || !e_mod || text_digits < 0 || text_digits > 17) return ERLBM_E_INVAL;
+    const Geo &a = sim->g, &b = ref->g;
+    if (a.nz != 1 || b.nz != 1 || b.nx % a.nx != 0 || b.ny % a.ny != 0 || b.nx / a.nx != b.ny / a.ny) {
+        set_error("the reference grid must refine the simulation grid by one integer factor (nz = 1)%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    if (sim->device != ref->device) {
+        set_error("both lattices must live on the same GPU%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
+    const int stride = b.nx / a.nx;
+    StreamBuf vr, vs;
+    if ((rc = vr.alloc(field_values(ref, 1) * sizeof(double), ref->stream))) return rc;
+    if ((rc = field_on_device(ref, ref_stage, 1, (double *)vr.p))) return rc;
+    CK(cudaStreamSynchronize(ref->stream));
+    if ((rc = vs.alloc(field_values(sim, 1) * sizeof(double), sim->stream))) return rc;
+    if ((rc = field_on_device(sim, sim_stage, 1, (double *)vs.p))) return rc;
+    double sums[3];
+    if (text_digits == 0) {
+        StreamBuf scr;
+        if ((rc = scr.alloc((3 * 1024 + 3) * sizeof(double), sim->stream))) return rc;
+        double *d_out = (double *)scr.p + 3 * 1024;
+        CKL(launch_velocity_error_sums((const double *)vs.p, a.nx, a.ny, (const double *)vr.p, b.nx, stride,
+                                       (double *)scr.p, d_out, sim->stream),
+            "velocity_error");
+        CK(cudaMemcpyAsync(sums, d_out, sizeof(sums), cudaMemcpyDeviceToHost, sim->stream));
+        CK(cudaStreamSynchronize(sim->stream));
+    } else {
+        std::vector<double> hs(field_values(sim, 1)), hr(field_values(ref, 1));
+        CK(cudaMemcpyAsync(hs.data(), vs.p, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, sim->stream));
+        CK(cudaMemcpyAsync(hr.data(), vr.p, hr.size() * sizeof(double), cudaMemcpyDeviceToHost, sim->stream));
+        CK(cudaStreamSynchronize(sim->stream));
+        error_sums_host(hs.data(), a.nx, a.ny, hr.data(), b.nx, stride, text_digits, sums);
+    }
+    *e_mod = std::sqrt(sums[0] / sums[2]);
+    *e_vec = std::sqrt(sums[1] / sums[2]);
+    return ERLBM_OK;
+}
+
+}  // extern "C"

@@ -192,6 +192,11 @@ int launch_node_fields_fp32(int q, const Geo &g, long long n, const int *nof, co
     return node_fields_any<PrecShifted32>(q, g, n, nof, buf, e, rho, u, s);
 }
 
+int launch_box_field_fp32(int q, const Geo &g, const float *buf, int field, double *out, cudaStream_t s)
+{
+    return box_field_any<PrecShifted32>(q, g, buf, field, out, s);
+}
+
 
 // Initial fields on the device (lattice_kernels.cuh): kind 1 = D2Q9 Taylor-Green program init,
 // 4 = D3Q19 3-D Taylor-Green equilibrium, 0 = rest equilibrium.

@@ -33,6 +33,11 @@ int launch_node_fields_fp64(int q, const Geo &g, long long n, const int *nof, co
     return node_fields_any<PrecExact64>(q, g, n, nof, buf, e, rho, u, s);
 }
 
+int launch_box_field_fp64(int q, const Geo &g, const double *buf, int field, double *out, cudaStream_t s)
+{
+    return box_field_any<PrecExact64>(q, g, buf, field, out, s);
+}
+
 // ------------------------------------------------------------------------------------------------
 // Reductions (FP64; deterministic)
 // ------------------------------------------------------------------------------------------------

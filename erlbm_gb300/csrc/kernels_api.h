@@ -77,6 +77,31 @@ int launch_node_fields_fp64(int q, const Geo &g, long long n_fluid, const int *n
 int launch_node_fields_fp32(int q, const Geo &g, long long n_fluid, const int *node_of_fluid, const float *buf,
                             double *e_out, double *rho_out, double *u_out, cudaStream_t s);
 
+// Box fields of the reference's rec_* writers (every node, x fastest, solid nodes 0): field 1 =
+// velocity (3 doubles per node), 3 = density (1 per node).
+int launch_box_field_fp64(int q, const Geo &g, const double *buf, int field, double *out, cudaStream_t s);
+int launch_box_field_fp32(int q, const Geo &g, const float *buf, int field, double *out, cudaStream_t s);
+// vorticity() (LBM_functions.cpp:3761-3872) at every box node from the box velocity field vel.
+int launch_vorticity(const Geo &g, const double *vel, double *vor, cudaStream_t s);
+// n doubles as big-endian float (as_double = 0) or double bytes, vtk_push_real's encoding.
+int launch_encode_be(const double *in, long long n, int as_double, unsigned char *out, cudaStream_t s);
+// tools/error_calculator.cpp sums over an nx x ny velocity field against a reference field of
+// nx_ref columns sampled with stride `stride`: out[0..2] = sum (|u_s| - |u_r|)^2, sum |u_s - u_r|^2,
+// sum |u_r|^2 (fixed-shape tree, deterministic).  scratch holds >= 3 * 1024 doubles.
+int launch_velocity_error_sums(const double *vel, int nx, int ny, const double *vel_ref, int nx_ref, int stride,
+                               double *scratch, double *out, cudaStream_t s);
+
+// Host side of the VTK writers (fields.cu): the reference's header text, then ASCII values (printf
+// %g with `digits` significant digits, as an ostream writes them) or the given big-endian bytes.
+int write_vtk_file(const char *path, int field, int format, int nx, int ny, int nz, const double *vals,
+                   const unsigned char *bytes, size_t n_bytes);
+// Each value of v rounded as text with `digits` significant digits and read back (threads).
+void text_round(double *v, size_t n, int digits);
+// tools/error_calculator.cpp's loop on the host, in its order: out = {sum (|u_s| - |u_r|)^2,
+// sum |u_s - u_r|^2, sum |u_r|^2}; digits > 0 first rounds each value read as its text input does.
+void error_sums_host(const double *vs, int nx, int ny, const double *vr, int nx_ref, int stride, int digits,
+                     double out[3]);
+
 // Sum of n doubles: serial in index order when n <= serial_limit (the reference's order), else a
 // fixed-shape tree (deterministic).  scratch holds >= 1024 doubles.  Result in *out (device).
 int launch_sum(const double *x, long long n, long long serial_limit, double *scratch, double *out, cudaStream_t s);

@@ -312,11 +312,51 @@ __global__ void __launch_bounds__(256) k_node_fields(Geo g, long long n_fluid, c
     }
 }
 
+// Field of the reference's rec_* writers at every box node, x fastest (LBM_functions.cpp:4218-4470,
+// 4979-5241): field 1 = calcula's (vx, vy, vz), 3 values per node; field 3 = density(); solid nodes
+// are written as 0.
+template <class P, int Q>
+__global__ void __launch_bounds__(256) k_box_field(Geo g, const typename P::T *__restrict__ buf, int field,
+                                                   double *__restrict__ out)
+{
+    using T = typename P::T;
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= g.nbox) return;
+    const bool solid = g.solid != nullptr && g.solid[node];
+    T f[Q];
+    if (!solid) {
+#pragma unroll
+        for (int i = 0; i < Q; i++) f[i] = buf[(long long)i * g.plane + node];
+    }
+    if (field == 3) {
+        out[node] = solid ? 0.0 : P::template density<Q>(f);
+        return;
+    }
+    double rho, ux = 0.0, uy = 0.0, uz = 0.0;
+    if (!solid) P::template macro<Q>(f, rho, ux, uy, uz);
+    out[3 * node] = ux;
+    out[3 * node + 1] = uy;
+    out[3 * node + 2] = uz;
+}
+
 // ------------------------------------------------------------------------------------------------
 // Launch helpers
 // ------------------------------------------------------------------------------------------------
 
 inline unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+template <class P>
+int box_field_any(int q, const Geo &g, const typename P::T *buf, int field, double *out, cudaStream_t s)
+{
+    const unsigned nb = blocks_for(g.nbox, 256);
+    if (q == 9)
+        k_box_field<P, 9><<<nb, 256, 0, s>>>(g, buf, field, out);
+    else if (q == 19)
+        k_box_field<P, 19><<<nb, 256, 0, s>>>(g, buf, field, out);
+    else
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
 
 template <class P, int Q>
 int step_dispatch(int op, const Geo &g, const BCp &bc, const Relax &R, const StepArgs &a,

@@ -120,6 +120,34 @@ int erlbm_max_abs_density(erlbm_handle *h, int stage, double *max_abs_rho, int *
 /* per-fluid-node density and velocity (calcula, LBM_functions.cpp:3518-3589) of the chosen stage:
  * rho[n_fluid] and u[3 * n_fluid] (ux, uy, uz per node); either may be NULL */
 int erlbm_macroscopic(erlbm_handle *h, int stage, double *rho, double *u);
+/* Fields of the reference's writers (SimBoltz_Functions/LBM_functions.cpp) computed on the device
+ * for the chosen stage, at every node of the box, x fastest, solid nodes 0:
+ *   ERLBM_FIELD_VELOCITY   calcula's (vx, vy, vz), 3 values per node (rec_velocity :4218)
+ *   ERLBM_FIELD_VORTICITY  vorticity(): central differences of the neighbours' velocities, periodic
+ *                          wrap, a solid neighbour counting as 0 (:3761-3872), 3 values per node
+ *   ERLBM_FIELD_DENSITY    density(), 1 value per node (rec_density :4416)
+ * Only the field crosses to the host, not the populations. */
+#define ERLBM_FIELD_VELOCITY 1
+#define ERLBM_FIELD_VORTICITY 2
+#define ERLBM_FIELD_DENSITY 3
+int erlbm_field(erlbm_handle *h, int stage, int field, double *out, size_t n);
+/* The same field written as a legacy VTK file, byte for byte what the reference's writers produce:
+ * ERLBM_VTK_ASCII as rec_velocity / rec_vorticity / rec_density (values printed with 6 significant
+ * digits); ERLBM_VTK_BINARY_FLOAT / _DOUBLE as rec_*_bin (:4979, :5061, :5179; big-endian, encoded
+ * on the device).  The caller chooses the path (the reference names files vel_<t*>.vtk,
+ * vor_<step>.vtk, rho_<step>.vtk). */
+#define ERLBM_VTK_ASCII 0
+#define ERLBM_VTK_BINARY_FLOAT 1
+#define ERLBM_VTK_BINARY_DOUBLE 2
+int erlbm_write_vtk(erlbm_handle *h, int stage, int field, int format, const char *path);
+/* tools/error_calculator.cpp:60-105 on two lattices of one GPU: the velocity of `sim` (nx x ny, nz = 1)
+ * against that of `ref` sampled at (s x, s y), s = ref nx / sim nx (an integer, the same in y):
+ * E_vec = sqrt(sum |u_s - u_r|^2 / sum |u_r|^2), E_mod = sqrt(sum (|u_s| - |u_r|)^2 / sum |u_r|^2).
+ * text_digits = 0: full precision, summed on the device (fixed-shape tree).  text_digits > 0: every
+ * value is first rounded to that many significant digits, as the tool reads it from the ASCII files
+ * rec_velocity writes (6), and summed in the tool's order: the tool's own result. */
+int erlbm_velocity_error(erlbm_handle *sim, int sim_stage, erlbm_handle *ref, int ref_stage, int text_digits,
+                         double *e_vec, double *e_mod);
 /* roda_ponto on this lattice: up to n_steps steps with the given checks; stops at the first
  * failing check as the reference does */
 int erlbm_run(erlbm_handle *h, int n_steps, const erlbm_bc *bc, const erlbm_checks *chk, erlbm_run_result *res);

@@ -21,6 +21,7 @@
  */
 #define _DEFAULT_SOURCE /* M_PI, as the reference gets it from <cmath> */
 #include <math.h>
+#include <stdio.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -872,4 +873,176 @@ int orc_max_threads(void)
 #else
     return 1;
 #endif
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Fields and VTK output (LBM_functions.cpp:3761-3872 vorticity; rec_velocity :4218,            */
+/* rec_vorticity :4302, rec_density :4416; rec_velocity_bin :4979, rec_vorticity_bin :5061,     */
+/* rec_density_bin :5179 with the helpers of :4795-4883), and tools/error_calculator.cpp.       */
+/* ------------------------------------------------------------------------------------------ */
+
+/* geometry.ini of a box with an optional solid mask: 0 solid, else the 1-based fluid index */
+static int *box_ini(int nx, int ny, int nz, const uint8_t *solid)
+{
+    const long long n = (long long)nx * ny * nz;
+    int *ini = (int *)malloc((size_t)n * sizeof(int));
+    int k = 0;
+    for (long long i = 0; i < n; i++) ini[i] = (solid && solid[i]) ? 0 : ++k;
+    return ini;
+}
+
+/* calcula's velocity at every box node, 3 values per node, 0 at solid nodes */
+static void box_velocity(const tables_t *t, int nx, int ny, int nz, const int *ini, const double *aos, double *v)
+{
+    const long long n = (long long)nx * ny * nz;
+    for (long long i = 0; i < n; i++) {
+        double u[3] = {0.0, 0.0, 0.0}, rho;
+        if (ini[i]) moments(t, aos + (size_t)(ini[i] - 1) * t->q, u, &rho);
+        v[3 * i] = u[0];
+        v[3 * i + 1] = u[1];
+        v[3 * i + 2] = u[2];
+    }
+}
+
+void orc_field(int q, int nx, int ny, int nz, const uint8_t *solid, const double *aos, int field, double *out)
+{
+    const tables_t *t = tables_for(q);
+    const long long n = (long long)nx * ny * nz;
+    int *ini = box_ini(nx, ny, nz, solid);
+    if (field == 3) {
+        for (long long i = 0; i < n; i++) out[i] = ini[i] ? site_density(aos + (size_t)(ini[i] - 1) * q, q) : 0.0;
+    } else if (field == 1) {
+        box_velocity(t, nx, ny, nz, ini, aos, out);
+    } else {
+        /* vorticity (:3761-3872): central differences of the neighbours' calcula velocities with
+         * periodic wrap; a solid neighbour contributes 0; solid nodes are written as 0 */
+        double *v = (double *)malloc((size_t)n * 3 * sizeof(double));
+        box_velocity(t, nx, ny, nz, ini, aos, v);
+        for (int z = 0; z < nz; z++)
+            for (int y = 0; y < ny; y++)
+                for (int x = 0; x < nx; x++) {
+                    const long long i = x + (long long)nx * (y + (long long)ny * z);
+                    if (!ini[i]) {
+                        out[3 * i] = out[3 * i + 1] = out[3 * i + 2] = 0.0;
+                        continue;
+                    }
+                    const long long xp = (x + 1) % nx + (long long)nx * (y + (long long)ny * z);
+                    const long long xm = (x - 1 + nx) % nx + (long long)nx * (y + (long long)ny * z);
+                    const long long yp = x + (long long)nx * ((y + 1) % ny + (long long)ny * z);
+                    const long long ym = x + (long long)nx * ((y - 1 + ny) % ny + (long long)ny * z);
+                    const long long zp = x + (long long)nx * (y + (long long)ny * ((z + 1) % nz));
+                    const long long zm = x + (long long)nx * (y + (long long)ny * ((z - 1 + nz) % nz));
+                    const double *a = v + 3 * xp, *b = v + 3 * xm, *c = v + 3 * yp, *d = v + 3 * ym;
+                    const double *e = v + 3 * zp, *g = v + 3 * zm;
+                    const double dvz_y = (c[2] - d[2]) / 2.0, dvy_z = (e[1] - g[1]) / 2.0;
+                    const double dvx_z = (e[0] - g[0]) / 2.0, dvz_x = (a[2] - b[2]) / 2.0;
+                    const double dvy_x = (a[1] - b[1]) / 2.0, dvx_y = (c[0] - d[0]) / 2.0;
+                    out[3 * i] = dvz_y - dvy_z;
+                    out[3 * i + 1] = dvx_z - dvz_x;
+                    out[3 * i + 2] = dvy_x - dvx_y;
+                }
+        free(v);
+    }
+    free(ini);
+}
+
+/* value in big-endian byte order, as vtk_push does on a little-endian host */
+static void put_be(FILE *fp, double v, int as_double)
+{
+    unsigned char b[8];
+    if (as_double) {
+        uint64_t u;
+        memcpy(&u, &v, 8);
+        for (int k = 0; k < 8; k++) b[k] = (unsigned char)(u >> (56 - 8 * k));
+        fwrite(b, 1, 8, fp);
+    } else {
+        const float f = (float)v;
+        uint32_t u;
+        memcpy(&u, &f, 4);
+        for (int k = 0; k < 4; k++) b[k] = (unsigned char)(u >> (24 - 8 * k));
+        fwrite(b, 1, 4, fp);
+    }
+}
+
+int orc_write_vtk(int q, int nx, int ny, int nz, const uint8_t *solid, const double *aos, int field, int format,
+                  const char *path)
+{
+    const long long n = (long long)nx * ny * nz;
+    const int nc = field == 3 ? 1 : 3;
+    double *val = (double *)malloc((size_t)n * nc * sizeof(double));
+    orc_field(q, nx, ny, nz, solid, aos, field, val);
+    FILE *fp = fopen(path, "wb");
+    if (!fp) {
+        free(val);
+        return -1;
+    }
+    static const char *ascii_title[] = {"", "Velocidade", "Velocidade", "Densidade"};
+    static const char *bin_title[] = {"", "Velocidade", "Vorticidade", "Densidade"};
+    static const char *name[] = {"", "velocidade", "vorticity", "densidade"};
+    fprintf(fp, "# vtk DataFile Version 2.0\n%s\n%s\nDATASET STRUCTURED_POINTS\n", format ? bin_title[field] : ascii_title[field],
+            format ? "BINARY" : "ASCII");
+    fprintf(fp, "DIMENSIONS %d %d %d\nASPECT_RATIO 1 1 1\nORIGIN 0 0 0\n", nx, ny, nz);
+    if (format)
+        fprintf(fp, "POINT_DATA %lld\n", n);
+    else
+        fprintf(fp, "POINT_DATA %d\n", nx * ny * nz);
+    const char *type = format == 1 ? "float" : "double";
+    if (field == 3)
+        fprintf(fp, "SCALARS %s %s\nLOOKUP_TABLE default\n", name[field], type);
+    else
+        fprintf(fp, "VECTORS %s %s\n", name[field], type);
+    if (format == 0) {
+        /* ostream << double with the default precision: printf's %g with 6 significant digits */
+        for (long long r = 0; r < (long long)ny * nz; r++) {
+            for (int x = 0; x < nx; x++)
+                for (int c = 0; c < nc; c++) fprintf(fp, "%g ", val[(r * nx + x) * nc + c]);
+            fputc('\n', fp);
+        }
+    } else {
+        for (long long i = 0; i < n * nc; i++) put_be(fp, val[i], format == 2);
+        fputc('\n', fp);
+    }
+    fclose(fp);
+    free(val);
+    return 0;
+}
+
+/* a value written as text with `digits` significant digits and read back (ostream << / >>) */
+static double text_round(double v, int digits)
+{
+    char buf[64];
+    snprintf(buf, sizeof buf, "%.*g", digits, v);
+    return strtod(buf, NULL);
+}
+
+/* tools/error_calculator.cpp:60-105: the reference field sampled at (s x, s y), s = nx_ref / nx;
+ * E_vec = sqrt(sum |u_s - u_r|^2 / sum |u_r|^2), E_mod = sqrt(sum (|u_s| - |u_r|)^2 / sum |u_r|^2).
+ * vel and vel_ref hold 3 values per node; text_digits > 0 first rounds every value as the tool's
+ * ASCII input files carry it (rec_velocity writes 6 significant digits). */
+int orc_velocity_error(int nx, int ny, const double *vel, int nx_ref, int ny_ref, const double *vel_ref,
+                       int text_digits, double *e_vec, double *e_mod)
+{
+    if (nx_ref % nx != 0 || ny_ref % ny != 0 || nx_ref / nx != ny_ref / ny) return -1;
+    const int amost = nx_ref / nx;
+    double sum_dif2 = 0.0, sum_vec2 = 0.0, sum_ur2 = 0.0;
+    for (int y = 0; y < ny; y++)
+        for (int x = 0; x < nx; x++) {
+            const size_t pc = 3 * ((size_t)x + (size_t)y * nx);
+            const size_t pr = 3 * ((size_t)x * amost + (size_t)y * amost * nx_ref);
+            double vx_ref = vel_ref[pr], vy_ref = vel_ref[pr + 1], vx_cal = vel[pc], vy_cal = vel[pc + 1];
+            if (text_digits > 0) {
+                vx_ref = text_round(vx_ref, text_digits);
+                vy_ref = text_round(vy_ref, text_digits);
+                vx_cal = text_round(vx_cal, text_digits);
+                vy_cal = text_round(vy_cal, text_digits);
+            }
+            const double u_r = sqrt(vx_ref * vx_ref + vy_ref * vy_ref);
+            const double u_s = sqrt(vx_cal * vx_cal + vy_cal * vy_cal);
+            sum_dif2 = sum_dif2 + (u_s - u_r) * (u_s - u_r);
+            sum_vec2 = sum_vec2 + (vx_cal - vx_ref) * (vx_cal - vx_ref) + (vy_cal - vy_ref) * (vy_cal - vy_ref);
+            sum_ur2 = sum_ur2 + u_r * u_r;
+        }
+    *e_mod = sqrt(sum_dif2 / sum_ur2);
+    *e_vec = sqrt(sum_vec2 / sum_ur2);
+    return 0;
 }

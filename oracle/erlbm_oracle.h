@@ -62,6 +62,15 @@ void orc_obstacle_map(int n_tau, int n_nu, double ma, int n_pts, const int *pi, 
                       int nthreads, int *labels, int *decided, double *margins);
 int orc_max_threads(void);
 
+/* Fields, VTK files and the error calculator (LBM_functions.cpp rec_* writers and vorticity,
+ * tools/error_calculator.cpp).  field: 1 velocity, 2 vorticity (3 values per node), 3 density;
+ * format: 0 ASCII, 1 binary float, 2 binary double. */
+void orc_field(int q, int nx, int ny, int nz, const uint8_t *solid, const double *aos, int field, double *out);
+int orc_write_vtk(int q, int nx, int ny, int nz, const uint8_t *solid, const double *aos, int field, int format,
+                  const char *path);
+int orc_velocity_error(int nx, int ny, const double *vel, int nx_ref, int ny_ref, const double *vel_ref,
+                       int text_digits, double *e_vec, double *e_mod);
+
 #ifdef __cplusplus
 }
 #endif

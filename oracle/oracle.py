@@ -74,6 +74,10 @@ def load():
         "orc_obstacle_map": (None, [C.c_int, C.c_int, C.c_double, C.c_int, _ip, _ip, C.c_int, C.c_int,
                                     _ip, _ip, _dp]),
         "orc_max_threads": (C.c_int, []),
+        "orc_field": (None, [C.c_int, C.c_int, C.c_int, C.c_int, vp, _dp, C.c_int, _dp]),
+        "orc_write_vtk": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, vp, _dp, C.c_int, C.c_int, C.c_char_p]),
+        "orc_velocity_error": (C.c_int, [C.c_int, C.c_int, _dp, C.c_int, C.c_int, _dp, C.c_int,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -216,6 +220,46 @@ def obstacle_map(points, n_tau=400, n_nu=400, ma=0.1, max_steps=0, threads=0):
     return lab, dec, mg
 
 
+FIELD_VELOCITY, FIELD_VORTICITY, FIELD_DENSITY = 1, 2, 3
+VTK_ASCII, VTK_BINARY_FLOAT, VTK_BINARY_DOUBLE = 0, 1, 2
+
+
+def _solid_ptr(solid):
+    if solid is None:
+        return None, None
+    s = np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1)
+    return s, s.ctypes.data
+
+
+def field(q, nx, ny, nz, solid, aos, kind):
+    """The rec_* writers' field at every box node (x fastest, solid nodes 0): velocity or vorticity
+    (3 values per node) or density."""
+    s, sp = _solid_ptr(solid)
+    n = nx * ny * nz * (1 if kind == FIELD_DENSITY else 3)
+    out = np.empty(n)
+    load().orc_field(q, nx, ny, nz, sp, np.ascontiguousarray(aos, dtype=np.float64), kind, out)
+    return out
+
+
+def write_vtk(q, nx, ny, nz, solid, aos, kind, fmt, path):
+    s, sp = _solid_ptr(solid)
+    rc = load().orc_write_vtk(q, nx, ny, nz, sp, np.ascontiguousarray(aos, dtype=np.float64), kind, fmt,
+                              os.fsencode(path))
+    if rc:
+        raise OSError(f"cannot write {path}")
+
+
+def velocity_error(nx, ny, vel, nx_ref, ny_ref, vel_ref, text_digits=0):
+    """tools/error_calculator.cpp on two velocity fields (3 values per node); returns (E_vec, E_mod)."""
+    ev, em = C.c_double(), C.c_double()
+    rc = load().orc_velocity_error(nx, ny, np.ascontiguousarray(vel, dtype=np.float64), nx_ref, ny_ref,
+                                   np.ascontiguousarray(vel_ref, dtype=np.float64), text_digits, C.byref(ev),
+                                   C.byref(em))
+    if rc:
+        raise ValueError("the reference grid must refine the simulation grid by one integer factor")
+    return ev.value, em.value
+
+
 # ---------------------------------------------------------------------------------------------
 # The reference library compiled from its own sources (present only where it could be built)
 # ---------------------------------------------------------------------------------------------
@@ -238,11 +282,13 @@ def load_ref(q: int):
         lib.ref9_init_taylor_green.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, _dp]
         lib.ref9_init_double_shear.argtypes = [C.c_int, C.c_double, _dp]
         lib.ref9_taylor_green_main.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+        lib.ref9_rec_field.argtypes = [C.c_int, C.c_int, C.c_int, vp, _dp, C.c_int, C.c_int, C.c_double, C.c_uint]
     else:
         lib.ref19_tg_map_point.restype = C.c_int
         lib.ref19_tg_map_point.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double]
         lib.ref19_obstacle_map_point.restype = C.c_int
         lib.ref19_obstacle_map_point.argtypes = [C.c_double, C.c_double, C.c_double]
+        lib.ref19_rec_field.argtypes = [C.c_int, C.c_int, C.c_int, vp, _dp, C.c_int, C.c_int, C.c_double, C.c_uint]
     _ref[q] = lib
     return lib
 

@@ -155,6 +155,33 @@ void ref9_init_double_shear(int L, double rho_ini, double *f_out)
 int ref9_taylor_green_main(int argc, char **argv) { return erlbm_ref_main_taylor_green(argc, argv); }
 #endif
 
+// The reference's field writers (LBM_functions.cpp: rec_velocity :4218, rec_vorticity :4302,
+// rec_density :4416 in ASCII; rec_velocity_bin :4979, rec_vorticity_bin :5061, rec_density_bin
+// :5179 in big-endian binary) on the given AoS populations.  field: 1 velocity, 2 vorticity,
+// 3 density; format: 0 ASCII, 1 binary float, 2 binary double.  The file is written into the current
+// directory under the reference's own name (vel_<tempo>.vtk, vor_<passo>.vtk, rho_<passo>.vtk).
+int REF_PREFIX(rec_field)(int nx, int ny, int nz, const uint8_t *solid, const double *f_aos, int field, int format,
+                          double tempo, unsigned passo)
+{
+    RefCase c;
+    make_case(c, nx, ny, nz, solid);
+    const int n = c.geometry.fluid * nvel;
+    for (int k = 0; k < n; k++) c.lattice.inif[k] = f_aos[k];
+    const bool dp = format == 2;
+    if (field == 1) {
+        if (format == 0) rec_velocity(c.geometry, c.lattice, tempo);
+        else rec_velocity_bin(c.geometry, c.lattice, tempo, dp);
+    } else if (field == 2) {
+        if (format == 0) rec_vorticity(c.geometry, c.lattice, passo);
+        else rec_vorticity_bin(c.geometry, c.lattice, passo, dp);
+    } else {
+        if (format == 0) rec_density(c.geometry, c.lattice, passo);
+        else rec_density_bin(c.geometry, c.lattice, passo, dp);
+    }
+    free_case(c);
+    return 0;
+}
+
 #if REF_Q == 19
 // roda_ponto of the Taylor-Green map (main_stability-map_taylor-green.cpp:41-104).
 int ref19_tg_map_point(int L, int col, double tau, double tau_nh, double u_0)

@@ -190,6 +190,43 @@ def vectors():
     f_dsl = np.empty(32 * 32 * 9)
     O.load_ref(9).ref9_init_double_shear(32, 1.0, f_dsl)
     vec["dsl32_init"] = f_dsl
+    # the reference's field writers on two stored states: the bytes of every file they write
+    import tempfile
+    cwd = os.getcwd()
+    tmp = tempfile.mkdtemp()
+    states = ((9, 16, 16, None, vec["tg16_erlbm_40_post_collision"], "tg16"),
+              (19, nx, ny, solid, vec["obstacle_post_collision"], "obstacle"))
+    names = {1: "vel_0.500000.vtk", 2: "vor_7.vtk", 3: "rho_7.vtk"}
+    for q, a, b, s, f, tag in states:
+        sp = None if s is None else np.ascontiguousarray(s, dtype=np.uint8).ctypes.data
+        for kind in (1, 2, 3):
+            for fmt in (0, 1, 2):
+                os.chdir(tmp)
+                try:
+                    getattr(O.load_ref(q), f"ref{q}_rec_field")(a, b, 1, sp, np.ascontiguousarray(f), kind, fmt,
+                                                                 0.5, 7)
+                    data = open(names[kind], "rb").read()
+                finally:
+                    os.chdir(cwd)
+                vec[f"vtk_{tag}_field{kind}_format{fmt}"] = np.frombuffer(data, dtype=np.uint8)
+    # tools/error_calculator on the ASCII velocity files of two double-shear-layer runs: L = 16 E-RLBM
+    # (20 steps) against L = 32 RLBM (40 steps); its erro_L2.dat line carries 10 significant digits
+    paths = []
+    for L, op, tnh, steps in ((16, 4, 0.65, 20), (32, 3, 1.0, 40)):
+        fi = np.empty(L * L * 9)
+        O.load_ref(9).ref9_init_double_shear(L, 1.0, fi)
+        _, pc, _ = O.ref_run(9, L, L, 1, None, op, 0.5 + 3 * (1 / 32) * L / 80000, tnh, fi, steps)
+        os.chdir(tmp)
+        try:
+            O.load_ref(9).ref9_rec_field(L, L, 1, None, pc, 1, 0, 1.0, 0)
+            os.replace("vel_1.000000.vtk", f"vel_L{L}.vtk")
+        finally:
+            os.chdir(cwd)
+        paths.append(f"vel_L{L}.vtk")
+    subprocess.run([os.path.join(ROOT, "oracle", "_ref", "error_calculator")] + paths, cwd=tmp, check=True,
+                   capture_output=True)
+    line = open(os.path.join(tmp, "erro_L2.dat")).read().split()
+    vec["errcalc_dsl16_vs_dsl32"] = np.array([16, 32, 20, 40, float(line[1]), float(line[2])])
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
     print("wrote", sorted(os.listdir(HERE)))
 

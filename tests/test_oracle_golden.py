@@ -142,3 +142,37 @@ def test_oracle_maps_vs_reference_fast_points():
     sel = list(range(0, 400, 41))
     lab, dec, _ = O.obstacle_map([opts[k] for k in sel])
     assert list(lab) == [m["obstacle"][k] for k in sel]
+
+
+@pytest.mark.parametrize("tag", ["tg16", "obstacle"])
+def test_vtk_writers_byte_identical(tag, tmp_path):
+    """rec_velocity / rec_vorticity / rec_density (ASCII) and their _bin variants (big-endian float and
+    double): the oracle writes the same bytes as the reference's writers on the same populations."""
+    v = vectors()
+    if tag == "tg16":
+        q, nx, ny, solid, f = 9, 16, 16, None, v["tg16_erlbm_40_post_collision"]
+    else:
+        nx, ny, solid = O.obstacle_geometry()
+        q, f = 19, v["obstacle_post_collision"]
+    for kind in (1, 2, 3):
+        for fmt in (0, 1, 2):
+            path = tmp_path / f"{kind}_{fmt}.vtk"
+            O.write_vtk(q, nx, ny, 1, solid, f, kind, fmt, str(path))
+            assert path.read_bytes() == v[f"vtk_{tag}_field{kind}_format{fmt}"].tobytes(), (kind, fmt)
+
+
+def test_error_calculator_matches_tool():
+    """tools/error_calculator.cpp on the reference's ASCII velocity files (6 significant digits): the
+    oracle's text-rounded errors equal the tool's erro_L2.dat values to their 10 printed digits."""
+    v = vectors()
+    Ls, Lr, ns, nr, ev, em = v["errcalc_dsl16_vs_dsl32"]
+    fields = []
+    for L, op, tnh, n in ((int(Ls), O.OP_EXTREG, 0.65, int(ns)), (int(Lr), O.OP_REG, 1.0, int(nr))):
+        lat = O.Lattice(9, L, L, 1, None, 0.5 + 3 * (1 / 32) * L / 80000, tnh, op)
+        lat.set(O.init_double_shear(L))
+        lat.step(n)
+        fields.append(O.field(9, L, L, 1, None, lat.get(1), O.FIELD_VELOCITY))
+    e = O.velocity_error(int(Ls), int(Ls), fields[0], int(Lr), int(Lr), fields[1], text_digits=6)
+    assert float(f"{e[0]:.10g}") == ev and float(f"{e[1]:.10g}") == em
+    full = O.velocity_error(int(Ls), int(Ls), fields[0], int(Lr), int(Lr), fields[1])
+    assert full != e and abs(full[0] - e[0]) < 1e-4 * e[0]
