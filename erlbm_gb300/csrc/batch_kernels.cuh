@@ -116,15 +116,16 @@ __device__ __forceinline__ void tg_map_init(typename P::T *f, int x, int y, doub
     for (int i = 0; i < Q; i++) f[i] = P::template from_f<Q>(feq[i], i);
 }
 
-// Deterministic block sum of one double per thread.  Exact path: serial in node order (thread
-// order), like kinectic_energy; FP32 path: fixed shuffle tree + serial over warps.
+// Deterministic block sum of one double per thread.  Exact path: serial in fluid-index order (slot =
+// the thread's fluid index, -1 for a thread without a node), like kinectic_energy; FP32 path: fixed
+// shuffle tree + serial over warps.
 template <bool SERIAL>
-__device__ double block_sum(double v, double *sh, int n_vals)
+__device__ double block_sum(double v, double *sh, int n_vals, int slot)
 {
     const int tid = threadIdx.x;
     double total;
     if (SERIAL) {
-        sh[tid] = v;
+        if (slot >= 0) sh[slot] = v;
         __syncthreads();
         if (tid == 0) {
             double s = 0;
@@ -168,14 +169,16 @@ __device__ __forceinline__ double block_max(double v, double *sh)
     return t;
 }
 
-// Shared memory: populations Q * NB of T, the solid mask (NB bytes), reduction scratch.
+// Shared memory: populations Q * NB of T, reduction scratch, the solid mask (NB bytes), the node
+// order (NB shorts) and the number of fluid nodes.
 template <class P, int Q>
 __host__ __device__ inline size_t batch_smem_bytes(int nb, int block)
 {
     const size_t pop = (size_t)Q * nb * sizeof(typename P::T);
     const size_t red = ((size_t)block + 1) * sizeof(double);
     const size_t mask = ((size_t)nb + 15) / 16 * 16;
-    return (pop + 15) / 16 * 16 + red + mask + 16;
+    const size_t order = ((size_t)nb * sizeof(short) + 15) / 16 * 16;
+    return (pop + 15) / 16 * 16 + red + mask + order + 16 + 32;
 }
 
 // Register budget: one node per thread (the map lattices: 256 or 264 nodes) wants several
@@ -193,13 +196,36 @@ struct BatchSmem {
     typename P::T *buf;
     double *red;
     uint8_t *solid;
+    short *order;   // node of each thread slot: fluid nodes only, boundary-plane nodes first
+    int *n_fluid;
+    double *zh;     // the run's Zou-He closure constants (P::ZouHe, <= 32 bytes)
     __device__ BatchSmem(unsigned char *raw, int nb)
     {
         buf = reinterpret_cast<typename P::T *>(raw);
         red = reinterpret_cast<double *>(raw + ((size_t)Q * nb * sizeof(typename P::T) + 15) / 16 * 16);
         solid = reinterpret_cast<uint8_t *>(red + blockDim.x + 1);
+        order = reinterpret_cast<short *>(solid + ((size_t)nb + 15) / 16 * 16);
+        n_fluid = reinterpret_cast<int *>(order + ((size_t)nb * sizeof(short) + 15) / 16 * 16 / sizeof(short));
+        zh = reinterpret_cast<double *>(n_fluid + 4);
     }
 };
+
+// Thread slots of a geometry (one thread, after sm.solid is loaded): the fluid nodes in node order,
+// except that the nodes of the boundary planes come first.  Those run the inlet and outlet closures
+// (with FP64 operations in the FP32 path); packed into the first warp, they no longer put that work
+// on every warp of the CTA in every step.  Solid nodes get no thread.
+__device__ inline void make_order(const BatchGeo &g, short *order, int *n_fluid, const uint8_t *solid)
+{
+    int k = 0;
+    for (int pass = 0; pass < 2; pass++)
+        for (int n = 0; n < g.nb; n++) {
+            if (solid[n]) continue;
+            const int x = n % g.nx;
+            const bool plane = x == g.inlet_x || x == g.outlet_x;
+            if (plane == (pass == 0)) order[k++] = (short)n;
+        }
+    *n_fluid = k;
+}
 
 // One run of one lattice by the whole CTA.  sm.solid must hold the geometry's mask.  The result is
 // returned to every thread.
@@ -217,13 +243,28 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
 
     int node[NPT], nx_[NPT], ny_[NPT];
     bool fluid[NPT];
+    const int n_fluid = *sm.n_fluid;
 #pragma unroll
     for (int s = 0; s < NPT; s++) {
-        node[s] = tid + s * blockDim.x;
+        const int slot = tid + s * blockDim.x;
+        fluid[s] = slot < n_fluid;
+        node[s] = fluid[s] ? sm.order[slot] : 0;
         nx_[s] = node[s] % g.nx;
         ny_[s] = node[s] / g.nx;
-        fluid[s] = node[s] < NB && !solid[node[s]];
     }
+    constexpr bool SERIAL = NPT == 1 && sizeof(T) == 8;
+    // fluid index of a thread's node (solid nodes before it skipped): the serial energy sum's order
+    // and the AoS initial populations' position
+    int fidx = -1;
+    if (fluid[0] && (g.init == INIT_AOS || (SERIAL && g.energy_every > 0))) {
+        fidx = 0;
+        for (int k = 0; k < node[0]; k++) fidx += !solid[k];
+    }
+    // the Zou-He constants live in shared memory: only the boundary threads read them, and keeping
+    // them in registers for the whole run would cost every thread
+    using ZH = typename P::ZouHe;
+    static_assert(sizeof(ZH) <= 32, "ZouHe constants exceed their shared-memory slot");
+    if (tid == 0) *reinterpret_cast<ZH *>(sm.zh) = P::zou_he_prep(r.u0);
 
     // ---- initial populations (post-stream state of step 0) ----
     T f[NPT][Q];
@@ -233,9 +274,11 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
         if (g.init == INIT_TG_MAP) {
             tg_map_init<P, Q>(f[s], nx_[s], ny_[s], r.u0, g);
         } else if (g.init == INIT_AOS) {
-            // fluid index of this node: count of fluid nodes before it (solid masks are small)
-            int p = 0;
-            for (int k = 0; k < node[s]; k++) p += !solid[k];
+            int p = fidx;
+            if (s > 0) {
+                p = 0;
+                for (int k = 0; k < node[s]; k++) p += !solid[k];
+            }
             const double *src = aos + r.aos_off + (long long)p * Q;
 #pragma unroll
             for (int i = 0; i < Q; i++) f[s][i] = P::template from_f<Q>(src[i], i);
@@ -251,13 +294,12 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
     double E0 = 0.0, E = 0.0, margin = 0.0, max_rho = 0.0;
     float dmax = -INFINITY, dmin = INFINITY;  // FP32 path: extreme drho seen by this thread
     int label = 0, decided = r.n_steps, status = 0, steps_done = r.n_steps;
-    constexpr bool SERIAL = NPT == 1 && sizeof(T) == 8;
     if (g.energy_every > 0) {
         double e = 0.0;
 #pragma unroll
         for (int s = 0; s < NPT; s++)
             if (fluid[s]) e += P::template energy<Q>(f[s]);
-        E0 = block_sum<SERIAL>(e, red, NB);
+        E0 = block_sum<SERIAL>(e, red, n_fluid, fidx);
         E = E0;
     }
 
@@ -299,7 +341,7 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
 #pragma unroll
             for (int s = 0; s < NPT; s++)
                 if (fluid[s]) e += P::template energy<Q>(f[s]);
-            E = block_sum<SERIAL>(e, red, NB);
+            E = block_sum<SERIAL>(e, red, n_fluid, fidx);
             const double lim = g.energy_factor * E0;
             const double rr = isfinite(E) ? E / lim : INFINITY;
             margin = fmax(margin, rr);
@@ -320,13 +362,14 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
             const int x = nx_[s];
             if (x == g.outlet_x) {
                 const int xn = x + ((g.outlet_x < g.nx / 2) ? 1 : -1);
-                if (Q == 19 && xn == g.inlet_x) P::zou_he(f[s], r.u0, g.inlet_x < g.nx / 2);
+                if (Q == 19 && xn == g.inlet_x)
+                    P::zou_he(f[s], *reinterpret_cast<const ZH *>(sm.zh), g.inlet_x < g.nx / 2);
                 if (any_solid && solid[node[s] + (xn - x)])
                     P::template rest<Q>(f[s], g.rho0);
                 else
                     P::template outlet<Q>(f[s], g.rho0);
             } else if (Q == 19 && x == g.inlet_x) {
-                P::zou_he(f[s], r.u0, g.inlet_x < g.nx / 2);
+                P::zou_he(f[s], *reinterpret_cast<const ZH *>(sm.zh), g.inlet_x < g.nx / 2);
             }
             batch_collide<P, Q>(f[s], r);
             if (g.density_check) {
@@ -396,6 +439,8 @@ __global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
     __shared__ int s_run;
     const int tid = threadIdx.x;
     for (int k = tid; k < g.nb; k += blockDim.x) sm.solid[k] = g.solid ? g.solid[k] : 0;
+    __syncthreads();
+    if (tid == 0) make_order(g, sm.order, sm.n_fluid, sm.solid);
     for (;;) {
         __syncthreads();
         if (tid == 0) s_run = atomicAdd(counter, 1);
@@ -499,6 +544,8 @@ __global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
         const BatchGeo g = ring.geos[gi];
         // the launch's shared memory is sized for max_nb nodes; a smaller lattice uses its prefix
         for (int k = tid; k < g.nb && k < max_nb; k += blockDim.x) sm.solid[k] = g.solid ? g.solid[k] : 0;
+        __syncthreads();
+        if (tid == 0 && g.nb <= max_nb) make_order(g, sm.order, sm.n_fluid, sm.solid);
         __syncthreads();
         BatchResult o;
         if (g.nb > max_nb || g.nb > NPT * (int)blockDim.x) {

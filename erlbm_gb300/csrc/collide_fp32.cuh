@@ -297,18 +297,32 @@ __device__ __forceinline__ float node_drho(const float *g)
 // Zou-He velocity inlet (ZouHeD3Q19_vx_x, Boundary_conditions.cpp:350-436) on shifted
 // populations.  With f = w + g the weight sums of the two index sets are 1/6 and 2/3 and the
 // transverse corrections carry no weight, so rho = (1 + 2 G_minus + G_zero) / (1 - vx).  The
-// closure (rho and rho vx / 3, rho vx / 6) is evaluated in FP64; the small population sums and the
-// corrections stay in FP32, which keeps the FP64 work of an inlet node to a handful of operations
-// (on GB300 FP64 issues at a small fraction of the FP32 rate, and every warp holds inlet nodes).
-__device__ __forceinline__ void zou_he(float g[19], double vx, bool left)
+// closure (rho and rho vx / 3, rho vx / 6) is evaluated in FP64, with 1 / (1 - vx), vx / 3 and
+// vx / 6 formed once per run (zou_he_prep); the small population sums and the corrections stay in
+// FP32.  That keeps the FP64 work of an inlet node to a handful of multiplies: on GB300 FP64 issues
+// at a small fraction of the FP32 rate.
+struct ZouHe {
+    double inv_1mvx, vx3, vx6;
+};
+
+__device__ __forceinline__ ZouHe zou_he_prep(double vx)
+{
+    ZouHe z;
+    z.inv_1mvx = 1.0 / (1.0 - vx);
+    z.vx3 = vx / 3.0;
+    z.vx6 = vx / 6.0;
+    return z;
+}
+
+__device__ __forceinline__ void zou_he(float g[19], const ZouHe &z, bool left)
 {
     const float ty = ((((g[18] + g[3]) + g[16]) - g[15]) - g[4]) - g[17];
     const float tz = ((((g[17] + g[5]) + g[16]) - g[15]) - g[6]) - g[18];
     const float gz = (((g[0] + g[3]) + (g[4] + g[5])) + ((g[6] + g[15]) + (g[16] + g[17]))) + g[18];
     if (left) {
         const float gm = ((g[1] + g[7]) + (g[9] + g[11])) + g[13];
-        const double rho = (1.0 + 2.0 * (double)gm + (double)gz) / (1.0 - vx);
-        const float a3 = (float)(rho * vx / 3.0), a6 = (float)(rho * vx / 6.0);
+        const double rho = (1.0 + (2.0 * (double)gm + (double)gz)) * z.inv_1mvx;
+        const float a3 = (float)(rho * z.vx3), a6 = (float)(rho * z.vx6);
         g[1] = g[1] + a3;
         g[7] = g[7] + fmaf(-0.5f, ty, a6);
         g[9] = g[9] + fmaf(0.5f, ty, a6);
@@ -316,8 +330,8 @@ __device__ __forceinline__ void zou_he(float g[19], double vx, bool left)
         g[13] = g[13] + fmaf(0.5f, tz, a6);
     } else {
         const float gp = ((g[2] + g[8]) + (g[10] + g[12])) + g[14];
-        const double rho = (1.0 + 2.0 * (double)gp + (double)gz) / (1.0 - vx);
-        const float a3 = (float)(rho * vx / 3.0), a6 = (float)(rho * vx / 6.0);
+        const double rho = (1.0 + (2.0 * (double)gp + (double)gz)) * z.inv_1mvx;
+        const float a3 = (float)(rho * z.vx3), a6 = (float)(rho * z.vx6);
         g[2] = g[2] - a3;
         g[10] = g[10] - fmaf(0.5f, ty, a6);
         g[8] = g[8] - fmaf(-0.5f, ty, a6);

@@ -59,12 +59,17 @@ struct PrecExact64 {
             exact::moments19(f, rho, ux, uy, uz);
         }
     }
-    __device__ static __forceinline__ void zou_he(T *f, double vx, bool left)
+    // Zou-He closure constants of one inlet velocity: the exact path uses vx as the reference does
+    struct ZouHe {
+        double vx;
+    };
+    __device__ static __forceinline__ ZouHe zou_he_prep(double vx) { return ZouHe{vx}; }
+    __device__ static __forceinline__ void zou_he(T *f, const ZouHe &z, bool left)
     {
         if (left)
-            exact::zou_he_left(f, vx);
+            exact::zou_he_left(f, z.vx);
         else
-            exact::zou_he_right(f, vx);
+            exact::zou_he_right(f, z.vx);
     }
     // devnull_rho_x (Boundary_conditions.cpp:119-125): f = f_adj * (rho / density(f_adj)).
     template <int Q>
@@ -117,16 +122,20 @@ struct PrecShifted32 {
         uy = fy;
         uz = fz;
     }
-    __device__ static __forceinline__ void zou_he(T *f, double vx, bool left) { shifted::zou_he(f, vx, left); }
+    using ZouHe = shifted::ZouHe;
+    __device__ static __forceinline__ ZouHe zou_he_prep(double vx) { return shifted::zou_he_prep(vx); }
+    __device__ static __forceinline__ void zou_he(T *f, const ZouHe &z, bool left) { shifted::zou_he(f, z, left); }
     // devnull_rho_x on shifted populations: f = f_adj * (rho / rho_adj) becomes
-    // g = g_adj s + w (s - 1), s = rho / rho_adj; s and s - 1 are formed in FP64, the update in FP32.
+    // g = g_adj + (s - 1) (g_adj + w),  s - 1 = (rho - rho_adj) / rho_adj = ((rho - 1) - drho) / (1 + drho),
+    // all of it small quantities, so FP32 carries it (the error of s - 1, ~1e-7 of a ~1e-3 quantity,
+    // stays far below an ulp of g).
     template <int Q>
     __device__ static __forceinline__ void outlet(T *f, double rho)
     {
-        const double r = 1.0 + (double)shifted::node_drho<Q>(f);
-        const float s = (float)(rho / r), sm1 = (float)((rho - r) / r);
+        const float drho = shifted::node_drho<Q>(f);
+        const float sm1 = __fdiv_rn((float)(rho - 1.0) - drho, 1.f + drho);
 #pragma unroll
-        for (int i = 0; i < Q; i++) f[i] = fmaf(f[i], s, (float)Lat<Q>::w(i) * sm1);
+        for (int i = 0; i < Q; i++) f[i] = fmaf(sm1, f[i] + (float)Lat<Q>::w(i), f[i]);
     }
     template <int Q>
     __device__ static __forceinline__ void rest(T *f, double rho)
@@ -213,7 +222,7 @@ __global__ void __launch_bounds__(256) k_step(const typename P::T *__restrict__ 
             P::template rest<Q>(f, bc.rho_out);
         } else {
             gather<P, Q>(src, g, a.mode, gx, y, z, gnode, f);
-            if (Q == 19 && gx == bc.inlet_x) P::zou_he(f, bc.u_in, bc.inlet_x < g.nx / 2);
+            if (Q == 19 && gx == bc.inlet_x) P::zou_he(f, P::zou_he_prep(bc.u_in), bc.inlet_x < g.nx / 2);
             if (outlet) P::template outlet<Q>(f, bc.rho_out);
         }
         P::template collide<Q, OP>(f, prm);
