@@ -73,15 +73,19 @@ int pick_shape(int prec, int q, int nb, int slots, int n_runs, LaunchShape *out)
         int block = ((nb + npt - 1) / npt + 31) / 32 * 32;
         if (block < 32) block = 32;
         if (block > (npt == 1 ? 288 : 512)) continue;
-        const size_t smem = batch_smem(prec, q, nb, block);
-        const int occ = batch_occupancy(prec, q, npt, block, smem);
-        if (occ <= 0) continue;
-        const int per_sm = slots > 0 ? std::min(slots, occ) : occ;
-        out->npt = npt;
-        out->block = block;
-        out->smem = smem;
-        out->grid = std::max(1, std::min(n_runs, per_sm * sm_count()));
-        return ERLBM_OK;
+        // two population buffers (one barrier per step) when they fit, else one
+        for (int dbl = 1; dbl >= 0; dbl--) {
+            const size_t smem = batch_smem(prec, q, nb, block, dbl);
+            const int occ = batch_occupancy(prec, q, npt, block, smem);
+            if (occ <= 0) continue;
+            const int per_sm = slots > 0 ? std::min(slots, occ) : occ;
+            out->npt = npt;
+            out->block = block;
+            out->smem = smem;
+            out->dbl = dbl;
+            out->grid = std::max(1, std::min(n_runs, per_sm * sm_count()));
+            return ERLBM_OK;
+        }
     }
     set_error("lattice of %s nodes does not fit one CTA's shared memory%s", std::to_string(nb).c_str(), "");
     return ERLBM_E_UNSUPPORTED;
@@ -209,9 +213,9 @@ int run_batch(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec *runs,
     cudaMemsetAsync(d_counter, 0, sizeof(int), stream);
     const int lrc = d->precision == ERLBM_FP64
                         ? launch_batch_fp64(d->q, sh.npt, g, d_runs, n_runs, d_counter, d_res, d_aos, sh.grid,
-                                            sh.block, sh.smem, stream)
+                                            sh.block, sh.smem, sh.dbl, stream)
                         : launch_batch_fp32(d->q, sh.npt, g, d_runs, n_runs, d_counter, d_res, d_aos, sh.grid,
-                                            sh.block, sh.smem, stream);
+                                            sh.block, sh.smem, sh.dbl, stream);
     cudaError_t ce = cudaStreamEndCapture(stream, &graph);
     if (lrc != 0 || ce != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);

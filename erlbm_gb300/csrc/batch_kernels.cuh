@@ -169,12 +169,12 @@ __device__ __forceinline__ double block_max(double v, double *sh)
     return t;
 }
 
-// Shared memory: populations Q * NB of T, reduction scratch, the solid mask (NB bytes), the node
-// order (NB shorts) and the number of fluid nodes.
+// Shared memory: populations Q * NB of T (twice when ping-ponged), reduction scratch, the solid mask
+// (NB bytes), the node order (NB shorts), the number of fluid nodes and the Zou-He constants.
 template <class P, int Q>
-__host__ __device__ inline size_t batch_smem_bytes(int nb, int block)
+__host__ __device__ inline size_t batch_smem_bytes(int nb, int block, int dbl)
 {
-    const size_t pop = (size_t)Q * nb * sizeof(typename P::T);
+    const size_t pop = (size_t)Q * nb * sizeof(typename P::T) * (dbl ? 2 : 1);
     const size_t red = ((size_t)block + 1) * sizeof(double);
     const size_t mask = ((size_t)nb + 15) / 16 * 16;
     const size_t order = ((size_t)nb * sizeof(short) + 15) / 16 * 16;
@@ -193,16 +193,18 @@ struct BatchBounds {
 // Shared-memory carve-up of a batched CTA (sizes from batch_smem_bytes).
 template <class P, int Q>
 struct BatchSmem {
-    typename P::T *buf;
+    typename P::T *buf0, *buf1;  // the same buffer unless ping-ponged
     double *red;
     uint8_t *solid;
     short *order;   // node of each thread slot: fluid nodes only, boundary-plane nodes first
     int *n_fluid;
     double *zh;     // the run's Zou-He closure constants (P::ZouHe, <= 32 bytes)
-    __device__ BatchSmem(unsigned char *raw, int nb)
+    __device__ BatchSmem(unsigned char *raw, int nb, int dbl)
     {
-        buf = reinterpret_cast<typename P::T *>(raw);
-        red = reinterpret_cast<double *>(raw + ((size_t)Q * nb * sizeof(typename P::T) + 15) / 16 * 16);
+        const size_t one = (size_t)Q * nb * sizeof(typename P::T);
+        buf0 = reinterpret_cast<typename P::T *>(raw);
+        buf1 = dbl ? reinterpret_cast<typename P::T *>(raw + one) : buf0;
+        red = reinterpret_cast<double *>(raw + (one * (dbl ? 2 : 1) + 15) / 16 * 16);
         solid = reinterpret_cast<uint8_t *>(red + blockDim.x + 1);
         order = reinterpret_cast<short *>(solid + ((size_t)nb + 15) / 16 * 16);
         n_fluid = reinterpret_cast<int *>(order + ((size_t)nb * sizeof(short) + 15) / 16 * 16 / sizeof(short));
@@ -235,7 +237,10 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
 {
     using T = typename P::T;
     const int NB = g.nb;
-    T *buf = sm.buf;
+    // populations of the current step are read from cur and the next step's are stored to nxt; with
+    // two buffers one barrier per step suffices (a step's stores never touch what it reads)
+    T *cur = sm.buf0, *nxt = sm.buf1;
+    const bool dbl = sm.buf1 != sm.buf0;
     double *red = sm.red;
     const uint8_t *solid = sm.solid;
     const int tid = threadIdx.x;
@@ -287,7 +292,7 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
             for (int i = 0; i < Q; i++) f[s][i] = P::template from_f<Q>(Lat<Q>::w(i) * g.rho0, i);
         }
 #pragma unroll
-        for (int i = 0; i < Q; i++) buf[i * NB + node[s]] = f[s][i];
+        for (int i = 0; i < Q; i++) cur[i * NB + node[s]] = f[s][i];
     }
     __syncthreads();
 
@@ -321,7 +326,7 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
                     const int xs = wrap1(x - Lat<Q>::cx(i), g.nx);
                     const int ys = wrap1(y - Lat<Q>::cy(i), g.ny);
                     const int src = xs + g.nx * ys;
-                    f[s][i] = (any_solid && solid[src]) ? buf[Lat<Q>::opp(i) * NB + me] : buf[i * NB + src];
+                    f[s][i] = (any_solid && solid[src]) ? cur[Lat<Q>::opp(i) * NB + me] : cur[i * NB + src];
                 }
             }
         } else if (g.outlet_x >= 0) {
@@ -330,10 +335,10 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
                 if (!fluid[s] || nx_[s] != g.outlet_x) continue;
                 const int me = node[s] + ((g.outlet_x < g.nx / 2) ? 1 : -1);
 #pragma unroll
-                for (int i = 0; i < Q; i++) f[s][i] = buf[i * NB + me];
+                for (int i = 0; i < Q; i++) f[s][i] = cur[i * NB + me];
             }
         }
-        __syncthreads();
+        if (!dbl) __syncthreads();
 
         // ---- energy check on the post-stream populations ----
         if (g.energy_every > 0 && step > 0 && step % g.energy_every == 0) {
@@ -394,7 +399,12 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
                 }
             }
 #pragma unroll
-            for (int i = 0; i < Q; i++) buf[i * NB + node[s]] = f[s][i];
+            for (int i = 0; i < Q; i++) nxt[i * NB + node[s]] = f[s][i];
+        }
+        if (dbl) {
+            T *t = cur;
+            cur = nxt;
+            nxt = t;
         }
         if (g.density_check) {
             // finish the step everywhere, then stop if any node failed
@@ -432,10 +442,10 @@ template <class P, int Q, int NPT>
 __global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
                                   BatchBounds<NPT, sizeof(typename P::T)>::MINB)
     k_batch(BatchGeo g, const BatchRun *__restrict__ runs, int n_runs, int *__restrict__ counter,
-            BatchResult *__restrict__ res, const double *__restrict__ aos)
+            BatchResult *__restrict__ res, const double *__restrict__ aos, int dbl)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const BatchSmem<P, Q> sm(smem_raw, g.nb);
+    const BatchSmem<P, Q> sm(smem_raw, g.nb, dbl);
     __shared__ int s_run;
     const int tid = threadIdx.x;
     for (int k = tid; k < g.nb; k += blockDim.x) sm.solid[k] = g.solid ? g.solid[k] : 0;
@@ -499,10 +509,10 @@ __device__ __forceinline__ void st_release_sys(int *p, int v)
 template <class P, int Q, int NPT>
 __global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
                                   BatchBounds<NPT, sizeof(typename P::T)>::MINB)
-    k_slot_server(SlotRing ring, int max_nb)
+    k_slot_server(SlotRing ring, int max_nb, int dbl)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const BatchSmem<P, Q> sm(smem_raw, max_nb);
+    const BatchSmem<P, Q> sm(smem_raw, max_nb, dbl);
     __shared__ int s_idx;
     __shared__ SlotEntry s_entry;
     const int tid = threadIdx.x;

@@ -118,20 +118,23 @@ struct BatchResult;
 
 // Persistent batched launch (batch_kernels.cuh).  block = threads per CTA, npt = nodes per thread,
 // grid = CTAs; smem = dynamic shared bytes.  Returns 0, -1 (no such instantiation) or -3.
+// dbl: two population buffers in shared memory (one barrier per step) instead of one.
 int launch_batch_fp64(int q, int npt, const BatchGeo &g, const BatchRun *runs, int n_runs, int *counter,
-                      BatchResult *res, const double *aos, int grid, int block, size_t smem, cudaStream_t s);
+                      BatchResult *res, const double *aos, int grid, int block, size_t smem, int dbl,
+                      cudaStream_t s);
 int launch_batch_fp32(int q, int npt, const BatchGeo &g, const BatchRun *runs, int n_runs, int *counter,
-                      BatchResult *res, const double *aos, int grid, int block, size_t smem, cudaStream_t s);
+                      BatchResult *res, const double *aos, int grid, int block, size_t smem, int dbl,
+                      cudaStream_t s);
 // Launch shape of a batch: nodes per thread, threads per CTA, CTAs, dynamic shared bytes.
 struct LaunchShape {
-    int npt, block, grid;
+    int npt, block, grid, dbl;
     size_t smem;
 };
 int pick_shape(int prec, int q, int nb, int slots, int n_runs, LaunchShape *out);
 
 // Resident CTAs per SM for a configuration (0 if it cannot run).
 int batch_occupancy(int prec, int q, int npt, int block, size_t smem);
-size_t batch_smem(int prec, int q, int nb, int block);
+size_t batch_smem(int prec, int q, int nb, int block, int dbl);
 
 }  // namespace erlbm
 
@@ -140,8 +143,10 @@ namespace erlbm {
 struct SlotRing;
 
 // Device-resident request loop for D3Q19 lattices of <= 288 nodes (batch_kernels.cuh).
-int launch_slot_server_fp64(const SlotRing &ring, int max_nb, int grid, int block, size_t smem, cudaStream_t s);
-int launch_slot_server_fp32(const SlotRing &ring, int max_nb, int grid, int block, size_t smem, cudaStream_t s);
+int launch_slot_server_fp64(const SlotRing &ring, int max_nb, int grid, int block, size_t smem, int dbl,
+                            cudaStream_t s);
+int launch_slot_server_fp32(const SlotRing &ring, int max_nb, int grid, int block, size_t smem, int dbl,
+                            cudaStream_t s);
 int slot_server_occupancy_fp64(int block, size_t smem);
 int slot_server_occupancy_fp32(int block, size_t smem);
 

@@ -156,9 +156,9 @@ extern "C" int erlbm_batch_run_noalloc(const erlbm_batch_desc *d, int n_runs, co
     if ((rc = pick_shape(d->precision, d->q, g.nb, d->slots, n_runs, &sh))) return rc;
     const int lrc = d->precision == ERLBM_FP64
                         ? launch_batch_fp64(d->q, sh.npt, g, prepared, n_runs, counter, (BatchResult *)out, nullptr,
-                                            sh.grid, sh.block, sh.smem, s)
+                                            sh.grid, sh.block, sh.smem, sh.dbl, s)
                         : launch_batch_fp32(d->q, sh.npt, g, prepared, n_runs, counter, (BatchResult *)out, nullptr,
-                                            sh.grid, sh.block, sh.smem, s);
+                                            sh.grid, sh.block, sh.smem, sh.dbl, s);
     if (lrc == -1) {
         set_error("no batched kernel for this lattice shape%s%s", "", "");
         return ERLBM_E_UNSUPPORTED;

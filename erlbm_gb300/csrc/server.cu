@@ -264,7 +264,7 @@ int lane_setup(erlbm_server *s, SlotLane &L, int prec)
         (e = cudaEventCreateWithFlags(&L.exited, cudaEventDisableTiming)) != cudaSuccess)
         return cuda_fail(e, "server lane stream");
     L.block = 288;
-    L.smem = batch_smem(prec, 19, MAX_SLOT_NODES, L.block);
+    L.smem = batch_smem(prec, 19, MAX_SLOT_NODES, L.block, 1);
     const int occ = prec == ERLBM_FP64 ? slot_server_occupancy_fp64(L.block, L.smem)
                                        : slot_server_occupancy_fp32(L.block, L.smem);
     if (occ <= 0) {
@@ -277,9 +277,9 @@ int lane_setup(erlbm_server *s, SlotLane &L, int prec)
 
 int lane_launch(SlotLane &L)
 {
-    const int rc = L.prec == ERLBM_FP64 ? launch_slot_server_fp64(L.ring, MAX_SLOT_NODES, L.grid, L.block, L.smem,
+    const int rc = L.prec == ERLBM_FP64 ? launch_slot_server_fp64(L.ring, MAX_SLOT_NODES, L.grid, L.block, L.smem, 1,
                                                                   L.stream)
-                                        : launch_slot_server_fp32(L.ring, MAX_SLOT_NODES, L.grid, L.block, L.smem,
+                                        : launch_slot_server_fp32(L.ring, MAX_SLOT_NODES, L.grid, L.block, L.smem, 1,
                                                                   L.stream);
     if (rc) return cuda_fail(cudaGetLastError(), "slot loop launch");
     cudaEventRecord(L.exited, L.stream);
