@@ -454,6 +454,124 @@ static void zou_he_inlet(orc_lattice *L, int px, double vx)
         }
 }
 
+/* ZouHeD2Q9_vx_x (Boundary_conditions.cpp:710-744): the +x movers set from the closure density */
+static void zou_he_d2q9(orc_lattice *L, int px, double vx)
+{
+    for (int y = 0; y < L->ny; y++) {
+        const int m = L->ini[px + y * L->nx];
+        if (!m) continue;
+        double *f = L->f + (size_t)(m - 1) * 9;
+        const double rho = (f[0] + f[3] + f[4] + 2 * (f[2] + f[8] + f[6])) / (1. - vx);
+        f[1] = (rho / 9.0) * (1.0 + 3.0 * vx + 3.0 * vx * vx);
+        f[5] = (rho / 36.0) * (1.0 + 3.0 * vx + 3.0 * vx * vx);
+        f[7] = (rho / 36.0) * (1.0 + 3.0 * vx + 3.0 * vx * vx);
+    }
+}
+
+/* the parabolic profile of parabolic_D3Q19_x / parabolic_D2Q9_x (:467-472, :759-764) at the h-th
+ * fluid node of a column (h from 1) */
+static double parabolic_vel(int h, double vx_max, int Lw)
+{
+    const double d_h = (double)h - 0.5;
+    return -4.0 * vx_max / (Lw * Lw) * (d_h) * (d_h - Lw);
+}
+
+/* parabolic_D3Q19_x (:456-530) and parabolic_D2Q9_x (:748-800): a Zou-He closure with the profile's
+ * velocity, the h-th fluid node of each column (per z) taking the h-th value; D3Q19 sets the +x
+ * movers from their opposites */
+static void parabolic_inlet(orc_lattice *L, int px, double vx_max, int Lw)
+{
+    for (int z = 0; z < L->nz; z++) {
+        int h = 0;
+        for (int y = 0; y < L->ny; y++) {
+            const int m = L->ini[px + y * L->nx + z * L->ny * L->nx];
+            if (!m) continue;
+            h++;
+            const double vx = parabolic_vel(h, vx_max, Lw);
+            double *f = L->f + (size_t)(m - 1) * L->q;
+            if (L->q == 9) {
+                const double rho = (f[0] + f[3] + f[4] + 2 * (f[2] + f[8] + f[6])) / (1. - vx);
+                f[1] = (rho / 9.0) * (1.0 + 3.0 * vx + 3.0 * vx * vx);
+                f[5] = (rho / 36.0) * (1.0 + 3.0 * vx + 3.0 * vx * vx);
+                f[7] = (rho / 36.0) * (1.0 + 3.0 * vx + 3.0 * vx * vx);
+                continue;
+            }
+            const double sum_f_xminus = f[2] + f[8] + f[10] + f[12] + f[14];
+            const double sum_f_xzero = f[0] + f[3] + f[4] + f[5] + f[6] + f[15] + f[16] + f[17] + f[18];
+            const double rho = (2.0 * sum_f_xminus + sum_f_xzero) / (1.0 - vx);
+            const double vy = 0.0, vz = 0.0;
+            f[1] = f[2] + rho * vx / 3.0;
+            f[7] = f[8] + rho * vx / 6.0 + 0.5 * rho * vy - 0.5 * (f[18] + f[3] + f[16] - f[15] - f[4] - f[17]);
+            f[9] = f[10] + rho * vx / 6.0 - 0.5 * rho * vy + 0.5 * (f[18] + f[3] + f[16] - f[15] - f[4] - f[17]);
+            f[11] = f[12] + rho * vx / 6.0 + 0.5 * rho * vz - 0.5 * (f[17] + f[5] + f[16] - f[15] - f[6] - f[18]);
+            f[13] = f[14] + rho * vx / 6.0 - 0.5 * rho * vz + 0.5 * (f[17] + f[5] + f[16] - f[15] - f[6] - f[18]);
+        }
+    }
+}
+
+/* OpenBoundaryD2Q9_x (:584-621): the populations entering from outside copied from the inner
+ * neighbour (solid nodes, which the reference does not test for, are skipped) */
+static void open_x(orc_lattice *L, int px)
+{
+    const int d = (px < L->nx / 2) ? 1 : -1;
+    for (int y = 0; y < L->ny; y++) {
+        const int m = L->ini[px + y * L->nx], ma = L->ini[px + d + y * L->nx];
+        if (!m || !ma) continue;
+        double *f = L->f + (size_t)(m - 1) * 9;
+        const double *fa = L->f + (size_t)(ma - 1) * 9;
+        if (d > 0) {
+            f[1] = fa[1];
+            f[5] = fa[5];
+            f[7] = fa[7];
+        } else {
+            f[2] = fa[2];
+            f[6] = fa[6];
+            f[8] = fa[8];
+        }
+    }
+}
+
+/* OpenBoundaryD2Q9_y (:542-580) */
+static void open_y(orc_lattice *L, int py)
+{
+    const int d = (py < L->ny / 2) ? 1 : -1;
+    for (int x = 0; x < L->nx; x++) {
+        const int m = L->ini[x + py * L->nx], ma = L->ini[x + (py + d) * L->nx];
+        if (!m || !ma) continue;
+        double *f = L->f + (size_t)(m - 1) * 9;
+        const double *fa = L->f + (size_t)(ma - 1) * 9;
+        if (d > 0) {
+            f[3] = fa[3];
+            f[5] = fa[5];
+            f[8] = fa[8];
+        } else {
+            f[4] = fa[4];
+            f[6] = fa[6];
+            f[7] = fa[7];
+        }
+    }
+}
+
+/* convective_x (:627-706): f = (f + U f_A) / (1 + U), U = the x velocity (calcula) of the inner
+ * neighbour A (solid neighbours, which the reference does not test for, are skipped) */
+static void convective_outlet(orc_lattice *L, int px)
+{
+    const int infx = (px < L->nx / 2) ? 1 : -1;
+    for (int y = 0; y < L->ny; y++)
+        for (int z = 0; z < L->nz; z++) {
+            const int m = L->ini[px + y * L->nx + z * L->ny * L->nx];
+            const int ma = L->ini[(px + infx) + y * L->nx + z * L->ny * L->nx];
+            if (!m || !ma) continue;
+            const double *fa = L->f + (size_t)(ma - 1) * L->q;
+            double u[3], rho;
+            moments(L->t, fa, u, &rho);
+            const double U = u[0];
+            double *f = L->f + (size_t)(m - 1) * L->q;
+            const double factor = 1.0 / (1.0 + U);
+            for (int i = 0; i < L->q; i++) f[i] = factor * (f[i] + U * fa[i]);
+        }
+}
+
 /* devnull_rho_x (Boundary_conditions.cpp:68-141): outlet plane copied from its inner neighbour
  * and rescaled to rho; rest equilibrium w_i rho when the neighbour is solid. */
 static void outlet_rescale(orc_lattice *L, int px, double rho)
@@ -481,8 +599,23 @@ static void outlet_rescale(orc_lattice *L, int px, double rho)
  * Returns the running max |rho| / flags when density checking is requested. */
 static void one_step(orc_lattice *L, const orc_bc *bc, int nthreads, double *max_abs_rho, int *nonfinite)
 {
-    if (bc && bc->inlet_x >= 0) zou_he_inlet(L, bc->inlet_x, bc->u_in);
-    if (bc && bc->outlet_x >= 0) outlet_rescale(L, bc->outlet_x, bc->rho_out);
+    if (bc && bc->inlet_x >= 0) {
+        if (bc->inlet_kind == 1)
+            parabolic_inlet(L, bc->inlet_x, bc->u_in, bc->parabolic_L);
+        else if (L->q == 9)
+            zou_he_d2q9(L, bc->inlet_x, bc->u_in);
+        else
+            zou_he_inlet(L, bc->inlet_x, bc->u_in);
+    }
+    if (bc && bc->outlet_x >= 0) {
+        if (bc->outlet_kind == 1 && L->q == 9)
+            open_x(L, bc->outlet_x);
+        else if (bc->outlet_kind == 2)
+            convective_outlet(L, bc->outlet_x);
+        else
+            outlet_rescale(L, bc->outlet_x, bc->rho_out);
+    }
+    if (bc && bc->open_y >= 0 && L->q == 9) open_y(L, bc->open_y);
     const int q = L->q;
     const tables_t *t = L->t;
     double mx = 0.0;
@@ -1045,4 +1178,54 @@ int orc_velocity_error(int nx, int ny, const double *vel, int nx_ref, int ny_ref
     *e_mod = sqrt(sum_dif2 / sum_ur2);
     *e_vec = sqrt(sum_vec2 / sum_ur2);
     return 0;
+}
+
+/* read_geo (LBM_functions.cpp:282-353): four header lines, "DIMENSIONS nx ny nz", five more header
+ * lines, then one integer per node of the file's box, x fastest; the added layers are fluid, except
+ * that with `wall` the planes x = 0 and x = nx - 1 of the widened box are solid. */
+int orc_read_geo(const char *path, int pts_in, int pts_out, int wall, int *nx_out, int *ny_out, int *nz_out,
+                 uint8_t *solid)
+{
+    FILE *fp = fopen(path, "r");
+    if (!fp) return -1;
+    char line[4096];
+    for (int i = 0; i < 4; i++)
+        if (!fgets(line, sizeof line, fp)) {
+            fclose(fp);
+            return -1;
+        }
+    int nx, ny, nz;
+    if (!fgets(line, sizeof line, fp) || sscanf(line, "%*s %d %d %d", &nx, &ny, &nz) != 3) {
+        fclose(fp);
+        return -1;
+    }
+    for (int i = 0; i < 5; i++)
+        if (!fgets(line, sizeof line, fp)) {
+            fclose(fp);
+            return -1;
+        }
+    nx = nx + pts_in + pts_out;
+    *nx_out = nx;
+    *ny_out = ny;
+    *nz_out = nz;
+    int poros = 0;
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                const long long pos = x + (long long)y * nx + (long long)z * ny * nx;
+                int fluid;
+                if (x >= pts_in && x < nx - pts_out) {
+                    int v = 0;
+                    if (fscanf(fp, "%d", &v) != 1) v = 0;
+                    fluid = v != 0;
+                } else if ((x == 0 || x == nx - 1) && wall) {
+                    fluid = 0;
+                } else {
+                    fluid = 1;
+                }
+                poros += fluid;
+                if (solid) solid[pos] = (uint8_t)!fluid;
+            }
+    fclose(fp);
+    return poros;
 }

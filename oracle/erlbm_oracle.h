@@ -21,10 +21,14 @@ extern "C" {
 typedef struct orc_lattice orc_lattice;
 
 typedef struct orc_bc {
-    int inlet_x;    /* Zou-He velocity inlet plane, -1 = none */
-    double u_in;    /* imposed x velocity */
-    int outlet_x;   /* copy-and-rescale outlet plane, -1 = none */
-    double rho_out; /* density the outlet is rescaled to */
+    int inlet_x;     /* velocity inlet plane, -1 = none */
+    double u_in;     /* imposed x velocity (the profile maximum for a parabolic inlet) */
+    int outlet_x;    /* outlet plane, -1 = none */
+    double rho_out;  /* density a copy-and-rescale outlet is rescaled to */
+    int inlet_kind;  /* 0 Zou-He (ZouHeD3Q19_vx_x / ZouHeD2Q9_vx_x), 1 parabolic (parabolic_D3Q19_x / _D2Q9_x) */
+    int parabolic_L; /* channel width of the parabolic profile */
+    int outlet_kind; /* 0 devnull_rho_x, 1 OpenBoundaryD2Q9_x, 2 convective_x */
+    int open_y;      /* OpenBoundaryD2Q9_y plane, -1 = none */
 } orc_bc;
 
 orc_lattice *orc_create(int q, int nx, int ny, int nz, const uint8_t *solid, double tau, double tau_nh, int op);
@@ -68,6 +72,11 @@ int orc_max_threads(void);
 void orc_field(int q, int nx, int ny, int nz, const uint8_t *solid, const double *aos, int field, double *out);
 int orc_write_vtk(int q, int nx, int ny, int nz, const uint8_t *solid, const double *aos, int field, int format,
                   const char *path);
+/* read_geo (LBM_functions.cpp:282-353): the solid mask (1 = solid) of a legacy ASCII VTK geometry
+ * file (nonzero = fluid) with pts_in / pts_out layers added in x; with `wall` the first and last x
+ * planes of the added layers are solid.  solid may be NULL to read the dimensions only; returns the
+ * fluid count, -1 if the file cannot be read. */
+int orc_read_geo(const char *path, int pts_in, int pts_out, int wall, int *nx, int *ny, int *nz, uint8_t *solid);
 int orc_velocity_error(int nx, int ny, const double *vel, int nx_ref, int ny_ref, const double *vel_ref,
                        int text_digits, double *e_vec, double *e_mod);
 

@@ -25,7 +25,17 @@ _u8 = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 
 
 class OrcBC(C.Structure):
-    _fields_ = [("inlet_x", C.c_int), ("u_in", C.c_double), ("outlet_x", C.c_int), ("rho_out", C.c_double)]
+    _fields_ = [("inlet_x", C.c_int), ("u_in", C.c_double), ("outlet_x", C.c_int), ("rho_out", C.c_double),
+                ("inlet_kind", C.c_int), ("parabolic_L", C.c_int), ("outlet_kind", C.c_int), ("open_y", C.c_int)]
+
+
+INLET_ZOUHE, INLET_PARABOLIC = 0, 1
+OUTLET_DENSITY, OUTLET_OPEN, OUTLET_CONVECTIVE = 0, 1, 2
+
+
+def orc_bc(bc: dict) -> OrcBC:
+    return OrcBC(bc.get("inlet_x", -1), bc.get("u_in", 0.0), bc.get("outlet_x", -1), bc.get("rho_out", 1.0),
+                 bc.get("inlet_kind", 0), bc.get("parabolic_L", 0), bc.get("outlet_kind", 0), bc.get("open_y", -1))
 
 
 def build(force: bool = False) -> str:
@@ -75,6 +85,8 @@ def load():
                                     _ip, _ip, _dp]),
         "orc_max_threads": (C.c_int, []),
         "orc_field": (None, [C.c_int, C.c_int, C.c_int, C.c_int, vp, _dp, C.c_int, _dp]),
+        "orc_read_geo": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), vp]),
         "orc_write_vtk": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, vp, _dp, C.c_int, C.c_int, C.c_char_p]),
         "orc_velocity_error": (C.c_int, [C.c_int, C.c_int, _dp, C.c_int, C.c_int, _dp, C.c_int,
                                          C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -121,8 +133,7 @@ class Lattice:
     def step(self, n, bc=None, threads=1):
         b = None
         if bc is not None:
-            b = C.byref(OrcBC(bc.get("inlet_x", -1), bc.get("u_in", 0.0), bc.get("outlet_x", -1),
-                              bc.get("rho_out", 1.0)))
+            b = C.byref(orc_bc(bc))
         load().orc_step(self.h, int(n), b, int(threads))
 
     def kinetic_energy(self, stage=0):
@@ -249,6 +260,18 @@ def write_vtk(q, nx, ny, nz, solid, aos, kind, fmt, path):
         raise OSError(f"cannot write {path}")
 
 
+def read_geo(path, pts_in=0, pts_out=0, wall=True):
+    """read_geo's solid mask: (nx, ny, nz, solid uint8 array, fluid count)."""
+    nx, ny, nz = C.c_int(), C.c_int(), C.c_int()
+    n = load().orc_read_geo(os.fsencode(path), pts_in, pts_out, int(wall), C.byref(nx), C.byref(ny), C.byref(nz), None)
+    if n < 0:
+        raise OSError(f"cannot read {path}")
+    solid = np.zeros(nx.value * ny.value * nz.value, np.uint8)
+    n = load().orc_read_geo(os.fsencode(path), pts_in, pts_out, int(wall), C.byref(nx), C.byref(ny), C.byref(nz),
+                            solid.ctypes.data)
+    return nx.value, ny.value, nz.value, solid, n
+
+
 def velocity_error(nx, ny, vel, nx_ref, ny_ref, vel_ref, text_digits=0):
     """tools/error_calculator.cpp on two velocity fields (3 values per node); returns (E_vec, E_mod)."""
     ev, em = C.c_double(), C.c_double()
@@ -278,6 +301,11 @@ def load_ref(q: int):
     getattr(lib, p + "run").restype = C.c_int
     getattr(lib, p + "run").argtypes = [C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_double, C.c_double, _dp,
                                        C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, vp, vp, vp]
+    getattr(lib, p + "run_bc").restype = C.c_int
+    getattr(lib, p + "run_bc").argtypes = [C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_double, C.c_double, vp, C.c_int,
+                                          vp, vp, vp, vp]
+    getattr(lib, p + "read_geo").restype = C.c_int
+    getattr(lib, p + "read_geo").argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]
     if q == 9:
         lib.ref9_init_taylor_green.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, _dp]
         lib.ref9_init_double_shear.argtypes = [C.c_int, C.c_double, _dp]

@@ -155,6 +155,71 @@ void ref9_init_double_shear(int L, double rho_ini, double *f_out)
 int ref9_taylor_green_main(int argc, char **argv) { return erlbm_ref_main_taylor_green(argc, argv); }
 #endif
 
+// A driver loop with the channel boundaries of the library (Boundary_conditions.cpp), called before
+// the node loop in this order: inlet (bci[1] = 0: ZouHeD3Q19_vx_x or ZouHeD2Q9_vx_x; 1: parabolic_D3Q19_x
+// or parabolic_D2Q9_x with width bci[2]), outlet (bci[4] = 0: devnull_rho_x; 1: OpenBoundaryD2Q9_x;
+// 2: convective_x), then OpenBoundaryD2Q9_y.  bci = {inlet_x, inlet_kind, L, outlet_x, outlet_kind,
+// open_y} (-1 = none), bcd = {u_in, rho_out}.  Outputs as in run().
+int REF_PREFIX(run_bc)(int nx, int ny, int nz, const uint8_t *solid, int col, double tau, double tau_nh,
+                       const double *f_in, int n_steps, const int *bci, const double *bcd, double *f_post_stream,
+                       double *f_post_collision)
+{
+    RefCase c;
+    make_case(c, nx, ny, nz, solid);
+    const int n = c.geometry.fluid * nvel;
+    for (int k = 0; k < n; k++) c.lattice.inif[k] = f_in[k];
+    for (int k = 0; k < n; k++) c.lattice.inif_new[k] = 0.0;
+    PARAMETERS p;
+    p.tau = tau;
+    p.tau_nh = tau_nh;
+    p.visc = (tau - 0.5) / 3.;
+    p.rho_ini = 1.0;
+    for (int step = 0; step < n_steps; step++) {
+        if (bci[0] >= 0) {
+#if REF_Q == 19
+            if (bci[1] == 1) parabolic_D3Q19_x(bci[0], bcd[0], bci[2], c.geometry, c.lattice);
+            else ZouHeD3Q19_vx_x(bci[0], bcd[0], c.geometry, c.lattice);
+#else
+            if (bci[1] == 1) parabolic_D2Q9_x(bci[0], bcd[0], bci[2], c.geometry, c.lattice);
+            else ZouHeD2Q9_vx_x(bci[0], bcd[0], c.geometry, c.lattice);
+#endif
+        }
+        if (bci[3] >= 0) {
+            if (bci[4] == 2) convective_x(bci[3], c.geometry, c.lattice);
+#if REF_Q == 9
+            else if (bci[4] == 1) OpenBoundaryD2Q9_x(bci[3], c.geometry, c.lattice);
+#endif
+            else devnull_rho_x(bci[3], bcd[1], c.geometry, c.lattice);
+        }
+#if REF_Q == 9
+        if (bci[5] >= 0) OpenBoundaryD2Q9_y(bci[5], c.geometry, c.lattice);
+#endif
+        for (int pto = 0; pto < c.geometry.fluid; pto++) {
+            double *f = c.lattice.inif + pto * nvel;
+            colisao_sitio(f, 0., 0., 0., c.lattice, p, col);
+            double mx, my, mz;
+            propag_site(c.lattice, pto, mx, my, mz);
+        }
+        double *t = c.lattice.inif;
+        c.lattice.inif = c.lattice.inif_new;
+        c.lattice.inif_new = t;
+    }
+    if (f_post_stream)
+        for (int k = 0; k < n; k++) f_post_stream[k] = c.lattice.inif[k];
+    if (f_post_collision)
+        for (int k = 0; k < n; k++) f_post_collision[k] = c.lattice.inif_new[k];
+    free_case(c);
+    return 0;
+}
+
+// read_geo (LBM_functions.cpp:282-353, the overload with the wall flag): geometry.ini of a legacy
+// VTK geometry file with pts_in / pts_out layers added in x.  meio must hold (nx + pts_in + pts_out)
+// * ny * nz ints; returns the number of fluid nodes.
+int REF_PREFIX(read_geo)(const char *path, int pts_in, int pts_out, int wall, int *meio)
+{
+    return read_geo(std::string(path), meio, pts_in, pts_out, wall != 0);
+}
+
 // The reference's field writers (LBM_functions.cpp: rec_velocity :4218, rec_vorticity :4302,
 // rec_density :4416 in ASCII; rec_velocity_bin :4979, rec_vorticity_bin :5061, rec_density_bin
 // :5179 in big-endian binary) on the given AoS populations.  field: 1 velocity, 2 vorticity,

@@ -23,6 +23,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import hashlib
 import json
 import multiprocessing as mp
 import os
@@ -61,6 +62,29 @@ def read_map(path):
 
 
 TG_SUB = [(20 * (i + 1) - 1, 20 * j) for j in range(20) for i in range(20)]
+
+# channel-boundary cases: (q, nx, ny, nz, walls at y = 0 and ny - 1 (else only at ny - 1), bc)
+BC_CASES = (
+    (9, 16, 10, 1, True, dict(inlet_x=1, inlet_kind=0, u_in=0.04, outlet_x=14, outlet_kind=0, rho_out=1.0)),
+    (9, 16, 10, 1, True, dict(inlet_x=1, inlet_kind=1, parabolic_L=8, u_in=0.06, outlet_x=14, outlet_kind=1)),
+    (9, 16, 10, 1, True, dict(inlet_x=1, inlet_kind=0, u_in=0.04, outlet_x=14, outlet_kind=2)),
+    (9, 16, 10, 1, False, dict(inlet_x=1, inlet_kind=1, parabolic_L=9, u_in=0.05, outlet_x=14, outlet_kind=1,
+                               open_y=0)),
+    (19, 12, 8, 2, True, dict(inlet_x=1, inlet_kind=1, parabolic_L=6, u_in=0.05, outlet_x=10, outlet_kind=0,
+                              rho_out=1.0)),
+    (19, 12, 8, 2, True, dict(inlet_x=1, inlet_kind=0, u_in=0.04, outlet_x=10, outlet_kind=2)),
+)
+
+
+def channel_mask(nx, ny, nz, walls_y):
+    """Solid planes x = 0 and x = nx - 1, and y = 0 and y = ny - 1 (walls_y) or y = ny - 1 alone."""
+    s = np.zeros((nz, ny, nx), np.uint8)
+    s[:, :, 0] = 1
+    s[:, :, nx - 1] = 1
+    s[:, ny - 1, :] = 1
+    if walls_y:
+        s[:, 0, :] = 1
+    return s.reshape(-1)
 OB_SUB = [(20 * i, 20 * j) for j in range(20) for i in range(20)]
 
 
@@ -227,6 +251,51 @@ def vectors():
                    capture_output=True)
     line = open(os.path.join(tmp, "erro_L2.dat")).read().split()
     vec["errcalc_dsl16_vs_dsl32"] = np.array([16, 32, 20, 40, float(line[1]), float(line[2])])
+    # channel boundaries of the library (run_bc): walls at x = 0, nx - 1 and y = 0, ny - 1 (or only
+    # y = ny - 1), 25 steps of E-RLBM from a perturbed flow; meta = q nx ny nz walls_y tau tau_nh op
+    # steps inlet_x inlet_kind L u_in outlet_x outlet_kind rho_out open_y
+    brng = np.random.default_rng(20261204)
+    for k, (q, nx_, ny_, nz_, wy, bc) in enumerate(BC_CASES):
+        s = channel_mask(nx_, ny_, nz_, wy)
+        n_fl = int((s == 0).sum())
+        fs = []
+        for _ in range(n_fl):
+            u = brng.normal(0, 0.03, 3)
+            if q == 9:
+                u[2] = 0.0
+            fs.append(O.equilibrium(q, u[0] + 0.05, u[1], u[2], 1 + brng.normal(0, 0.01)))
+        f0 = np.concatenate(fs)
+        f0 = f0 + brng.normal(0, 1e-4, f0.size)
+        bci = np.array([bc.get("inlet_x", -1), bc.get("inlet_kind", 0), bc.get("parabolic_L", 0),
+                        bc.get("outlet_x", -1), bc.get("outlet_kind", 0), bc.get("open_y", -1)], np.int32)
+        bcd = np.array([bc.get("u_in", 0.0), bc.get("rho_out", 1.0)])
+        ps, pc = np.empty_like(f0), np.empty_like(f0)
+        fn = getattr(O.load_ref(q), f"ref{q}_run_bc")
+        fn(nx_, ny_, nz_, s.ctypes.data, 4, 0.56, 0.7, f0.ctypes.data, 25, bci.ctypes.data, bcd.ctypes.data,
+           ps.ctypes.data, pc.ctypes.data)
+        vec[f"bc{k}_in"] = f0
+        vec[f"bc{k}_post_collision"] = pc
+        vec[f"bc{k}_post_stream_sha256"] = np.frombuffer(hashlib.sha256(ps.tobytes()).digest(), dtype=np.uint8)
+        vec[f"bc{k}_meta"] = np.array([q, nx_, ny_, nz_, int(wy), 0.56, 0.7, 4, 25, bci[0], bci[1], bci[2], bcd[0],
+                                       bci[3], bci[4], bcd[1], bci[5]], dtype=np.float64)
+    # read_geo on a generated geometry file (the file's text is stored too)
+    grng = np.random.default_rng(7)
+    gx, gy, gz = 9, 5, 2
+    vals = (grng.random(gx * gy * gz) > 0.3).astype(int)
+    text = ("# vtk DataFile Version 2.0\nGeometria\nASCII\nDATASET STRUCTURED_POINTS\n"
+            f"DIMENSIONS {gx} {gy} {gz}\nASPECT_RATIO 1 1 1\nORIGIN 0 0 0\nPOINT_DATA {gx * gy * gz}\n"
+            "SCALARS geometria int\nLOOKUP_TABLE default\n" + " ".join(str(v) for v in vals) + "\n")
+    gpath = os.path.join(tmp, "geo.vtk")
+    with open(gpath, "w") as fgeo:
+        fgeo.write(text)
+    vec["geo_file"] = np.frombuffer(text.encode(), dtype=np.uint8)
+    for pin, pout, wall in ((0, 0, 1), (2, 3, 1), (2, 3, 0)):
+        meio = np.zeros((gx + pin + pout) * gy * gz, np.int32)
+        lib = O.load_ref(9)
+        lib.ref9_read_geo.restype = C.c_int
+        nfl = lib.ref9_read_geo(gpath.encode(), pin, pout, wall, meio.ctypes.data_as(C.POINTER(C.c_int)))
+        vec[f"geo_ini_{pin}_{pout}_{wall}"] = meio
+        vec[f"geo_fluid_{pin}_{pout}_{wall}"] = np.array([nfl])
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
     print("wrote", sorted(os.listdir(HERE)))
 

@@ -176,3 +176,51 @@ def test_error_calculator_matches_tool():
     assert float(f"{e[0]:.10g}") == ev and float(f"{e[1]:.10g}") == em
     full = O.velocity_error(int(Ls), int(Ls), fields[0], int(Lr), int(Lr), fields[1])
     assert full != e and abs(full[0] - e[0]) < 1e-4 * e[0]
+
+
+def channel_mask(nx, ny, nz, walls_y):
+    """Solid planes x = 0, x = nx - 1 and y = ny - 1, plus y = 0 when walls_y (make_golden.py's)."""
+    s = np.zeros((nz, ny, nx), np.uint8)
+    s[:, :, 0] = 1
+    s[:, :, nx - 1] = 1
+    s[:, ny - 1, :] = 1
+    if walls_y:
+        s[:, 0, :] = 1
+    return s.reshape(-1)
+
+
+def bc_case(v, k):
+    m = v[f"bc{k}_meta"]
+    q, nx, ny, nz, wy = (int(x) for x in m[:5])
+    tau, tnh, op, steps = m[5], m[6], int(m[7]), int(m[8])
+    bc = dict(inlet_x=int(m[9]), inlet_kind=int(m[10]), parabolic_L=int(m[11]), u_in=m[12], outlet_x=int(m[13]),
+              outlet_kind=int(m[14]), rho_out=m[15], open_y=int(m[16]))
+    return q, nx, ny, nz, channel_mask(nx, ny, nz, bool(wy)), tau, tnh, op, steps, bc
+
+
+@pytest.mark.parametrize("k", range(6))
+def test_channel_boundaries_bitwise(k):
+    """ZouHeD2Q9_vx_x, parabolic_D2Q9_x / parabolic_D3Q19_x, OpenBoundaryD2Q9_x / _y, convective_x and
+    devnull_rho_x (Boundary_conditions.cpp) in 25-step runs of the reference library: the oracle
+    reproduces them bit for bit."""
+    import hashlib
+    v = vectors()
+    q, nx, ny, nz, solid, tau, tnh, op, steps, bc = bc_case(v, k)
+    lat = O.Lattice(q, nx, ny, nz, solid, tau, tnh, op)
+    lat.set(v[f"bc{k}_in"])
+    lat.step(steps, bc)
+    assert np.array_equal(lat.get(1), v[f"bc{k}_post_collision"])
+    assert hashlib.sha256(lat.get(0).tobytes()).digest() == v[f"bc{k}_post_stream_sha256"].tobytes()
+
+
+@pytest.mark.parametrize("layers", [(0, 0, 1), (2, 3, 1), (2, 3, 0)])
+def test_read_geo(layers, tmp_path):
+    """read_geo (LBM_functions.cpp:282-353) with added inlet/outlet layers, with and without walls."""
+    v = vectors()
+    path = tmp_path / "geo.vtk"
+    path.write_bytes(v["geo_file"].tobytes())
+    pin, pout, wall = layers
+    nx, ny, nz, solid, n = O.read_geo(str(path), pin, pout, bool(wall))
+    ini = v[f"geo_ini_{pin}_{pout}_{wall}"]
+    assert n == int(v[f"geo_fluid_{pin}_{pout}_{wall}"][0]) and solid.size == ini.size
+    assert np.array_equal(solid == 0, ini != 0)
