@@ -15,7 +15,8 @@ import numpy as np
 
 from . import _lib
 from ._lib import (FIELD_DENSITY, FIELD_VELOCITY, FIELD_VORTICITY, FP32_SHIFTED, FP64, INIT_AOS, INIT_REST,
-                   INIT_TG_MAP, MAP_OBSTACLE, MAP_TAYLOR_GREEN, OP_BGK, OP_EXTREG, OP_MRT, OP_REG, REQ_OBSTACLE,
+                   INIT_TG_MAP, INLET_PARABOLIC, INLET_ZOUHE, MAP_OBSTACLE, MAP_TAYLOR_GREEN, OP_BGK, OP_EXTREG,
+                   OP_MRT, OP_REG, OUTLET_CONVECTIVE, OUTLET_DENSITY, OUTLET_OPEN, REQ_OBSTACLE,
                    REQ_TG2D, REQ_TG3D, REQ_TG_MAP_POINT, STAGE_POST_COLLISION, STAGE_POST_STREAM, VTK_ASCII,
                    VTK_BINARY_DOUBLE, VTK_BINARY_FLOAT, ErlbmError, check, lib)
 
@@ -25,7 +26,8 @@ __all__ = ["Lattice", "ErlbmError", "lib", "OP_BGK", "OP_MRT", "OP_REG", "OP_EXT
            "obstacle_map_params", "operator_from_name", "map_run", "map_run_refined", "batch_run", "INIT_REST",
            "INIT_TG_MAP", "INIT_AOS", "Server", "REQ_TG2D", "REQ_TG_MAP_POINT", "REQ_OBSTACLE", "REQ_TG3D",
            "FIELD_VELOCITY", "FIELD_VORTICITY", "FIELD_DENSITY", "VTK_ASCII", "VTK_BINARY_FLOAT",
-           "VTK_BINARY_DOUBLE", "velocity_error"]
+           "VTK_BINARY_DOUBLE", "velocity_error", "INLET_ZOUHE", "INLET_PARABOLIC", "OUTLET_DENSITY", "OUTLET_OPEN",
+           "OUTLET_CONVECTIVE", "read_geo"]
 
 _OPS = {"bgk": OP_BGK, "mrt": OP_MRT, "reg": OP_REG, "erlbm": OP_EXTREG}
 
@@ -150,6 +152,19 @@ class Lattice:
         return dict(label=r.label, decided_step=r.decided_step, steps_done=r.steps_done, margin=r.margin)
 
 
+def read_geo(path: str, pts_in: int = 0, pts_out: int = 0, wall: bool = True):
+    """read_geo (LBM_functions.cpp:282-353): (nx, ny, nz, solid) of a legacy VTK geometry file, with
+    fluid layers added in x; `solid` is the uint8 mask erlbm_desc takes (x fastest, 1 = solid)."""
+    nx, ny, nz = C.c_int(), C.c_int(), C.c_int()
+    p = os.fsencode(path)
+    check(lib().erlbm_read_geo(p, pts_in, pts_out, int(wall), C.byref(nx), C.byref(ny), C.byref(nz), None, 0),
+          "erlbm_read_geo")
+    solid = np.zeros(nx.value * ny.value * nz.value, np.uint8)
+    check(lib().erlbm_read_geo(p, pts_in, pts_out, int(wall), C.byref(nx), C.byref(ny), C.byref(nz), _dptr(solid),
+                               solid.size), "erlbm_read_geo")
+    return nx.value, ny.value, nz.value, solid
+
+
 def velocity_error(sim: Lattice, ref: Lattice, text_digits: int = 0, sim_stage: int = STAGE_POST_COLLISION,
                    ref_stage: int = STAGE_POST_COLLISION):
     """tools/error_calculator.cpp between two lattices on the GPU: (E_vec, E_mod) of sim's velocity
@@ -162,10 +177,14 @@ def velocity_error(sim: Lattice, ref: Lattice, text_digits: int = 0, sim_stage: 
 
 
 def _bc(bc: dict | None):
+    """erlbm_bc from a dict: inlet_x, u_in, outlet_x, rho_out, inlet_kind, parabolic_L, outlet_kind and
+    open_y (-1 or absent = no open y plane)."""
     if bc is None:
         return None
+    oy = int(bc.get("open_y", -1))
     return _lib.BC(int(bc.get("inlet_x", -1)), float(bc.get("u_in", 0.0)), int(bc.get("outlet_x", -1)),
-                   float(bc.get("rho_out", 1.0)))
+                   float(bc.get("rho_out", 1.0)), int(bc.get("inlet_kind", 0)), int(bc.get("parabolic_L", 0)),
+                   int(bc.get("outlet_kind", 0)), 1 if oy >= 0 else 0, max(oy, 0))
 
 
 # ---- program inputs (host functions of the library) --------------------------------------------

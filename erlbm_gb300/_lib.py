@@ -34,8 +34,14 @@ class Desc(C.Structure):
                 ("tau", C.c_double), ("tau_nh", C.c_double), ("op", C.c_int), ("precision", C.c_int)]
 
 
+INLET_ZOUHE, INLET_PARABOLIC = 0, 1
+OUTLET_DENSITY, OUTLET_OPEN, OUTLET_CONVECTIVE = 0, 1, 2
+
+
 class BC(C.Structure):
-    _fields_ = [("inlet_x", C.c_int), ("u_in", C.c_double), ("outlet_x", C.c_int), ("rho_out", C.c_double)]
+    _fields_ = [("inlet_x", C.c_int), ("u_in", C.c_double), ("outlet_x", C.c_int), ("rho_out", C.c_double),
+                ("inlet_kind", C.c_int), ("parabolic_L", C.c_int), ("outlet_kind", C.c_int), ("open_y_on", C.c_int),
+                ("open_y", C.c_int)]
 
 
 class Checks(C.Structure):
@@ -105,6 +111,8 @@ _SIGS = {
     "erlbm_max_abs_density": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "erlbm_macroscopic": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "erlbm_field": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
+    "erlbm_read_geo": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_int), C.c_void_p, C.c_size_t]),
     "erlbm_write_vtk": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_char_p]),
     "erlbm_velocity_error": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double),
                                        C.POINTER(C.c_double)]),

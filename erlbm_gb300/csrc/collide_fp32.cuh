@@ -340,5 +340,35 @@ __device__ __forceinline__ void zou_he(float g[19], const ZouHe &z, bool left)
     }
 }
 
+// ZouHeD2Q9_vx_x (Boundary_conditions.cpp:710-744) on shifted populations: the weights of the
+// closure's index set sum to 1, so rho = (1 + G) / (1 - vx) with G = g0 + g3 + g4 + 2 (g2 + g8 + g6),
+// and g_i = w_i (rho P - 1) with P = 1 + 3 vx + 3 vx^2 for the +x movers (rho P - 1 in FP64).
+__device__ __forceinline__ void zou_he_d2q9(float g[9], double vx)
+{
+    const float G = ((g[0] + g[3]) + g[4]) + 2.f * ((g[2] + g[8]) + g[6]);
+    const double rho = (1.0 + (double)G) / (1.0 - vx);
+    const double e = rho * ((1.0 + 3.0 * vx) + 3.0 * vx * vx) - 1.0;
+    g[1] = (float)(e / 9.0);
+    g[5] = (float)(e / 36.0);
+    g[7] = (float)(e / 36.0);
+}
+
+// parabolic_D3Q19_x's node update (:456-530) on shifted populations: an opposite pair has one weight,
+// so g_i = g_opp + rho vx / 3 (or / 6) and the transverse corrections carry no weight.
+__device__ __forceinline__ void parabolic_d3q19(float g[19], double vx)
+{
+    const float ty = ((((g[18] + g[3]) + g[16]) - g[15]) - g[4]) - g[17];
+    const float tz = ((((g[17] + g[5]) + g[16]) - g[15]) - g[6]) - g[18];
+    const float gz = (((g[0] + g[3]) + (g[4] + g[5])) + ((g[6] + g[15]) + (g[16] + g[17]))) + g[18];
+    const float gm = ((g[2] + g[8]) + (g[10] + g[12])) + g[14];
+    const double rho = (1.0 + (2.0 * (double)gm + (double)gz)) / (1.0 - vx);
+    const float a3 = (float)(rho * vx / 3.0), a6 = (float)(rho * vx / 6.0);
+    g[1] = g[2] + a3;
+    g[7] = g[8] + fmaf(-0.5f, ty, a6);
+    g[9] = g[10] + fmaf(0.5f, ty, a6);
+    g[11] = g[12] + fmaf(-0.5f, tz, a6);
+    g[13] = g[14] + fmaf(0.5f, tz, a6);
+}
+
 }  // namespace shifted
 }  // namespace erlbm

@@ -352,5 +352,34 @@ __device__ __forceinline__ void zou_he_right(double f[19], double vx)
     f[12] = ((f[12] - a6) - 0.5 * rho * vz) + 0.5 * tz;
 }
 
+// ZouHeD2Q9_vx_x (Boundary_conditions.cpp:710-744), also the node update of parabolic_D2Q9_x
+// (:748-800) with the profile's velocity: the +x movers from the closure density.
+__device__ __forceinline__ void zou_he_d2q9(double f[9], double vx)
+{
+    const double rho = (((f[0] + f[3]) + f[4]) + 2 * ((f[2] + f[8]) + f[6])) / (1. - vx);
+    const double p = (1.0 + 3.0 * vx) + 3.0 * vx * vx;
+    f[1] = (rho / 9.0) * p;
+    f[5] = (rho / 36.0) * p;
+    f[7] = (rho / 36.0) * p;
+}
+
+// Node update of parabolic_D3Q19_x (Boundary_conditions.cpp:456-530): the +x movers from their
+// opposites, rho from the closure (vy = vz = 0).
+__device__ __forceinline__ void parabolic_d3q19(double f[19], double vx)
+{
+    const double vy = 0.0, vz = 0.0;
+    const double s_minus = (((f[2] + f[8]) + f[10]) + f[12]) + f[14];
+    const double s_zero = (((((((f[0] + f[3]) + f[4]) + f[5]) + f[6]) + f[15]) + f[16]) + f[17]) + f[18];
+    const double rho = (2.0 * s_minus + s_zero) / (1.0 - vx);
+    const double ty = (((((f[18] + f[3]) + f[16]) - f[15]) - f[4]) - f[17]);
+    const double tz = (((((f[17] + f[5]) + f[16]) - f[15]) - f[6]) - f[18]);
+    const double a3 = rho * vx / 3.0, a6 = rho * vx / 6.0;
+    f[1] = f[2] + a3;
+    f[7] = ((f[8] + a6) + 0.5 * rho * vy) - 0.5 * ty;
+    f[9] = ((f[10] + a6) - 0.5 * rho * vy) + 0.5 * ty;
+    f[11] = ((f[12] + a6) + 0.5 * rho * vz) - 0.5 * tz;
+    f[13] = ((f[14] + a6) - 0.5 * rho * vz) + 0.5 * tz;
+}
+
 }  // namespace exact
 }  // namespace erlbm

@@ -80,6 +80,10 @@ struct erlbm_handle {
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the stream created at erlbm_create
     int shape = 0;                      // launch shape of the fused periodic kernel (erlbm_set_launch)
+    std::vector<uint8_t> h_solid;       // host copy of the solid mask (empty for periodic boxes)
+    std::vector<double> h_profile;      // parabolic inlet velocity per (y, z) of the inlet plane
+    double *d_profile = nullptr;
+    double profile_key[3] = {-1, 0, 0}; // inlet_x, u_in, L of the uploaded profile
     size_t elem() const { return prec == ERLBM_FP64 ? sizeof(double) : sizeof(float); }
 };
 
@@ -112,6 +116,7 @@ void free_handle(erlbm_handle *h)
 {
     if (!h) return;
     cudaFree(h->d_solid);
+    cudaFree(h->d_profile);
     cudaFree(h->d_nof);
     cudaFree(h->d_buf[0]);
     cudaFree(h->d_buf[1]);
@@ -176,37 +181,104 @@ int ensure_aos(erlbm_handle *h)
     return ERLBM_OK;
 }
 
-int validate_bc(const erlbm_handle *h, const erlbm_bc *bc, BCp *out)
+// The reference's parabolic profile (Boundary_conditions.cpp:467-472): the h-th fluid node of a column
+double parabolic_vel(int hh, double vx_max, int L)
+{
+    const double d_h = (double)hh - 0.5;
+    return -4.0 * vx_max / (L * L) * (d_h) * (d_h - L);
+}
+
+int validate_bc(erlbm_handle *h, const erlbm_bc *bc, BCp *out)
 {
     out->inlet_x = -1;
     out->outlet_x = -1;
     out->u_in = 0;
     out->rho_out = 1;
+    out->inlet_kind = ERLBM_INLET_ZOUHE;
+    out->outlet_kind = ERLBM_OUTLET_DENSITY;
+    out->open_y = -1;
+    out->profile = nullptr;
     if (!bc) return ERLBM_OK;
+    const Geo &g = h->g;
+    auto solid = [h](long long n) { return !h->h_solid.empty() && h->h_solid[n]; };
     if (bc->inlet_x >= 0) {
-        if (h->q != 19) {
-            set_error("the Zou-He inlet is a D3Q19 boundary (ZouHeD3Q19_vx_x)%s%s", "", "");
-            return ERLBM_E_UNSUPPORTED;
-        }
-        if (bc->inlet_x >= h->g.nx) {
+        if (bc->inlet_x >= g.nx) {
             set_error("inlet plane outside the box%s%s", "", "");
+            return ERLBM_E_INVAL;
+        }
+        if (bc->inlet_kind != ERLBM_INLET_ZOUHE && bc->inlet_kind != ERLBM_INLET_PARABOLIC) {
+            set_error("unknown inlet kind%s%s", "", "");
             return ERLBM_E_INVAL;
         }
         out->inlet_x = bc->inlet_x;
         out->u_in = bc->u_in;
+        out->inlet_kind = bc->inlet_kind;
+        if (bc->inlet_kind == ERLBM_INLET_PARABOLIC) {
+            const int L = bc->parabolic_L;
+            if (L < 1 || L >= g.ny) {
+                set_error("parabolic_L must lie in [1, ny) (the reference's profile table has ny entries)%s%s", "",
+                          "");
+                return ERLBM_E_INVAL;
+            }
+            const double key[3] = {(double)bc->inlet_x, bc->u_in, (double)L};
+            if (!h->d_profile || memcmp(key, h->profile_key, sizeof(key)) != 0) {
+                std::vector<double> prof((size_t)g.ny * g.nz, 0.0);
+                for (int z = 0; z < g.nz; z++) {
+                    int hh = 0;
+                    for (int y = 0; y < g.ny; y++) {
+                        if (solid(bc->inlet_x + (long long)g.nx * (y + (long long)g.ny * z))) continue;
+                        if (++hh > L) {
+                            set_error("a column of the inlet plane holds more than parabolic_L fluid nodes%s%s", "",
+                                      "");
+                            return ERLBM_E_INVAL;
+                        }
+                        prof[y + (size_t)g.ny * z] = parabolic_vel(hh, bc->u_in, L);
+                    }
+                }
+                if (!h->d_profile) CK(cudaMalloc(&h->d_profile, prof.size() * sizeof(double)));
+                CK(cudaStreamSynchronize(h->stream));  // the previous profile may still be in use
+                h->h_profile.swap(prof);
+                CK(cudaMemcpyAsync(h->d_profile, h->h_profile.data(), h->h_profile.size() * sizeof(double),
+                                   cudaMemcpyHostToDevice, h->stream));
+                memcpy(h->profile_key, key, sizeof(key));
+            }
+            out->profile = h->d_profile;
+        }
     }
     if (bc->outlet_x >= 0) {
-        if (bc->outlet_x >= h->g.nx || h->g.nx < 2) {
+        if (bc->outlet_x >= g.nx || g.nx < 2) {
             set_error("outlet plane outside the box%s%s", "", "");
             return ERLBM_E_INVAL;
         }
-        const int nb = bc->outlet_x + (bc->outlet_x < h->g.nx / 2 ? 1 : -1);
-        if (nb < 0 || nb >= h->g.nx) {
+        const int nb = bc->outlet_x + (bc->outlet_x < g.nx / 2 ? 1 : -1);
+        if (nb < 0 || nb >= g.nx) {
             set_error("outlet plane has no inner neighbour%s%s", "", "");
             return ERLBM_E_INVAL;
         }
+        if (bc->outlet_kind < ERLBM_OUTLET_DENSITY || bc->outlet_kind > ERLBM_OUTLET_CONVECTIVE ||
+            bc->outlet_x == bc->inlet_x) {
+            set_error("unknown outlet kind, or outlet and inlet on one plane%s%s", "", "");
+            return ERLBM_E_INVAL;
+        }
+        if (bc->outlet_kind == ERLBM_OUTLET_OPEN && h->q != 9) {
+            set_error("the open outlet is a D2Q9 boundary (OpenBoundaryD2Q9_x)%s%s", "", "");
+            return ERLBM_E_UNSUPPORTED;
+        }
         out->outlet_x = bc->outlet_x;
         out->rho_out = bc->rho_out;
+        out->outlet_kind = bc->outlet_kind;
+    }
+    if (bc->open_y_on) {
+        if (h->q != 9) {
+            set_error("the open y plane is a D2Q9 boundary (OpenBoundaryD2Q9_y)%s%s", "", "");
+            return ERLBM_E_UNSUPPORTED;
+        }
+        const int yn = bc->open_y + (bc->open_y < g.ny / 2 ? 1 : -1);
+        if (bc->open_y < 0 || bc->open_y >= g.ny || yn < 0 || yn >= g.ny) {
+            set_error("open y plane outside the box or without an inner neighbour%s%s", "", "");
+            return ERLBM_E_INVAL;
+        }
+        out->open_y = bc->open_y;
     }
     return ERLBM_OK;
 }
@@ -222,7 +294,8 @@ int enqueue_step(erlbm_handle *h, const BCp &bc, int check_density, double densi
     a.status = (check_density || stop_on_flag) ? h->d_status : nullptr;
     a.stop_on_flag = stop_on_flag ? 1 : 0;
     void *src = h->d_buf[h->cur], *dst = h->d_buf[h->cur ^ 1];
-    const bool plain = bc.inlet_x < 0 && bc.outlet_x < 0 && !check_density && !stop_on_flag && a.mode == 0;
+    const bool plain =
+        bc.inlet_x < 0 && bc.outlet_x < 0 && bc.open_y < 0 && !check_density && !stop_on_flag && a.mode == 0;
     if (h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && plain && periodic_d2q9_fp32_ok(h->g)) {
         CKL(launch_periodic_d2q9_fp32(h->op, h->g, h->R, (const float *)src, (float *)dst, h->stream, h->shape),
             "periodic_d2q9");
@@ -336,6 +409,7 @@ int erlbm_create(const erlbm_desc *d, erlbm_handle **out)
             for (long long k = 0; k < h->g.nbox; k++)
                 if (!d->solid[k]) nof.push_back((int)k);
             h->n_fluid = (long long)nof.size();
+            h->h_solid.assign(d->solid, d->solid + h->g.nbox);
         }
     }
     const size_t pop_bytes = (size_t)h->q * h->g.plane * h->elem();

@@ -19,12 +19,16 @@ struct Geo {
     const uint8_t *solid;
 };
 
-// Boundary planes of one step (ZouHeD3Q19_vx_x and devnull_rho_x); -1 disables a plane.
+// Boundary planes of one step; -1 disables a plane.  inlet_kind 0: ZouHeD3Q19_vx_x / ZouHeD2Q9_vx_x,
+// 1: parabolic_D3Q19_x / parabolic_D2Q9_x with the per-node velocity profile[y + ny z];
+// outlet_kind 0: devnull_rho_x, 1: OpenBoundaryD2Q9_x, 2: convective_x; open_y: OpenBoundaryD2Q9_y.
 struct BCp {
     int inlet_x;
     double u_in;
     int outlet_x;
     double rho_out;
+    int inlet_kind, outlet_kind, open_y;
+    const double *profile;
 };
 
 // Per-run device status used by the stability checks and early stop.

@@ -71,6 +71,27 @@ struct PrecExact64 {
         else
             exact::zou_he_right(f, z.vx);
     }
+    // ZouHeD2Q9_vx_x, and the node update of parabolic_D2Q9_x / parabolic_D3Q19_x with a profile velocity
+    __device__ static __forceinline__ void zou_he9(T *f, double vx) { exact::zou_he_d2q9(f, vx); }
+    template <int Q>
+    __device__ static __forceinline__ void parabolic(T *f, double vx)
+    {
+        if constexpr (Q == 9)
+            exact::zou_he_d2q9(f, vx);
+        else
+            exact::parabolic_d3q19(f, vx);
+    }
+    // convective_x (Boundary_conditions.cpp:676-703): U = calcula's vx of the inner neighbour a,
+    // f = (1 / (1 + U)) (f + U f_a).
+    template <int Q>
+    __device__ static __forceinline__ void convective(T *f, const T *a)
+    {
+        double rho, U, vy, vz;
+        macro<Q>(a, rho, U, vy, vz);
+        const double factor = 1.0 / (1.0 + U);
+#pragma unroll
+        for (int i = 0; i < Q; i++) f[i] = factor * (f[i] + U * a[i]);
+    }
     // devnull_rho_x (Boundary_conditions.cpp:119-125): f = f_adj * (rho / density(f_adj)).
     template <int Q>
     __device__ static __forceinline__ void outlet(T *f, double rho)
@@ -125,6 +146,25 @@ struct PrecShifted32 {
     using ZouHe = shifted::ZouHe;
     __device__ static __forceinline__ ZouHe zou_he_prep(double vx) { return shifted::zou_he_prep(vx); }
     __device__ static __forceinline__ void zou_he(T *f, const ZouHe &z, bool left) { shifted::zou_he(f, z, left); }
+    __device__ static __forceinline__ void zou_he9(T *f, double vx) { shifted::zou_he_d2q9(f, vx); }
+    template <int Q>
+    __device__ static __forceinline__ void parabolic(T *f, double vx)
+    {
+        if constexpr (Q == 9)
+            shifted::zou_he_d2q9(f, vx);
+        else
+            shifted::parabolic_d3q19(f, vx);
+    }
+    // convective_x on shifted populations: (f + U f_a) / (1 + U) - w = (g + U g_a) / (1 + U)
+    template <int Q>
+    __device__ static __forceinline__ void convective(T *f, const T *a)
+    {
+        double rho, U, vy, vz;
+        macro<Q>(a, rho, U, vy, vz);
+        const float u = (float)U, factor = __frcp_rn(1.f + u);
+#pragma unroll
+        for (int i = 0; i < Q; i++) f[i] = factor * fmaf(u, a[i], f[i]);
+    }
     // devnull_rho_x on shifted populations: f = f_adj * (rho / rho_adj) becomes
     // g = g_adj + (s - 1) (g_adj + w),  s - 1 = (rho - rho_adj) / rho_adj = ((rho - 1) - drho) / (1 + drho),
     // all of it small quantities, so FP32 carries it (the error of s - 1, ~1e-7 of a ~1e-3 quantity,
@@ -188,6 +228,98 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 }
 
 // ------------------------------------------------------------------------------------------------
+// Boundary planes.  The reference applies each plane's function to the whole plane in place, in the
+// order inlet, outlet, open y plane, before the node loop; a plane that reads its inner neighbour
+// sees that neighbour after the planes applied before it.  Here every node builds its own state:
+// its post-stream populations (pulled), then the planes that touch it, recomputing a neighbour's
+// state where a plane reads one.
+// ------------------------------------------------------------------------------------------------
+
+template <class P, int Q>
+__device__ __forceinline__ void apply_inlet(typename P::T *f, const Geo &g, const BCp &bc, int y, int z)
+{
+    if (bc.inlet_kind == 1) {
+        P::template parabolic<Q>(f, bc.profile[y + (long long)g.ny * z]);
+    } else {
+        if constexpr (Q == 19)
+            P::zou_he(f, P::zou_he_prep(bc.u_in), bc.inlet_x < g.nx / 2);
+        else
+            P::zou_he9(f, bc.u_in);
+    }
+}
+
+// Populations of fluid node (x, y, z) after this step's inlet and outlet planes.
+template <class P, int Q>
+__device__ void state_after_x_planes(const typename P::T *__restrict__ src, const Geo &g, const BCp &bc, int mode,
+                                     int x, int y, int z, long long node, typename P::T *f)
+{
+    using T = typename P::T;
+    if (x == bc.outlet_x) {
+        const int xn = x + ((bc.outlet_x < g.nx / 2) ? 1 : -1);
+        const long long nn = node + (xn - x);
+        const bool nsolid = g.solid != nullptr && g.solid[nn];
+        if (bc.outlet_kind == 0) {  // devnull_rho_x: the inner neighbour, rescaled
+            if (nsolid) {
+                P::template rest<Q>(f, bc.rho_out);
+                return;
+            }
+            gather<P, Q>(src, g, mode, xn, y, z, nn, f);
+            if (xn == bc.inlet_x) apply_inlet<P, Q>(f, g, bc, y, z);
+            P::template outlet<Q>(f, bc.rho_out);
+            return;
+        }
+        gather<P, Q>(src, g, mode, x, y, z, node, f);
+        if (nsolid) return;  // the reference reads no neighbour there (it would read outside the array)
+        T a[Q];
+        gather<P, Q>(src, g, mode, xn, y, z, nn, a);
+        if (xn == bc.inlet_x) apply_inlet<P, Q>(a, g, bc, y, z);
+        if (bc.outlet_kind == 1) {
+            if constexpr (Q == 9) {  // OpenBoundaryD2Q9_x: the populations entering from outside
+                if (xn > x) {
+                    f[1] = a[1];
+                    f[5] = a[5];
+                    f[7] = a[7];
+                } else {
+                    f[2] = a[2];
+                    f[6] = a[6];
+                    f[8] = a[8];
+                }
+            }
+        } else {
+            P::template convective<Q>(f, a);
+        }
+        return;
+    }
+    gather<P, Q>(src, g, mode, x, y, z, node, f);
+    if (x == bc.inlet_x) apply_inlet<P, Q>(f, g, bc, y, z);
+}
+
+// Post-boundary populations of fluid node (x, y, z): the x planes, then OpenBoundaryD2Q9_y.
+template <class P, int Q>
+__device__ void state_after_planes(const typename P::T *__restrict__ src, const Geo &g, const BCp &bc, int mode, int x,
+                                   int y, int z, long long node, typename P::T *f)
+{
+    state_after_x_planes<P, Q>(src, g, bc, mode, x, y, z, node, f);
+    if constexpr (Q == 9) {
+        if (y != bc.open_y) return;
+        const int yn = y + ((bc.open_y < g.ny / 2) ? 1 : -1);
+        const long long nn = node + (long long)(yn - y) * g.nx;
+        if (g.solid != nullptr && g.solid[nn]) return;
+        typename P::T a[Q];
+        state_after_x_planes<P, Q>(src, g, bc, mode, x, yn, z, nn, a);
+        if (yn > y) {
+            f[3] = a[3];
+            f[5] = a[5];
+            f[8] = a[8];
+        } else {
+            f[4] = a[4];
+            f[6] = a[6];
+            f[7] = a[7];
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
 // Generic step kernel: any box, solid mask, boundary planes, density check
 // ------------------------------------------------------------------------------------------------
 
@@ -214,17 +346,7 @@ __global__ void __launch_bounds__(256) k_step(const typename P::T *__restrict__ 
         const int y = (int)(r % g.ny);
         const int z = (int)(r / g.ny);
         T f[Q];
-        int gx = x;
-        const bool outlet = (x == bc.outlet_x);
-        if (outlet) gx = x + ((bc.outlet_x < g.nx / 2) ? 1 : -1);
-        const long long gnode = node + (gx - x);
-        if (outlet && g.solid != nullptr && g.solid[gnode]) {
-            P::template rest<Q>(f, bc.rho_out);
-        } else {
-            gather<P, Q>(src, g, a.mode, gx, y, z, gnode, f);
-            if (Q == 19 && gx == bc.inlet_x) P::zou_he(f, P::zou_he_prep(bc.u_in), bc.inlet_x < g.nx / 2);
-            if (outlet) P::template outlet<Q>(f, bc.rho_out);
-        }
+        state_after_planes<P, Q>(src, g, bc, a.mode, x, y, z, node, f);
         P::template collide<Q, OP>(f, prm);
         if (a.check_density) {
             const double rho = P::template density<Q>(f);

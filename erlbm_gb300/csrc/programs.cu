@@ -6,8 +6,12 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
 
 #include "../../include/erlbm_gb300.h"
+#include "abi_internal.h"
 
 namespace {
 
@@ -203,6 +207,58 @@ int erlbm_obstacle_map_params(int i, int j, int n_tau, int n_nu, double ma, doub
     *tau = 3. * pow(10., log_nu) + 0.5;
     *tau_nh = tau_nh_min + (double)i * (tau_nh_max - tau_nh_min) / n_tau;
     *u_imp = ma / sqrt(3.);
+    return ERLBM_OK;
+}
+
+// read_geo (LBM_functions.cpp:282-353): skip four header lines, read "DIMENSIONS nx ny nz", skip five
+// more, then one integer per node of the file's box (x fastest, nonzero = fluid).  pts_in / pts_out
+// layers of fluid are added before and after in x; with `wall` the first and last x planes of the
+// widened box are solid (the reference's overload without the flag always adds them).
+int erlbm_read_geo(const char *path, int pts_in, int pts_out, int wall, int *nx, int *ny, int *nz, uint8_t *solid,
+                   size_t n)
+{
+    if (!path || !nx || !ny || !nz || pts_in < 0 || pts_out < 0) return ERLBM_E_INVAL;
+    std::ifstream fm(path);
+    if (!fm) {
+        erlbm::set_error("cannot open %s%s", path, "");
+        return ERLBM_E_INVAL;
+    }
+    std::string line, dump;
+    for (int i = 0; i < 4; i++) std::getline(fm, dump);
+    std::getline(fm, line);
+    std::stringstream dados(line);
+    int fx = 0, fy = 0, fz = 0;
+    dados >> dump >> fx >> fy >> fz;
+    for (int i = 0; i < 5; i++) std::getline(fm, dump);
+    if (!fm || fx < 1 || fy < 1 || fz < 1) {
+        erlbm::set_error("%s is not a legacy VTK geometry file%s", path, "");
+        return ERLBM_E_INVAL;
+    }
+    const int X = fx + pts_in + pts_out;
+    *nx = X;
+    *ny = fy;
+    *nz = fz;
+    const size_t total = (size_t)X * fy * fz;
+    if (!solid) return ERLBM_OK;  // dimensions only
+    if (n != total) return ERLBM_E_INVAL;
+    for (int z = 0; z < fz; z++)
+        for (int y = 0; y < fy; y++)
+            for (int x = 0; x < X; x++) {
+                const size_t pos = x + (size_t)y * X + (size_t)z * fy * X;
+                bool fluid;
+                if (x >= pts_in && x < X - pts_out) {
+                    int v = 0;
+                    fm >> v;
+                    if (!fm) {
+                        erlbm::set_error("%s ends before its last node%s", path, "");
+                        return ERLBM_E_INVAL;
+                    }
+                    fluid = v != 0;
+                } else {
+                    fluid = !((x == 0 || x == X - 1) && wall);
+                }
+                solid[pos] = fluid ? 0 : 1;
+            }
     return ERLBM_OK;
 }
 

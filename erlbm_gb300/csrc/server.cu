@@ -431,6 +431,9 @@ int job_admit(erlbm_server *s, int64_t ticket, const erlbm_request &q, Job **out
     j->bc.inlet_x = j->bc.outlet_x = -1;
     j->bc.u_in = 0;
     j->bc.rho_out = 1.0;
+    j->bc.inlet_kind = j->bc.outlet_kind = 0;
+    j->bc.open_y = -1;
+    j->bc.profile = nullptr;
     if (q.kind == ERLBM_REQ_OBSTACLE) {
         j->bc.inlet_x = 1;
         j->bc.outlet_x = j->g.nx - 2;

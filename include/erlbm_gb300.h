@@ -68,12 +68,27 @@ typedef struct erlbm_desc {
 } erlbm_desc;
 
 /* Boundary planes applied to the post-stream populations at the start of each step, in this
- * order (main_stability-map_obstacle.cpp:92-94).  -1 disables a plane. */
+ * order: inlet, outlet (main_stability-map_obstacle.cpp:92-94), then the open y plane.  -1 disables
+ * a plane.  The first four fields are the obstacle program's; a zero-initialised remainder keeps
+ * its boundaries (Zou-He inlet, density outlet, no open y plane). */
+#define ERLBM_INLET_ZOUHE 0         /* ZouHeD3Q19_vx_x (Boundary_conditions.cpp:350-442) or, on D2Q9,
+                                       ZouHeD2Q9_vx_x (:710-744) */
+#define ERLBM_INLET_PARABOLIC 1     /* parabolic_D3Q19_x (:456-530) / parabolic_D2Q9_x (:748-800) */
+#define ERLBM_OUTLET_DENSITY 0      /* devnull_rho_x (:68-141): copy of the inner plane rescaled to rho_out */
+#define ERLBM_OUTLET_OPEN 1         /* OpenBoundaryD2Q9_x (:584-621), D2Q9 only */
+#define ERLBM_OUTLET_CONVECTIVE 2   /* convective_x (:627-706) */
 typedef struct erlbm_bc {
-    int inlet_x;    /* ZouHeD3Q19_vx_x(inlet_x, u_in) (Boundary_conditions.cpp:350-442); D3Q19 only */
-    double u_in;
-    int outlet_x;   /* devnull_rho_x(outlet_x, rho_out) (Boundary_conditions.cpp:68-141) */
-    double rho_out;
+    int inlet_x;     /* velocity inlet plane */
+    double u_in;     /* its x velocity; the profile's maximum for ERLBM_INLET_PARABOLIC */
+    int outlet_x;    /* outlet plane */
+    double rho_out;  /* ERLBM_OUTLET_DENSITY's density */
+    int inlet_kind;  /* ERLBM_INLET_* */
+    int parabolic_L; /* profile width L: the h-th fluid node of a column (from y = 0, per z) gets
+                        u = -4 u_in / L^2 (h - 1/2) (h - 1/2 - L); each column may hold at most L fluid
+                        nodes and L < ny, as the reference's profile table requires */
+    int outlet_kind; /* ERLBM_OUTLET_* */
+    int open_y_on;   /* 1: OpenBoundaryD2Q9_y (:542-580) on plane open_y (D2Q9) */
+    int open_y;
 } erlbm_bc;
 
 /* Stability checks of a run (roda_ponto, main_stability-map_taylor-green.cpp:41-104 and
@@ -257,6 +272,13 @@ int erlbm_map_run(const erlbm_map_desc *d, int32_t *labels, int32_t *decided_ste
  * results that came from FP64.  Arrays are laid out as in erlbm_map_run. */
 int erlbm_map_run_refined(const erlbm_map_desc *d, int radius, double late_fraction, int32_t *labels,
                           int32_t *decided_step, double *margins, uint8_t *refined);
+
+/* read_geo (SimBoltz_Functions/LBM_functions.cpp:282-353): the solid mask (1 = solid, the layout of
+ * erlbm_desc.solid) of a legacy ASCII VTK geometry file, nonzero values fluid, with pts_in / pts_out
+ * fluid layers added in x and, with `wall`, the first and last x planes of the widened box solid.
+ * solid = NULL returns the dimensions only; otherwise n must be nx * ny * nz. */
+int erlbm_read_geo(const char *path, int pts_in, int pts_out, int wall, int *nx, int *ny, int *nz, uint8_t *solid,
+                   size_t n);
 
 /* ---- request server (continuous batching) ---------------------------------------------------- */
 /* No counterpart in the reference, which runs one program per invocation.  A server owns a fixed

@@ -119,3 +119,21 @@ def test_sharded_map_gloo_world2():
     for p in ps:
         p.join(timeout=60)
     assert res == (True, True, True)
+
+
+def test_read_geo_equals_oracle_and_reference(tmp_path):
+    """erlbm_read_geo (host code of the library) against read_geo's geometry.ini from the reference
+    library (tests/golden) and the oracle, with and without added layers and walls."""
+    import os
+    m = E()
+    from oracle import oracle as O
+    v = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_vectors.npz"))
+    path = tmp_path / "geo.vtk"
+    path.write_bytes(v["geo_file"].tobytes())
+    for pin, pout, wall in ((0, 0, 1), (2, 3, 1), (2, 3, 0)):
+        nx, ny, nz, solid = m.read_geo(str(path), pin, pout, bool(wall))
+        assert (nx, ny, nz) == (9 + pin + pout, 5, 2)
+        assert np.array_equal(solid == 0, v[f"geo_ini_{pin}_{pout}_{wall}"] != 0)
+        assert np.array_equal(solid, O.read_geo(str(path), pin, pout, bool(wall))[3])
+    with pytest.raises(m.ErlbmError):
+        m.read_geo(str(tmp_path / "missing.vtk"))
