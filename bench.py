@@ -93,13 +93,14 @@ def peaks():
 
 
 def ncu_traffic(L: int, precision: str):
-    """DRAM bytes per launch from the committed ncu summary of the same kernel, scaled to L."""
+    """DRAM bytes per launch from the committed ncu summary of the same kernel ("fp32", "fp64", or
+    "fp32_x2" for the two-step kernel), scaled to L."""
     path = os.path.join(ROOT, "profiles", "dsl_periodic_d2q9_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
         rec = d[precision]
-        return rec["dram_bytes_per_lu"] * L * L
+        return rec.get("dram_bytes_per_node_per_launch", rec.get("dram_bytes_per_lu")) * L * L
     except Exception:
         return None
 
@@ -287,7 +288,9 @@ def run_ours(args):
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    launches = K * inner
+    two = bool(shape and shape.get("two_step"))
+    # a two-step launch advances every node by two steps: inner // 2 of them, plus one single step if odd
+    launches = K * (inner // 2 + inner % 2) if two else K * inner
     value = world * L * L * inner * K / (ms / 1e3) / 1e6
     launch_ms = ms / launches
     algo_bytes = BYTES_PER_LU[args.precision] * L * L
@@ -339,11 +342,15 @@ def run_ours(args):
                    "l2": f"working set {2 * BYTES_PER_LU[args.precision] // 2 * L * L / 1e6:.0f} MB > 129 MB L2, "
                          "no flush",
                    "launch_shape": None if shape is None else {"block_threads": shape["block_threads"],
-                                                               "streaming_stores": shape["streaming_stores"]}},
+                                                               "streaming_stores": shape["streaming_stores"],
+                                                               "two_step": two}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": ncu_traffic(L, args.precision) if args.op == "erlbm" else None,
+                     "peak_kind": peak_kind,
+                     "traffic": ncu_traffic(L, "fp32_x2" if two else args.precision) if args.op == "erlbm" else None,
                      "algorithmic_bytes_per_launch": algo_bytes, "launch_us": launch_ms * 1e3,
-                     "kernel": f"k_periodic_d2q9<{op}>" if args.precision == "fp32" else f"k_step<PrecExact64,9,{op}>"},
+                     "lattice_updates_per_launch": L * L * (2 if two else 1),
+                     "kernel": (f"k_periodic_d2q9_x2<{op}>" if two else f"k_periodic_d2q9<{op}>")
+                     if args.precision == "fp32" else f"k_step<PrecExact64,9,{op}>"},
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,

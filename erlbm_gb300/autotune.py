@@ -1,8 +1,8 @@
 """Autotuner for the launch shapes of the hot kernels.
 
 Two shapes are tuned by measurement on the GPU at hand:
-  * the fused periodic D2Q9 FP32 kernel: threads per block (128 / 256 / 512) and plain or streaming
-    (evict-first) stores, per lattice side L;
+  * the fused periodic D2Q9 FP32 kernel: threads per block (128 / 256 / 512), plain or streaming
+    (evict-first) stores, and one or two steps per launch, per lattice side L;
   * the persistent map kernel: resident lattices ("slots") per SM, per map kind and precision.
 Each candidate is timed with CUDA events after a warm-up; the winner is cached in a JSON file
 ($ERLBM_TUNE_CACHE, default ~/.cache/erlbm_gb300/autotune.json) keyed by the device name, so later
@@ -57,10 +57,12 @@ def _time_steps(lat, stream, n: int) -> float:
 
 
 PERIODIC_CANDIDATES = [(128, False), (256, False), (512, False), (128, True), (256, True), (512, True)]
+# two steps per launch (the odd remainder of a call uses the one-step shape given with it)
+TWO_STEP_CANDIDATES = [(128, False), (256, False)]
 
 
 def tune_periodic(L: int, steps: int = 200, force: bool = False) -> dict:
-    """Best (block_threads, streaming_stores) of the fused D2Q9 FP32 kernel on an L x L lattice."""
+    """Best (block_threads, streaming_stores, two_step) of the fused D2Q9 FP32 kernel on an L x L lattice."""
     import torch
     import erlbm_gb300 as E
     key = f"{_device_key()}/periodic_d2q9_fp32/L{L}"
@@ -75,11 +77,15 @@ def tune_periodic(L: int, steps: int = 200, force: bool = False) -> dict:
         lat.set_stream(stream.cuda_stream)
         lat.set_populations(E.init_double_shear(L))
         lat.step(1)
-        for block, st in PERIODIC_CANDIDATES:
-            lat.set_launch(block, st)
+        cands = [(b, s, False) for b, s in PERIODIC_CANDIDATES]
+        if L % 256 == 0:
+            cands += [(b, s, True) for b, s in TWO_STEP_CANDIDATES]
+        for block, st, two in cands:
+            lat.set_launch(block, st, two)
             lat.step(20)
             t = min(_time_steps(lat, stream, steps) for _ in range(3))
-            results.append(dict(block_threads=block, streaming_stores=st, mlups=L * L * steps / t / 1e6))
+            results.append(dict(block_threads=block, streaming_stores=st, two_step=two,
+                                mlups=L * L * steps / t / 1e6))
     best = max(results, key=lambda r: r["mlups"])
     out = dict(best, candidates=results)
     _store(key, out)
@@ -91,7 +97,7 @@ def apply_periodic(lat) -> dict | None:
     if lat.q != 9 or lat.precision != 1 or lat.nx % 128 or lat.nz != 1:
         return None
     best = tune_periodic(lat.nx)
-    lat.set_launch(best["block_threads"], best["streaming_stores"])
+    lat.set_launch(best["block_threads"], best["streaming_stores"], best.get("two_step", False))
     return best
 
 

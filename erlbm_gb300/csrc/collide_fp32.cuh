@@ -92,32 +92,89 @@ __device__ __forceinline__ void moments9(const float g[9], float &drho, float &m
     uy = my * inv;
 }
 
-template <int OP>
-__device__ __forceinline__ void collide9(float g[9], const Coef &k)
+// Lane arithmetic of the D2Q9 update, written once for one node (LaneF1: float) and for two nodes
+// in the halves of a float2 (LaneF2: Blackwell's packed FP32x2 FFMA2 / FADD2 / FMUL2, which issue
+// one instruction for both).  Every operation is an explicitly rounded intrinsic (nothing is left to
+// the compiler's contraction), so both forms compute the same bits.
+struct LaneF1 {
+    using V = float;
+    static __device__ __forceinline__ V c(float x) { return x; }
+    static __device__ __forceinline__ V add(V a, V b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ V sub(V a, V b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ V mul(V a, V b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ V fma(V a, V b, V d) { return __fmaf_rn(a, b, d); }
+    static __device__ __forceinline__ V neg(V a) { return -a; }
+    static __device__ __forceinline__ V rcp(V a) { return __frcp_rn(a); }
+};
+
+struct LaneF2 {
+    using V = float2;
+    static __device__ __forceinline__ V c(float x) { return make_float2(x, x); }
+    static __device__ __forceinline__ V add(V a, V b) { return __fadd2_rn(a, b); }
+    static __device__ __forceinline__ V sub(V a, V b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+    static __device__ __forceinline__ V mul(V a, V b) { return __fmul2_rn(a, b); }
+    static __device__ __forceinline__ V fma(V a, V b, V d) { return __ffma2_rn(a, b, d); }
+    static __device__ __forceinline__ V neg(V a) { return make_float2(-a.x, -a.y); }
+    static __device__ __forceinline__ V rcp(V a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
+};
+
+// update_pair / update_rest in lane arithmetic
+template <class M, int OP>
+__device__ __forceinline__ void update_pair_l(typename M::V &gi, typename M::V &gj, typename M::V de,
+                                              typename M::V dO, typename M::V f1, const Coef &k)
 {
-    constexpr float W1 = 1.f / 9.f, W2 = 1.f / 36.f;
-    const float eX = 0.5f * (g[1] + g[2]), oX = 0.5f * (g[1] - g[2]);
-    const float eY = 0.5f * (g[3] + g[4]), oY = 0.5f * (g[3] - g[4]);
-    const float eP = 0.5f * (g[5] + g[6]), oP = 0.5f * (g[5] - g[6]);
-    const float eM = 0.5f * (g[7] + g[8]), oM = 0.5f * (g[7] - g[8]);
-    const float drho = g[0] + 2.f * ((eX + eY) + (eP + eM));
-    const float mx = 2.f * (oX + (oP + oM));
-    const float my = 2.f * (oY + (oP - oM));
-    const float inv = __frcp_rn(1.f + drho);
-    const float ux = mx * inv, uy = my * inv;
-    const float mu15 = -1.5f * fmaf(mx, ux, my * uy);
+    using V = typename M::V;
+    const V d1 = M::c(k.d1), m2 = M::c(-2.f);
+    if (OP == OP_BGK) {
+        const V di = M::add(de, dO), dj = M::sub(de, dO);
+        gi = M::add(gi, M::fma(d1, di, M::mul(m2, di)));
+        gj = M::add(gj, M::fma(d1, dj, M::mul(m2, dj)));
+    } else {
+        const V kd = M::c(k.kd);
+        const V a = M::sub(de, f1), t = M::mul(m2, f1);
+        gi = M::add(gi, M::fma(d1, f1, M::fma(kd, M::add(a, dO), t)));
+        gj = M::add(gj, M::fma(d1, f1, M::fma(kd, M::sub(a, dO), t)));
+    }
+}
+
+template <class M, int OP>
+__device__ __forceinline__ typename M::V update_rest_l(typename M::V g0, typename M::V de0, typename M::V f10,
+                                                       const Coef &k)
+{
+    const typename M::V d1 = M::c(k.d1), m2 = M::c(-2.f);
+    if (OP == OP_BGK) return M::add(g0, M::fma(d1, de0, M::mul(m2, de0)));
+    return M::add(g0, M::fma(d1, f10, M::fma(M::c(k.kd), M::sub(de0, f10), M::mul(m2, f10))));
+}
+
+template <class M, int OP>
+__device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
+{
+    using V = typename M::V;
+    constexpr float W1 = 1.f / 9.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
+    const V half = M::c(0.5f), two = M::c(2.f);
+    const V eX = M::mul(half, M::add(g[1], g[2])), oX = M::mul(half, M::sub(g[1], g[2]));
+    const V eY = M::mul(half, M::add(g[3], g[4])), oY = M::mul(half, M::sub(g[3], g[4]));
+    const V eP = M::mul(half, M::add(g[5], g[6])), oP = M::mul(half, M::sub(g[5], g[6]));
+    const V eM = M::mul(half, M::add(g[7], g[8])), oM = M::mul(half, M::sub(g[7], g[8]));
+    const V drho = M::fma(two, M::add(M::add(eX, eY), M::add(eP, eM)), g[0]);
+    const V mx = M::mul(two, M::add(oX, M::add(oP, oM)));
+    const V my = M::mul(two, M::add(oY, M::sub(oP, oM)));
+    const V inv = M::rcp(M::add(M::c(1.f), drho));
+    const V ux = M::mul(mx, inv), uy = M::mul(my, inv);
+    const V mu15 = M::mul(M::c(-1.5f), M::fma(mx, ux, M::mul(my, uy)));
+    const V k45 = M::c(4.5f), mw1 = M::c(-W1), mw2 = M::c(-W2);
     // even non-equilibrium parts
-    const float deX = fmaf(-W1, fmaf(4.5f * mx, ux, mu15), fmaf(-W1, drho, eX));
-    const float deY = fmaf(-W1, fmaf(4.5f * my, uy, mu15), fmaf(-W1, drho, eY));
-    const float cmP = mx + my, cmM = mx - my;
-    const float deP = fmaf(-W2, fmaf(4.5f * cmP, ux + uy, mu15), fmaf(-W2, drho, eP));
-    const float deM = fmaf(-W2, fmaf(4.5f * cmM, ux - uy, mu15), fmaf(-W2, drho, eM));
-    const float de0 = -2.f * ((deX + deY) + (deP + deM));
+    const V deX = M::fma(mw1, M::fma(M::mul(k45, mx), ux, mu15), M::fma(mw1, drho, eX));
+    const V deY = M::fma(mw1, M::fma(M::mul(k45, my), uy, mu15), M::fma(mw1, drho, eY));
+    const V cmP = M::add(mx, my), cmM = M::sub(mx, my);
+    const V deP = M::fma(mw2, M::fma(M::mul(k45, cmP), M::add(ux, uy), mu15), M::fma(mw2, drho, eP));
+    const V deM = M::fma(mw2, M::fma(M::mul(k45, cmM), M::sub(ux, uy), mu15), M::fma(mw2, drho, eM));
+    const V de0 = M::mul(M::c(-2.f), M::add(M::add(deX, deY), M::add(deP, deM)));
     // odd non-equilibrium parts; the axis pairs close the momentum
-    const float doP = fmaf(-3.f * W2, cmP, oP);
-    const float doM = fmaf(-3.f * W2, cmM, oM);
-    const float doX = -(doP + doM);
-    const float doY = -(doP - doM);
+    const V doP = M::fma(M::c(M3W2), cmP, oP);
+    const V doM = M::fma(M::c(M3W2), cmM, oM);
+    const V doX = M::neg(M::add(doP, doM));
+    const V doY = M::neg(M::sub(doP, doM));
     if constexpr (OP == OP_MRT) {
         // coll_MRT (Collision_operators.cpp:583-699) as an increment on the non-equilibrium part n:
         // f* = f - M^-1 S M n.  With A = deX + deY, B = deP + deM and the closed parts substituted,
@@ -125,44 +182,59 @@ __device__ __forceinline__ void collide9(float g[9], const Coef &k)
         // qy = 6 (doP - doM), pxx = 2 (deX - deY), pxy = 2 (deP - deM); back through M^-1 the odd
         // parts relax with s_q alone, and the even parts take hE = s_e e / 36, hP = s_eps eps / 36 and
         // the shear part, written with delta = 2 - 1/tau as s_nu x / 2 = x - delta x / 2.
-        const float A = deX + deY, B = deP + deM;
-        const float hE = (float)(MRT9_SE / 6.0) * fmaf(2.f, B, A);
-        const float hP = (float)(MRT9_SEPS / 6.0) * fmaf(-2.f, A, -B);
-        const float sX = deX - deY, sP = deP - deM;
-        const float vX = fmaf(-0.5f * k.d1, sX, sX), vP = fmaf(-0.5f * k.d1, sP, sP);
-        const float ax = fmaf(2.f, hP, hE), ap = -fmaf(2.f, hE, hP);
-        const float eX = ax - vX, eY = ax + vX, eP = ap - vP, eM = ap + vP;
-        const float oP = (float)-MRT9_SQ * doP, oM = (float)-MRT9_SQ * doM;
-        const float oX = -(oP + oM), oY = -(oP - oM);
-        g[0] += -2.f * ((eX + eY) + (eP + eM));
-        g[1] += eX + oX;
-        g[2] += eX - oX;
-        g[3] += eY + oY;
-        g[4] += eY - oY;
-        g[5] += eP + oP;
-        g[6] += eP - oP;
-        g[7] += eM + oM;
-        g[8] += eM - oM;
+        const V A = M::add(deX, deY), B = M::add(deP, deM);
+        const V hE = M::mul(M::c((float)(MRT9_SE / 6.0)), M::fma(two, B, A));
+        const V hP = M::mul(M::c((float)(MRT9_SEPS / 6.0)), M::fma(M::c(-2.f), A, M::neg(B)));
+        const V sX = M::sub(deX, deY), sP = M::sub(deP, deM);
+        const V hd = M::c(-0.5f * k.d1);
+        const V vX = M::fma(hd, sX, sX), vP = M::fma(hd, sP, sP);
+        const V ax = M::fma(two, hP, hE), ap = M::neg(M::fma(two, hE, hP));
+        const V xX = M::sub(ax, vX), xY = M::add(ax, vX), xP = M::sub(ap, vP), xM = M::add(ap, vP);
+        const V sq = M::c((float)-MRT9_SQ);
+        const V qP = M::mul(sq, doP), qM = M::mul(sq, doM);
+        const V qX = M::neg(M::add(qP, qM)), qY = M::neg(M::sub(qP, qM));
+        g[0] = M::add(g[0], M::mul(M::c(-2.f), M::add(M::add(xX, xY), M::add(xP, xM))));
+        g[1] = M::add(g[1], M::add(xX, qX));
+        g[2] = M::add(g[2], M::sub(xX, qX));
+        g[3] = M::add(g[3], M::add(xY, qY));
+        g[4] = M::add(g[4], M::sub(xY, qY));
+        g[5] = M::add(g[5], M::add(xP, qP));
+        g[6] = M::add(g[6], M::sub(xP, qP));
+        g[7] = M::add(g[7], M::add(xM, qM));
+        g[8] = M::add(g[8], M::sub(xM, qM));
         return;
     }
-    float f10 = 0.f, f1X = 0.f, f1Y = 0.f, f1P = 0.f, f1M = 0.f;
+    V f10 = M::c(0.f), f1X = M::c(0.f), f1Y = M::c(0.f), f1P = M::c(0.f), f1M = M::c(0.f);
     if (OP != OP_BGK) {
-        const float pxx = 2.f * (deX + (deP + deM));
-        const float pyy = 2.f * (deY + (deP + deM));
-        const float pxy = 2.f * (deP - deM);
-        const float tr = pxx + pyy;
-        f10 = (-2.f / 3.f) * tr;
-        f1X = fmaf(pxx, 1.f / 3.f, pyy * (-1.f / 6.f));
-        f1Y = fmaf(pyy, 1.f / 3.f, pxx * (-1.f / 6.f));
-        const float t12 = tr * (1.f / 12.f);
-        f1P = fmaf(pxy, 0.25f, t12);
-        f1M = fmaf(pxy, -0.25f, t12);
+        const V pxx = M::mul(two, M::add(deX, M::add(deP, deM)));
+        const V pyy = M::mul(two, M::add(deY, M::add(deP, deM)));
+        const V pxy = M::mul(two, M::sub(deP, deM));
+        const V tr = M::add(pxx, pyy);
+        f10 = M::mul(M::c(-2.f / 3.f), tr);
+        f1X = M::fma(pxx, M::c(1.f / 3.f), M::mul(pyy, M::c(-1.f / 6.f)));
+        f1Y = M::fma(pyy, M::c(1.f / 3.f), M::mul(pxx, M::c(-1.f / 6.f)));
+        const V t12 = M::mul(tr, M::c(1.f / 12.f));
+        f1P = M::fma(pxy, M::c(0.25f), t12);
+        f1M = M::fma(pxy, M::c(-0.25f), t12);
     }
-    g[0] = update_rest<OP>(g[0], de0, f10, k);
-    update_pair<OP>(g[1], g[2], deX, doX, f1X, k);
-    update_pair<OP>(g[3], g[4], deY, doY, f1Y, k);
-    update_pair<OP>(g[5], g[6], deP, doP, f1P, k);
-    update_pair<OP>(g[7], g[8], deM, doM, f1M, k);
+    g[0] = update_rest_l<M, OP>(g[0], de0, f10, k);
+    update_pair_l<M, OP>(g[1], g[2], deX, doX, f1X, k);
+    update_pair_l<M, OP>(g[3], g[4], deY, doY, f1Y, k);
+    update_pair_l<M, OP>(g[5], g[6], deP, doP, f1P, k);
+    update_pair_l<M, OP>(g[7], g[8], deM, doM, f1M, k);
+}
+
+template <int OP>
+__device__ __forceinline__ void collide9(float g[9], const Coef &k)
+{
+    collide9l<LaneF1, OP>(g, k);
+}
+
+// Two nodes at once, one in each half of a float2: the same bits as collide9 on each.
+template <int OP>
+__device__ __forceinline__ void collide9x2(float2 g[9], const Coef &k)
+{
+    collide9l<LaneF2, OP>(g, k);
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -80,6 +80,7 @@ struct erlbm_handle {
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the stream created at erlbm_create
     int shape = 0;                      // launch shape of the fused periodic kernel (erlbm_set_launch)
+    bool two_step = false;              // pairs of fused periodic steps as one launch (erlbm_set_launch)
     std::vector<uint8_t> h_solid;       // host copy of the solid mask (empty for periodic boxes)
     std::vector<double> h_profile;      // parabolic inlet velocity per (y, z) of the inlet plane
     double *d_profile = nullptr;
@@ -531,8 +532,22 @@ int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc)
     if (n_steps < 0) return ERLBM_E_INVAL;
     BCp b;
     if ((rc = validate_bc(h, bc, &b))) return rc;
-    for (int s = 0; s < n_steps; s++)
+    const bool fused2 = h->two_step && h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && b.inlet_x < 0 &&
+                        b.outlet_x < 0 && b.open_y < 0 && periodic_d2q9_x2_ok(h->g);
+    for (int s = 0; s < n_steps;) {
+        if (fused2 && h->kind == 1 && n_steps - s >= 2) {
+            // two plain periodic steps in one launch: step s and s + 1
+            CKL(launch_periodic_d2q9_fp32_x2(h->op, h->g, h->R, (const float *)h->d_buf[h->cur],
+                                             (float *)h->d_buf[h->cur ^ 1], h->stream),
+                "periodic_d2q9_x2");
+            h->cur ^= 1;
+            h->steps_done += 2;
+            s += 2;
+            continue;
+        }
         if ((rc = enqueue_step(h, b, 0, 0.0, false))) return rc;
+        s++;
+    }
     return ERLBM_OK;
 }
 
@@ -544,8 +559,9 @@ int erlbm_set_launch(erlbm_handle *h, int block_threads, int flags)
         set_error("block_threads must be 0, 128, 256 or 512%s%s", "", "");
         return ERLBM_E_INVAL;
     }
-    if (flags & ~ERLBM_LAUNCH_STREAMING_STORES) return ERLBM_E_INVAL;
+    if (flags & ~(ERLBM_LAUNCH_STREAMING_STORES | ERLBM_LAUNCH_TWO_STEP)) return ERLBM_E_INVAL;
     h->shape = block_threads | ((flags & ERLBM_LAUNCH_STREAMING_STORES) ? 0x1000 : 0);
+    h->two_step = (flags & ERLBM_LAUNCH_TWO_STEP) != 0;
     return ERLBM_OK;
 }
 

@@ -132,7 +132,186 @@ int periodic_shape(int block, bool st, const Geo &g, const shifted::Coef &k, con
     return 0;
 }
 
+// Two steps per launch (temporal blocking).  A CTA owns a strip of W columns and a chunk of HC rows
+// and walks down it with a rolling window: four rows of the input populations P (W + 4 columns: the
+// two-step pull reaches two columns out) and four rows of the intermediate step P' (W + 2 columns),
+// both in shared memory.  Per iteration two output rows j, j + 1 are made: rows j + 2, j + 3 of P
+// enter the window (their global loads were issued one iteration ahead), rows j + 1, j + 2 of P' are
+// collided from P, and rows j, j + 1 of the output from P'; only the output goes back to HBM.  The
+// two rows of each stage are collided together as the two halves of float2 lanes (packed FP32x2
+// instructions), with the same bits as the one-step kernel.  Each node is read once and written once
+// per two steps, plus a margin for the window's start (four rows per chunk) and the strip edges.
+template <int W>
+struct X2 {
+    static constexpr int T = W + 32;  // threads: W + 4 loaders, W + 2 for P', W for the output
+    static constexpr int WA = W + 4;
+    static constexpr int WB = W + 2;
+    static constexpr size_t SMEM = (size_t)4 * 9 * (WA + WB) * sizeof(float);
+};
+
+__device__ __forceinline__ int slot4(int r) { return (r + 8) & 3; }  // rows from y0 - 8 up
+
+
+template <int OP, int W>
+__global__ void __launch_bounds__(X2<W>::T) k_periodic_d2q9_x2(const float *__restrict__ src, float *__restrict__ dst,
+                                                               int nx, int ny, long long plane, int hc,
+                                                               shifted::Coef k)
+{
+    constexpr int WA = X2<W>::WA, WB = X2<W>::WB;
+    extern __shared__ float x2_smem[];
+    float *A = x2_smem;              // [4][9][WA]
+    float *B = x2_smem + 4 * 9 * WA;  // [4][9][WB]
+    const int t = threadIdx.x;
+    const int strips = nx / W;
+    const int x0 = (blockIdx.x % strips) * W;
+    const int y0 = (blockIdx.x / strips) * hc;
+    const int y1 = min(y0 + hc, ny);
+    int cw = x0 - 2 + t;  // this thread's column of the P window (periodic in x)
+    cw = cw < 0 ? cw + nx : (cw >= nx ? cw - nx : cw);
+
+    auto load_row = [&](int r, float v[9]) {
+        const int rr = ((r % ny) + ny) % ny;
+        const float *p = src + (long long)rr * nx + cw;
+#pragma unroll
+        for (int i = 0; i < 9; i++) v[i] = __ldg(p + i * plane);
+    };
+    auto put_row = [&](int r, const float v[9]) {
+        float *a = A + slot4(r) * 9 * WA + t;
+#pragma unroll
+        for (int i = 0; i < 9; i++) a[i * WA] = v[i];
+    };
+    // P' rows r and r + 1 at column x0 - 1 + t, from the P window
+    auto mid2 = [&](int r) {
+        if (t >= WB) return;
+        float2 g[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            const int c = (t + 1) - Lat<9>::cx(i);
+            g[i].x = A[(slot4(r - Lat<9>::cy(i)) * 9 + i) * WA + c];
+            g[i].y = A[(slot4(r + 1 - Lat<9>::cy(i)) * 9 + i) * WA + c];
+        }
+        shifted::collide9x2<OP>(g, k);
+        float *b0 = B + slot4(r) * 9 * WB + t, *b1 = B + slot4(r + 1) * 9 * WB + t;
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            b0[i * WB] = g[i].x;
+            b1[i * WB] = g[i].y;
+        }
+    };
+    // output rows r and r + 1 at column x0 + t, from the P' window
+    auto out2 = [&](int r) {
+        if (t >= W) return;
+        float2 g[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            const int c = (t + 1) - Lat<9>::cx(i);
+            g[i].x = B[(slot4(r - Lat<9>::cy(i)) * 9 + i) * WB + c];
+            g[i].y = B[(slot4(r + 1 - Lat<9>::cy(i)) * 9 + i) * WB + c];
+        }
+        shifted::collide9x2<OP>(g, k);
+        float *d0 = dst + (long long)r * nx + x0 + t, *d1 = d0 + nx;
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            d0[i * plane] = g[i].x;
+            d1[i * plane] = g[i].y;
+        }
+    };
+
+    const bool loader = t < WA;
+    float va[9], vb[9];
+    // prologue: P rows y0 - 2 .. y0 + 1 and P' rows y0 - 1, y0; va, vb hold P rows y0 + 2, y0 + 3
+    if (loader) {
+        load_row(y0 - 2, va);
+        put_row(y0 - 2, va);
+        load_row(y0 - 1, va);
+        put_row(y0 - 1, va);
+        load_row(y0, va);
+        put_row(y0, va);
+        load_row(y0 + 1, va);
+        put_row(y0 + 1, va);
+    }
+    __syncthreads();
+    mid2(y0 - 1);
+    if (loader) {
+        load_row(y0 + 2, va);
+        load_row(y0 + 3, vb);
+    }
+    __syncthreads();  // mid2 has read P rows y0 - 2, y0 - 1, whose slots rows y0 + 2, y0 + 3 take
+    for (int j = y0; j < y1; j += 2) {
+        if (loader) {
+            put_row(j + 2, va);
+            put_row(j + 3, vb);
+            if (j + 2 < y1) {  // one iteration ahead
+                load_row(j + 4, va);
+                load_row(j + 5, vb);
+            }
+        }
+        __syncthreads();
+        mid2(j + 1);
+        __syncthreads();
+        out2(j);
+    }
+}
+
+
 }  // namespace
+
+// Chunk height of the two-step kernel: one wave of CTAs (resident CTAs per SM x SMs) over the
+// (nx / W) x ny lattice, so that no second, partial wave runs, and even (two rows per iteration).
+static int x2_chunk(int nx, int ny, int W, int resident_per_sm)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long slots = (long long)(resident_per_sm > 0 ? resident_per_sm : 1) * (sms > 0 ? sms : 1);
+    const long long strips = nx / W;
+    long long hc = (ny * strips + slots - 1) / slots;
+    if (hc < 8) hc = 8;
+    hc += hc & 1;
+    if (hc > ny) hc = ny;
+    return (int)hc;
+}
+
+bool periodic_d2q9_x2_ok(const Geo &g)
+{
+    return periodic_d2q9_fp32_ok(g) && g.nx % 256 == 0 && g.ny >= 4 && g.ny % 2 == 0;
+}
+
+template <int OP, int W>
+static void go_x2w(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
+{
+    auto kern = k_periodic_d2q9_x2<OP, W>;
+    static int occ = -1;  // attribute and occupancy once per instantiation
+    if (occ < 0) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)X2<W>::SMEM);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, X2<W>::T, X2<W>::SMEM) != cudaSuccess)
+            occ = 1;
+    }
+    const int hc = x2_chunk(g.nx, g.ny, W, occ);
+    const unsigned nb = (unsigned)((g.nx / W) * ((g.ny + hc - 1) / hc));
+    kern<<<nb, X2<W>::T, X2<W>::SMEM, s>>>(src, dst, g.nx, g.ny, g.plane, hc, k);
+}
+
+template <int OP>
+static void go_x2(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
+{
+    go_x2w<OP, 256>(g, k, src, dst, s);  // 512-column strips measured the same on GB300
+}
+
+// Two steps of the fused periodic D2Q9 FP32 update in one launch (periodic_d2q9_x2_ok(g) required).
+int launch_periodic_d2q9_fp32_x2(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s)
+{
+    if (!periodic_d2q9_x2_ok(g)) return -1;
+    const shifted::Coef k = shifted::make_coef(R);
+    switch (op) {
+    case OP_BGK: go_x2<OP_BGK>(g, k, src, dst, s); break;
+    case OP_MRT: go_x2<OP_MRT>(g, k, src, dst, s); break;
+    case OP_REG: go_x2<OP_REG>(g, k, src, dst, s); break;
+    case OP_EXTREG: go_x2<OP_EXTREG>(g, k, src, dst, s); break;
+    default: return -1;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
 
 // shape: threads per block (128, 256 or 512; 0 = 256) and bit 0x1000 for streaming stores.
 int launch_periodic_d2q9_fp32(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s,

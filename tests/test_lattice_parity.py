@@ -180,6 +180,24 @@ def test_run_energy_check_matches_oracle():
         assert r["margin"] == mg
 
 
+@pytest.mark.parametrize("op", [1, 2, 3, 4])
+@pytest.mark.parametrize("L,steps", [(256, 17), (512, 40)])
+def test_two_step_kernel_equals_one_step(op, L, steps):
+    """Two steps per launch (the intermediate step kept in shared memory) give the one-step kernel's
+    populations bit for bit, for every operator and for odd step counts."""
+    tau = 0.5 + 3 * (1 / 32) * L / 80000
+    f0 = eg().init_double_shear(L)
+    outs = []
+    for two in (False, True):
+        with eg().Lattice(9, L, L, 1, None, tau, 0.65, op, eg().FP32_SHIFTED) as lat:
+            lat.set_launch(256, False, two)
+            lat.set_populations(f0)
+            lat.step(steps)
+            lat.step(3)
+            outs.append((lat.get_populations(0), lat.get_populations(1)))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
 def test_fused_kernel_launch_shapes_identical_and_tuned(tmp_path, monkeypatch):
     """Every launch shape of the fused D2Q9 kernel computes the same bits; the autotuner picks one."""
     monkeypatch.setenv("ERLBM_TUNE_CACHE", str(tmp_path / "tune.json"))
@@ -188,15 +206,17 @@ def test_fused_kernel_launch_shapes_identical_and_tuned(tmp_path, monkeypatch):
     f0 = eg().init_double_shear(L)
     tau = 0.5 + 3 * (1 / 32) * L / 80000
     outs = []
-    for block, st in autotune.PERIODIC_CANDIDATES:
+    shapes = [(b, s, False) for b, s in autotune.PERIODIC_CANDIDATES] + \
+        [(b, s, True) for b, s in autotune.TWO_STEP_CANDIDATES]
+    for block, st, two in shapes:
         with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
-            lat.set_launch(block, st)
+            lat.set_launch(block, st, two)
             lat.set_populations(f0)
-            lat.step(30)
+            lat.step(30)  # 1 local step, then 29: fourteen two-step launches and one single step
             outs.append(lat.get_populations(1))
     assert all(np.array_equal(o, outs[0]) for o in outs[1:])
     best = autotune.tune_periodic(L, steps=50)
-    assert (best["block_threads"], best["streaming_stores"]) in autotune.PERIODIC_CANDIDATES
+    assert (best["block_threads"], best["streaming_stores"], best["two_step"]) in shapes
     assert autotune.tune_periodic(L)["mlups"] == best["mlups"]  # served from the cache
     with pytest.raises(eg().ErlbmError):
         with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
