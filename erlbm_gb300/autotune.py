@@ -78,7 +78,7 @@ def tune_periodic(L: int, steps: int = 200, force: bool = False) -> dict:
         lat.set_populations(E.init_double_shear(L))
         lat.step(1)
         cands = [(b, s, False) for b, s in PERIODIC_CANDIDATES]
-        if L % 256 == 0:
+        if L % 2 == 0:
             cands += [(b, s, True) for b, s in TWO_STEP_CANDIDATES]
         for block, st, two in cands:
             lat.set_launch(block, st, two)

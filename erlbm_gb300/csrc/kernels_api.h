@@ -58,7 +58,7 @@ int launch_step_fp32(int q, int op, const Geo &g, const BCp &bc, const Relax &R,
 int launch_periodic_d2q9_fp32(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s,
                               int shape = 0);
 bool periodic_d2q9_fp32_ok(const Geo &g);
-// Two steps per launch of the same update (temporal blocking; nx % 256 == 0, ny >= 4).
+// Two steps per launch of the same update (temporal blocking; nx % 128 == 0, ny even and >= 4).
 int launch_periodic_d2q9_fp32_x2(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s);
 bool periodic_d2q9_x2_ok(const Geo &g);
 

@@ -171,7 +171,8 @@ int erlbm_sync(erlbm_handle *h);
 /* launch shape of the fused periodic D2Q9 FP32 kernel (the double-shear-layer lattices): threads per
  * block (128, 256, 512; 0 = default 256) and flags (ERLBM_LAUNCH_STREAMING_STORES: evict-first
  * stores; ERLBM_LAUNCH_TWO_STEP: pairs of consecutive steps run as one launch that keeps the
- * intermediate step in shared memory, where nx % 256 == 0 -- the same results, half the HBM traffic).
+ * intermediate step in shared memory, where nx % 128 == 0 and ny is even -- the same results, half the
+ * HBM traffic).
  * Chosen by erlbm_gb300.autotune; no counterpart in the reference. */
 #define ERLBM_LAUNCH_STREAMING_STORES 1
 #define ERLBM_LAUNCH_TWO_STEP 2
