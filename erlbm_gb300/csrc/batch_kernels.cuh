@@ -100,6 +100,38 @@ __device__ __forceinline__ void batch_collide(typename P::T *f, const BatchRun &
         P::template collide<Q, OP_EXTREG>(f, prm);
 }
 
+// Two nodes of the FP32 path at once, in the halves of float2 lanes (packed FP32x2 instructions): the
+// same bits as batch_collide on each.
+template <int Q>
+__device__ __forceinline__ void batch_collide_pair(float *fa, float *fb, const BatchRun &r)
+{
+    float2 g[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) g[i] = make_float2(fa[i], fb[i]);
+    if constexpr (Q == 9) {
+        if (r.op == OP_MRT)
+            shifted::collide9x2<OP_MRT>(g, r.k);
+        else if (r.op == OP_BGK)
+            shifted::collide9x2<OP_BGK>(g, r.k);
+        else if (r.op == OP_REG)
+            shifted::collide9x2<OP_REG>(g, r.k);
+        else
+            shifted::collide9x2<OP_EXTREG>(g, r.k);
+    } else {
+        if (r.op == OP_BGK)
+            shifted::collide19x2<OP_BGK>(g, r.k);
+        else if (r.op == OP_REG)
+            shifted::collide19x2<OP_REG>(g, r.k);
+        else
+            shifted::collide19x2<OP_EXTREG>(g, r.k);
+    }
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        fa[i] = g[i].x;
+        fb[i] = g[i].y;
+    }
+}
+
 // Initial equilibrium of the Taylor-Green map (main_stability-map_taylor-green.cpp:49-61): rho = 1,
 // u_x = U0 sin(kx) cos(ky), u_y = -U0 cos(kx) sin(ky), u_z = 0.
 template <class P, int Q>
@@ -376,7 +408,24 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
             } else if (Q == 19 && x == g.inlet_x) {
                 P::zou_he(f[s], *reinterpret_cast<const ZH *>(sm.zh), g.inlet_x < g.nx / 2);
             }
-            batch_collide<P, Q>(f[s], r);
+        }
+        // FP32: the nodes of a thread in pairs, in packed FP32x2 instructions
+        constexpr bool PAIRS = sizeof(T) == 4 && NPT % 2 == 0;
+        if constexpr (PAIRS) {
+#pragma unroll
+            for (int s = 0; s < NPT; s += 2) {
+                if (fluid[s] && fluid[s + 1]) {
+                    batch_collide_pair<Q>(f[s], f[s + 1], r);
+                } else {
+                    if (fluid[s]) batch_collide<P, Q>(f[s], r);
+                    if (fluid[s + 1]) batch_collide<P, Q>(f[s + 1], r);
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < NPT; s++) {
+            if (!fluid[s]) continue;
+            if constexpr (!PAIRS) batch_collide<P, Q>(f[s], r);
             if (g.density_check) {
                 if constexpr (sizeof(T) == 4) {
                     const float d = shifted::node_drho<Q>(f[s]);

@@ -52,30 +52,6 @@ __host__ __device__ inline Coef make_coef(const Relax &R)
     return k;
 }
 
-// Update of one opposite pair from its even/odd non-equilibrium parts (de, do) and f1.  The
-// increment is formed from the small quantities first and added to the stored population once,
-// so only that last addition rounds at the scale of g.
-template <int OP>
-__device__ __forceinline__ void update_pair(float &gi, float &gj, float de, float dO, float f1, const Coef &k)
-{
-    if (OP == OP_BGK) {
-        const float di = de + dO, dj = de - dO;
-        gi += fmaf(k.d1, di, -2.f * di);
-        gj += fmaf(k.d1, dj, -2.f * dj);
-    } else {
-        const float a = de - f1, t = -2.f * f1;
-        gi += fmaf(k.d1, f1, fmaf(k.kd, a + dO, t));
-        gj += fmaf(k.d1, f1, fmaf(k.kd, a - dO, t));
-    }
-}
-
-template <int OP>
-__device__ __forceinline__ float update_rest(float g0, float de0, float f10, const Coef &k)
-{
-    if (OP == OP_BGK) return g0 + fmaf(k.d1, de0, -2.f * de0);
-    return g0 + fmaf(k.d1, f10, fmaf(k.kd, de0 - f10, -2.f * f10));
-}
-
 // ------------------------------------------------------------------------------------------------
 // D2Q9: pairs X = (1,2) c = (1,0); Y = (3,4) c = (0,1); P = (5,6) c = (1,1); M = (7,8) c = (1,-1)
 // ------------------------------------------------------------------------------------------------
@@ -118,7 +94,9 @@ struct LaneF2 {
     static __device__ __forceinline__ V rcp(V a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
 };
 
-// update_pair / update_rest in lane arithmetic
+// Update of one opposite pair from its even/odd non-equilibrium parts (de, do) and f1, and of the
+// rest population.  The increment is formed from the small quantities first and added to the stored
+// population once, so only that last addition rounds at the scale of g.
 template <class M, int OP>
 __device__ __forceinline__ void update_pair_l(typename M::V &gi, typename M::V &gj, typename M::V de,
                                               typename M::V dO, typename M::V f1, const Coef &k)
@@ -259,76 +237,99 @@ __device__ __forceinline__ void moments19(const float g[19], float &drho, float 
     uz = mz * inv;
 }
 
+// The D3Q19 update in lane arithmetic (one node per float lane, or two per float2 lane).
+template <class M, int OP>
+__device__ __forceinline__ void collide19l(typename M::V g[19], const Coef &k)
+{
+    using V = typename M::V;
+    constexpr float W1 = 1.f / 18.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
+    const V half = M::c(0.5f), two = M::c(2.f);
+    const V eX = M::mul(half, M::add(g[1], g[2])), oX = M::mul(half, M::sub(g[1], g[2]));
+    const V eY = M::mul(half, M::add(g[3], g[4])), oY = M::mul(half, M::sub(g[3], g[4]));
+    const V eZ = M::mul(half, M::add(g[5], g[6])), oZ = M::mul(half, M::sub(g[5], g[6]));
+    const V eA = M::mul(half, M::add(g[7], g[8])), oA = M::mul(half, M::sub(g[7], g[8]));
+    const V eB = M::mul(half, M::add(g[9], g[10])), oB = M::mul(half, M::sub(g[9], g[10]));
+    const V eC = M::mul(half, M::add(g[11], g[12])), oC = M::mul(half, M::sub(g[11], g[12]));
+    const V eD = M::mul(half, M::add(g[13], g[14])), oD = M::mul(half, M::sub(g[13], g[14]));
+    const V eE = M::mul(half, M::add(g[16], g[15])), oE = M::mul(half, M::sub(g[16], g[15]));
+    const V eF = M::mul(half, M::add(g[17], g[18])), oF = M::mul(half, M::sub(g[17], g[18]));
+    const V drho = M::fma(two, M::add(M::add(M::add(eX, eY), M::add(eZ, eA)),
+                                      M::add(M::add(eB, eC), M::add(eD, M::add(eE, eF)))), g[0]);
+    const V mx = M::mul(two, M::add(M::add(oX, M::add(oA, oB)), M::add(oC, oD)));
+    const V my = M::mul(two, M::add(M::add(oY, M::sub(oA, oB)), M::sub(oE, oF)));
+    const V mz = M::mul(two, M::add(M::add(oZ, M::sub(oC, oD)), M::add(oE, oF)));
+    const V inv = M::rcp(M::add(M::c(1.f), drho));
+    const V ux = M::mul(mx, inv), uy = M::mul(my, inv), uz = M::mul(mz, inv);
+    const V mu15 = M::mul(M::c(-1.5f), M::fma(mx, ux, M::fma(my, uy, M::mul(mz, uz))));
+    const V mw1 = M::c(-W1), mw2 = M::c(-W2), k45 = M::c(4.5f);
+    const V r1 = M::mul(mw1, drho), r2 = M::mul(mw2, drho);
+    const V deX = M::fma(mw1, M::fma(M::mul(k45, mx), ux, mu15), M::add(eX, r1));
+    const V deY = M::fma(mw1, M::fma(M::mul(k45, my), uy, mu15), M::add(eY, r1));
+    const V deZ = M::fma(mw1, M::fma(M::mul(k45, mz), uz, mu15), M::add(eZ, r1));
+    const V cmA = M::add(mx, my), cmB = M::sub(mx, my), cmC = M::add(mx, mz), cmD = M::sub(mx, mz);
+    const V cmE = M::add(my, mz), cmF = M::sub(mz, my);
+    const V deA = M::fma(mw2, M::fma(M::mul(k45, cmA), M::add(ux, uy), mu15), M::add(eA, r2));
+    const V deB = M::fma(mw2, M::fma(M::mul(k45, cmB), M::sub(ux, uy), mu15), M::add(eB, r2));
+    const V deC = M::fma(mw2, M::fma(M::mul(k45, cmC), M::add(ux, uz), mu15), M::add(eC, r2));
+    const V deD = M::fma(mw2, M::fma(M::mul(k45, cmD), M::sub(ux, uz), mu15), M::add(eD, r2));
+    const V deE = M::fma(mw2, M::fma(M::mul(k45, cmE), M::add(uy, uz), mu15), M::add(eE, r2));
+    const V deF = M::fma(mw2, M::fma(M::mul(k45, cmF), M::sub(uz, uy), mu15), M::add(eF, r2));
+    const V de0 = M::mul(M::c(-2.f), M::add(M::add(M::add(deX, deY), M::add(deZ, deA)),
+                                             M::add(M::add(deB, deC), M::add(deD, M::add(deE, deF)))));
+    const V m3w2 = M::c(M3W2);
+    const V doA = M::fma(m3w2, cmA, oA), doB = M::fma(m3w2, cmB, oB);
+    const V doC = M::fma(m3w2, cmC, oC), doD = M::fma(m3w2, cmD, oD);
+    const V doE = M::fma(m3w2, cmE, oE), doF = M::fma(m3w2, cmF, oF);
+    const V doX = M::neg(M::add(M::add(doA, doB), M::add(doC, doD)));
+    const V doY = M::neg(M::add(M::sub(doA, doB), M::sub(doE, doF)));
+    const V doZ = M::neg(M::add(M::sub(doC, doD), M::add(doE, doF)));
+    const V zero = M::c(0.f);
+    V f10 = zero, f1X = zero, f1Y = zero, f1Z = zero, f1A = zero, f1B = zero, f1C = zero, f1D = zero, f1E = zero,
+      f1F = zero;
+    if (OP != OP_BGK) {
+        const V pxx = M::mul(two, M::add(M::add(deX, M::add(deA, deB)), M::add(deC, deD)));
+        const V pyy = M::mul(two, M::add(M::add(deY, M::add(deA, deB)), M::add(deE, deF)));
+        const V pzz = M::mul(two, M::add(M::add(deZ, M::add(deC, deD)), M::add(deE, deF)));
+        const V pxy = M::mul(two, M::sub(deA, deB)), pxz = M::mul(two, M::sub(deC, deD));
+        const V pyz = M::mul(two, M::sub(deE, deF));
+        const V tr3 = M::mul(M::add(M::add(pxx, pyy), pzz), M::c(1.f / 3.f));
+        const V q4 = M::c(0.25f), q8 = M::c(0.125f), mq4 = M::c(-0.25f);
+        f10 = M::mul(M::c(-1.5f), tr3);
+        f1X = M::mul(q4, M::sub(pxx, tr3));
+        f1Y = M::mul(q4, M::sub(pyy, tr3));
+        f1Z = M::mul(q4, M::sub(pzz, tr3));
+        const V bxy = M::mul(q8, M::sub(M::add(pxx, pyy), tr3));
+        const V bxz = M::mul(q8, M::sub(M::add(pxx, pzz), tr3));
+        const V byz = M::mul(q8, M::sub(M::add(pyy, pzz), tr3));
+        f1A = M::fma(q4, pxy, bxy);
+        f1B = M::fma(mq4, pxy, bxy);
+        f1C = M::fma(q4, pxz, bxz);
+        f1D = M::fma(mq4, pxz, bxz);
+        f1E = M::fma(q4, pyz, byz);
+        f1F = M::fma(mq4, pyz, byz);
+    }
+    g[0] = update_rest_l<M, OP>(g[0], de0, f10, k);
+    update_pair_l<M, OP>(g[1], g[2], deX, doX, f1X, k);
+    update_pair_l<M, OP>(g[3], g[4], deY, doY, f1Y, k);
+    update_pair_l<M, OP>(g[5], g[6], deZ, doZ, f1Z, k);
+    update_pair_l<M, OP>(g[7], g[8], deA, doA, f1A, k);
+    update_pair_l<M, OP>(g[9], g[10], deB, doB, f1B, k);
+    update_pair_l<M, OP>(g[11], g[12], deC, doC, f1C, k);
+    update_pair_l<M, OP>(g[13], g[14], deD, doD, f1D, k);
+    update_pair_l<M, OP>(g[16], g[15], deE, doE, f1E, k);
+    update_pair_l<M, OP>(g[17], g[18], deF, doF, f1F, k);
+}
+
 template <int OP>
 __device__ __forceinline__ void collide19(float g[19], const Coef &k)
 {
-    constexpr float W1 = 1.f / 18.f, W2 = 1.f / 36.f;
-    const float eX = 0.5f * (g[1] + g[2]), oX = 0.5f * (g[1] - g[2]);
-    const float eY = 0.5f * (g[3] + g[4]), oY = 0.5f * (g[3] - g[4]);
-    const float eZ = 0.5f * (g[5] + g[6]), oZ = 0.5f * (g[5] - g[6]);
-    const float eA = 0.5f * (g[7] + g[8]), oA = 0.5f * (g[7] - g[8]);
-    const float eB = 0.5f * (g[9] + g[10]), oB = 0.5f * (g[9] - g[10]);
-    const float eC = 0.5f * (g[11] + g[12]), oC = 0.5f * (g[11] - g[12]);
-    const float eD = 0.5f * (g[13] + g[14]), oD = 0.5f * (g[13] - g[14]);
-    const float eE = 0.5f * (g[16] + g[15]), oE = 0.5f * (g[16] - g[15]);
-    const float eF = 0.5f * (g[17] + g[18]), oF = 0.5f * (g[17] - g[18]);
-    const float drho = g[0] + 2.f * (((eX + eY) + (eZ + eA)) + ((eB + eC) + (eD + (eE + eF))));
-    const float mx = 2.f * ((oX + (oA + oB)) + (oC + oD));
-    const float my = 2.f * ((oY + (oA - oB)) + (oE - oF));
-    const float mz = 2.f * ((oZ + (oC - oD)) + (oE + oF));
-    const float inv = __frcp_rn(1.f + drho);
-    const float ux = mx * inv, uy = my * inv, uz = mz * inv;
-    const float mu15 = -1.5f * fmaf(mx, ux, fmaf(my, uy, mz * uz));
-    const float r1 = -W1 * drho, r2 = -W2 * drho;
-    const float deX = fmaf(-W1, fmaf(4.5f * mx, ux, mu15), eX + r1);
-    const float deY = fmaf(-W1, fmaf(4.5f * my, uy, mu15), eY + r1);
-    const float deZ = fmaf(-W1, fmaf(4.5f * mz, uz, mu15), eZ + r1);
-    const float cmA = mx + my, cmB = mx - my, cmC = mx + mz, cmD = mx - mz, cmE = my + mz, cmF = mz - my;
-    const float deA = fmaf(-W2, fmaf(4.5f * cmA, ux + uy, mu15), eA + r2);
-    const float deB = fmaf(-W2, fmaf(4.5f * cmB, ux - uy, mu15), eB + r2);
-    const float deC = fmaf(-W2, fmaf(4.5f * cmC, ux + uz, mu15), eC + r2);
-    const float deD = fmaf(-W2, fmaf(4.5f * cmD, ux - uz, mu15), eD + r2);
-    const float deE = fmaf(-W2, fmaf(4.5f * cmE, uy + uz, mu15), eE + r2);
-    const float deF = fmaf(-W2, fmaf(4.5f * cmF, uz - uy, mu15), eF + r2);
-    const float de0 = -2.f * (((deX + deY) + (deZ + deA)) + ((deB + deC) + (deD + (deE + deF))));
-    const float doA = fmaf(-3.f * W2, cmA, oA), doB = fmaf(-3.f * W2, cmB, oB);
-    const float doC = fmaf(-3.f * W2, cmC, oC), doD = fmaf(-3.f * W2, cmD, oD);
-    const float doE = fmaf(-3.f * W2, cmE, oE), doF = fmaf(-3.f * W2, cmF, oF);
-    const float doX = -((doA + doB) + (doC + doD));
-    const float doY = -((doA - doB) + (doE - doF));
-    const float doZ = -((doC - doD) + (doE + doF));
-    float f10 = 0.f, f1X = 0.f, f1Y = 0.f, f1Z = 0.f, f1A = 0.f, f1B = 0.f, f1C = 0.f, f1D = 0.f, f1E = 0.f,
-          f1F = 0.f;
-    if (OP != OP_BGK) {
-        const float pxx = 2.f * ((deX + (deA + deB)) + (deC + deD));
-        const float pyy = 2.f * ((deY + (deA + deB)) + (deE + deF));
-        const float pzz = 2.f * ((deZ + (deC + deD)) + (deE + deF));
-        const float pxy = 2.f * (deA - deB), pxz = 2.f * (deC - deD), pyz = 2.f * (deE - deF);
-        const float tr3 = (pxx + pyy + pzz) * (1.f / 3.f);
-        f10 = -1.5f * tr3;
-        f1X = 0.25f * (pxx - tr3);
-        f1Y = 0.25f * (pyy - tr3);
-        f1Z = 0.25f * (pzz - tr3);
-        const float bxy = 0.125f * ((pxx + pyy) - tr3);
-        const float bxz = 0.125f * ((pxx + pzz) - tr3);
-        const float byz = 0.125f * ((pyy + pzz) - tr3);
-        f1A = fmaf(0.25f, pxy, bxy);
-        f1B = fmaf(-0.25f, pxy, bxy);
-        f1C = fmaf(0.25f, pxz, bxz);
-        f1D = fmaf(-0.25f, pxz, bxz);
-        f1E = fmaf(0.25f, pyz, byz);
-        f1F = fmaf(-0.25f, pyz, byz);
-    }
-    g[0] = update_rest<OP>(g[0], de0, f10, k);
-    update_pair<OP>(g[1], g[2], deX, doX, f1X, k);
-    update_pair<OP>(g[3], g[4], deY, doY, f1Y, k);
-    update_pair<OP>(g[5], g[6], deZ, doZ, f1Z, k);
-    update_pair<OP>(g[7], g[8], deA, doA, f1A, k);
-    update_pair<OP>(g[9], g[10], deB, doB, f1B, k);
-    update_pair<OP>(g[11], g[12], deC, doC, f1C, k);
-    update_pair<OP>(g[13], g[14], deD, doD, f1D, k);
-    update_pair<OP>(g[16], g[15], deE, doE, f1E, k);
-    update_pair<OP>(g[17], g[18], deF, doF, f1F, k);
+    collide19l<LaneF1, OP>(g, k);
+}
+
+template <int OP>
+__device__ __forceinline__ void collide19x2(float2 g[19], const Coef &k)
+{
+    collide19l<LaneF2, OP>(g, k);
 }
 
 template <int Q, int OP>
