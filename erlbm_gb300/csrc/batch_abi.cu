@@ -64,8 +64,9 @@ namespace erlbm {
 int pick_shape(int prec, int q, int nb, int slots, int n_runs, LaunchShape *out)
 {
     static const int NPT_64[] = {1, 2, 4};
-    // FP32 prefers two nodes per thread: their collisions run as pairs in packed FP32x2 instructions
-    // (Taylor-Green map on GB300: 42.2 k runs/s against 33.9 k with one node per thread)
+    // FP32 prefers two nodes per thread (more independent work per thread; D2Q9 pairs also collide in
+    // packed FP32x2 instructions): Taylor-Green map on GB300 42.2 k runs/s against 33.9 k with one
+    // node per thread
     static const int NPT_32[] = {2, 1, 4, 8};
     const int *list = prec == ERLBM_FP64 ? NPT_64 : NPT_32;
     const int nl = prec == ERLBM_FP64 ? 3 : 4;

@@ -100,31 +100,23 @@ __device__ __forceinline__ void batch_collide(typename P::T *f, const BatchRun &
         P::template collide<Q, OP_EXTREG>(f, prm);
 }
 
-// Two nodes of the FP32 path at once, in the halves of float2 lanes (packed FP32x2 instructions): the
-// same bits as batch_collide on each.
+// Two D2Q9 nodes of the FP32 path at once, in the halves of float2 lanes (packed FP32x2
+// instructions): the same bits as batch_collide on each.
 template <int Q>
 __device__ __forceinline__ void batch_collide_pair(float *fa, float *fb, const BatchRun &r)
 {
+    static_assert(Q == 9, "packed pairs are used for D2Q9");
     float2 g[Q];
 #pragma unroll
     for (int i = 0; i < Q; i++) g[i] = make_float2(fa[i], fb[i]);
-    if constexpr (Q == 9) {
-        if (r.op == OP_MRT)
-            shifted::collide9x2<OP_MRT>(g, r.k);
-        else if (r.op == OP_BGK)
-            shifted::collide9x2<OP_BGK>(g, r.k);
-        else if (r.op == OP_REG)
-            shifted::collide9x2<OP_REG>(g, r.k);
-        else
-            shifted::collide9x2<OP_EXTREG>(g, r.k);
-    } else {
-        if (r.op == OP_BGK)
-            shifted::collide19x2<OP_BGK>(g, r.k);
-        else if (r.op == OP_REG)
-            shifted::collide19x2<OP_REG>(g, r.k);
-        else
-            shifted::collide19x2<OP_EXTREG>(g, r.k);
-    }
+    if (r.op == OP_MRT)
+        shifted::collide9x2<OP_MRT>(g, r.k);
+    else if (r.op == OP_BGK)
+        shifted::collide9x2<OP_BGK>(g, r.k);
+    else if (r.op == OP_REG)
+        shifted::collide9x2<OP_REG>(g, r.k);
+    else
+        shifted::collide9x2<OP_EXTREG>(g, r.k);
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         fa[i] = g[i].x;
@@ -137,6 +129,19 @@ __device__ __forceinline__ void batch_collide_pair(float *fa, float *fb, const B
 template <class P, int Q>
 __device__ __forceinline__ void tg_map_init(typename P::T *f, int x, int y, double u0, const BatchGeo &g)
 {
+    if constexpr (sizeof(typename P::T) == 4) {
+        // FP32 path: the shifted equilibrium at rho = 1, g_i = w_i (3 cu + 4.5 cu^2 - 1.5 u^2), formed in
+        // FP32 from small quantities (within an ulp or two of the FP64 equilibrium rounded to float)
+        const float ux = (float)(u0 * g.sinx[x] * g.cosx[y]);
+        const float uy = (float)(-u0 * g.cosx[x] * g.sinx[y]);
+        const float mu = -1.5f * fmaf(ux, ux, uy * uy);
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const float cu = (float)Lat<Q>::cx(i) * ux + (float)Lat<Q>::cy(i) * uy;
+            f[i] = (float)Lat<Q>::w(i) * fmaf(cu, fmaf(4.5f, cu, 3.f), mu);
+        }
+        return;
+    }
     const double ux = u0 * g.sinx[x] * g.cosx[y];
     const double uy = -u0 * g.cosx[x] * g.sinx[y];
     double feq[Q];
@@ -340,7 +345,8 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
         E = E0;
     }
 
-    for (int step = 0; step < r.n_steps; step++) {
+    int until_check = g.energy_every;  // steps to the next energy check (no division in the loop)
+    for (int step = 0; step < r.n_steps; step++, until_check--) {
         // ---- stream: post-stream populations of this step ----
         if (step > 0) {
 #pragma unroll
@@ -373,7 +379,8 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
         if (!dbl) __syncthreads();
 
         // ---- energy check on the post-stream populations ----
-        if (g.energy_every > 0 && step > 0 && step % g.energy_every == 0) {
+        if (g.energy_every > 0 && until_check == 0) {  // step > 0 && step % energy_every == 0
+            until_check = g.energy_every;
             double e = 0.0;
 #pragma unroll
             for (int s = 0; s < NPT; s++)
@@ -410,7 +417,10 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
             }
         }
         // FP32: the nodes of a thread in pairs, in packed FP32x2 instructions
-        constexpr bool PAIRS = sizeof(T) == 4 && NPT % 2 == 0;
+        // D2Q9 only: for D3Q19 the packed form measured no faster than two scalar collisions on GB300
+        // and put part of its work on the FP64 pipe (ncu, Taylor-Green map), which the FP64 lattices of
+        // a mixed workload need
+        constexpr bool PAIRS = sizeof(T) == 4 && NPT % 2 == 0 && Q == 9;
         if constexpr (PAIRS) {
 #pragma unroll
             for (int s = 0; s < NPT; s += 2) {

@@ -237,7 +237,7 @@ __device__ __forceinline__ void moments19(const float g[19], float &drho, float 
     uz = mz * inv;
 }
 
-// The D3Q19 update in lane arithmetic (one node per float lane, or two per float2 lane).
+// The D3Q19 update in lane arithmetic (explicitly rounded operations).
 template <class M, int OP>
 __device__ __forceinline__ void collide19l(typename M::V g[19], const Coef &k)
 {
@@ -326,12 +326,6 @@ __device__ __forceinline__ void collide19(float g[19], const Coef &k)
     collide19l<LaneF1, OP>(g, k);
 }
 
-template <int OP>
-__device__ __forceinline__ void collide19x2(float2 g[19], const Coef &k)
-{
-    collide19l<LaneF2, OP>(g, k);
-}
-
 template <int Q, int OP>
 __device__ __forceinline__ void collide(float *g, const Coef &k)
 {
@@ -342,18 +336,19 @@ __device__ __forceinline__ void collide(float *g, const Coef &k)
         collide19<OP>(g, k);
 }
 
-// 1/2 |u|^2 of a node (FP32 velocity, returned in FP64 for the FP64 energy reduction)
+// 1/2 |u|^2 of a node, from the FP32 velocity in FP32 (one conversion for the FP64 energy reduction:
+// on GB300 every FP64 operation and conversion is issued at a small fraction of the FP32 rate)
 template <int Q>
 __device__ __forceinline__ double node_energy(const float *g)
 {
     if constexpr (Q == 9) {
         float drho, mx, my, ux, uy;
         moments9(g, drho, mx, my, ux, uy);
-        return 0.5 * ((double)ux * ux + (double)uy * uy);
+        return (double)(0.5f * fmaf(ux, ux, uy * uy));
     } else {
         float drho, mx, my, mz, ux, uy, uz;
         moments19(g, drho, mx, my, mz, ux, uy, uz);
-        return 0.5 * (((double)ux * ux + (double)uy * uy) + (double)uz * uz);
+        return (double)(0.5f * fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
     }
 }
 
