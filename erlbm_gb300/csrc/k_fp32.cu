@@ -258,11 +258,8 @@ __global__ void __launch_bounds__(X2<W>::T) k_periodic_d2q9_x2(const float *__re
 
 // Chunk height of the two-step kernel: one wave of CTAs (resident CTAs per SM x SMs) over the
 // (nx / W) x ny lattice, so that no second, partial wave runs, and even (two rows per iteration).
-static int x2_chunk(int nx, int ny, int W, int resident_per_sm)
+static int x2_chunk(int nx, int ny, int W, int resident_per_sm, int sms)
 {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long slots = (long long)(resident_per_sm > 0 ? resident_per_sm : 1) * (sms > 0 ? sms : 1);
     const long long strips = nx / W;
     long long hc = (ny * strips + slots - 1) / slots;
@@ -281,13 +278,23 @@ template <int OP, int W>
 static void go_x2w(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
 {
     auto kern = k_periodic_d2q9_x2<OP, W>;
-    static int occ = -1;  // attribute and occupancy once per instantiation
-    if (occ < 0) {
+    // shared-memory attribute, occupancy and SM count once per device and instantiation (settings
+    // are per device; concurrent first calls set the same values)
+    constexpr int MAXDEV = 64;
+    static int occ[MAXDEV], sms[MAXDEV];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int d = dev >= 0 && dev < MAXDEV ? dev : 0;
+    if (occ[d] <= 0) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)X2<W>::SMEM);
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, X2<W>::T, X2<W>::SMEM) != cudaSuccess)
-            occ = 1;
+        int o = 0, n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, X2<W>::T, X2<W>::SMEM) != cudaSuccess || o < 1)
+            o = 1;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        sms[d] = n > 0 ? n : 1;
+        occ[d] = o;
     }
-    const int hc = x2_chunk(g.nx, g.ny, W, occ);
+    const int hc = x2_chunk(g.nx, g.ny, W, occ[d], sms[d]);
     const unsigned nb = (unsigned)((g.nx / W) * ((g.ny + hc - 1) / hc));
     kern<<<nb, X2<W>::T, X2<W>::SMEM, s>>>(src, dst, g.nx, g.ny, g.plane, hc, k);
 }
