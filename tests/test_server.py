@@ -96,3 +96,32 @@ def test_server_results_match_oracle():
         r = srv.wait(srv.submit(m.REQ_OBSTACLE, m.FP64, sx=2, sy=2, tau=tau, tau_nh=tnh, u0=u, n_steps=500))
         lab, dec, mg = O.obstacle_map_point(tau, tnh, u, sx=2, sy=2, max_steps=500)
         assert (r["label"], r["decided_step"]) == (lab, dec)
+
+
+def test_resident_loop_relaunches_after_idling_out():
+    """The resident loop's CTAs leave after about half a second without work (a bounded wait); a
+    request that arrives later relaunches it and gets the same result."""
+    import time
+    m = E()
+    with m.Server(hbm_budget_bytes=1 << 28) as srv:
+        u0, tau, tnh = m.tg_map_params(250, 40)
+        a = srv.wait(srv.submit(m.REQ_TG_MAP_POINT, m.FP32_SHIFTED, tau=tau, tau_nh=tnh, u0=u0, n_steps=700))
+        time.sleep(1.5)  # longer than the loop's idle limit
+        b = srv.wait(srv.submit(m.REQ_TG_MAP_POINT, m.FP32_SHIFTED, tau=tau, tau_nh=tnh, u0=u0, n_steps=700),
+                     timeout=60)
+        for k in ("status", "label", "steps_done", "decided_step", "energy", "margin", "lane"):
+            assert a[k] == b[k] or (a[k] != a[k] and b[k] != b[k]), k  # an unstable run reports NaN
+        assert a["lane"] == 0
+
+
+def test_wait_times_out_and_the_result_arrives_later():
+    """erlbm_server_wait with a short limit returns ERLBM_E_TIMEOUT (-4) while the run is still going;
+    the run finishes and a later wait returns it."""
+    m = E()
+    with m.Server(hbm_budget_bytes=1 << 30) as srv:
+        t = srv.submit(m.REQ_TG3D, m.FP64, op=m.OP_EXTREG, L=64, tau=0.55, tau_nh=0.65, u0=0.05, n_steps=3000)
+        with pytest.raises(m.ErlbmError) as ei:
+            srv.wait(t, timeout=1e-3)
+        assert ei.value.code == -4
+        r = srv.wait(t, timeout=600)
+        assert r["status"] == 0 and r["steps_done"] == 3000
