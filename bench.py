@@ -414,10 +414,11 @@ def run_map(args):
 
     def one_map(points):
         if refined:  # the whole P x P grid of the map's axes; refinement needs neighbours
-            lab, dec, _, ref = E.map_run_refined(kind, op=op, n_i=P, n_j=P, max_steps=args.max_steps, slots=-1)
-            return lab, dec, int(ref.sum())
+            lab, dec, _, ref, passes = E.map_run_refined(kind, op=op, n_i=P, n_j=P, max_steps=args.max_steps,
+                                                         slots=-1, return_passes=True)
+            return lab, dec, int(ref.sum()), passes
         lab, dec, _ = E.map_run(kind, points, precision=prec, op=op, max_steps=args.max_steps, slots=-1)
-        return lab, dec, 0
+        return lab, dec, 0, 0
 
     op = 0 if kind == E.MAP_TAYLOR_GREEN else E.OP_EXTREG
     nodes = 256 if kind == E.MAP_TAYLOR_GREEN else 232
@@ -431,11 +432,12 @@ def run_map(args):
     clocks = Clocks(0)
     clocks.start()
     t0 = time.perf_counter()
-    runs, lus, n_ref = 0, 0, 0
+    runs, lus, n_ref, n_pass = 0, 0, 0, 0
     for _ in range(args.steps):
-        lab, dec, nr = one_map(pts)
+        lab, dec, nr, npass = one_map(pts)
         runs += len(lab)
         n_ref += nr
+        n_pass += npass
         lus += int(np.sum(dec.astype(np.int64))) * nodes
     dt = time.perf_counter() - t0
     clk = clocks.stop()
@@ -451,9 +453,10 @@ def run_map(args):
             "lattice_updates_per_s": lus / dt, "roofline": None,
             "e2e": {"value": value, "unit": "runs/s", "h2d_bytes_per_step": len(pts) * 48,
                     "d2h_bytes_per_step": len(pts) * 32},
-            "gpu_launches": args.steps * (2 if refined else 1), "clocks": clk}
+            "gpu_launches": args.steps + n_pass, "clocks": clk}
     if refined:
         line["refined_fraction"] = n_ref / runs
+        line["fp64_passes_per_map"] = n_pass / args.steps
     if not args.no_cpu:
         from oracle import oracle as O
         few = pts[:: max(1, len(pts) // 16)]

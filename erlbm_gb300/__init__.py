@@ -284,21 +284,29 @@ def map_run(kind: int, points=None, precision: int = FP64, op: int = OP_EXTREG, 
 
 def map_run_refined(kind: int, op: int = OP_EXTREG, tau_nh: float = 0.65, L: int = 16, ma: float = 0.1,
                     n_i: int = 400, n_j: int = 400, max_steps: int = 0, slots: int = 0, radius: int = 2,
-                    late_fraction: float = 0.3):
+                    late_fraction: float = 0.3, probe_stride: int = 16, max_passes: int = 0,
+                    return_passes: bool = False):
     """A whole stability map screened in FP32-shifted, with the boundary points refined in FP64.
 
-    Points whose FP32 label differs from a neighbour within `radius` map steps, or whose FP32 run
-    turned unstable after `late_fraction` of its budget, are run again in FP64 (the reference's
-    results).  Returns (labels, decided_step, margins, refined) with refined a boolean mask.
+    Pass 1 runs again in FP64 (the reference's results) the points within `radius` map steps of an
+    FP32 label change, the FP32 runs that turned unstable after `late_fraction` of their budget and
+    the probe points (every `probe_stride`-th point in i and j, 0 = none); each further pass runs the
+    FP32 points within `radius` of a label change of the map as it stands, until none is left (or
+    `max_passes`, 0 = no cap).  Returns (labels, decided_step, margins, refined) with refined a boolean
+    mask, and the number of FP64 passes after them when return_passes is set.
     """
     d = _lib.MapDesc(kind, FP32_SHIFTED, op, tau_nh, L, ma, n_i, n_j, 0, None, None, max_steps, slots)
+    r = _lib.RefineDesc(radius, late_fraction, probe_stride, max_passes)
     m = n_i * n_j * (2 if (kind == MAP_TAYLOR_GREEN and op == 0) else 1)
     labels = np.zeros(m, np.int32)
     dec = np.zeros(m, np.int32)
     mg = np.zeros(m, np.float64)
     ref = np.zeros(m, np.uint8)
-    check(lib().erlbm_map_run_refined(C.byref(d), radius, late_fraction, _dptr(labels), _dptr(dec), _dptr(mg),
-                                      _dptr(ref)), "erlbm_map_run_refined")
+    passes = C.c_int(0)
+    check(lib().erlbm_map_run_refined(C.byref(d), C.byref(r), _dptr(labels), _dptr(dec), _dptr(mg), _dptr(ref),
+                                      C.byref(passes)), "erlbm_map_run_refined")
+    if return_passes:
+        return labels, dec, mg, ref.astype(bool), passes.value
     return labels, dec, mg, ref.astype(bool)
 
 

@@ -59,6 +59,11 @@ class MapDesc(C.Structure):
                 ("pi", C.c_void_p), ("pj", C.c_void_p), ("max_steps", C.c_int), ("slots", C.c_int)]
 
 
+class RefineDesc(C.Structure):
+    _fields_ = [("radius", C.c_int), ("late_fraction", C.c_double), ("probe_stride", C.c_int),
+                ("max_passes", C.c_int)]
+
+
 class BatchDesc(C.Structure):
     _fields_ = [("q", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("solid", C.c_void_p), ("inlet_x", C.c_int),
                 ("outlet_x", C.c_int), ("rho0", C.c_double), ("energy_every", C.c_int),
@@ -123,8 +128,8 @@ _SIGS = {
     "erlbm_batch_run": (C.c_int, [C.POINTER(BatchDesc), C.c_int, C.POINTER(RunSpec), C.c_void_p, C.c_size_t,
                                   C.POINTER(BatchResult)]),
     "erlbm_map_run": (C.c_int, [C.POINTER(MapDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
-    "erlbm_map_run_refined": (C.c_int, [C.POINTER(MapDesc), C.c_int, C.c_double, C.c_void_p, C.c_void_p,
-                                        C.c_void_p, C.c_void_p]),
+    "erlbm_map_run_refined": (C.c_int, [C.POINTER(MapDesc), C.POINTER(RefineDesc), C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "erlbm_server_start": (C.c_int, [C.POINTER(ServerDesc), C.POINTER(C.c_void_p)]),
     "erlbm_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),
     "erlbm_server_poll": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(Result)]),

@@ -357,16 +357,18 @@ int erlbm_map_run(const erlbm_map_desc *d, int32_t *labels, int32_t *decided_ste
     return ERLBM_OK;
 }
 
-int erlbm_map_run_refined(const erlbm_map_desc *d, int radius, double late_fraction, int32_t *labels,
-                          int32_t *decided_step, double *margins, uint8_t *refined)
+int erlbm_map_run_refined(const erlbm_map_desc *d, const erlbm_refine_desc *r, int32_t *labels,
+                          int32_t *decided_step, double *margins, uint8_t *refined, int *n_passes)
 {
-    if (!d || !labels) return ERLBM_E_INVAL;
+    if (!d || !r || !labels) return ERLBM_E_INVAL;
     if (d->n_points != 0) {
         set_error("a refined map needs the whole n_i x n_j grid (n_points = 0)%s%s", "", "");
         return ERLBM_E_INVAL;
     }
-    if (radius < 0 || radius > 64 || !(late_fraction <= 1.0)) {
-        set_error("refine radius must lie in [0, 64] and late_fraction be at most 1%s%s", "", "");
+    if (r->radius < 0 || r->radius > 64 || !(r->late_fraction <= 1.0) || r->probe_stride < 0 ||
+        r->max_passes < 0) {
+        set_error("refine radius must lie in [0, 64], late_fraction be at most 1, probe_stride and "
+                  "max_passes be non-negative%s%s", "", "");
         return ERLBM_E_INVAL;
     }
     erlbm_batch_desc bd;
@@ -375,45 +377,76 @@ int erlbm_map_run_refined(const erlbm_map_desc *d, int radius, double late_fract
     int n_ops = 0;
     int rc = build_map_runs(d, &bd, &runs, &solid, &n_ops);
     if (rc) return rc;
-    const int ni = d->n_i, nj = d->n_j, n_runs = (int)runs.size();
-    // pass 1: every point in FP32-shifted
+    const int ni = d->n_i, nj = d->n_j, n_runs = (int)runs.size(), rad = r->radius;
+    const size_t plane_n = (size_t)ni * nj;
+    // pass 0: every point in FP32-shifted
     std::vector<erlbm_batch_result> res(n_runs);
     bd.precision = ERLBM_FP32_SHIFTED;
     rc = erlbm_batch_run(&bd, n_runs, runs.data(), nullptr, 0, res.data());
     if (rc) return rc;
-    // selection, per operator plane: a label differs inside the (2r+1)^2 window of map neighbours
-    // (the stability boundary), or an FP32 instability was found after late_fraction of the budget
-    std::vector<int> pick;
-    for (int o = 0; o < n_ops; o++) {
-        const erlbm_batch_result *plane = res.data() + (size_t)o * ni * nj;
+    std::vector<uint8_t> done(n_runs, 0), change(plane_n);
+    std::vector<int32_t> lab(plane_n), hi(plane_n), lo(plane_n);
+    // change[k] = 1 when the window of half-width rad around k (clipped to the grid) holds two labels;
+    // the max and min filters are taken along i and then along j
+    auto find_changes = [&](const erlbm_batch_result *plane) {
+        for (size_t k = 0; k < plane_n; k++) lab[k] = plane[k].label;
         for (int j = 0; j < nj; j++)
             for (int i = 0; i < ni; i++) {
-                const int k = j * ni + i, lab = plane[k].label;
-                bool sel = late_fraction > 0.0 && lab == 1 &&
-                           plane[k].decided_step > late_fraction * runs[(size_t)o * ni * nj + k].n_steps;
-                for (int jj = std::max(0, j - radius); !sel && jj <= std::min(nj - 1, j + radius); jj++)
-                    for (int ii = std::max(0, i - radius); ii <= std::min(ni - 1, i + radius); ii++)
-                        if (plane[jj * ni + ii].label != lab) {
-                            sel = true;
-                            break;
-                        }
-                if (sel) pick.push_back(o * ni * nj + k);
+                int32_t a = lab[(size_t)j * ni + i], b = a;
+                for (int ii = std::max(0, i - rad); ii <= std::min(ni - 1, i + rad); ii++) {
+                    a = std::max(a, lab[(size_t)j * ni + ii]);
+                    b = std::min(b, lab[(size_t)j * ni + ii]);
+                }
+                hi[(size_t)j * ni + i] = a;
+                lo[(size_t)j * ni + i] = b;
             }
-    }
-    // pass 2: the selected runs again in FP64, whose results are the reference's
-    if (!pick.empty()) {
+        for (int j = 0; j < nj; j++)
+            for (int i = 0; i < ni; i++) {
+                int32_t a = hi[(size_t)j * ni + i], b = lo[(size_t)j * ni + i];
+                for (int jj = std::max(0, j - rad); jj <= std::min(nj - 1, j + rad); jj++) {
+                    a = std::max(a, hi[(size_t)jj * ni + i]);
+                    b = std::min(b, lo[(size_t)jj * ni + i]);
+                }
+                change[(size_t)j * ni + i] = a != b;
+            }
+    };
+    const int s = r->probe_stride;
+    int passes = 0;
+    std::vector<int> pick;
+    for (;;) {
+        pick.clear();
+        for (int o = 0; o < n_ops; o++) {
+            const size_t base = (size_t)o * plane_n;
+            find_changes(res.data() + base);
+            for (int j = 0; j < nj; j++)
+                for (int i = 0; i < ni; i++) {
+                    const size_t k = (size_t)j * ni + i;
+                    if (done[base + k]) continue;
+                    bool sel = change[k] != 0;
+                    if (passes == 0) {
+                        sel = sel || (s > 0 && i % s == s / 2 && j % s == s / 2) ||
+                              (r->late_fraction > 0.0 && res[base + k].label == 1 &&
+                               res[base + k].decided_step > r->late_fraction * runs[base + k].n_steps);
+                    }
+                    if (sel) pick.push_back((int)(base + k));
+                }
+        }
+        if (pick.empty() || (r->max_passes > 0 && passes == r->max_passes)) break;
+        // the selected runs again in FP64, whose results are the reference's
         std::vector<erlbm_run_spec> sub(pick.size());
         for (size_t m = 0; m < pick.size(); m++) sub[m] = runs[pick[m]];
         std::vector<erlbm_batch_result> r64(pick.size());
         bd.precision = ERLBM_FP64;
         rc = erlbm_batch_run(&bd, (int)sub.size(), sub.data(), nullptr, 0, r64.data());
         if (rc) return rc;
-        for (size_t m = 0; m < pick.size(); m++) res[pick[m]] = r64[m];
+        for (size_t m = 0; m < pick.size(); m++) {
+            res[pick[m]] = r64[m];
+            done[pick[m]] = 1;
+        }
+        passes++;
     }
-    if (refined) {
-        memset(refined, 0, (size_t)n_runs);
-        for (int k : pick) refined[k] = 1;
-    }
+    if (refined) memcpy(refined, done.data(), (size_t)n_runs);
+    if (n_passes) *n_passes = passes;
     for (int k = 0; k < n_runs; k++) {
         labels[k] = res[k].label;
         if (decided_step) decided_step[k] = res[k].decided_step;

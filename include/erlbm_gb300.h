@@ -266,16 +266,29 @@ typedef struct erlbm_map_desc {
 /* labels (and optionally decided steps and margins) of n_points (x 2 when op = 0) runs */
 int erlbm_map_run(const erlbm_map_desc *d, int32_t *labels, int32_t *decided_step, double *margins);
 
+/* Which points of an FP32-screened map are run again in FP64 (erlbm_map_run_refined). */
+typedef struct erlbm_refine_desc {
+    int radius;            /* half-width in map steps (i and j) of the window searched for a label change */
+    double late_fraction;  /* FP32 runs that turned unstable after this fraction of their budget; <= 0: off */
+    int probe_stride;      /* FP64 probes at i, j = stride/2 + m*stride (finds unstable islands the FP32
+                              map misses entirely); 0: none */
+    int max_passes;        /* FP64 passes; 0: until no label change is left with an FP32 point near it */
+} erlbm_refine_desc;
+
 /* A stability map screened in FP32-shifted and refined in FP64.  No counterpart in the reference,
  * whose maps (main_stability-map_*.cpp) run every point in FP64.  Every point runs first in
- * ERLBM_FP32_SHIFTED (d->precision is ignored); a point is then run again in ERLBM_FP64, whose
- * results replace the FP32 ones and equal the reference's, when its FP32 label differs from any label
- * within `radius` map steps in i and j (same operator: the stability boundary), or when its FP32 run
- * turned unstable after `late_fraction` of its step budget (late_fraction <= 0 turns that rule off).
+ * ERLBM_FP32_SHIFTED (d->precision is ignored).  Points are then run again in ERLBM_FP64, whose results
+ * replace the FP32 ones and equal the reference's, in passes:
+ *   pass 1: points within r->radius of a label change of the FP32 map (the stability boundary, same
+ *           operator), FP32 runs that turned unstable late, and the probe points;
+ *   pass n: the FP32 points within r->radius of a label change of the map as it stands (FP64 labels where
+ *           refined), so that the refinement follows the FP64 boundary where it lies away from the FP32
+ *           one, and spreads over an island that a probe found.
  * The whole grid only (d->n_points = 0).  refined (optional, one byte per result) is set to 1 for the
- * results that came from FP64.  Arrays are laid out as in erlbm_map_run. */
-int erlbm_map_run_refined(const erlbm_map_desc *d, int radius, double late_fraction, int32_t *labels,
-                          int32_t *decided_step, double *margins, uint8_t *refined);
+ * results that came from FP64; n_passes (optional) receives the number of FP64 passes.  Arrays are
+ * laid out as in erlbm_map_run. */
+int erlbm_map_run_refined(const erlbm_map_desc *d, const erlbm_refine_desc *r, int32_t *labels,
+                          int32_t *decided_step, double *margins, uint8_t *refined, int *n_passes);
 
 /* read_geo (SimBoltz_Functions/LBM_functions.cpp:282-353): the solid mask (1 = solid, the layout of
  * erlbm_desc.solid) of a legacy ASCII VTK geometry file, nonzero values fluid, with pts_in / pts_out

@@ -46,7 +46,7 @@ def test_argument_checks_before_any_device_work():
     with pytest.raises(ValueError):
         m.operator_from_name("trt")
     assert [m.operator_from_name(n) for n in ("bgk", "mrt", "reg", "erlbm")] == [1, 2, 3, 4]
-    for kw in (dict(radius=-1), dict(late_fraction=1.5)):
+    for kw in (dict(radius=-1), dict(late_fraction=1.5), dict(probe_stride=-1), dict(max_passes=-1)):
         with pytest.raises(m.ErlbmError) as ei:
             m.map_run_refined(m.MAP_OBSTACLE, n_i=4, n_j=4, **kw)
         assert ei.value.code == -1

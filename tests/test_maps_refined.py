@@ -1,9 +1,10 @@
-"""FP32-screened stability maps with FP64 refinement of the boundary points (erlbm_map_run_refined).
+"""FP32-screened stability maps with FP64 refinement that tracks the FP64 boundary (erlbm_map_run_refined).
 
 The refined map must hold, at every refined point, exactly the FP64 map's result (the reference's
 labels, decided steps and margins), at every other point exactly the FP32-shifted map's result, and
-its selection must be the documented rule applied to the FP32 labels.  Small grids with capped run
-budgets keep each map to seconds.
+its selection must be the documented rule: the FP32 boundary, late runs and probes first, then the
+FP32 points near a label change of the map as refined so far, pass after pass.  Small grids with
+capped run budgets keep each map to seconds.
 """
 import numpy as np
 import pytest
@@ -16,19 +17,34 @@ def E():
     return m
 
 
-def selection(lab32, dec32, budgets, n_i, n_j, radius, late):
-    """The refinement rule restated in numpy on one operator plane."""
-    L = lab32.reshape(n_j, n_i)
+def changes(lab, n_i, n_j, radius):
+    """1 where the window of half-width radius around a point (clipped to the grid) holds two labels."""
+    L = lab.reshape(n_j, n_i)
     P = np.pad(L, radius, mode="edge")
     hi, lo = L.copy(), L.copy()
     for dj in range(-radius, radius + 1):
         for di in range(-radius, radius + 1):
             S = P[radius + dj:radius + dj + n_j, radius + di:radius + di + n_i]
             hi, lo = np.maximum(hi, S), np.minimum(lo, S)
-    sel = (hi != lo).reshape(-1)
+    return (hi != lo).reshape(-1)
+
+
+def selection(lab32, dec32, lab64, budgets, n_i, n_j, radius, late, stride, max_passes=0):
+    """The refinement rule restated in numpy on one operator plane, the FP64 labels taken from the
+    whole FP64 map: returns (refined mask, FP64 passes)."""
+    sel = changes(lab32, n_i, n_j, radius)
     if late > 0:
         sel |= (lab32 == 1) & (dec32 > late * budgets)
-    return sel
+    if stride:
+        J, I = np.divmod(np.arange(n_i * n_j), n_i)
+        sel |= (I % stride == stride // 2) & (J % stride == stride // 2)
+    done = np.zeros(n_i * n_j, bool)
+    passes = 0
+    while sel.any() and not (max_passes and passes == max_passes):
+        done |= sel
+        passes += 1
+        sel = changes(np.where(done, lab64, lab32), n_i, n_j, radius) & ~done
+    return done, passes
 
 
 def budgets(kind, n_i, n_j, op, cap):
@@ -50,9 +66,9 @@ def budgets(kind, n_i, n_j, op, cap):
 def test_refined_map_takes_fp64_results_where_it_refines(kind, n, cap):
     m = E()
     op = 0 if kind == m.MAP_TAYLOR_GREEN else m.OP_EXTREG
-    radius, late = 1, 0.3
-    lab, dec, mg, ref = m.map_run_refined(kind, op=op, n_i=n, n_j=n, max_steps=cap, radius=radius,
-                                          late_fraction=late)
+    radius, late, stride = 1, 0.3, 8
+    lab, dec, mg, ref, passes = m.map_run_refined(kind, op=op, n_i=n, n_j=n, max_steps=cap, radius=radius,
+                                                  late_fraction=late, probe_stride=stride, return_passes=True)
     l64, d64, m64 = m.map_run(kind, None, precision=m.FP64, op=op, n_i=n, n_j=n, max_steps=cap)
     l32, d32, m32 = m.map_run(kind, None, precision=m.FP32_SHIFTED, op=op, n_i=n, n_j=n, max_steps=cap)
     assert ref.any()
@@ -64,9 +80,31 @@ def test_refined_map_takes_fp64_results_where_it_refines(kind, n, cap):
     np.testing.assert_array_equal(mg[~ref], m32[~ref])
     ops = [m.OP_REG, m.OP_EXTREG] if op == 0 else [op]
     planes = n * n
+    want_passes = 0
     for o, opk in enumerate(ops):
         sl = slice(o * planes, (o + 1) * planes)
-        want = selection(l32[sl], d32[sl], budgets(kind, n, n, opk, cap), n, n, radius, late)
+        want, p = selection(l32[sl], d32[sl], l64[sl], budgets(kind, n, n, opk, cap), n, n, radius, late, stride)
         np.testing.assert_array_equal(ref[sl], want)
+        want_passes = max(want_passes, p)
+    assert passes == want_passes
+    # every label change of the refined map has only FP64 results within the radius
+    for o in range(len(ops)):
+        sl = slice(o * planes, (o + 1) * planes)
+        assert not (changes(lab[sl], n, n, radius) & ~ref[sl]).any()
     assert np.mean(lab == l64) >= np.mean(l32 == l64)
 
+
+def test_one_pass_keeps_the_first_selection():
+    """max_passes = 1 runs only the first FP64 pass: the FP32 boundary, late runs and probes."""
+    m = E()
+    n, cap, radius, late, stride = 20, 3000, 1, 0.3, 8
+    lab, dec, mg, ref, passes = m.map_run_refined(m.MAP_TAYLOR_GREEN, op=m.OP_EXTREG, n_i=n, n_j=n, max_steps=cap,
+                                                  radius=radius, late_fraction=late, probe_stride=stride,
+                                                  max_passes=1, return_passes=True)
+    l64, _, _ = m.map_run(m.MAP_TAYLOR_GREEN, None, precision=m.FP64, op=m.OP_EXTREG, n_i=n, n_j=n, max_steps=cap)
+    l32, d32, _ = m.map_run(m.MAP_TAYLOR_GREEN, None, precision=m.FP32_SHIFTED, op=m.OP_EXTREG, n_i=n, n_j=n,
+                            max_steps=cap)
+    want, p = selection(l32, d32, l64, budgets(m.MAP_TAYLOR_GREEN, n, n, m.OP_EXTREG, cap), n, n, radius, late,
+                        stride, max_passes=1)
+    assert passes == p == 1
+    np.testing.assert_array_equal(ref, want)
