@@ -349,7 +349,7 @@ def run_ours(args):
                      "traffic": ncu_traffic(L, "fp32_x2" if two else args.precision) if args.op == "erlbm" else None,
                      "algorithmic_bytes_per_launch": algo_bytes, "launch_us": launch_ms * 1e3,
                      "lattice_updates_per_launch": L * L * (2 if two else 1),
-                     "kernel": (f"k_periodic_d2q9_x2<{op}>" if two else f"k_periodic_d2q9<{op}>")
+                     "kernel": (f"k_periodic_d2q9_x2s<{op}>" if two else f"k_periodic_d2q9<{op}>")
                      if args.precision == "fp32" else f"k_step<PrecExact64,9,{op}>"},
         "e2e": e2e,
         "gpu_launches": launches,

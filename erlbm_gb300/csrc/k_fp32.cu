@@ -132,179 +132,198 @@ int periodic_shape(int block, bool st, const Geo &g, const shifted::Coef &k, con
     return 0;
 }
 
-// Two steps per launch (temporal blocking).  A CTA owns a strip of W columns and a chunk of HC rows
-// and walks down it with a rolling window: four rows of the input populations P (W + 4 columns: the
-// two-step pull reaches two columns out) and four rows of the intermediate step P' (W + 2 columns),
-// both in shared memory.  Per iteration two output rows j, j + 1 are made: rows j + 2, j + 3 of P
-// enter the window (their global loads were issued one iteration ahead), rows j + 1, j + 2 of P' are
-// collided from P, and rows j, j + 1 of the output from P'; only the output goes back to HBM.  The
-// two rows of each stage are collided together as the two halves of float2 lanes (packed FP32x2
-// instructions), with the same bits as the one-step kernel.  Each node is read once and written once
-// per two steps, plus a margin for the window's start (four rows per chunk) and the strip edges.
-template <int W>
-struct X2 {
-    static constexpr int T = W + 32;  // threads: W + 4 loaders, W + 2 for P', W for the output
-    static constexpr int WA = W + 4;
-    static constexpr int WB = W + 2;
-    static constexpr size_t SMEM = (size_t)4 * 9 * (WA + WB) * sizeof(float);
-};
+// Two steps per launch with warp strips: each warp owns XS_W = 30 output columns and a chunk of rows
+// and walks down it on its own (no shared memory, no block barrier).  Lane l holds column
+// xs - 1 + l.  A population that comes from the next column over reaches a lane through a warp
+// shuffle; lanes 0 and 31, whose neighbour column lies outside the warp, load those three populations
+// themselves.  All 32 lanes collide the intermediate step P' (columns xs - 1 .. xs + 30); lanes 1 .. 30
+// collide and store the output.  Per iteration two output rows j, j + 1 are made from P' rows j - 1 ..
+// j + 2, and P' rows j + 1, j + 2 from P rows j .. j + 3, of which rows j + 2, j + 3 were loaded one
+// iteration ahead.  Every value is carried in registers already moved to the lane that pulls it, and
+// only the populations a later row still needs are kept: the cy = +1 group of the older row and the
+// cy = 0 and cy = +1 groups of the newer one.  The two rows of each stage are collided together in
+// packed FP32x2 lanes with the same bits as the one-step kernel.
+constexpr int XS_W = 30;
+constexpr unsigned XS_FULL = 0xffffffffu;
 
-__device__ __forceinline__ int slot4(int r) { return (r + 8) & 3; }  // rows from y0 - 8 up
-
-
-template <int OP, int W>
-__global__ void __launch_bounds__(X2<W>::T) k_periodic_d2q9_x2(const float *__restrict__ src, float *__restrict__ dst,
-                                                               int nx, int ny, long long plane, int hc,
-                                                               shifted::Coef k)
+template <int OP>
+__global__ void __launch_bounds__(128) k_periodic_d2q9_x2s(const float *__restrict__ src, float *__restrict__ dst,
+                                                          int nx, int ny, long long plane, int hc, int strips,
+                                                          int n_warps, shifted::Coef k)
 {
-    constexpr int WA = X2<W>::WA, WB = X2<W>::WB;
-    extern __shared__ float x2_smem[];
-    float *A = x2_smem;              // [4][9][WA]
-    float *B = x2_smem + 4 * 9 * WA;  // [4][9][WB]
-    const int t = threadIdx.x;
-    const int strips = nx / W;
-    const int x0 = (blockIdx.x % strips) * W;
-    const int y0 = (blockIdx.x / strips) * hc;
+    const int lane = threadIdx.x & 31;
+    const int wid = (int)blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
+    if (wid >= n_warps) return;  // the whole warp leaves together
+    const int xs = (wid % strips) * XS_W;
+    const int y0 = (wid / strips) * hc;
     const int y1 = min(y0 + hc, ny);
-    int cw = x0 - 2 + t;  // this thread's column of the P window (periodic in x)
-    cw = cw < 0 ? cw + nx : (cw >= nx ? cw - nx : cw);
+    int c = xs - 1 + lane;  // in [-1, nx + 29]
+    const bool store = lane >= 1 && lane <= XS_W && c < nx;
+    c = c < 0 ? c + nx : (c >= nx ? c - nx : c);
+    // halo: lane 0 pulls populations 1, 5, 7 (cx = +1) from column xs - 2, lane 31 pulls 2, 6, 8
+    // (cx = -1) from column xs + 31
+    const bool halo = lane == 0 || lane == 31;
+    int hcol = lane == 0 ? xs - 2 : xs + 31;
+    hcol = hcol < 0 ? hcol + nx : (hcol >= nx ? hcol - nx : hcol);
+    const long long h0 = hcol + (lane == 0 ? 1 : 2) * plane, h1 = hcol + (lane == 0 ? 5 : 6) * plane,
+                    h2 = hcol + (lane == 0 ? 7 : 8) * plane;
 
-    auto load_row = [&](int r, float v[9]) {
-        const int rr = ((r % ny) + ny) % ny;
-        const float *p = src + (long long)rr * nx + cw;
+    auto load = [&](int r, float v[9], float h[3]) {
+        r = r < 0 ? r + ny : (r >= ny ? r - ny : r);
+        const float *p = src + (long long)r * nx;
 #pragma unroll
-        for (int i = 0; i < 9; i++) v[i] = __ldg(p + i * plane);
-    };
-    auto put_row = [&](int r, const float v[9]) {
-        float *a = A + slot4(r) * 9 * WA + t;
-#pragma unroll
-        for (int i = 0; i < 9; i++) a[i * WA] = v[i];
-    };
-    // P' rows r and r + 1 at column x0 - 1 + t, from the P window
-    auto mid2 = [&](int r) {
-        if (t >= WB) return;
-        float2 g[9];
-#pragma unroll
-        for (int i = 0; i < 9; i++) {
-            const int c = (t + 1) - Lat<9>::cx(i);
-            g[i].x = A[(slot4(r - Lat<9>::cy(i)) * 9 + i) * WA + c];
-            g[i].y = A[(slot4(r + 1 - Lat<9>::cy(i)) * 9 + i) * WA + c];
-        }
-        shifted::collide9x2<OP>(g, k);
-        float *b0 = B + slot4(r) * 9 * WB + t, *b1 = B + slot4(r + 1) * 9 * WB + t;
-#pragma unroll
-        for (int i = 0; i < 9; i++) {
-            b0[i * WB] = g[i].x;
-            b1[i * WB] = g[i].y;
+        for (int i = 0; i < 9; i++) v[i] = __ldg(p + c + i * plane);
+        if (halo) {
+            h[0] = __ldg(p + h0);
+            h[1] = __ldg(p + h1);
+            h[2] = __ldg(p + h2);
         }
     };
-    // output rows r and r + 1 at column x0 + t, from the P' window
-    auto out2 = [&](int r) {
-        if (t >= W) return;
-        float2 g[9];
-#pragma unroll
-        for (int i = 0; i < 9; i++) {
-            const int c = (t + 1) - Lat<9>::cx(i);
-            g[i].x = B[(slot4(r - Lat<9>::cy(i)) * 9 + i) * WB + c];
-            g[i].y = B[(slot4(r + 1 - Lat<9>::cy(i)) * 9 + i) * WB + c];
-        }
-        shifted::collide9x2<OP>(g, k);
-        float *d0 = dst + (long long)r * nx + x0 + t, *d1 = d0 + nx;
-#pragma unroll
-        for (int i = 0; i < 9; i++) {
-            d0[i * plane] = g[i].x;
-            d1[i * plane] = g[i].y;
-        }
+    // a[i] = P(column - cx_i) of the loaded row
+    auto align = [&](const float v[9], const float h[3], float a[9]) {
+        a[0] = v[0];
+        a[3] = v[3];
+        a[4] = v[4];
+        float u;
+        u = __shfl_up_sync(XS_FULL, v[1], 1);
+        a[1] = lane == 0 ? h[0] : u;
+        u = __shfl_up_sync(XS_FULL, v[5], 1);
+        a[5] = lane == 0 ? h[1] : u;
+        u = __shfl_up_sync(XS_FULL, v[7], 1);
+        a[7] = lane == 0 ? h[2] : u;
+        u = __shfl_down_sync(XS_FULL, v[2], 1);
+        a[2] = lane == 31 ? h[0] : u;
+        u = __shfl_down_sync(XS_FULL, v[6], 1);
+        a[6] = lane == 31 ? h[1] : u;
+        u = __shfl_down_sync(XS_FULL, v[8], 1);
+        a[8] = lane == 31 ? h[2] : u;
+    };
+    // the same for both rows of a collided pair; lanes 0 and 31 get values no stored output uses
+    auto align2 = [&](float2 g[9]) {
+        g[1].x = __shfl_up_sync(XS_FULL, g[1].x, 1);
+        g[1].y = __shfl_up_sync(XS_FULL, g[1].y, 1);
+        g[5].x = __shfl_up_sync(XS_FULL, g[5].x, 1);
+        g[5].y = __shfl_up_sync(XS_FULL, g[5].y, 1);
+        g[7].x = __shfl_up_sync(XS_FULL, g[7].x, 1);
+        g[7].y = __shfl_up_sync(XS_FULL, g[7].y, 1);
+        g[2].x = __shfl_down_sync(XS_FULL, g[2].x, 1);
+        g[2].y = __shfl_down_sync(XS_FULL, g[2].y, 1);
+        g[6].x = __shfl_down_sync(XS_FULL, g[6].x, 1);
+        g[6].y = __shfl_down_sync(XS_FULL, g[6].y, 1);
+        g[8].x = __shfl_down_sync(XS_FULL, g[8].x, 1);
+        g[8].y = __shfl_down_sync(XS_FULL, g[8].y, 1);
+    };
+    // the pulled populations of rows m (x) and m + 1 (y) from the aligned rows m - 1 (o: cy = +1
+    // group), m (n: cy = 0 and +1 groups), m + 1 (all) and m + 2 (cy = -1 group)
+    auto gather = [](float2 g[9], const float o[9], const float n[9], const float p[9], const float q[9]) {
+        g[3] = make_float2(o[3], n[3]);
+        g[5] = make_float2(o[5], n[5]);
+        g[8] = make_float2(o[8], n[8]);
+        g[0] = make_float2(n[0], p[0]);
+        g[1] = make_float2(n[1], p[1]);
+        g[2] = make_float2(n[2], p[2]);
+        g[4] = make_float2(p[4], q[4]);
+        g[6] = make_float2(p[6], q[6]);
+        g[7] = make_float2(p[7], q[7]);
     };
 
-    const bool loader = t < WA;
-    float va[9], vb[9];
-    // prologue: P rows y0 - 2 .. y0 + 1 and P' rows y0 - 1, y0; va, vb hold P rows y0 + 2, y0 + 3
-    if (loader) {
-        load_row(y0 - 2, va);
-        put_row(y0 - 2, va);
-        load_row(y0 - 1, va);
-        put_row(y0 - 1, va);
-        load_row(y0, va);
-        put_row(y0, va);
-        load_row(y0 + 1, va);
-        put_row(y0 + 1, va);
+    float va[9], vb[9], ha[3] = {0.f, 0.f, 0.f}, hb[3] = {0.f, 0.f, 0.f};
+    float aA[9], aB[9], aC[9], aD[9];  // aligned P rows
+    float bA[9], bB[9];                // aligned P' rows j - 1 (cy = +1 group) and j (cy = 0, +1 groups)
+    float2 g[9];
+    // prologue: P rows y0 - 2 .. y0 + 1, P' rows y0 - 1, y0
+    load(y0 - 2, va, ha);
+    load(y0 - 1, vb, hb);
+    align(va, ha, aA);
+    align(vb, hb, aB);
+    load(y0, va, ha);
+    load(y0 + 1, vb, hb);
+    align(va, ha, aC);
+    align(vb, hb, aD);
+    load(y0 + 2, va, ha);
+    load(y0 + 3, vb, hb);
+    gather(g, aA, aB, aC, aD);
+    shifted::collide9x2<OP>(g, k);
+    align2(g);
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+        bA[i] = g[i].x;
+        bB[i] = g[i].y;
+        aA[i] = aC[i];
+        aB[i] = aD[i];
     }
-    __syncthreads();
-    mid2(y0 - 1);
-    if (loader) {
-        load_row(y0 + 2, va);
-        load_row(y0 + 3, vb);
-    }
-    __syncthreads();  // mid2 has read P rows y0 - 2, y0 - 1, whose slots rows y0 + 2, y0 + 3 take
     for (int j = y0; j < y1; j += 2) {
-        if (loader) {
-            put_row(j + 2, va);
-            put_row(j + 3, vb);
-            if (j + 2 < y1) {  // one iteration ahead
-                load_row(j + 4, va);
-                load_row(j + 5, vb);
+        align(va, ha, aC);  // P row j + 2
+        align(vb, hb, aD);  // P row j + 3
+        if (j + 2 < y1) {   // one iteration ahead
+            load(j + 4, va, ha);
+            load(j + 5, vb, hb);
+        }
+        gather(g, aA, aB, aC, aD);  // P' rows j + 1, j + 2
+        shifted::collide9x2<OP>(g, k);
+        align2(g);
+        float nA[9], nB[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            nA[i] = g[i].x;
+            nB[i] = g[i].y;
+        }
+        gather(g, bA, bB, nA, nB);  // output rows j, j + 1
+        shifted::collide9x2<OP>(g, k);
+        if (store) {
+            float *d0 = dst + (long long)j * nx + c, *d1 = d0 + nx;
+#pragma unroll
+            for (int i = 0; i < 9; i++) {
+                d0[i * plane] = g[i].x;
+                d1[i * plane] = g[i].y;
             }
         }
-        __syncthreads();
-        mid2(j + 1);
-        __syncthreads();
-        out2(j);
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            aA[i] = aC[i];
+            aB[i] = aD[i];
+            bA[i] = nA[i];
+            bB[i] = nB[i];
+        }
     }
 }
 
-
 }  // namespace
-
-// Chunk height of the two-step kernel: one wave of CTAs (resident CTAs per SM x SMs) over the
-// (nx / W) x ny lattice, so that no second, partial wave runs, and even (two rows per iteration).
-static int x2_chunk(int nx, int ny, int W, int resident_per_sm, int sms)
-{
-    const long long slots = (long long)(resident_per_sm > 0 ? resident_per_sm : 1) * (sms > 0 ? sms : 1);
-    const long long strips = nx / W;
-    long long hc = (ny * strips + slots - 1) / slots;
-    if (hc < 8) hc = 8;
-    hc += hc & 1;
-    if (hc > ny) hc = ny;
-    return (int)hc;
-}
 
 bool periodic_d2q9_x2_ok(const Geo &g)
 {
     return periodic_d2q9_fp32_ok(g) && g.ny >= 4 && g.ny % 2 == 0;  // nx % 128 == 0 from the one-step check
 }
 
-template <int OP, int W>
-static void go_x2w(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
+// Two-step launch: 128-thread CTAs of four independent warps, and rows per chunk such that one wave
+// of resident warps covers the ceil(nx / 30) x (ny / hc) warp strips (no second, partial wave).
+template <int OP>
+static void go_x2(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
 {
-    auto kern = k_periodic_d2q9_x2<OP, W>;
-    // shared-memory attribute, occupancy and SM count once per device and instantiation (settings
-    // are per device; concurrent first calls set the same values)
+    auto kern = k_periodic_d2q9_x2s<OP>;
     constexpr int MAXDEV = 64;
     static int occ[MAXDEV], sms[MAXDEV];
     int dev = 0;
     cudaGetDevice(&dev);
     const int d = dev >= 0 && dev < MAXDEV ? dev : 0;
     if (occ[d] <= 0) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)X2<W>::SMEM);
         int o = 0, n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, X2<W>::T, X2<W>::SMEM) != cudaSuccess || o < 1)
-            o = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, 128, 0) != cudaSuccess || o < 1) o = 1;
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         sms[d] = n > 0 ? n : 1;
         occ[d] = o;
     }
-    const int hc = x2_chunk(g.nx, g.ny, W, occ[d], sms[d]);
-    const unsigned nb = (unsigned)((g.nx / W) * ((g.ny + hc - 1) / hc));
-    kern<<<nb, X2<W>::T, X2<W>::SMEM, s>>>(src, dst, g.nx, g.ny, g.plane, hc, k);
-}
-
-template <int OP>
-static void go_x2(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
-{
-    // 128-column strips: 160-thread CTAs, five resident per SM.  On GB300 at L = 2048: 113.8 G LU/s,
-    // against 110.7 with 256-column strips (two 288-thread CTAs per SM) and 110.4 with 512
-    go_x2w<OP, 128>(g, k, src, dst, s);
+    const int strips = (g.nx + XS_W - 1) / XS_W;
+    const long long slots = (long long)occ[d] * 4 * sms[d];
+    long long chunks = slots / strips;
+    if (chunks < 1) chunks = 1;
+    long long hc = (g.ny + chunks - 1) / chunks;
+    if (hc < 8) hc = 8;
+    hc += hc & 1;
+    if (hc > g.ny) hc = g.ny;
+    const int n_warps = strips * (int)((g.ny + hc - 1) / hc);
+    const unsigned nb = (unsigned)((n_warps + 3) / 4);
+    kern<<<nb, 128, 0, s>>>(src, dst, g.nx, g.ny, g.plane, (int)hc, strips, n_warps, k);
 }
 
 // Two steps of the fused periodic D2Q9 FP32 update in one launch (periodic_d2q9_x2_ok(g) required).
