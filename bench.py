@@ -350,7 +350,13 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": algo_bytes, "launch_us": launch_ms * 1e3,
                      "lattice_updates_per_launch": L * L * (2 if two else 1),
                      "kernel": (f"k_periodic_d2q9_x2s<{op}>" if two else f"k_periodic_d2q9<{op}>")
-                     if args.precision == "fp32" else f"k_step<PrecExact64,9,{op}>"},
+                     if args.precision == "fp32" else f"k_step<PrecExact64,9,{op}>",
+                     # the update rate against the roofline of one step per launch, where every
+                     # update reads and writes each population once (2 Q sizeof(real) bytes): the
+                     # two-step kernel moves half of those bytes, so this fraction can exceed 1
+                     "one_step_equivalent": {"bytes_per_update": BYTES_PER_LU[args.precision],
+                                             "gbs": value * 1e6 * BYTES_PER_LU[args.precision] / 1e9,
+                                             "frac": value * 1e6 * BYTES_PER_LU[args.precision] / 1e9 / peak}},
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
