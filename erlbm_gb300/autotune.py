@@ -57,8 +57,9 @@ def _time_steps(lat, stream, n: int) -> float:
 
 
 PERIODIC_CANDIDATES = [(128, False), (256, False), (512, False), (128, True), (256, True), (512, True)]
-# two steps per launch (the odd remainder of a call uses the one-step shape given with it)
-TWO_STEP_CANDIDATES = [(128, False), (256, False)]
+# two steps per launch: one kernel shape (warp strips in 128-thread CTAs); the block size given with it
+# is the one-step shape used for the odd remainder of a call
+TWO_STEP_CANDIDATES = [(128, False)]
 
 
 def tune_periodic(L: int, steps: int = 200, force: bool = False) -> dict:
