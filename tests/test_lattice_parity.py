@@ -183,7 +183,7 @@ def test_run_energy_check_matches_oracle():
 @pytest.mark.parametrize("op", [1, 2, 3, 4])
 @pytest.mark.parametrize("L,steps", [(256, 17), (512, 40)])
 def test_two_step_kernel_equals_one_step(op, L, steps):
-    """Two steps per launch (the intermediate step kept in shared memory) give the one-step kernel's
+    """Two steps per launch (the intermediate step kept in registers) give the one-step kernel's
     populations bit for bit, for every operator and for odd step counts."""
     tau = 0.5 + 3 * (1 / 32) * L / 80000
     f0 = eg().init_double_shear(L)
@@ -196,6 +196,24 @@ def test_two_step_kernel_equals_one_step(op, L, steps):
             lat.step(3)
             outs.append((lat.get_populations(0), lat.get_populations(1)))
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("nx,ny", [(128, 4), (128, 6), (384, 10), (128, 130), (640, 258)])
+def test_two_step_kernel_equals_one_step_on_uneven_strips(nx, ny):
+    """The two-step kernel's warp strips are 30 columns wide, so nx = 128, 384 and 640 end in a
+    partial strip; its chunks of rows are clamped at small ny.  Random near-equilibrium populations,
+    every wrap of the periodic box exercised: the one-step kernel's bits after an odd step count."""
+    rng = np.random.default_rng(nx * 1000 + ny)
+    w = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+    f0 = (w[None, :] * (1.0 + 0.05 * rng.standard_normal((nx * ny, 9)))).ravel()
+    outs = []
+    for two in (False, True):
+        with eg().Lattice(9, nx, ny, 1, None, 0.53, 0.65, eg().OP_EXTREG, eg().FP32_SHIFTED) as lat:
+            lat.set_launch(128, False, two)
+            lat.set_populations(f0)
+            lat.step(9)
+            outs.append(lat.get_populations(0))
+    assert np.array_equal(outs[0], outs[1])
 
 
 def test_fused_kernel_launch_shapes_identical_and_tuned(tmp_path, monkeypatch):
