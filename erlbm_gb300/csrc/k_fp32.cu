@@ -6,7 +6,11 @@
 // and written with 128-bit accesses.  The pull from x - c_x needs one neighbour column per
 // lane; it comes from the adjacent lane by a warp shuffle, and only the two warp-edge lanes
 // issue an extra 4-byte load (an L2 hit: the neighbouring warp reads that line too).
-// Algorithmic traffic is 2 * 9 * 4 = 72 bytes per lattice update.
+// Algorithmic traffic is 2 * 9 * 4 = 72 bytes per lattice update.  The two-step kernel
+// (k_periodic_d2q9_x2s) advances every node by two steps per launch in independent warp strips,
+// 36 bytes per lattice update.
+#include <atomic>
+
 #include "lattice_kernels.cuh"
 
 namespace erlbm {
@@ -301,20 +305,23 @@ template <int OP>
 static void go_x2(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
 {
     auto kern = k_periodic_d2q9_x2s<OP>;
+    // resident warps per device, found once per device and instantiation (handles on several host
+    // threads may launch concurrently; they store the same value)
     constexpr int MAXDEV = 64;
-    static int occ[MAXDEV], sms[MAXDEV];
+    static std::atomic<int> warps_cache[MAXDEV];
     int dev = 0;
     cudaGetDevice(&dev);
     const int d = dev >= 0 && dev < MAXDEV ? dev : 0;
-    if (occ[d] <= 0) {
+    int resident = warps_cache[d].load(std::memory_order_relaxed);
+    if (resident <= 0) {
         int o = 0, n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, 128, 0) != cudaSuccess || o < 1) o = 1;
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        sms[d] = n > 0 ? n : 1;
-        occ[d] = o;
+        resident = o * 4 * (n > 0 ? n : 1);
+        warps_cache[d].store(resident, std::memory_order_relaxed);
     }
     const int strips = (g.nx + XS_W - 1) / XS_W;
-    const long long slots = (long long)occ[d] * 4 * sms[d];
+    const long long slots = resident;
     long long chunks = slots / strips;
     if (chunks < 1) chunks = 1;
     long long hc = (g.ny + chunks - 1) / chunks;
