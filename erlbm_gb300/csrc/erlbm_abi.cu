@@ -85,6 +85,11 @@ struct erlbm_handle {
     std::vector<double> h_profile;      // parabolic inlet velocity per (y, z) of the inlet plane
     double *d_profile = nullptr;
     double profile_key[3] = {-1, 0, 0}; // inlet_x, u_in, L of the uploaded profile
+    // CUDA graphs of GRAPH_STEPS plain fused periodic steps, one per buffer parity, for the launch
+    // shape and parameters in graph_key (rebuilt when erlbm_set_launch or erlbm_set_params changes them)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    long long graph_key = -1;
+    cudaStream_t capture_stream = nullptr;
     size_t elem() const { return prec == ERLBM_FP64 ? sizeof(double) : sizeof(float); }
 };
 
@@ -113,6 +118,15 @@ int check_op(int op, int q)
     return ERLBM_E_INVAL;
 }
 
+void drop_graphs(erlbm_handle *h)
+{
+    for (cudaGraphExec_t &x : h->graph) {
+        if (x) cudaGraphExecDestroy(x);
+        x = nullptr;
+    }
+    h->graph_key = -1;
+}
+
 void free_handle(erlbm_handle *h)
 {
     if (!h) return;
@@ -125,6 +139,8 @@ void free_handle(erlbm_handle *h)
     cudaFree(h->d_scr);
     cudaFree(h->d_out);
     cudaFree(h->d_status);
+    drop_graphs(h);
+    if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
 }
@@ -311,6 +327,52 @@ int enqueue_step(erlbm_handle *h, const BCp &bc, int check_density, double densi
     return ERLBM_OK;
 }
 
+// GRAPH_STEPS plain periodic steps of the fused FP32 D2Q9 kernels (two per launch when `two`) as one
+// CUDA graph launch: the launches of a block are captured once per buffer parity and replayed, so a
+// small lattice is not bound by the host's launch rate.  An even number of launches leaves the
+// buffer parity unchanged.
+constexpr int GRAPH_STEPS = 64;
+
+int graph_steps(erlbm_handle *h, bool two)
+{
+    const long long key = (two ? 1 : 0) | ((long long)h->shape << 1);
+    if (h->graph_key != key) {
+        drop_graphs(h);
+        h->graph_key = key;
+    }
+    cudaGraphExec_t &x = h->graph[h->cur];
+    if (!x) {
+        if (!h->capture_stream) CK(cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking));
+        CK(cudaStreamBeginCapture(h->capture_stream, cudaStreamCaptureModeRelaxed));
+        int c = h->cur, lrc = 0;
+        for (int k = 0; k < (two ? GRAPH_STEPS / 2 : GRAPH_STEPS) && lrc == 0; k++) {
+            const float *src = (const float *)h->d_buf[c];
+            float *dst = (float *)h->d_buf[c ^ 1];
+            lrc = two ? launch_periodic_d2q9_fp32_x2(h->op, h->g, h->R, src, dst, h->capture_stream)
+                      : launch_periodic_d2q9_fp32(h->op, h->g, h->R, src, dst, h->capture_stream, h->shape);
+            c ^= 1;
+        }
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->capture_stream, &graph);
+        if (lrc != 0 || e != cudaSuccess || !graph) {
+            if (graph) cudaGraphDestroy(graph);
+            const cudaError_t le = cudaGetLastError();
+            return cuda_fail(e != cudaSuccess ? e : (le != cudaSuccess ? le : cudaErrorInvalidValue),
+                             "capture of the periodic step graph");
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&x, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            x = nullptr;
+            return cuda_fail(ie, "cudaGraphInstantiate");
+        }
+    }
+    CK(cudaGraphLaunch(x, h->stream));
+    h->steps_done += GRAPH_STEPS;
+    h->kind = 1;
+    return ERLBM_OK;
+}
+
 int energy_now(erlbm_handle *h, int stage, double *E)
 {
     const void *buf;
@@ -477,6 +539,7 @@ int erlbm_set_params(erlbm_handle *h, double tau, double tau_nh, int op)
     h->tau_nh = tau_nh;
     h->op = op;
     h->R = make_relax(tau, tau_nh, op);
+    drop_graphs(h);  // a graph in flight finishes with the parameters it was captured with
     return ERLBM_OK;
 }
 
@@ -532,9 +595,15 @@ int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc)
     if (n_steps < 0) return ERLBM_E_INVAL;
     BCp b;
     if ((rc = validate_bc(h, bc, &b))) return rc;
-    const bool fused2 = h->two_step && h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && b.inlet_x < 0 &&
-                        b.outlet_x < 0 && b.open_y < 0 && periodic_d2q9_x2_ok(h->g);
+    const bool plain = h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && b.inlet_x < 0 && b.outlet_x < 0 &&
+                       b.open_y < 0 && periodic_d2q9_fp32_ok(h->g);
+    const bool fused2 = plain && h->two_step && periodic_d2q9_x2_ok(h->g);
     for (int s = 0; s < n_steps;) {
+        if (plain && h->kind == 1 && n_steps - s >= GRAPH_STEPS) {
+            if ((rc = graph_steps(h, fused2))) return rc;
+            s += GRAPH_STEPS;
+            continue;
+        }
         if (fused2 && h->kind == 1 && n_steps - s >= 2) {
             // two plain periodic steps in one launch: step s and s + 1
             CKL(launch_periodic_d2q9_fp32_x2(h->op, h->g, h->R, (const float *)h->d_buf[h->cur],
@@ -562,7 +631,7 @@ int erlbm_set_launch(erlbm_handle *h, int block_threads, int flags)
     if (flags & ~(ERLBM_LAUNCH_STREAMING_STORES | ERLBM_LAUNCH_TWO_STEP)) return ERLBM_E_INVAL;
     h->shape = block_threads | ((flags & ERLBM_LAUNCH_STREAMING_STORES) ? 0x1000 : 0);
     h->two_step = (flags & ERLBM_LAUNCH_TWO_STEP) != 0;
-    return ERLBM_OK;
+    return ERLBM_OK;  // graphs of another shape are rebuilt on their next use (graph_key)
 }
 
 int erlbm_set_stream(erlbm_handle *h, void *stream)

@@ -198,6 +198,33 @@ def test_two_step_kernel_equals_one_step(op, L, steps):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
+@pytest.mark.parametrize("two", [False, True])
+def test_graph_replay_equals_single_launches(two):
+    """Blocks of 64 plain periodic steps run as a replayed CUDA graph (captured once per buffer
+    parity); the populations equal those of the same steps launched one call at a time, also after a
+    parameter change (which drops the captured graphs) and a launch-shape change."""
+    L = 256
+    f0 = eg().init_double_shear(L)
+    tau1, tau2 = 0.5 + 3 * (1 / 32) * L / 80000, 0.56
+    outs = []
+    for blocks in (True, False):
+        with eg().Lattice(9, L, L, 1, None, tau1, 0.65, eg().OP_EXTREG, eg().FP32_SHIFTED) as lat:
+            lat.set_launch(256, False, two)
+            lat.set_populations(f0)
+            run = (lambda n: lat.step(n)) if blocks else (lambda n: [lat.step(1) for _ in range(n)])
+            run(1)
+            run(131)          # two graph blocks of 64 and three single steps
+            a = lat.get_populations(1)
+            lat.set_params(tau2, 0.65, eg().OP_REG)
+            run(70)
+            b = lat.get_populations(1)
+            lat.set_launch(128, False, not two)
+            run(128)
+            outs.append((a, b, lat.get_populations(1), lat.get_populations(0)))
+    for x, y in zip(outs[0], outs[1]):
+        assert np.array_equal(x, y)
+
+
 @pytest.mark.parametrize("nx,ny", [(128, 4), (128, 6), (384, 10), (128, 130), (640, 258)])
 def test_two_step_kernel_equals_one_step_on_uneven_strips(nx, ny):
     """The two-step kernel's warp strips are 30 columns wide, so nx = 128, 384 and 640 end in a
