@@ -162,6 +162,14 @@ struct Job {
     double t_admit = 0;
 };
 
+// A stream-lane request waiting for admission, with its submission time and estimated GPU time.
+struct Pending {
+    int64_t ticket = 0;
+    erlbm_request req{};
+    double t_submit = 0;
+    double est = 0;  // seconds
+};
+
 }  // namespace
 
 struct erlbm_server {
@@ -177,7 +185,7 @@ struct erlbm_server {
     std::vector<StreamSlot *> all_streams;
     std::vector<Job *> active;
     std::deque<std::pair<int64_t, erlbm_request>> pending_a[2];  // slot-lane requests waiting for ring space
-    std::deque<std::pair<int64_t, erlbm_request>> pending_b;
+    std::vector<Pending> pending_b;  // stream-lane requests waiting for memory and a stream
     // submission and results (shared with user threads)
     std::mutex mu;
     std::condition_variable cv_done, cv_work;
@@ -632,12 +640,76 @@ bool job_progress(erlbm_server *s, Job *j, int chunk)
     return false;
 }
 
+// Estimated GPU seconds of a stream-lane run: lattice updates at a nominal rate (FP64 ~30x the cost
+// of FP32 on GB300's FP64 pipe, D3Q19 ~2x D2Q9), with a floor per step for small lattices, whose
+// chunks of steps are bound by launch latency.  It only orders admission.
+double estimate_seconds(const erlbm_request &q)
+{
+    double nodes = 0;
+    int qv = 19;
+    switch (q.kind) {
+    case ERLBM_REQ_TG2D:
+        nodes = (double)q.L * q.L;
+        qv = 9;
+        break;
+    case ERLBM_REQ_TG3D:
+        nodes = (double)q.L * q.L * q.L;
+        break;
+    case ERLBM_REQ_OBSTACLE: {
+        int nx = 0, ny = 0;
+        erlbm_obstacle_geometry(std::max(1, q.sx), std::max(1, q.sy), &nx, &ny, nullptr);
+        nodes = (double)nx * ny;
+        break;
+    }
+    default:
+        nodes = (double)q.L * q.L;
+    }
+    const double cost = (q.precision == ERLBM_FP64 ? 30.0 : 1.0) * (qv == 19 ? 2.0 : 1.0);
+    return std::max(1, q.n_steps) * std::max(nodes * cost / 4e10, 4e-6);
+}
+
+// Admission order of the stream lane: shortest estimated work first, with aging (the key of a
+// request falls as it waits, so a large run is not passed over for ever).  The first request in
+// that order that does not fit stops the pass, so memory frees up for it instead of for requests
+// behind it.
+constexpr double AGING_SECONDS = 1.0;
+
+void admit_stream_lane(erlbm_server *s)
+{
+    if (s->pending_b.empty()) return;
+    const double now = s->now();
+    std::vector<size_t> order(s->pending_b.size());
+    for (size_t k = 0; k < order.size(); k++) order[k] = k;
+    auto key = [&](size_t k) {
+        const Pending &p = s->pending_b[k];
+        return p.est / (1.0 + std::max(0.0, now - p.t_submit) / AGING_SECONDS);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return key(a) < key(b); });
+    std::vector<uint8_t> gone(s->pending_b.size(), 0);
+    for (size_t k : order) {
+        const Pending &p = s->pending_b[k];
+        Job *j = nullptr;
+        const int rc = job_admit(s, p.ticket, p.req, &j);
+        if (rc == 1) break;
+        if (rc != 0)
+            finish(s, p.ticket, error_result(rc, 1));
+        else
+            s->active.push_back(j);
+        gone[k] = 1;
+    }
+    size_t w = 0;
+    for (size_t k = 0; k < s->pending_b.size(); k++)
+        if (!gone[k]) s->pending_b[w++] = s->pending_b[k];
+    s->pending_b.resize(w);
+}
+
 void scheduler(erlbm_server *s)
 {
     cudaSetDevice(s->device);
     const int chunk = 64;
     for (;;) {
         std::deque<std::pair<int64_t, erlbm_request>> in;
+        std::vector<double> t_in;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             const bool idle = s->active.empty() && s->pending_b.empty() && s->pending_a[0].empty() &&
@@ -648,12 +720,20 @@ void scheduler(erlbm_server *s)
                 s->cv_work.wait_for(lk, std::chrono::milliseconds(2));
             }
             in.swap(s->inbox);
+            for (auto &p : in) t_in.push_back(s->t_submit[p.first]);
         }
-        for (auto &p : in) {
-            if (slot_eligible(p.second))
+        for (size_t k = 0; k < in.size(); k++) {
+            auto &p = in[k];
+            if (slot_eligible(p.second)) {
                 s->pending_a[p.second.precision == ERLBM_FP64 ? 0 : 1].push_back(p);
-            else
-                s->pending_b.push_back(p);
+            } else {
+                Pending q;
+                q.ticket = p.first;
+                q.req = p.second;
+                q.t_submit = t_in[k];
+                q.est = estimate_seconds(p.second);
+                s->pending_b.push_back(q);
+            }
         }
         // publish slot-lane requests while their ring has space
         for (int l = 0; l < 2; l++) {
@@ -666,19 +746,8 @@ void scheduler(erlbm_server *s)
             }
             if (any && !L.running) lane_launch(L);
         }
-        // admit stream-lane runs while memory and streams allow (first come, first served)
-        while (!s->pending_b.empty()) {
-            auto &p = s->pending_b.front();
-            Job *j = nullptr;
-            const int rc = job_admit(s, p.first, p.second, &j);
-            if (rc == 1) break;
-            if (rc != 0) {
-                finish(s, p.first, error_result(rc, 1));
-            } else {
-                s->active.push_back(j);
-            }
-            s->pending_b.pop_front();
-        }
+        // admit stream-lane runs while memory and streams allow
+        admit_stream_lane(s);
         for (size_t k = 0; k < s->active.size();) {
             if (job_progress(s, s->active[k], chunk)) {
                 s->active[k] = s->active.back();

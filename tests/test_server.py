@@ -125,3 +125,20 @@ def test_wait_times_out_and_the_result_arrives_later():
         assert ei.value.code == -4
         r = srv.wait(t, timeout=600)
         assert r["status"] == 0 and r["steps_done"] == 3000
+
+
+def test_stream_lane_admits_the_shortest_runs_first():
+    """With one stream the stream lane admits by estimated work (shortest first, aging with the
+    wait), not by arrival: small lattices submitted after a large one start before it."""
+    m = E()
+    with m.Server(hbm_budget_bytes=1 << 30, max_streams=1) as srv:
+        blocker = srv.submit(m.REQ_TG2D, m.FP64, L=256, tau=0.6, tau_nh=0.65, u0=0.05, n_steps=3000)
+        big = srv.submit(m.REQ_TG3D, m.FP64, op=m.OP_EXTREG, L=64, tau=0.55, tau_nh=0.65, u0=0.05, n_steps=2000)
+        small = [srv.submit(m.REQ_TG2D, m.FP32_SHIFTED, L=128, tau=0.6, tau_nh=0.65, u0=0.05, n_steps=100)
+                 for _ in range(4)]
+        rb = srv.wait(big, timeout=600)
+        rs = [srv.wait(t, timeout=600) for t in small]
+        r0 = srv.wait(blocker, timeout=600)
+        assert all(r["status"] == 0 for r in rs + [rb, r0])
+        assert max(r["t_admit"] for r in rs) <= rb["t_admit"]
+        assert r0["t_admit"] <= rb["t_admit"]
