@@ -28,6 +28,10 @@ Other workloads (--workload; the default is the one above):
                          FP32 or FP64; budgets 1..10000 steps) through the request server; runs/s
                          with p50 / p99 latency, beside the plain path (one run at a time, FP64,
                          one launch per step) on an evenly strided sample of the same stream.
+  snapshot               the double shear layer's output at an interval (main_double-shear-layer.cpp:
+                         187-208): kinetic energy, rec_velocity and rec_vorticity as ASCII VTK, from
+                         the resident populations (fields on the device); snapshots/s, wall-clock,
+                         beside the CPU restatement writing the same files from host populations.
 """
 from __future__ import annotations
 
@@ -67,7 +71,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extras", action="store_true")
-    p.add_argument("--workload", default="dsl", choices=["dsl", "tg-map", "obstacle-map", "serve"])
+    p.add_argument("--workload", default="dsl", choices=["dsl", "tg-map", "obstacle-map", "serve", "snapshot"])
     p.add_argument("--op", default="erlbm", choices=list(DSL_OPS),
                    help="dsl: collision operator (main_double-shear-layer.cpp --collision)")
     p.add_argument("--map-points", type=int, default=100, help="P: P x P map points per bench step")
@@ -586,6 +590,83 @@ def run_serve(args):
     return 0
 
 
+def run_snapshot(args):
+    """Snapshots of the double shear layer as the program writes them at each interval: the kinetic
+    energy and the ASCII velocity and vorticity files (rec_velocity, rec_vorticity), wall-clock per
+    snapshot, the files written to a scratch directory and removed after each timed snapshot."""
+    import shutil
+    import tempfile
+    import numpy as np
+    import torch
+    import erlbm_gb300 as E
+    torch.cuda.set_device(0)
+    L = args.L
+    prec = E.FP64 if args.precision == "fp64" else E.FP32_SHIFTED
+    op, tnh, op_label = DSL_OPS[args.op]
+    lat = E.Lattice(9, L, L, 1, None, tau_of(L), tnh, op, prec)
+    lat.set_populations(E.init_double_shear(L))
+    lat.step(101)
+    lat.sync()
+    d = tempfile.mkdtemp(prefix="erlbm_snap_")
+
+    def snap(fmt):
+        t = time.perf_counter()
+        lat.kinetic_energy(E.STAGE_POST_COLLISION)
+        lat.write_vtk(os.path.join(d, "vel.vtk"), E.FIELD_VELOCITY, fmt)
+        lat.write_vtk(os.path.join(d, "vor.vtk"), E.FIELD_VORTICITY, fmt)
+        dt = time.perf_counter() - t
+        size = os.path.getsize(os.path.join(d, "vel.vtk")) + os.path.getsize(os.path.join(d, "vor.vtk"))
+        os.remove(os.path.join(d, "vel.vtk"))
+        os.remove(os.path.join(d, "vor.vtk"))
+        return dt, size
+
+    try:
+        for _ in range(args.warmup):
+            snap(E.VTK_ASCII)
+        clocks = Clocks(0)
+        clocks.start()
+        ts = [snap(E.VTK_ASCII) for _ in range(args.steps)]
+        clk = clocks.stop()
+        tb = [snap(E.VTK_BINARY_FLOAT) for _ in range(max(1, args.steps // 2))]
+        cpu = None
+        if not args.no_cpu:
+            from oracle import oracle as O
+            aos = lat.get_populations(E.STAGE_POST_COLLISION)
+            ol = O.Lattice(9, L, L, 1, None, tau_of(L), tnh, op)
+            ol.set(aos)
+            t = time.perf_counter()
+            ol.kinetic_energy(0)
+            O.write_vtk(9, L, L, 1, None, aos, O.FIELD_VELOCITY, O.VTK_ASCII, os.path.join(d, "vel.vtk"))
+            O.write_vtk(9, L, L, 1, None, aos, O.FIELD_VORTICITY, O.VTK_ASCII, os.path.join(d, "vor.vtk"))
+            tc = time.perf_counter() - t
+            cpu = {"value": 1.0 / tc, "unit": "snapshots/s", "cores": 1, "kind": "port",
+                   "sample": f"one snapshot at L={L} from host AoS FP64 populations (energy, ASCII velocity "
+                             "and vorticity VTK, one thread as the reference's writers)"}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+        lat.close()
+    sec = sum(t for t, _ in ts) / len(ts)
+    n = L * L
+    line = {"metric": "snapshots/s", "value": 1.0 / sec, "unit": "snapshots/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if prec == E.FP32_SHIFTED else "f64",
+            "data": "synthetic (double shear layer after 101 steps)",
+            "config": {"workload": f"double shear layer snapshot L={L} ({op_label}): kinetic energy + "
+                                   "rec_velocity + rec_vorticity ASCII VTK", "L": L,
+                       "precision": args.precision},
+            "bytes_written_per_snapshot": ts[0][1],
+            "binary_float": {"value": len(tb) / sum(t for t, _ in tb), "unit": "snapshots/s",
+                             "bytes_written_per_snapshot": tb[0][1]},
+            "roofline": None,
+            "e2e": {"value": 1.0 / sec, "unit": "snapshots/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 8 + 2 * 3 * n * 8},
+            "gpu_launches": None, "clocks": clk}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -594,6 +675,8 @@ def main():
         return run_map(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "snapshot":
+        return run_snapshot(args)
     return run_ours(args)
 
 
