@@ -32,6 +32,9 @@ Other workloads (--workload; the default is the one above):
                          187-208): kinetic energy, rec_velocity and rec_vorticity as ASCII VTK, from
                          the resident populations (fields on the device); snapshots/s, wall-clock,
                          beside the CPU restatement writing the same files from host populations.
+  channel                a D2Q9 channel (the library's channel boundaries, Boundary_conditions.cpp:
+                         456-806): walls, a circular cylinder, parabolic inlet, convective outlet,
+                         nx = 4 ny (ny = L / 4); `inner` steps per bench step; MLUPS over fluid nodes.
 """
 from __future__ import annotations
 
@@ -71,7 +74,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extras", action="store_true")
-    p.add_argument("--workload", default="dsl", choices=["dsl", "tg-map", "obstacle-map", "serve", "snapshot"])
+    p.add_argument("--workload", default="dsl",
+                   choices=["dsl", "tg-map", "obstacle-map", "serve", "snapshot", "channel"])
     p.add_argument("--op", default="erlbm", choices=list(DSL_OPS),
                    help="dsl: collision operator (main_double-shear-layer.cpp --collision)")
     p.add_argument("--map-points", type=int, default=100, help="P: P x P map points per bench step")
@@ -667,6 +671,107 @@ def run_snapshot(args):
     return 0
 
 
+def channel_geometry(ny: int):
+    """Solid mask of the channel workload: x and y walls, a cylinder of radius ny / 12 at (ny, ny / 2)."""
+    import numpy as np
+    nx = 4 * ny
+    s = np.zeros((ny, nx), np.uint8)
+    s[:, 0] = s[:, nx - 1] = 1
+    s[0, :] = s[ny - 1, :] = 1
+    yy, xx = np.mgrid[0:ny, 0:nx]
+    s[(xx - ny) ** 2 + (yy - ny // 2) ** 2 <= (ny // 12) ** 2] = 1
+    return nx, s.reshape(-1)
+
+
+def run_channel(args):
+    import numpy as np
+    import torch
+    import erlbm_gb300 as E
+    torch.cuda.set_device(0)
+    ny = max(64, args.L // 4)
+    nx, solid = channel_geometry(ny)
+    prec = E.FP64 if args.precision == "fp64" else E.FP32_SHIFTED
+    tau, tnh, op = 0.55, 0.7, E.OP_EXTREG
+    bc = dict(inlet_x=1, inlet_kind=E.INLET_PARABOLIC, parabolic_L=ny - 2, u_in=0.05, outlet_x=nx - 2,
+              outlet_kind=E.OUTLET_CONVECTIVE)
+    lat = E.Lattice(9, nx, ny, 1, solid, tau, tnh, op, prec)
+    n_fluid = lat.n_fluid
+    f0 = np.tile(np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4), n_fluid)
+    stream = torch.cuda.Stream()
+    lat.set_stream(stream.cuda_stream)
+    lat.set_populations(f0)
+    inner, K, W = args.inner, args.steps, args.warmup
+    for _ in range(W):
+        lat.step(inner, bc)
+    lat.sync()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(K):
+        lat.step(inner, bc)
+    ev1.record(stream)
+    stream.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    value = n_fluid * inner * K / (ms / 1e3) / 1e6
+    launch_ms = ms / (K * inner)
+    bpl = BYTES_PER_LU["fp64" if prec == E.FP64 else "fp32"]
+    peak, peak_kind = peaks()
+    achieved = bpl * n_fluid / (launch_ms / 1e3) / 1e9
+    # end to end through the C ABI: populations from pinned host memory, inner steps, energy back
+    pinned = torch.empty(f0.size, dtype=torch.float64, pin_memory=True)
+    pinned.numpy()[:] = f0
+    host = pinned.numpy()
+    lat.set_populations(host)
+    lat.step(inner, bc)
+    lat.kinetic_energy(E.STAGE_POST_COLLISION)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        lat.set_populations(host)
+        lat.step(inner, bc)
+        lat.kinetic_energy(E.STAGE_POST_COLLISION)
+    t_e2e = time.perf_counter() - t0
+    lat.close()
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        ol = O.Lattice(9, nx, ny, 1, solid, tau, tnh, op)
+        ol.set(f0)
+        ol.step(10, bc, threads=threads)
+        n_cpu = 10
+        t = time.perf_counter()
+        while True:
+            ol.step(n_cpu, bc, threads=threads)
+            dt = time.perf_counter() - t
+            if dt > 0.5 or n_cpu > 100000:
+                break
+            t = time.perf_counter()
+            n_cpu *= 4
+        cpu = {"value": n_fluid * n_cpu / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+               "sample": f"the same channel, FP64, {n_cpu} steps, {threads} OpenMP threads"}
+    line = {"metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": 1, "steps": K, "warmup": W,
+            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == E.FP64 else "f32", "data": "synthetic (channel at rest, parabolic inflow)",
+            "config": {"workload": f"D2Q9 channel {nx}x{ny} with a cylinder, parabolic inlet, convective outlet, "
+                                   f"E-RLBM tau=0.55 tau_nh=0.7", "nx": nx, "ny": ny, "n_fluid": n_fluid,
+                       "lbm_steps_per_step": inner, "precision": args.precision,
+                       "l2": f"working set {2 * bpl // 2 * n_fluid / 1e6:.0f} MB"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": bpl * n_fluid,
+                         "launch_us": launch_ms * 1e3, "lattice_updates_per_launch": n_fluid,
+                         "kernel": f"k_step<{'PrecExact64' if prec == E.FP64 else 'PrecShifted32'},9,4>"},
+            "e2e": {"value": n_fluid * inner * K / t_e2e / 1e6, "unit": "MLUPS",
+                    "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": 8},
+            "gpu_launches": K * inner, "clocks": clk}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -677,6 +782,8 @@ def main():
         return run_serve(args)
     if args.workload == "snapshot":
         return run_snapshot(args)
+    if args.workload == "channel":
+        return run_channel(args)
     return run_ours(args)
 
 

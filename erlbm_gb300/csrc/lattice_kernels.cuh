@@ -195,21 +195,48 @@ struct PrecShifted32 {
 
 __device__ __forceinline__ int wrap1(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
-// Post-stream populations of node (x, y, z) gathered from the post-collision buffer.
+// Coordinates of box node `node` (x fastest); 32-bit division when the box index fits in 31 bits.
+__device__ __forceinline__ void node_xyz(const Geo &g, long long node, int &x, int &y, int &z)
+{
+    if (g.nbox < (1LL << 31)) {
+        const unsigned n = (unsigned)node, r = n / (unsigned)g.nx;
+        x = (int)(n - r * (unsigned)g.nx);
+        y = (int)(r % (unsigned)g.ny);
+        z = (int)(r / (unsigned)g.ny);
+    } else {
+        x = (int)(node % g.nx);
+        const long long r = node / g.nx;
+        y = (int)(r % g.ny);
+        z = (int)(r / g.ny);
+    }
+}
+
+// Post-stream populations of node (x, y, z) gathered from the post-collision buffer.  The source of
+// direction i is node (x - c_x, y - c_y, z - c_z) with periodic wrap: its index is the node's plus
+// one offset per axis, set once for the node's position.
 template <class P, int Q>
 __device__ __forceinline__ void gather(const typename P::T *__restrict__ src, const Geo &g, int mode, int x, int y,
                                        int z, long long node, typename P::T *f)
 {
+    if (mode == 1) {
+#pragma unroll
+        for (int i = 0; i < Q; i++) f[i] = src[(long long)i * g.plane + node];
+        return;
+    }
+    const long long nx = g.nx, nxy = (long long)g.nx * g.ny;
+    // offsets to x - 1 and x + 1 (wrapped), and likewise in y and z
+    const long long xm = x == 0 ? nx - 1 : -1, xp = x == g.nx - 1 ? 1 - nx : 1;
+    const long long ym = y == 0 ? (long long)(g.ny - 1) * nx : -nx, yp = y == g.ny - 1 ? (long long)(1 - g.ny) * nx : nx;
+    long long zm = 0, zp = 0;
+    if (Q == 19) {
+        zm = z == 0 ? (long long)(g.nz - 1) * nxy : -nxy;
+        zp = z == g.nz - 1 ? (long long)(1 - g.nz) * nxy : nxy;
+    }
 #pragma unroll
     for (int i = 0; i < Q; i++) {
-        if (mode == 1) {
-            f[i] = src[(long long)i * g.plane + node];
-            continue;
-        }
-        const int xs = wrap1(x - Lat<Q>::cx(i), g.nx);
-        const int ys = wrap1(y - Lat<Q>::cy(i), g.ny);
-        const int zs = (Q == 19) ? wrap1(z - Lat<Q>::cz(i), g.nz) : 0;
-        const long long s = (long long)xs + (long long)g.nx * ((long long)ys + (long long)g.ny * zs);
+        const int cx = Lat<Q>::cx(i), cy = Lat<Q>::cy(i), cz = Lat<Q>::cz(i);
+        const long long s = node + (cx == 1 ? xm : (cx == -1 ? xp : 0)) + (cy == 1 ? ym : (cy == -1 ? yp : 0)) +
+                            (cz == 1 ? zm : (cz == -1 ? zp : 0));
         if (g.solid != nullptr && g.solid[s])
             f[i] = src[(long long)Lat<Q>::opp(i) * g.plane + node];
         else
@@ -341,10 +368,8 @@ __global__ void __launch_bounds__(256) k_step(const typename P::T *__restrict__ 
     unsigned long long rho_bits = 0;
     int flag = 0;
     if (active) {
-        const int x = (int)(node % g.nx);
-        const long long r = node / g.nx;
-        const int y = (int)(r % g.ny);
-        const int z = (int)(r / g.ny);
+        int x, y, z;
+        node_xyz(g, node, x, y, z);
         T f[Q];
         state_after_planes<P, Q>(src, g, bc, a.mode, x, y, z, node, f);
         P::template collide<Q, OP>(f, prm);
@@ -382,10 +407,8 @@ __global__ void __launch_bounds__(256) k_stream_only(const typename P::T *__rest
     const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= g.nbox) return;
     if (g.solid != nullptr && g.solid[node]) return;
-    const int x = (int)(node % g.nx);
-    const long long r = node / g.nx;
-    const int y = (int)(r % g.ny);
-    const int z = (int)(r / g.ny);
+    int x, y, z;
+    node_xyz(g, node, x, y, z);
     T f[Q];
     gather<P, Q>(src, g, 0, x, y, z, node, f);
 #pragma unroll
