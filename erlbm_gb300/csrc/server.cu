@@ -668,11 +668,11 @@ double estimate_seconds(const erlbm_request &q)
     return std::max(1, q.n_steps) * std::max(nodes * cost / 4e10, 4e-6);
 }
 
-// Admission order of the stream lane: shortest estimated work first, with aging (the key of a
-// request falls as it waits, so a large run is not passed over for ever).  The first request in
-// that order that does not fit stops the pass, so memory frees up for it instead of for requests
-// behind it.
-constexpr double AGING_SECONDS = 1.0;
+// Admission order of the stream lane: shortest estimated work first, with aging.  The key of a
+// request is its estimated GPU time minus the time it has waited, so a request that has waited
+// longer than its own estimate comes before any new one: a large run is passed over for at most
+// about its own run time.  The first request in that order that does not fit stops the pass, so
+// memory frees up for it instead of for requests behind it.
 
 void admit_stream_lane(erlbm_server *s)
 {
@@ -682,7 +682,7 @@ void admit_stream_lane(erlbm_server *s)
     for (size_t k = 0; k < order.size(); k++) order[k] = k;
     auto key = [&](size_t k) {
         const Pending &p = s->pending_b[k];
-        return p.est / (1.0 + std::max(0.0, now - p.t_submit) / AGING_SECONDS);
+        return p.est - std::max(0.0, now - p.t_submit);
     };
     std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return key(a) < key(b); });
     std::vector<uint8_t> gone(s->pending_b.size(), 0);
