@@ -237,10 +237,15 @@ __device__ __forceinline__ void gather(const typename P::T *__restrict__ src, co
         const int cx = Lat<Q>::cx(i), cy = Lat<Q>::cy(i), cz = Lat<Q>::cz(i);
         const long long s = node + (cx == 1 ? xm : (cx == -1 ? xp : 0)) + (cy == 1 ? ym : (cy == -1 ? yp : 0)) +
                             (cz == 1 ? zm : (cz == -1 ? zp : 0));
-        if (g.solid != nullptr && g.solid[s])
-            f[i] = src[(long long)Lat<Q>::opp(i) * g.plane + node];
-        else
-            f[i] = src[(long long)i * g.plane + s];
+        const typename P::T pulled = src[(long long)i * g.plane + s];
+        if (g.solid != nullptr) {
+            // both candidates are loaded before the solid byte is known (every address is a node of
+            // the box), so the loads do not wait for the mask
+            const typename P::T back = src[(long long)Lat<Q>::opp(i) * g.plane + node];
+            f[i] = g.solid[s] ? back : pulled;
+        } else {
+            f[i] = pulled;
+        }
     }
 }
 
