@@ -137,3 +137,15 @@ def test_read_geo_equals_oracle_and_reference(tmp_path):
         assert np.array_equal(solid, O.read_geo(str(path), pin, pout, bool(wall))[3])
     with pytest.raises(m.ErlbmError):
         m.read_geo(str(tmp_path / "missing.vtk"))
+
+
+def test_channel_bench_geometry_fits_the_parabolic_inlet():
+    """bench.py's channel workload: walls on all four sides and a cylinder; every column holds at
+    most ny - 2 fluid nodes, the parabolic profile's L, so erlbm_step accepts the inlet."""
+    import bench
+    for ny in (64, 128, 512):
+        nx, solid = bench.channel_geometry(ny)
+        s = solid.reshape(ny, nx)
+        assert nx == 4 * ny and s[:, 0].all() and s[:, -1].all() and s[0, :].all() and s[-1, :].all()
+        assert (1 - s).sum(axis=0).max() == ny - 2
+        assert s[ny // 2, ny] == 1 and s[ny // 2, 2 * ny] == 0  # the cylinder, and open channel behind it
