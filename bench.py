@@ -100,9 +100,24 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def launches_of(n: int, per: int) -> int:
+    """Kernel launches of erlbm_step(n) on a lattice whose last step was a collision: blocks of 64 steps
+    (66 with three steps per launch) replayed as graphs, then multi-step launches, then single steps."""
+    g = 66 if per == 3 else 64
+    count, s = 0, 0
+    while s < n:
+        if n - s >= g:
+            count, s = count + g // per, s + g
+        elif per > 1 and n - s >= per:
+            count, s = count + 1, s + per
+        else:
+            count, s = count + 1, s + 1
+    return count
+
+
 def ncu_traffic(L: int, precision: str):
-    """DRAM bytes per launch from the committed ncu summary of the same kernel ("fp32", "fp64", or
-    "fp32_x2" for the two-step kernel), scaled to L."""
+    """DRAM bytes per launch from the committed ncu summary of the same kernel ("fp32", "fp64",
+    "fp32_x2" or "fp32_x3" for the two- and three-step kernels), scaled to L."""
     path = os.path.join(ROOT, "profiles", "dsl_periodic_d2q9_traffic.json")
     try:
         with open(path) as f:
@@ -296,9 +311,8 @@ def run_ours(args):
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    two = bool(shape and shape.get("two_step"))
-    # a two-step launch advances every node by two steps: inner // 2 of them, plus one single step if odd
-    launches = K * (inner // 2 + inner % 2) if two else K * inner
+    per = 3 if (shape and shape.get("three_step")) else (2 if (shape and shape.get("two_step")) else 1)
+    launches = K * launches_of(inner, per)
     value = world * L * L * inner * K / (ms / 1e3) / 1e6
     launch_ms = ms / launches
     algo_bytes = BYTES_PER_LU[args.precision] * L * L
@@ -351,17 +365,19 @@ def run_ours(args):
                          "no flush",
                    "launch_shape": None if shape is None else {"block_threads": shape["block_threads"],
                                                                "streaming_stores": shape["streaming_stores"],
-                                                               "two_step": two}},
+                                                               "steps_per_launch": per}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
-                     "traffic": ncu_traffic(L, "fp32_x2" if two else args.precision) if args.op == "erlbm" else None,
+                     "traffic": ncu_traffic(L, {1: args.precision, 2: "fp32_x2", 3: "fp32_x3"}[per])
+                     if args.op == "erlbm" else None,
                      "algorithmic_bytes_per_launch": algo_bytes, "launch_us": launch_ms * 1e3,
-                     "lattice_updates_per_launch": L * L * (2 if two else 1),
-                     "kernel": (f"k_periodic_d2q9_x2s<{op}>" if two else f"k_periodic_d2q9<{op}>")
+                     "lattice_updates_per_launch": L * L * per,
+                     "kernel": {1: f"k_periodic_d2q9<{op}>", 2: f"k_periodic_d2q9_x2s<{op}>",
+                                3: f"k_periodic_d2q9_x3s<{op}>"}[per]
                      if args.precision == "fp32" else f"k_step<PrecExact64,9,{op}>",
                      # the update rate against the roofline of one step per launch, where every
                      # update reads and writes each population once (2 Q sizeof(real) bytes): the
-                     # two-step kernel moves half of those bytes, so this fraction can exceed 1
+                     # multi-step kernels move a half or a third of those bytes, so this fraction can exceed 1
                      "one_step_equivalent": {"bytes_per_update": BYTES_PER_LU[args.precision],
                                              "gbs": value * 1e6 * BYTES_PER_LU[args.precision] / 1e9,
                                              "frac": value * 1e6 * BYTES_PER_LU[args.precision] / 1e9 / peak}},

@@ -108,10 +108,12 @@ class Lattice:
         check(lib().erlbm_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None),
               "erlbm_set_stream")
 
-    def set_launch(self, block_threads: int = 0, streaming_stores: bool = False, two_step: bool = False) -> None:
-        """Launch shape of the fused periodic D2Q9 FP32 kernel (see erlbm_gb300.autotune); two_step runs
-        pairs of steps as one launch (nx % 256 == 0)."""
-        flags = (1 if streaming_stores else 0) | (2 if two_step else 0)
+    def set_launch(self, block_threads: int = 0, streaming_stores: bool = False, two_step: bool = False,
+                   three_step: bool = False) -> None:
+        """Launch shape of the fused periodic D2Q9 FP32 kernel (see erlbm_gb300.autotune): two_step or
+        three_step run two or three consecutive steps as one launch (nx % 128 == 0, ny even); the same
+        bits in every shape."""
+        flags = (1 if streaming_stores else 0) | (2 if two_step else 0) | (4 if three_step else 0)
         check(lib().erlbm_set_launch(self._h, int(block_threads), flags), "erlbm_set_launch")
 
     def kinetic_energy(self, stage: int = STAGE_POST_STREAM) -> float:

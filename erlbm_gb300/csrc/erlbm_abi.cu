@@ -81,11 +81,12 @@ struct erlbm_handle {
     cudaStream_t own_stream = nullptr;  // the stream created at erlbm_create
     int shape = 0;                      // launch shape of the fused periodic kernel (erlbm_set_launch)
     bool two_step = false;              // pairs of fused periodic steps as one launch (erlbm_set_launch)
+    bool three_step = false;            // triples of fused periodic steps as one launch (erlbm_set_launch)
     std::vector<uint8_t> h_solid;       // host copy of the solid mask (empty for periodic boxes)
     std::vector<double> h_profile;      // parabolic inlet velocity per (y, z) of the inlet plane
     double *d_profile = nullptr;
     double profile_key[3] = {-1, 0, 0}; // inlet_x, u_in, L of the uploaded profile
-    // CUDA graphs of GRAPH_STEPS plain fused periodic steps, one per buffer parity, for the launch
+    // CUDA graphs of a block of plain fused periodic steps, one per buffer parity, for the launch
     // shape and parameters in graph_key (rebuilt when erlbm_set_launch or erlbm_set_params changes them)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long graph_key = -1;
@@ -327,15 +328,17 @@ int enqueue_step(erlbm_handle *h, const BCp &bc, int check_density, double densi
     return ERLBM_OK;
 }
 
-// GRAPH_STEPS plain periodic steps of the fused FP32 D2Q9 kernels (two per launch when `two`) as one
+// A block of plain periodic steps of the fused FP32 D2Q9 kernels (per_launch steps per launch) as one
 // CUDA graph launch: the launches of a block are captured once per buffer parity and replayed, so a
 // small lattice is not bound by the host's launch rate.  An even number of launches leaves the
 // buffer parity unchanged.
-constexpr int GRAPH_STEPS = 64;
+// steps per graph: an even number of launches of every shape (1, 2 or 3 steps each)
+int graph_steps_of(int per_launch) { return per_launch == 3 ? 66 : 64; }
 
-int graph_steps(erlbm_handle *h, bool two)
+int graph_steps(erlbm_handle *h, int per_launch)
 {
-    const long long key = (two ? 1 : 0) | ((long long)h->shape << 1);
+    const int n_steps = graph_steps_of(per_launch);
+    const long long key = per_launch | ((long long)h->shape << 2);
     if (h->graph_key != key) {
         drop_graphs(h);
         h->graph_key = key;
@@ -345,11 +348,13 @@ int graph_steps(erlbm_handle *h, bool two)
         if (!h->capture_stream) CK(cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking));
         CK(cudaStreamBeginCapture(h->capture_stream, cudaStreamCaptureModeRelaxed));
         int c = h->cur, lrc = 0;
-        for (int k = 0; k < (two ? GRAPH_STEPS / 2 : GRAPH_STEPS) && lrc == 0; k++) {
+        for (int k = 0; k < n_steps / per_launch && lrc == 0; k++) {
             const float *src = (const float *)h->d_buf[c];
             float *dst = (float *)h->d_buf[c ^ 1];
-            lrc = two ? launch_periodic_d2q9_fp32_x2(h->op, h->g, h->R, src, dst, h->capture_stream)
-                      : launch_periodic_d2q9_fp32(h->op, h->g, h->R, src, dst, h->capture_stream, h->shape);
+            lrc = per_launch == 3   ? launch_periodic_d2q9_fp32_x3(h->op, h->g, h->R, src, dst, h->capture_stream)
+                  : per_launch == 2 ? launch_periodic_d2q9_fp32_x2(h->op, h->g, h->R, src, dst, h->capture_stream)
+                                    : launch_periodic_d2q9_fp32(h->op, h->g, h->R, src, dst, h->capture_stream,
+                                                                h->shape);
             c ^= 1;
         }
         cudaGraph_t graph = nullptr;
@@ -368,7 +373,7 @@ int graph_steps(erlbm_handle *h, bool two)
         }
     }
     CK(cudaGraphLaunch(x, h->stream));
-    h->steps_done += GRAPH_STEPS;
+    h->steps_done += n_steps;
     h->kind = 1;
     return ERLBM_OK;
 }
@@ -597,11 +602,23 @@ int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc)
     if ((rc = validate_bc(h, bc, &b))) return rc;
     const bool plain = h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && b.inlet_x < 0 && b.outlet_x < 0 &&
                        b.open_y < 0 && periodic_d2q9_fp32_ok(h->g);
+    const bool fused3 = plain && h->three_step && periodic_d2q9_x2_ok(h->g);
     const bool fused2 = plain && h->two_step && periodic_d2q9_x2_ok(h->g);
+    const int per_launch = fused3 ? 3 : (fused2 ? 2 : 1);
     for (int s = 0; s < n_steps;) {
-        if (plain && h->kind == 1 && n_steps - s >= GRAPH_STEPS) {
-            if ((rc = graph_steps(h, fused2))) return rc;
-            s += GRAPH_STEPS;
+        if (plain && h->kind == 1 && n_steps - s >= graph_steps_of(per_launch)) {
+            if ((rc = graph_steps(h, per_launch))) return rc;
+            s += graph_steps_of(per_launch);
+            continue;
+        }
+        if (fused3 && h->kind == 1 && n_steps - s >= 3) {
+            // three plain periodic steps in one launch
+            CKL(launch_periodic_d2q9_fp32_x3(h->op, h->g, h->R, (const float *)h->d_buf[h->cur],
+                                             (float *)h->d_buf[h->cur ^ 1], h->stream),
+                "periodic_d2q9_x3");
+            h->cur ^= 1;
+            h->steps_done += 3;
+            s += 3;
             continue;
         }
         if (fused2 && h->kind == 1 && n_steps - s >= 2) {
@@ -628,9 +645,14 @@ int erlbm_set_launch(erlbm_handle *h, int block_threads, int flags)
         set_error("block_threads must be 0, 128, 256 or 512%s%s", "", "");
         return ERLBM_E_INVAL;
     }
-    if (flags & ~(ERLBM_LAUNCH_STREAMING_STORES | ERLBM_LAUNCH_TWO_STEP)) return ERLBM_E_INVAL;
+    if (flags & ~(ERLBM_LAUNCH_STREAMING_STORES | ERLBM_LAUNCH_TWO_STEP | ERLBM_LAUNCH_THREE_STEP)) return ERLBM_E_INVAL;
+    if ((flags & ERLBM_LAUNCH_TWO_STEP) && (flags & ERLBM_LAUNCH_THREE_STEP)) {
+        set_error("set_launch: at most one of ERLBM_LAUNCH_TWO_STEP and ERLBM_LAUNCH_THREE_STEP%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
     h->shape = block_threads | ((flags & ERLBM_LAUNCH_STREAMING_STORES) ? 0x1000 : 0);
     h->two_step = (flags & ERLBM_LAUNCH_TWO_STEP) != 0;
+    h->three_step = (flags & ERLBM_LAUNCH_THREE_STEP) != 0;
     return ERLBM_OK;  // graphs of another shape are rebuilt on their next use (graph_key)
 }
 

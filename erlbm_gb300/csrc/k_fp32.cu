@@ -6,9 +6,9 @@
 // and written with 128-bit accesses.  The pull from x - c_x needs one neighbour column per
 // lane; it comes from the adjacent lane by a warp shuffle, and only the two warp-edge lanes
 // issue an extra 4-byte load (an L2 hit: the neighbouring warp reads that line too).
-// Algorithmic traffic is 2 * 9 * 4 = 72 bytes per lattice update.  The two-step kernel
-// (k_periodic_d2q9_x2s) advances every node by two steps per launch in independent warp strips,
-// 36 bytes per lattice update.
+// Algorithmic traffic is 2 * 9 * 4 = 72 bytes per lattice update.  The two- and three-step kernels
+// (k_periodic_d2q9_x2s, k_periodic_d2q9_x3s) advance every node by two or three steps per launch in
+// independent warp strips: 36 and 24 bytes per lattice update.
 #include <atomic>
 
 #include "lattice_kernels.cuh"
@@ -292,6 +292,176 @@ __global__ void __launch_bounds__(128) k_periodic_d2q9_x2s(const float *__restri
     }
 }
 
+// Three steps per launch in the same warp-strip form, with strips of 28 output columns: lane l holds
+// column xs - 2 + l; the first stage P' is valid in every lane (lanes 0 and 31 load their halo
+// populations), the second P'' in lanes 1 .. 30, the output in lanes 2 .. 29.  Per iteration the
+// output rows j, j + 1 come from P'' rows j - 1 .. j + 2, P'' rows j + 1, j + 2 from P' rows j .. j + 3,
+// and P' rows j + 2, j + 3 from P rows j + 1 .. j + 4, of which rows j + 3, j + 4 were loaded one
+// iteration ahead.  Each node is read and written once per three steps (24 bytes per update).
+constexpr int X3_W = 28;
+
+template <int OP>
+__global__ void __launch_bounds__(128) k_periodic_d2q9_x3s(const float *__restrict__ src, float *__restrict__ dst,
+                                                          int nx, int ny, long long plane, int hc, int strips,
+                                                          int n_warps, shifted::Coef k)
+{
+    const int lane = threadIdx.x & 31;
+    const int wid = (int)blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
+    if (wid >= n_warps) return;
+    const int xs = (wid % strips) * X3_W;
+    const int y0 = (wid / strips) * hc;
+    const int y1 = min(y0 + hc, ny);
+    int c = xs - 2 + lane;  // in [-2, nx + 28]
+    const bool store = lane >= 2 && lane <= X3_W + 1 && c < nx;
+    c = c < 0 ? c + nx : (c >= nx ? c - nx : c);
+    const bool halo = lane == 0 || lane == 31;
+    int hcol = lane == 0 ? xs - 3 : xs + 30;
+    hcol = hcol < 0 ? hcol + nx : (hcol >= nx ? hcol - nx : hcol);
+    const long long h0 = hcol + (lane == 0 ? 1 : 2) * plane, h1 = hcol + (lane == 0 ? 5 : 6) * plane,
+                    h2 = hcol + (lane == 0 ? 7 : 8) * plane;
+    auto load = [&](int r, float v[9], float h[3]) {
+        r = r < 0 ? r + ny : (r >= ny ? r - ny : r);
+        const float *p = src + (long long)r * nx;
+#pragma unroll
+        for (int i = 0; i < 9; i++) v[i] = __ldg(p + c + i * plane);
+        if (halo) {
+            h[0] = __ldg(p + h0);
+            h[1] = __ldg(p + h1);
+            h[2] = __ldg(p + h2);
+        }
+    };
+    auto align = [&](const float v[9], const float h[3], float a[9]) {
+        a[0] = v[0];
+        a[3] = v[3];
+        a[4] = v[4];
+        float u;
+        u = __shfl_up_sync(XS_FULL, v[1], 1);
+        a[1] = lane == 0 ? h[0] : u;
+        u = __shfl_up_sync(XS_FULL, v[5], 1);
+        a[5] = lane == 0 ? h[1] : u;
+        u = __shfl_up_sync(XS_FULL, v[7], 1);
+        a[7] = lane == 0 ? h[2] : u;
+        u = __shfl_down_sync(XS_FULL, v[2], 1);
+        a[2] = lane == 31 ? h[0] : u;
+        u = __shfl_down_sync(XS_FULL, v[6], 1);
+        a[6] = lane == 31 ? h[1] : u;
+        u = __shfl_down_sync(XS_FULL, v[8], 1);
+        a[8] = lane == 31 ? h[2] : u;
+    };
+    auto align2 = [&](float2 g[9]) {
+        g[1].x = __shfl_up_sync(XS_FULL, g[1].x, 1);
+        g[1].y = __shfl_up_sync(XS_FULL, g[1].y, 1);
+        g[5].x = __shfl_up_sync(XS_FULL, g[5].x, 1);
+        g[5].y = __shfl_up_sync(XS_FULL, g[5].y, 1);
+        g[7].x = __shfl_up_sync(XS_FULL, g[7].x, 1);
+        g[7].y = __shfl_up_sync(XS_FULL, g[7].y, 1);
+        g[2].x = __shfl_down_sync(XS_FULL, g[2].x, 1);
+        g[2].y = __shfl_down_sync(XS_FULL, g[2].y, 1);
+        g[6].x = __shfl_down_sync(XS_FULL, g[6].x, 1);
+        g[6].y = __shfl_down_sync(XS_FULL, g[6].y, 1);
+        g[8].x = __shfl_down_sync(XS_FULL, g[8].x, 1);
+        g[8].y = __shfl_down_sync(XS_FULL, g[8].y, 1);
+    };
+    auto gather = [](float2 g[9], const float o[9], const float n[9], const float p[9], const float q[9]) {
+        g[3] = make_float2(o[3], n[3]);
+        g[5] = make_float2(o[5], n[5]);
+        g[8] = make_float2(o[8], n[8]);
+        g[0] = make_float2(n[0], p[0]);
+        g[1] = make_float2(n[1], p[1]);
+        g[2] = make_float2(n[2], p[2]);
+        g[4] = make_float2(p[4], q[4]);
+        g[6] = make_float2(p[6], q[6]);
+        g[7] = make_float2(p[7], q[7]);
+    };
+    auto split = [](const float2 g[9], float x[9], float y[9]) {
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            x[i] = g[i].x;
+            y[i] = g[i].y;
+        }
+    };
+
+    float va[9], vb[9], ha[3] = {0.f, 0.f, 0.f}, hb[3] = {0.f, 0.f, 0.f};
+    float aA[9], aB[9], aC[9], aD[9];  // aligned P rows
+    float bA[9], bB[9];                // aligned P' rows (carried)
+    float cA[9], cB[9];                // aligned P'' rows (carried)
+    float2 g[9];
+    // prologue: P rows y0 - 3 .. y0 + 2; P' rows y0 - 2 .. y0 + 1; P'' rows y0 - 1, y0
+    {
+        float p0[9], p1[9], p2[9], p3[9], p4[9], p5[9];
+        load(y0 - 3, va, ha);
+        load(y0 - 2, vb, hb);
+        align(va, ha, p0);
+        align(vb, hb, p1);
+        load(y0 - 1, va, ha);
+        load(y0, vb, hb);
+        align(va, ha, p2);
+        align(vb, hb, p3);
+        load(y0 + 1, va, ha);
+        load(y0 + 2, vb, hb);
+        align(va, ha, p4);
+        align(vb, hb, p5);
+        load(y0 + 3, va, ha);
+        load(y0 + 4, vb, hb);
+        float q0[9], q1[9], q2[9], q3[9];
+        gather(g, p0, p1, p2, p3);  // P' rows y0 - 2, y0 - 1
+        shifted::collide9x2<OP>(g, k);
+        align2(g);
+        split(g, q0, q1);
+        gather(g, p2, p3, p4, p5);  // P' rows y0, y0 + 1
+        shifted::collide9x2<OP>(g, k);
+        align2(g);
+        split(g, q2, q3);
+        gather(g, q0, q1, q2, q3);  // P'' rows y0 - 1, y0
+        shifted::collide9x2<OP>(g, k);
+        align2(g);
+        split(g, cA, cB);
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            aA[i] = p4[i];
+            aB[i] = p5[i];
+            bA[i] = q2[i];
+            bB[i] = q3[i];
+        }
+    }
+    for (int j = y0; j < y1; j += 2) {
+        align(va, ha, aC);  // P row j + 3
+        align(vb, hb, aD);  // P row j + 4
+        if (j + 2 < y1) {
+            load(j + 5, va, ha);
+            load(j + 6, vb, hb);
+        }
+        float nA[9], nB[9], mA[9], mB[9];
+        gather(g, aA, aB, aC, aD);  // P' rows j + 2, j + 3
+        shifted::collide9x2<OP>(g, k);
+        align2(g);
+        split(g, nA, nB);
+        gather(g, bA, bB, nA, nB);  // P'' rows j + 1, j + 2
+        shifted::collide9x2<OP>(g, k);
+        align2(g);
+        split(g, mA, mB);
+        gather(g, cA, cB, mA, mB);  // output rows j, j + 1
+        shifted::collide9x2<OP>(g, k);
+        if (store) {
+            float *d0 = dst + (long long)j * nx + c, *d1 = d0 + nx;
+#pragma unroll
+            for (int i = 0; i < 9; i++) {
+                d0[i * plane] = g[i].x;
+                d1[i * plane] = g[i].y;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            aA[i] = aC[i];
+            aB[i] = aD[i];
+            bA[i] = nA[i];
+            bB[i] = nB[i];
+            cA[i] = mA[i];
+            cB[i] = mB[i];
+        }
+    }
+}
+
 }  // namespace
 
 bool periodic_d2q9_x2_ok(const Geo &g)
@@ -331,6 +501,51 @@ static void go_x2(const Geo &g, const shifted::Coef &k, const float *src, float 
     const int n_warps = strips * (int)((g.ny + hc - 1) / hc);
     const unsigned nb = (unsigned)((n_warps + 3) / 4);
     kern<<<nb, 128, 0, s>>>(src, dst, g.nx, g.ny, g.plane, (int)hc, strips, n_warps, k);
+}
+
+// Three-step launch: as go_x2, over ceil(nx / 28) strips.
+template <int OP>
+static void go_x3(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
+{
+    auto kern = k_periodic_d2q9_x3s<OP>;
+    constexpr int MAXDEV = 64;
+    static std::atomic<int> warps_cache[MAXDEV];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int d = dev >= 0 && dev < MAXDEV ? dev : 0;
+    int resident = warps_cache[d].load(std::memory_order_relaxed);
+    if (resident <= 0) {
+        int o = 0, n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, 128, 0) != cudaSuccess || o < 1) o = 1;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        resident = o * 4 * (n > 0 ? n : 1);
+        warps_cache[d].store(resident, std::memory_order_relaxed);
+    }
+    const int strips = (g.nx + X3_W - 1) / X3_W;
+    const long long slots = resident;
+    long long chunks = slots / strips;
+    if (chunks < 1) chunks = 1;
+    long long hc = (g.ny + chunks - 1) / chunks;
+    if (hc < 8) hc = 8;
+    hc += hc & 1;
+    if (hc > g.ny) hc = g.ny;
+    const int n_warps = strips * (int)((g.ny + hc - 1) / hc);
+    kern<<<(unsigned)((n_warps + 3) / 4), 128, 0, s>>>(src, dst, g.nx, g.ny, g.plane, (int)hc, strips, n_warps, k);
+}
+
+// Three steps of the fused periodic D2Q9 FP32 update in one launch (periodic_d2q9_x2_ok(g) required).
+int launch_periodic_d2q9_fp32_x3(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s)
+{
+    if (!periodic_d2q9_x2_ok(g)) return -1;
+    const shifted::Coef k = shifted::make_coef(R);
+    switch (op) {
+    case OP_BGK: go_x3<OP_BGK>(g, k, src, dst, s); break;
+    case OP_MRT: go_x3<OP_MRT>(g, k, src, dst, s); break;
+    case OP_REG: go_x3<OP_REG>(g, k, src, dst, s); break;
+    case OP_EXTREG: go_x3<OP_EXTREG>(g, k, src, dst, s); break;
+    default: return -1;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
 // Two steps of the fused periodic D2Q9 FP32 update in one launch (periodic_d2q9_x2_ok(g) required).

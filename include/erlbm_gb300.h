@@ -169,13 +169,17 @@ int erlbm_run(erlbm_handle *h, int n_steps, const erlbm_bc *bc, const erlbm_chec
 /* wait for the handle's queued work */
 int erlbm_sync(erlbm_handle *h);
 /* launch shape of the fused periodic D2Q9 FP32 kernel (the double-shear-layer lattices): threads per
- * block (128, 256, 512; 0 = default 256) and flags (ERLBM_LAUNCH_STREAMING_STORES: evict-first
- * stores; ERLBM_LAUNCH_TWO_STEP: pairs of consecutive steps run as one launch that keeps the
- * intermediate step in shared memory, where nx % 128 == 0 and ny is even -- the same results, half the
- * HBM traffic).
- * Chosen by erlbm_gb300.autotune; no counterpart in the reference. */
+ * block of the one-step kernel (128, 256, 512; 0 = default 256) and flags
+ *   ERLBM_LAUNCH_STREAMING_STORES  evict-first stores (one-step kernel);
+ *   ERLBM_LAUNCH_TWO_STEP          two consecutive steps per launch, the intermediate step kept on
+ *                                  chip (nx % 128 == 0, ny even): half the HBM traffic per update;
+ *   ERLBM_LAUNCH_THREE_STEP        three steps per launch (same conditions): a third of the traffic.
+ * The results are the same bits in every shape; at most one of the two multi-step flags.  Steps left
+ * over (fewer than a launch takes) run one at a time.  Chosen by erlbm_gb300.autotune; no
+ * counterpart in the reference. */
 #define ERLBM_LAUNCH_STREAMING_STORES 1
 #define ERLBM_LAUNCH_TWO_STEP 2
+#define ERLBM_LAUNCH_THREE_STEP 4
 int erlbm_set_launch(erlbm_handle *h, int block_threads, int flags);
 /* run the handle's work on the caller's CUDA stream (a cudaStream_t; NULL = the handle's own
  * stream).  Waits for the work queued so far first.  No counterpart in the reference, whose loops

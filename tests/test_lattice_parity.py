@@ -182,34 +182,37 @@ def test_run_energy_check_matches_oracle():
 
 @pytest.mark.parametrize("op", [1, 2, 3, 4])
 @pytest.mark.parametrize("L,steps", [(256, 17), (512, 40)])
-def test_two_step_kernel_equals_one_step(op, L, steps):
-    """Two steps per launch (the intermediate step kept in registers) give the one-step kernel's
-    populations bit for bit, for every operator and for odd step counts."""
+def test_multi_step_kernels_equal_one_step(op, L, steps):
+    """Two and three steps per launch (the intermediate steps kept in registers) give the one-step
+    kernel's populations bit for bit, for every operator and for step counts that leave remainders."""
     tau = 0.5 + 3 * (1 / 32) * L / 80000
     f0 = eg().init_double_shear(L)
     outs = []
-    for two in (False, True):
+    for per in (1, 2, 3):
         with eg().Lattice(9, L, L, 1, None, tau, 0.65, op, eg().FP32_SHIFTED) as lat:
-            lat.set_launch(256, False, two)
+            lat.set_launch(256, False, per == 2, per == 3)
             lat.set_populations(f0)
             lat.step(steps)
             lat.step(3)
+            lat.step(5)
             outs.append((lat.get_populations(0), lat.get_populations(1)))
-    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    for o in outs[1:]:
+        assert np.array_equal(outs[0][0], o[0]) and np.array_equal(outs[0][1], o[1])
 
 
-@pytest.mark.parametrize("two", [False, True])
-def test_graph_replay_equals_single_launches(two):
-    """Blocks of 64 plain periodic steps run as a replayed CUDA graph (captured once per buffer
-    parity); the populations equal those of the same steps launched one call at a time, also after a
-    parameter change (which drops the captured graphs) and a launch-shape change."""
+@pytest.mark.parametrize("per", [1, 2, 3])
+def test_graph_replay_equals_single_launches(per):
+    """Blocks of 64 (or, three steps per launch, 66) plain periodic steps run as a replayed CUDA graph
+    (captured once per buffer parity); the populations equal those of the same steps launched one call
+    at a time, also after a parameter change (which drops the captured graphs) and a launch-shape
+    change."""
     L = 256
     f0 = eg().init_double_shear(L)
     tau1, tau2 = 0.5 + 3 * (1 / 32) * L / 80000, 0.56
     outs = []
     for blocks in (True, False):
         with eg().Lattice(9, L, L, 1, None, tau1, 0.65, eg().OP_EXTREG, eg().FP32_SHIFTED) as lat:
-            lat.set_launch(256, False, two)
+            lat.set_launch(256, False, per == 2, per == 3)
             lat.set_populations(f0)
             run = (lambda n: lat.step(n)) if blocks else (lambda n: [lat.step(1) for _ in range(n)])
             run(1)
@@ -218,29 +221,30 @@ def test_graph_replay_equals_single_launches(two):
             lat.set_params(tau2, 0.65, eg().OP_REG)
             run(70)
             b = lat.get_populations(1)
-            lat.set_launch(128, False, not two)
-            run(128)
+            lat.set_launch(128, False, per == 1, per == 2)
+            run(140)
             outs.append((a, b, lat.get_populations(1), lat.get_populations(0)))
     for x, y in zip(outs[0], outs[1]):
         assert np.array_equal(x, y)
 
 
 @pytest.mark.parametrize("nx,ny", [(128, 4), (128, 6), (384, 10), (128, 130), (640, 258)])
-def test_two_step_kernel_equals_one_step_on_uneven_strips(nx, ny):
-    """The two-step kernel's warp strips are 30 columns wide, so nx = 128, 384 and 640 end in a
-    partial strip; its chunks of rows are clamped at small ny.  Random near-equilibrium populations,
-    every wrap of the periodic box exercised: the one-step kernel's bits after an odd step count."""
+def test_multi_step_kernels_equal_one_step_on_uneven_strips(nx, ny):
+    """The two- and three-step kernels' warp strips are 30 and 28 columns wide, so nx = 128, 384 and 640
+    end in a partial strip; their chunks of rows are clamped at small ny.  Random near-equilibrium
+    populations, every wrap of the periodic box exercised: the one-step kernel's bits after ten steps,
+    which leave a remainder in both shapes."""
     rng = np.random.default_rng(nx * 1000 + ny)
     w = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
     f0 = (w[None, :] * (1.0 + 0.05 * rng.standard_normal((nx * ny, 9)))).ravel()
     outs = []
-    for two in (False, True):
+    for per in (1, 2, 3):
         with eg().Lattice(9, nx, ny, 1, None, 0.53, 0.65, eg().OP_EXTREG, eg().FP32_SHIFTED) as lat:
-            lat.set_launch(128, False, two)
+            lat.set_launch(128, False, per == 2, per == 3)
             lat.set_populations(f0)
-            lat.step(9)
+            lat.step(10)
             outs.append(lat.get_populations(0))
-    assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
 
 
 def test_fused_kernel_launch_shapes_identical_and_tuned(tmp_path, monkeypatch):
@@ -251,18 +255,21 @@ def test_fused_kernel_launch_shapes_identical_and_tuned(tmp_path, monkeypatch):
     f0 = eg().init_double_shear(L)
     tau = 0.5 + 3 * (1 / 32) * L / 80000
     outs = []
-    shapes = [(b, s, False) for b, s in autotune.PERIODIC_CANDIDATES] + \
-        [(b, s, True) for b, s in autotune.TWO_STEP_CANDIDATES]
-    for block, st, two in shapes:
+    shapes = [(b, s, 1) for b, s in autotune.PERIODIC_CANDIDATES] + list(autotune.MULTI_STEP_CANDIDATES)
+    for block, st, per in shapes:
         with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
-            lat.set_launch(block, st, two)
+            lat.set_launch(block, st, per == 2, per == 3)
             lat.set_populations(f0)
-            lat.step(30)  # 1 local step, then 29: fourteen two-step launches and one single step
+            lat.step(30)  # 1 local step, then 29 as multi-step launches and single steps
             outs.append(lat.get_populations(1))
     assert all(np.array_equal(o, outs[0]) for o in outs[1:])
     best = autotune.tune_periodic(L, steps=50)
-    assert (best["block_threads"], best["streaming_stores"], best["two_step"]) in shapes
+    per = 3 if best["three_step"] else (2 if best["two_step"] else 1)
+    assert (best["block_threads"], best["streaming_stores"], per) in shapes
     assert autotune.tune_periodic(L)["mlups"] == best["mlups"]  # served from the cache
+    with pytest.raises(eg().ErlbmError):  # two and three steps per launch at once
+        with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
+            lat.set_launch(128, False, True, True)
     with pytest.raises(eg().ErlbmError):
         with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
             lat.set_launch(100)
