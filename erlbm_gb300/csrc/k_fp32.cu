@@ -300,8 +300,10 @@ __global__ void __launch_bounds__(128) k_periodic_d2q9_x2s(const float *__restri
 // iteration ahead.  Each node is read and written once per three steps (24 bytes per update).
 constexpr int X3_W = 28;
 
+// Four resident CTAs per SM: the register cap (128) spills 8 bytes, and 16 warps per SM instead of
+// 12 run 4 % faster on GB300 (158.6 against 151.9 G LU/s at L = 2048).
 template <int OP>
-__global__ void __launch_bounds__(128) k_periodic_d2q9_x3s(const float *__restrict__ src, float *__restrict__ dst,
+__global__ void __launch_bounds__(128, 4) k_periodic_d2q9_x3s(const float *__restrict__ src, float *__restrict__ dst,
                                                           int nx, int ny, long long plane, int hc, int strips,
                                                           int n_warps, shifted::Coef k)
 {
