@@ -149,3 +149,15 @@ def test_channel_bench_geometry_fits_the_parabolic_inlet():
         assert nx == 4 * ny and s[:, 0].all() and s[:, -1].all() and s[0, :].all() and s[-1, :].all()
         assert (1 - s).sum(axis=0).max() == ny - 2
         assert s[ny // 2, ny] == 1 and s[ny // 2, 2 * ny] == 0  # the cylinder, and open channel behind it
+
+
+def test_bench_launch_count_follows_erlbm_step():
+    """bench.py's launch count per call of n steps: graph blocks of 64 steps (66 with three steps per
+    launch), then multi-step launches, then single steps -- the decomposition erlbm_step makes."""
+    import bench
+    assert bench.launches_of(1000, 1) == 1000
+    assert bench.launches_of(1000, 2) == 500
+    assert bench.launches_of(1000, 3) == 15 * 22 + 3 + 1  # 990 in graphs, 9 in three launches, 1 single
+    assert bench.launches_of(999, 3) == 15 * 22 + 3
+    assert bench.launches_of(65, 2) == 32 + 1
+    assert bench.launches_of(2, 3) == 2
