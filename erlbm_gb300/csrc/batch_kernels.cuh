@@ -6,10 +6,11 @@
 // obstacle map :75-123) on its own populations.
 //
 // Layout.  One CTA owns one lattice "slot": the whole lattice (nx * ny <= NPT * blockDim nodes,
-// nz = 1) lives in shared memory as one SoA buffer buf[i * NB + node].  A step is
-//   gather (pull; bounce-back from the solid mask) into registers -> barrier ->
-//   [energy check] -> boundary planes -> collide -> [density check] -> write own nodes -> barrier,
-// so one buffer suffices.  When a run ends (budget reached, or a check failed), thread 0 claims the
+// nz = 1) lives in shared memory as SoA, buf[i * NB + node].  A step is
+//   gather (pull; bounce-back from the solid mask) into registers -> [barrier] ->
+//   [energy check] -> boundary planes -> collide -> [density check] -> write own nodes -> barrier.
+// Where two buffers fit (dbl), the step reads one and writes the other, and the barrier after the
+// gather is not needed; otherwise one buffer is updated in place.  When a run ends (budget reached, or a check failed), thread 0 claims the
 // next run index from a global counter and the slot is refilled: the launch is persistent, with
 // grid = SMs x resident CTAs, and the host orders runs longest-first so the tail is short.
 //
