@@ -13,7 +13,8 @@
 //   f* = f + [delta d - 2 d],  delta = 2 - 1/tau           (BGK)
 //
 // Each opposite pair (i, j) is split into an even part e = (g_i + g_j)/2 and an odd part
-// o = (g_i - g_j)/2 (both exact).  Then
+// o = (g_i - g_j)/2 (both exact; the D2Q9 update carries them, and the non-equilibrium parts, at twice
+// this scale, which rounds identically and saves the scalings).  Then
 //   drho = g_0 + 2 sum e,   m = 2 sum c o,   u = m / (1 + drho),
 //   non-equilibrium even part  de = e - w (drho + 4.5 (c.m)(c.u) - 1.5 m.u),
 //   non-equilibrium odd part   do = o - 3 w (c.m),
@@ -124,42 +125,43 @@ __device__ __forceinline__ typename M::V update_rest_l(typename M::V g0, typenam
     return M::add(g0, M::fma(d1, f10, M::fma(M::c(k.kd), M::sub(de0, f10), M::mul(m2, f10))));
 }
 
+// The D2Q9 update with the pair sums and differences kept at twice their scale: E = g_i + g_j = 2e,
+// O = g_i - g_j = 2o, and the non-equilibrium parts D = 2 de, DO = 2 do.  Scaling by 2 or 1/2 is exact
+// in binary floating point (the magnitudes here are far from the subnormal range), so every rounded
+// operation below yields exactly twice (or, for the moments, exactly) what the half-scale form yields:
+// the same bits with 13 multiplications fewer.  The final 1/2 is folded into the fma that consumes D.
 template <class M, int OP>
 __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
 {
     using V = typename M::V;
     constexpr float W1 = 1.f / 9.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
-    const V half = M::c(0.5f), two = M::c(2.f);
-    const V eX = M::mul(half, M::add(g[1], g[2])), oX = M::mul(half, M::sub(g[1], g[2]));
-    const V eY = M::mul(half, M::add(g[3], g[4])), oY = M::mul(half, M::sub(g[3], g[4]));
-    const V eP = M::mul(half, M::add(g[5], g[6])), oP = M::mul(half, M::sub(g[5], g[6]));
-    const V eM = M::mul(half, M::add(g[7], g[8])), oM = M::mul(half, M::sub(g[7], g[8]));
-    const V drho = M::fma(two, M::add(M::add(eX, eY), M::add(eP, eM)), g[0]);
-    const V mx = M::mul(two, M::add(oX, M::add(oP, oM)));
-    const V my = M::mul(two, M::add(oY, M::sub(oP, oM)));
+    const V half = M::c(0.5f), two = M::c(2.f), mhalf = M::c(-0.5f);
+    const V EX = M::add(g[1], g[2]), OX = M::sub(g[1], g[2]);
+    const V EY = M::add(g[3], g[4]), OY = M::sub(g[3], g[4]);
+    const V EP = M::add(g[5], g[6]), OP_ = M::sub(g[5], g[6]);
+    const V EM = M::add(g[7], g[8]), OM = M::sub(g[7], g[8]);
+    const V drho = M::add(M::add(M::add(EX, EY), M::add(EP, EM)), g[0]);
+    const V mx = M::add(OX, M::add(OP_, OM));
+    const V my = M::add(OY, M::sub(OP_, OM));
     const V inv = M::rcp(M::add(M::c(1.f), drho));
     const V ux = M::mul(mx, inv), uy = M::mul(my, inv);
     const V mu15 = M::mul(M::c(-1.5f), M::fma(mx, ux, M::mul(my, uy)));
-    const V k45 = M::c(4.5f), mw1 = M::c(-W1), mw2 = M::c(-W2);
-    // even non-equilibrium parts
-    const V deX = M::fma(mw1, M::fma(M::mul(k45, mx), ux, mu15), M::fma(mw1, drho, eX));
-    const V deY = M::fma(mw1, M::fma(M::mul(k45, my), uy, mu15), M::fma(mw1, drho, eY));
+    const V k45 = M::c(4.5f), mw1x2 = M::c(-2.f * W1), mw2x2 = M::c(-2.f * W2);
+    // twice the even non-equilibrium parts
+    const V DX = M::fma(mw1x2, M::fma(M::mul(k45, mx), ux, mu15), M::fma(mw1x2, drho, EX));
+    const V DY = M::fma(mw1x2, M::fma(M::mul(k45, my), uy, mu15), M::fma(mw1x2, drho, EY));
     const V cmP = M::add(mx, my), cmM = M::sub(mx, my);
-    const V deP = M::fma(mw2, M::fma(M::mul(k45, cmP), M::add(ux, uy), mu15), M::fma(mw2, drho, eP));
-    const V deM = M::fma(mw2, M::fma(M::mul(k45, cmM), M::sub(ux, uy), mu15), M::fma(mw2, drho, eM));
-    const V de0 = M::mul(M::c(-2.f), M::add(M::add(deX, deY), M::add(deP, deM)));
-    // odd non-equilibrium parts; the axis pairs close the momentum
-    const V doP = M::fma(M::c(M3W2), cmP, oP);
-    const V doM = M::fma(M::c(M3W2), cmM, oM);
-    const V doX = M::neg(M::add(doP, doM));
-    const V doY = M::neg(M::sub(doP, doM));
+    const V DP = M::fma(mw2x2, M::fma(M::mul(k45, cmP), M::add(ux, uy), mu15), M::fma(mw2x2, drho, EP));
+    const V DM = M::fma(mw2x2, M::fma(M::mul(k45, cmM), M::sub(ux, uy), mu15), M::fma(mw2x2, drho, EM));
+    const V de0 = M::neg(M::add(M::add(DX, DY), M::add(DP, DM)));
+    // twice the odd non-equilibrium parts; the axis pairs close the momentum
+    const V DOP = M::fma(M::c(2.f * M3W2), cmP, OP_);
+    const V DOM = M::fma(M::c(2.f * M3W2), cmM, OM);
+    const V DOX = M::neg(M::add(DOP, DOM));
+    const V DOY = M::neg(M::sub(DOP, DOM));
     if constexpr (OP == OP_MRT) {
-        // coll_MRT (Collision_operators.cpp:583-699) as an increment on the non-equilibrium part n:
-        // f* = f - M^-1 S M n.  With A = deX + deY, B = deP + deM and the closed parts substituted,
-        // the relaxed moments of n are e = 6A + 12B, eps = -12A - 6B, qx = 6 (doP + doM),
-        // qy = 6 (doP - doM), pxx = 2 (deX - deY), pxy = 2 (deP - deM); back through M^-1 the odd
-        // parts relax with s_q alone, and the even parts take hE = s_e e / 36, hP = s_eps eps / 36 and
-        // the shear part, written with delta = 2 - 1/tau as s_nu x / 2 = x - delta x / 2.
+        const V deX = M::mul(half, DX), deY = M::mul(half, DY), deP = M::mul(half, DP), deM = M::mul(half, DM);
+        const V doP = M::mul(half, DOP), doM = M::mul(half, DOM);
         const V A = M::add(deX, deY), B = M::add(deP, deM);
         const V hE = M::mul(M::c((float)(MRT9_SE / 6.0)), M::fma(two, B, A));
         const V hP = M::mul(M::c((float)(MRT9_SEPS / 6.0)), M::fma(M::c(-2.f), A, M::neg(B)));
@@ -182,24 +184,43 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
         g[8] = M::add(g[8], M::sub(xM, qM));
         return;
     }
-    V f10 = M::c(0.f), f1X = M::c(0.f), f1Y = M::c(0.f), f1P = M::c(0.f), f1M = M::c(0.f);
-    if (OP != OP_BGK) {
-        const V pxx = M::mul(two, M::add(deX, M::add(deP, deM)));
-        const V pyy = M::mul(two, M::add(deY, M::add(deP, deM)));
-        const V pxy = M::mul(two, M::sub(deP, deM));
-        const V tr = M::add(pxx, pyy);
-        f10 = M::mul(M::c(-2.f / 3.f), tr);
-        f1X = M::fma(pxx, M::c(1.f / 3.f), M::mul(pyy, M::c(-1.f / 6.f)));
-        f1Y = M::fma(pyy, M::c(1.f / 3.f), M::mul(pxx, M::c(-1.f / 6.f)));
-        const V t12 = M::mul(tr, M::c(1.f / 12.f));
-        f1P = M::fma(pxy, M::c(0.25f), t12);
-        f1M = M::fma(pxy, M::c(-0.25f), t12);
+    const V d1 = M::c(k.d1), m2 = M::c(-2.f);
+    if constexpr (OP == OP_BGK) {
+        // di = de + do = (D + DO) / 2; the increment d1 di - 2 di is half of d1 DI - 2 DI
+        auto upd = [&](V &gi, V &gj, V D, V DO) {
+            const V DI = M::add(D, DO), DJ = M::sub(D, DO);
+            gi = M::fma(half, M::fma(d1, DI, M::mul(m2, DI)), gi);
+            gj = M::fma(half, M::fma(d1, DJ, M::mul(m2, DJ)), gj);
+        };
+        g[0] = M::add(g[0], M::fma(d1, de0, M::mul(m2, de0)));
+        upd(g[1], g[2], DX, DOX);
+        upd(g[3], g[4], DY, DOY);
+        upd(g[5], g[6], DP, DOP);
+        upd(g[7], g[8], DM, DOM);
+        return;
     }
-    g[0] = update_rest_l<M, OP>(g[0], de0, f10, k);
-    update_pair_l<M, OP>(g[1], g[2], deX, doX, f1X, k);
-    update_pair_l<M, OP>(g[3], g[4], deY, doY, f1Y, k);
-    update_pair_l<M, OP>(g[5], g[6], deP, doP, f1P, k);
-    update_pair_l<M, OP>(g[7], g[8], deM, doM, f1M, k);
+    const V pxx = M::add(DX, M::add(DP, DM));
+    const V pyy = M::add(DY, M::add(DP, DM));
+    const V pxy = M::sub(DP, DM);
+    const V tr = M::add(pxx, pyy);
+    const V f10 = M::mul(M::c(-2.f / 3.f), tr);
+    const V f1X = M::fma(pxx, M::c(1.f / 3.f), M::mul(pyy, M::c(-1.f / 6.f)));
+    const V f1Y = M::fma(pyy, M::c(1.f / 3.f), M::mul(pxx, M::c(-1.f / 6.f)));
+    const V t12 = M::mul(tr, M::c(1.f / 12.f));
+    const V f1P = M::fma(pxy, M::c(0.25f), t12);
+    const V f1M = M::fma(pxy, M::c(-0.25f), t12);
+    const V kd = M::c(k.kd);
+    // a = de - f1 = D / 2 - f1; a +- do = a +- DO / 2 (one rounding each, as before)
+    auto upd = [&](V &gi, V &gj, V D, V DO, V f1) {
+        const V a = M::fma(half, D, M::neg(f1)), t = M::mul(m2, f1);
+        gi = M::add(gi, M::fma(d1, f1, M::fma(kd, M::fma(half, DO, a), t)));
+        gj = M::add(gj, M::fma(d1, f1, M::fma(kd, M::fma(mhalf, DO, a), t)));
+    };
+    g[0] = M::add(g[0], M::fma(d1, f10, M::fma(kd, M::sub(de0, f10), M::mul(m2, f10))));
+    upd(g[1], g[2], DX, DOX, f1X);
+    upd(g[3], g[4], DY, DOY, f1Y);
+    upd(g[5], g[6], DP, DOP, f1P);
+    upd(g[7], g[8], DM, DOM, f1M);
 }
 
 template <int OP>
