@@ -106,26 +106,18 @@ __device__ __forceinline__ void batch_collide(typename P::T *f, const BatchRun &
 template <int Q>
 __device__ __forceinline__ void batch_collide_pair(float *fa, float *fb, const BatchRun &r)
 {
+    static_assert(Q == 9, "packed pairs are used for D2Q9");
     float2 g[Q];
 #pragma unroll
     for (int i = 0; i < Q; i++) g[i] = make_float2(fa[i], fb[i]);
-    if constexpr (Q == 19) {
-        if (r.op == OP_BGK)
-            shifted::collide19l<shifted::LaneF2, OP_BGK>(g, r.k);
-        else if (r.op == OP_REG)
-            shifted::collide19l<shifted::LaneF2, OP_REG>(g, r.k);
-        else
-            shifted::collide19l<shifted::LaneF2, OP_EXTREG>(g, r.k);
-    } else {
-        if (r.op == OP_MRT)
-            shifted::collide9x2<OP_MRT>(g, r.k);
-        else if (r.op == OP_BGK)
-            shifted::collide9x2<OP_BGK>(g, r.k);
-        else if (r.op == OP_REG)
-            shifted::collide9x2<OP_REG>(g, r.k);
-        else
-            shifted::collide9x2<OP_EXTREG>(g, r.k);
-    }
+    if (r.op == OP_MRT)
+        shifted::collide9x2<OP_MRT>(g, r.k);
+    else if (r.op == OP_BGK)
+        shifted::collide9x2<OP_BGK>(g, r.k);
+    else if (r.op == OP_REG)
+        shifted::collide9x2<OP_REG>(g, r.k);
+    else
+        shifted::collide9x2<OP_EXTREG>(g, r.k);
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         fa[i] = g[i].x;
@@ -277,9 +269,7 @@ __device__ inline void make_order(const BatchGeo &g, short *order, int *n_fluid,
 
 // One run of one lattice by the whole CTA.  sm.solid must hold the geometry's mask.  The result is
 // returned to every thread.
-// PK19: D3Q19 node pairs in packed FP32x2 too (faster for the Taylor-Green map's periodic lattices,
-// slower for the obstacle channel, whose runs check the density every step).
-template <class P, int Q, int NPT, bool PK19 = false>
+template <class P, int Q, int NPT>
 __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const BatchSmem<P, Q> &sm,
                                      const double *__restrict__ aos)
 {
@@ -427,9 +417,11 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
                 P::zou_he(f[s], *reinterpret_cast<const ZH *>(sm.zh), g.inlet_x < g.nx / 2);
             }
         }
-        // FP32: the nodes of a thread in pairs, in packed FP32x2 instructions (D2Q9 always; D3Q19 when
-        // the launch asks for it, see PK19)
-        constexpr bool PAIRS = sizeof(T) == 4 && NPT % 2 == 0 && (Q == 9 || PK19);
+        // FP32: the nodes of a thread in pairs, in packed FP32x2 instructions (D2Q9).  The D3Q19 pairs
+        // collide one after the other: the packed D3Q19 form measured 5 % faster on the Taylor-Green
+        // map but did not reproduce the scalar form's bits (final energies 3.5e-7 apart after 1500
+        // steps), and the scalar form is the one every other FP32 D3Q19 path uses.
+        constexpr bool PAIRS = sizeof(T) == 4 && NPT % 2 == 0 && Q == 9;
         if constexpr (PAIRS) {
 #pragma unroll
             for (int s = 0; s < NPT; s += 2) {
@@ -506,7 +498,7 @@ __device__ BatchResult batch_one_run(const BatchGeo &g, const BatchRun &r, const
     return o;
 }
 
-template <class P, int Q, int NPT, bool PK19 = false>
+template <class P, int Q, int NPT>
 __global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
                                   BatchBounds<NPT, sizeof(typename P::T)>::MINB)
     k_batch(BatchGeo g, const BatchRun *__restrict__ runs, int n_runs, int *__restrict__ counter,
@@ -526,7 +518,7 @@ __global__ void __launch_bounds__(BatchBounds<NPT, sizeof(typename P::T)>::MAXT,
         const int ri = s_run;
         if (ri >= n_runs) break;
         const BatchRun r = runs[ri];
-        const BatchResult o = batch_one_run<P, Q, NPT, PK19>(g, r, sm, aos);
+        const BatchResult o = batch_one_run<P, Q, NPT>(g, r, sm, aos);
         if (tid == 0) res[r.out] = o;
     }
 }

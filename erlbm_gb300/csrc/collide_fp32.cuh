@@ -95,24 +95,26 @@ struct LaneF2 {
     static __device__ __forceinline__ V rcp(V a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
 };
 
-// Update of one opposite pair from its even/odd non-equilibrium parts (de, do) and f1, and of the
-// rest population.  The increment is formed from the small quantities first and added to the stored
-// population once, so only that last addition rounds at the scale of g.
+// Update of one opposite pair from twice its even/odd non-equilibrium parts, D = 2 de and DO = 2 do,
+// and f1: the increment is formed from the small quantities first and added to the stored population
+// once, so only that last addition rounds at the scale of g.  The halving of D and DO is folded into
+// the fma that consumes them, which rounds exactly as the half-scale form would.  The rest population
+// (update_rest_l) takes its parts at their own scale.
 template <class M, int OP>
-__device__ __forceinline__ void update_pair_l(typename M::V &gi, typename M::V &gj, typename M::V de,
-                                              typename M::V dO, typename M::V f1, const Coef &k)
+__device__ __forceinline__ void update_pair2_l(typename M::V &gi, typename M::V &gj, typename M::V D,
+                                               typename M::V DO, typename M::V f1, const Coef &k)
 {
     using V = typename M::V;
-    const V d1 = M::c(k.d1), m2 = M::c(-2.f);
+    const V d1 = M::c(k.d1), m2 = M::c(-2.f), half = M::c(0.5f);
     if (OP == OP_BGK) {
-        const V di = M::add(de, dO), dj = M::sub(de, dO);
-        gi = M::add(gi, M::fma(d1, di, M::mul(m2, di)));
-        gj = M::add(gj, M::fma(d1, dj, M::mul(m2, dj)));
+        const V DI = M::add(D, DO), DJ = M::sub(D, DO);
+        gi = M::fma(half, M::fma(d1, DI, M::mul(m2, DI)), gi);
+        gj = M::fma(half, M::fma(d1, DJ, M::mul(m2, DJ)), gj);
     } else {
         const V kd = M::c(k.kd);
-        const V a = M::sub(de, f1), t = M::mul(m2, f1);
-        gi = M::add(gi, M::fma(d1, f1, M::fma(kd, M::add(a, dO), t)));
-        gj = M::add(gj, M::fma(d1, f1, M::fma(kd, M::sub(a, dO), t)));
+        const V a = M::fma(half, D, M::neg(f1)), t = M::mul(m2, f1);
+        gi = M::add(gi, M::fma(d1, f1, M::fma(kd, M::fma(half, DO, a), t)));
+        gj = M::add(gj, M::fma(d1, f1, M::fma(kd, M::fma(M::c(-0.5f), DO, a), t)));
     }
 }
 
@@ -135,7 +137,7 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
 {
     using V = typename M::V;
     constexpr float W1 = 1.f / 9.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
-    const V half = M::c(0.5f), two = M::c(2.f), mhalf = M::c(-0.5f);
+    const V half = M::c(0.5f), two = M::c(2.f);
     const V EX = M::add(g[1], g[2]), OX = M::sub(g[1], g[2]);
     const V EY = M::add(g[3], g[4]), OY = M::sub(g[3], g[4]);
     const V EP = M::add(g[5], g[6]), OP_ = M::sub(g[5], g[6]);
@@ -184,19 +186,13 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
         g[8] = M::add(g[8], M::sub(xM, qM));
         return;
     }
-    const V d1 = M::c(k.d1), m2 = M::c(-2.f);
+    const V zero = M::c(0.f);
     if constexpr (OP == OP_BGK) {
-        // di = de + do = (D + DO) / 2; the increment d1 di - 2 di is half of d1 DI - 2 DI
-        auto upd = [&](V &gi, V &gj, V D, V DO) {
-            const V DI = M::add(D, DO), DJ = M::sub(D, DO);
-            gi = M::fma(half, M::fma(d1, DI, M::mul(m2, DI)), gi);
-            gj = M::fma(half, M::fma(d1, DJ, M::mul(m2, DJ)), gj);
-        };
-        g[0] = M::add(g[0], M::fma(d1, de0, M::mul(m2, de0)));
-        upd(g[1], g[2], DX, DOX);
-        upd(g[3], g[4], DY, DOY);
-        upd(g[5], g[6], DP, DOP);
-        upd(g[7], g[8], DM, DOM);
+        g[0] = update_rest_l<M, OP>(g[0], de0, zero, k);
+        update_pair2_l<M, OP>(g[1], g[2], DX, DOX, zero, k);
+        update_pair2_l<M, OP>(g[3], g[4], DY, DOY, zero, k);
+        update_pair2_l<M, OP>(g[5], g[6], DP, DOP, zero, k);
+        update_pair2_l<M, OP>(g[7], g[8], DM, DOM, zero, k);
         return;
     }
     const V pxx = M::add(DX, M::add(DP, DM));
@@ -209,18 +205,11 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
     const V t12 = M::mul(tr, M::c(1.f / 12.f));
     const V f1P = M::fma(pxy, M::c(0.25f), t12);
     const V f1M = M::fma(pxy, M::c(-0.25f), t12);
-    const V kd = M::c(k.kd);
-    // a = de - f1 = D / 2 - f1; a +- do = a +- DO / 2 (one rounding each, as before)
-    auto upd = [&](V &gi, V &gj, V D, V DO, V f1) {
-        const V a = M::fma(half, D, M::neg(f1)), t = M::mul(m2, f1);
-        gi = M::add(gi, M::fma(d1, f1, M::fma(kd, M::fma(half, DO, a), t)));
-        gj = M::add(gj, M::fma(d1, f1, M::fma(kd, M::fma(mhalf, DO, a), t)));
-    };
-    g[0] = M::add(g[0], M::fma(d1, f10, M::fma(kd, M::sub(de0, f10), M::mul(m2, f10))));
-    upd(g[1], g[2], DX, DOX, f1X);
-    upd(g[3], g[4], DY, DOY, f1Y);
-    upd(g[5], g[6], DP, DOP, f1P);
-    upd(g[7], g[8], DM, DOM, f1M);
+    g[0] = update_rest_l<M, OP>(g[0], de0, f10, k);
+    update_pair2_l<M, OP>(g[1], g[2], DX, DOX, f1X, k);
+    update_pair2_l<M, OP>(g[3], g[4], DY, DOY, f1Y, k);
+    update_pair2_l<M, OP>(g[5], g[6], DP, DOP, f1P, k);
+    update_pair2_l<M, OP>(g[7], g[8], DM, DOM, f1M, k);
 }
 
 template <int OP>
@@ -259,60 +248,61 @@ __device__ __forceinline__ void moments19(const float g[19], float &drho, float 
 }
 
 // The D3Q19 update in lane arithmetic (explicitly rounded operations).
+// The D3Q19 update with the pair sums, differences and non-equilibrium parts at twice their scale,
+// as the D2Q9 one: the same bits, 28 multiplications fewer.
 template <class M, int OP>
 __device__ __forceinline__ void collide19l(typename M::V g[19], const Coef &k)
 {
     using V = typename M::V;
     constexpr float W1 = 1.f / 18.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
-    const V half = M::c(0.5f), two = M::c(2.f);
-    const V eX = M::mul(half, M::add(g[1], g[2])), oX = M::mul(half, M::sub(g[1], g[2]));
-    const V eY = M::mul(half, M::add(g[3], g[4])), oY = M::mul(half, M::sub(g[3], g[4]));
-    const V eZ = M::mul(half, M::add(g[5], g[6])), oZ = M::mul(half, M::sub(g[5], g[6]));
-    const V eA = M::mul(half, M::add(g[7], g[8])), oA = M::mul(half, M::sub(g[7], g[8]));
-    const V eB = M::mul(half, M::add(g[9], g[10])), oB = M::mul(half, M::sub(g[9], g[10]));
-    const V eC = M::mul(half, M::add(g[11], g[12])), oC = M::mul(half, M::sub(g[11], g[12]));
-    const V eD = M::mul(half, M::add(g[13], g[14])), oD = M::mul(half, M::sub(g[13], g[14]));
-    const V eE = M::mul(half, M::add(g[16], g[15])), oE = M::mul(half, M::sub(g[16], g[15]));
-    const V eF = M::mul(half, M::add(g[17], g[18])), oF = M::mul(half, M::sub(g[17], g[18]));
-    const V drho = M::fma(two, M::add(M::add(M::add(eX, eY), M::add(eZ, eA)),
-                                      M::add(M::add(eB, eC), M::add(eD, M::add(eE, eF)))), g[0]);
-    const V mx = M::mul(two, M::add(M::add(oX, M::add(oA, oB)), M::add(oC, oD)));
-    const V my = M::mul(two, M::add(M::add(oY, M::sub(oA, oB)), M::sub(oE, oF)));
-    const V mz = M::mul(two, M::add(M::add(oZ, M::sub(oC, oD)), M::add(oE, oF)));
+    const V EX = M::add(g[1], g[2]), OX = M::sub(g[1], g[2]);
+    const V EY = M::add(g[3], g[4]), OY = M::sub(g[3], g[4]);
+    const V EZ = M::add(g[5], g[6]), OZ = M::sub(g[5], g[6]);
+    const V EA = M::add(g[7], g[8]), OA = M::sub(g[7], g[8]);
+    const V EB = M::add(g[9], g[10]), OB = M::sub(g[9], g[10]);
+    const V EC = M::add(g[11], g[12]), OC = M::sub(g[11], g[12]);
+    const V ED = M::add(g[13], g[14]), OD = M::sub(g[13], g[14]);
+    const V EE = M::add(g[16], g[15]), OE = M::sub(g[16], g[15]);
+    const V EF = M::add(g[17], g[18]), OF = M::sub(g[17], g[18]);
+    const V drho = M::add(M::add(M::add(M::add(EX, EY), M::add(EZ, EA)),
+                                 M::add(M::add(EB, EC), M::add(ED, M::add(EE, EF)))), g[0]);
+    const V mx = M::add(M::add(OX, M::add(OA, OB)), M::add(OC, OD));
+    const V my = M::add(M::add(OY, M::sub(OA, OB)), M::sub(OE, OF));
+    const V mz = M::add(M::add(OZ, M::sub(OC, OD)), M::add(OE, OF));
     const V inv = M::rcp(M::add(M::c(1.f), drho));
     const V ux = M::mul(mx, inv), uy = M::mul(my, inv), uz = M::mul(mz, inv);
     const V mu15 = M::mul(M::c(-1.5f), M::fma(mx, ux, M::fma(my, uy, M::mul(mz, uz))));
-    const V mw1 = M::c(-W1), mw2 = M::c(-W2), k45 = M::c(4.5f);
-    const V r1 = M::mul(mw1, drho), r2 = M::mul(mw2, drho);
-    const V deX = M::fma(mw1, M::fma(M::mul(k45, mx), ux, mu15), M::add(eX, r1));
-    const V deY = M::fma(mw1, M::fma(M::mul(k45, my), uy, mu15), M::add(eY, r1));
-    const V deZ = M::fma(mw1, M::fma(M::mul(k45, mz), uz, mu15), M::add(eZ, r1));
+    const V mw1x2 = M::c(-2.f * W1), mw2x2 = M::c(-2.f * W2), k45 = M::c(4.5f);
+    const V R1 = M::mul(mw1x2, drho), R2 = M::mul(mw2x2, drho);
+    const V DX = M::fma(mw1x2, M::fma(M::mul(k45, mx), ux, mu15), M::add(EX, R1));
+    const V DY = M::fma(mw1x2, M::fma(M::mul(k45, my), uy, mu15), M::add(EY, R1));
+    const V DZ = M::fma(mw1x2, M::fma(M::mul(k45, mz), uz, mu15), M::add(EZ, R1));
     const V cmA = M::add(mx, my), cmB = M::sub(mx, my), cmC = M::add(mx, mz), cmD = M::sub(mx, mz);
     const V cmE = M::add(my, mz), cmF = M::sub(mz, my);
-    const V deA = M::fma(mw2, M::fma(M::mul(k45, cmA), M::add(ux, uy), mu15), M::add(eA, r2));
-    const V deB = M::fma(mw2, M::fma(M::mul(k45, cmB), M::sub(ux, uy), mu15), M::add(eB, r2));
-    const V deC = M::fma(mw2, M::fma(M::mul(k45, cmC), M::add(ux, uz), mu15), M::add(eC, r2));
-    const V deD = M::fma(mw2, M::fma(M::mul(k45, cmD), M::sub(ux, uz), mu15), M::add(eD, r2));
-    const V deE = M::fma(mw2, M::fma(M::mul(k45, cmE), M::add(uy, uz), mu15), M::add(eE, r2));
-    const V deF = M::fma(mw2, M::fma(M::mul(k45, cmF), M::sub(uz, uy), mu15), M::add(eF, r2));
-    const V de0 = M::mul(M::c(-2.f), M::add(M::add(M::add(deX, deY), M::add(deZ, deA)),
-                                             M::add(M::add(deB, deC), M::add(deD, M::add(deE, deF)))));
-    const V m3w2 = M::c(M3W2);
-    const V doA = M::fma(m3w2, cmA, oA), doB = M::fma(m3w2, cmB, oB);
-    const V doC = M::fma(m3w2, cmC, oC), doD = M::fma(m3w2, cmD, oD);
-    const V doE = M::fma(m3w2, cmE, oE), doF = M::fma(m3w2, cmF, oF);
-    const V doX = M::neg(M::add(M::add(doA, doB), M::add(doC, doD)));
-    const V doY = M::neg(M::add(M::sub(doA, doB), M::sub(doE, doF)));
-    const V doZ = M::neg(M::add(M::sub(doC, doD), M::add(doE, doF)));
+    const V DA = M::fma(mw2x2, M::fma(M::mul(k45, cmA), M::add(ux, uy), mu15), M::add(EA, R2));
+    const V DB = M::fma(mw2x2, M::fma(M::mul(k45, cmB), M::sub(ux, uy), mu15), M::add(EB, R2));
+    const V DC = M::fma(mw2x2, M::fma(M::mul(k45, cmC), M::add(ux, uz), mu15), M::add(EC, R2));
+    const V DD = M::fma(mw2x2, M::fma(M::mul(k45, cmD), M::sub(ux, uz), mu15), M::add(ED, R2));
+    const V DE = M::fma(mw2x2, M::fma(M::mul(k45, cmE), M::add(uy, uz), mu15), M::add(EE, R2));
+    const V DF = M::fma(mw2x2, M::fma(M::mul(k45, cmF), M::sub(uz, uy), mu15), M::add(EF, R2));
+    const V de0 = M::neg(M::add(M::add(M::add(DX, DY), M::add(DZ, DA)),
+                                M::add(M::add(DB, DC), M::add(DD, M::add(DE, DF)))));
+    const V m3w2x2 = M::c(2.f * M3W2);
+    const V DOA = M::fma(m3w2x2, cmA, OA), DOB = M::fma(m3w2x2, cmB, OB);
+    const V DOC = M::fma(m3w2x2, cmC, OC), DOD = M::fma(m3w2x2, cmD, OD);
+    const V DOE = M::fma(m3w2x2, cmE, OE), DOF = M::fma(m3w2x2, cmF, OF);
+    const V DOX = M::neg(M::add(M::add(DOA, DOB), M::add(DOC, DOD)));
+    const V DOY = M::neg(M::add(M::sub(DOA, DOB), M::sub(DOE, DOF)));
+    const V DOZ = M::neg(M::add(M::sub(DOC, DOD), M::add(DOE, DOF)));
     const V zero = M::c(0.f);
     V f10 = zero, f1X = zero, f1Y = zero, f1Z = zero, f1A = zero, f1B = zero, f1C = zero, f1D = zero, f1E = zero,
       f1F = zero;
     if (OP != OP_BGK) {
-        const V pxx = M::mul(two, M::add(M::add(deX, M::add(deA, deB)), M::add(deC, deD)));
-        const V pyy = M::mul(two, M::add(M::add(deY, M::add(deA, deB)), M::add(deE, deF)));
-        const V pzz = M::mul(two, M::add(M::add(deZ, M::add(deC, deD)), M::add(deE, deF)));
-        const V pxy = M::mul(two, M::sub(deA, deB)), pxz = M::mul(two, M::sub(deC, deD));
-        const V pyz = M::mul(two, M::sub(deE, deF));
+        const V pxx = M::add(M::add(DX, M::add(DA, DB)), M::add(DC, DD));
+        const V pyy = M::add(M::add(DY, M::add(DA, DB)), M::add(DE, DF));
+        const V pzz = M::add(M::add(DZ, M::add(DC, DD)), M::add(DE, DF));
+        const V pxy = M::sub(DA, DB), pxz = M::sub(DC, DD);
+        const V pyz = M::sub(DE, DF);
         const V tr3 = M::mul(M::add(M::add(pxx, pyy), pzz), M::c(1.f / 3.f));
         const V q4 = M::c(0.25f), q8 = M::c(0.125f), mq4 = M::c(-0.25f);
         f10 = M::mul(M::c(-1.5f), tr3);
@@ -330,15 +320,15 @@ __device__ __forceinline__ void collide19l(typename M::V g[19], const Coef &k)
         f1F = M::fma(mq4, pyz, byz);
     }
     g[0] = update_rest_l<M, OP>(g[0], de0, f10, k);
-    update_pair_l<M, OP>(g[1], g[2], deX, doX, f1X, k);
-    update_pair_l<M, OP>(g[3], g[4], deY, doY, f1Y, k);
-    update_pair_l<M, OP>(g[5], g[6], deZ, doZ, f1Z, k);
-    update_pair_l<M, OP>(g[7], g[8], deA, doA, f1A, k);
-    update_pair_l<M, OP>(g[9], g[10], deB, doB, f1B, k);
-    update_pair_l<M, OP>(g[11], g[12], deC, doC, f1C, k);
-    update_pair_l<M, OP>(g[13], g[14], deD, doD, f1D, k);
-    update_pair_l<M, OP>(g[16], g[15], deE, doE, f1E, k);
-    update_pair_l<M, OP>(g[17], g[18], deF, doF, f1F, k);
+    update_pair2_l<M, OP>(g[1], g[2], DX, DOX, f1X, k);
+    update_pair2_l<M, OP>(g[3], g[4], DY, DOY, f1Y, k);
+    update_pair2_l<M, OP>(g[5], g[6], DZ, DOZ, f1Z, k);
+    update_pair2_l<M, OP>(g[7], g[8], DA, DOA, f1A, k);
+    update_pair2_l<M, OP>(g[9], g[10], DB, DOB, f1B, k);
+    update_pair2_l<M, OP>(g[11], g[12], DC, DOC, f1C, k);
+    update_pair2_l<M, OP>(g[13], g[14], DD, DOD, f1D, k);
+    update_pair2_l<M, OP>(g[16], g[15], DE, DOE, f1E, k);
+    update_pair2_l<M, OP>(g[17], g[18], DF, DOF, f1F, k);
 }
 
 template <int OP>

@@ -9,13 +9,7 @@ template <int Q, int NPT>
 cudaError_t go(const BatchGeo &g, const BatchRun *runs, int n_runs, int *counter, BatchResult *res, const double *aos,
                int grid, int block, size_t smem, int dbl, cudaStream_t s)
 {
-    // D3Q19 node pairs in packed FP32x2 for runs without the per-step density check (Taylor-Green
-    // map: 42.6k against 40.6k runs/s on GB300); the obstacle channel runs faster one node at a time
-    // (7.29k against 6.72k runs/s)
     auto k = k_batch<PrecShifted32, Q, NPT>;
-    if constexpr (Q == 19 && NPT % 2 == 0) {
-        if (!g.density_check) k = k_batch<PrecShifted32, Q, NPT, true>;
-    }
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k<<<grid, block, smem, s>>>(g, runs, n_runs, counter, res, aos, dbl);
