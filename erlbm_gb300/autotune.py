@@ -40,7 +40,9 @@ def _store(key: str, value) -> None:
         d = _load()
         d[key] = value
         os.makedirs(os.path.dirname(cache_path()), exist_ok=True)
-        tmp = cache_path() + ".tmp"
+        # a file of this process's own, renamed over the cache: ranks of one job that tune at the
+        # same time each replace the whole file and never read a half-written one
+        tmp = f"{cache_path()}.{os.getpid()}.tmp"
         with open(tmp, "w") as f:
             json.dump(d, f, indent=1, sort_keys=True)
         os.replace(tmp, cache_path())

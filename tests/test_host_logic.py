@@ -161,3 +161,28 @@ def test_bench_launch_count_follows_erlbm_step():
     assert bench.launches_of(999, 3) == 15 * 22 + 3
     assert bench.launches_of(65, 2) == 32 + 1
     assert bench.launches_of(2, 3) == 2
+
+
+def test_autotune_cache_survives_concurrent_writers(tmp_path, monkeypatch):
+    """Processes storing tuning results at once (the ranks of one job) leave a readable cache that
+    holds one of the writers' complete entries."""
+    import multiprocessing as mp
+    monkeypatch.setenv("ERLBM_TUNE_CACHE", str(tmp_path / "tune.json"))
+    ctx = mp.get_context("spawn")
+    procs = [ctx.Process(target=_store_many, args=(str(tmp_path / "tune.json"), r)) for r in range(4)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(60)
+        assert p.exitcode == 0
+    from erlbm_gb300 import autotune
+    d = autotune._load()
+    assert d and all(isinstance(v, dict) and v["rank"] in range(4) for v in d.values())
+
+
+def _store_many(path, rank):
+    import os
+    os.environ["ERLBM_TUNE_CACHE"] = path
+    from erlbm_gb300 import autotune
+    for k in range(50):
+        autotune._store(f"key{k % 5}", {"rank": rank, "k": k})
