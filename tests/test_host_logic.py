@@ -186,3 +186,40 @@ def _store_many(path, rank):
     from erlbm_gb300 import autotune
     for k in range(50):
         autotune._store(f"key{k % 5}", {"rank": rank, "k": k})
+
+
+STRUCTS = [("erlbm_desc", "Desc"), ("erlbm_bc", "BC"), ("erlbm_checks", "Checks"),
+           ("erlbm_run_result", "RunResult"), ("erlbm_map_desc", "MapDesc"), ("erlbm_refine_desc", "RefineDesc"),
+           ("erlbm_batch_desc", "BatchDesc"), ("erlbm_run_spec", "RunSpec"), ("erlbm_batch_result", "BatchResult"),
+           ("erlbm_server_desc", "ServerDesc"), ("erlbm_request", "Request"), ("erlbm_result", "Result")]
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every struct of include/erlbm_gb300.h that the Python binding mirrors has the same size and the
+    same field names and offsets in both (a C program compiled against the header prints them)."""
+    import os
+    import shutil
+    import subprocess
+    from erlbm_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    include = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "erlbm_gb300.h"', "int main(void) {"]
+    for cname, pyname in STRUCTS:
+        cls = getattr(_lib, pyname)
+        lines.append(f'    printf("{pyname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'    printf("{pyname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", f"-I{include}", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, pyname in STRUCTS:
+        cls = getattr(_lib, pyname)
+        assert got[(pyname, "size")] == C.sizeof(cls), pyname
+        for fname, _ in cls._fields_:
+            assert got[(pyname, fname)] == getattr(cls, fname).offset, (pyname, fname)
