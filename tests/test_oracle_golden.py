@@ -224,3 +224,27 @@ def test_read_geo(layers, tmp_path):
     ini = v[f"geo_ini_{pin}_{pout}_{wall}"]
     assert n == int(v[f"geo_fluid_{pin}_{pout}_{wall}"][0]) and solid.size == ini.size
     assert np.array_equal(solid == 0, ini != 0)
+
+
+def test_oracle_bc_struct_matches_its_header(tmp_path):
+    """The oracle's ctypes OrcBC has orc_bc's size and field offsets (oracle/erlbm_oracle.h)."""
+    import ctypes as C
+    import os
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle")
+    body = ['#include <stdio.h>', '#include <stddef.h>', '#include <stdint.h>', '#include "erlbm_oracle.h"',
+            'int main(void) {', '    printf("size %zu\\n", sizeof(orc_bc));']
+    for fname, _ in O.OrcBC._fields_:
+        body.append(f'    printf("{fname} %zu\\n", offsetof(orc_bc, {fname}));')
+    body += ['    return 0;', '}']
+    (tmp_path / "l.c").write_text("\n".join(body) + "\n")
+    subprocess.run([cc, "-std=c11", f"-I{hdr}", str(tmp_path / "l.c"), "-o", str(tmp_path / "l")], check=True)
+    got = dict(l.split() for l in subprocess.run([str(tmp_path / "l")], check=True, capture_output=True,
+                                                 text=True).stdout.split("\n") if l.strip())
+    assert int(got["size"]) == C.sizeof(O.OrcBC)
+    for fname, _ in O.OrcBC._fields_:
+        assert int(got[fname]) == getattr(O.OrcBC, fname).offset, fname
