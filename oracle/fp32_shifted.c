@@ -1,0 +1,160 @@
+/*
+ * fp32_shifted.c -- test infrastructure: the GPU engine's FP32-shifted D2Q9 periodic update restated
+ * for the CPU, operation for operation.
+ *
+ * This is not the reference's algorithm (that is erlbm_oracle.c, in FP64).  It is the checker for the
+ * engine's own FP32 formulation.  The populations are stored as g_i = (float)(f_i - w_i).  The collision
+ * is E-RLBM / RLBM / BGK / MRT written as an increment on g, with the pair sums, differences and
+ * non-equilibrium parts carried at twice their scale.  Every operation below is one IEEE
+ * single-precision operation, rounded to nearest: the CPU's float +, -, * and /, and C99 fmaf.  The
+ * GPU forms use the same operations as explicitly rounded intrinsics (__fadd_rn, __fmul_rn,
+ * __fmaf_rn, __frcp_rn), so the two agree bit for bit.  This file is compiled with
+ * -ffp-contract=off, so the compiler fuses nothing.
+ *
+ * Step semantics are those of the engine's erlbm_step on a periodic box:
+ *   - the first step after setting the populations collides them in place;
+ *   - every later step pulls g_i from node (x - c_ix, y - c_iy) (periodic) and collides.
+ * The result is the post-collision populations, returned as f = (double)g + w.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "erlbm_oracle.h"
+
+static const int CX9[9] = {0, 1, -1, 0, 0, 1, -1, 1, -1};
+static const int CY9[9] = {0, 0, 0, 1, -1, 1, -1, -1, 1};
+
+static double w9(int i) { return i == 0 ? 4. / 9. : (i < 5 ? 1. / 9. : 1. / 36.); }
+
+/* one opposite pair from D = 2 de, DO = 2 do and f1 */
+static void pair_update(float *gi, float *gj, float D, float DO, float f1, float d1, float kd, int op)
+{
+    if (op == ORC_OP_BGK) {
+        const float DI = D + DO, DJ = D - DO;
+        *gi = fmaf(0.5f, fmaf(d1, DI, -2.f * DI), *gi);
+        *gj = fmaf(0.5f, fmaf(d1, DJ, -2.f * DJ), *gj);
+    } else {
+        const float a = fmaf(0.5f, D, -f1), t = -2.f * f1;
+        *gi = *gi + fmaf(d1, f1, fmaf(kd, fmaf(0.5f, DO, a), t));
+        *gj = *gj + fmaf(d1, f1, fmaf(kd, fmaf(-0.5f, DO, a), t));
+    }
+}
+
+static float rest_update(float g0, float de0, float f10, float d1, float kd, int op)
+{
+    if (op == ORC_OP_BGK) return g0 + fmaf(d1, de0, -2.f * de0);
+    return g0 + fmaf(d1, f10, fmaf(kd, de0 - f10, -2.f * f10));
+}
+
+static void collide9_f32(float g[9], float d1, float kd, int op)
+{
+    const float W1 = 1.f / 9.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
+    const float EX = g[1] + g[2], OX = g[1] - g[2];
+    const float EY = g[3] + g[4], OY = g[3] - g[4];
+    const float EP = g[5] + g[6], OP = g[5] - g[6];
+    const float EM = g[7] + g[8], OM = g[7] - g[8];
+    const float drho = ((EX + EY) + (EP + EM)) + g[0];
+    const float mx = OX + (OP + OM);
+    const float my = OY + (OP - OM);
+    const float inv = 1.f / (1.f + drho);
+    const float ux = mx * inv, uy = my * inv;
+    const float mu15 = -1.5f * fmaf(mx, ux, my * uy);
+    const float k45 = 4.5f, mw1x2 = -2.f * W1, mw2x2 = -2.f * W2;
+    const float DX = fmaf(mw1x2, fmaf(k45 * mx, ux, mu15), fmaf(mw1x2, drho, EX));
+    const float DY = fmaf(mw1x2, fmaf(k45 * my, uy, mu15), fmaf(mw1x2, drho, EY));
+    const float cmP = mx + my, cmM = mx - my;
+    const float DP = fmaf(mw2x2, fmaf(k45 * cmP, ux + uy, mu15), fmaf(mw2x2, drho, EP));
+    const float DM = fmaf(mw2x2, fmaf(k45 * cmM, ux - uy, mu15), fmaf(mw2x2, drho, EM));
+    const float de0 = -((DX + DY) + (DP + DM));
+    const float DOP = fmaf(2.f * M3W2, cmP, OP);
+    const float DOM = fmaf(2.f * M3W2, cmM, OM);
+    const float DOX = -(DOP + DOM);
+    const float DOY = -(DOP - DOM);
+    if (op == ORC_OP_MRT) {
+        const float deX = 0.5f * DX, deY = 0.5f * DY, deP = 0.5f * DP, deM = 0.5f * DM;
+        const float doP = 0.5f * DOP, doM = 0.5f * DOM;
+        const float A = deX + deY, B = deP + deM;
+        const float hE = (float)(1.6 / 6.0) * fmaf(2.f, B, A);
+        const float hP = (float)(1.8 / 6.0) * fmaf(-2.f, A, -B);
+        const float sX = deX - deY, sP = deP - deM;
+        const float hd = -0.5f * d1;
+        const float vX = fmaf(hd, sX, sX), vP = fmaf(hd, sP, sP);
+        const float ax = fmaf(2.f, hP, hE), ap = -fmaf(2.f, hE, hP);
+        const float xX = ax - vX, xY = ax + vX, xP = ap - vP, xM = ap + vP;
+        const float sq = (float)-1.9;
+        const float qP = sq * doP, qM = sq * doM;
+        const float qX = -(qP + qM), qY = -(qP - qM);
+        g[0] = g[0] + -2.f * ((xX + xY) + (xP + xM));
+        g[1] = g[1] + (xX + qX);
+        g[2] = g[2] + (xX - qX);
+        g[3] = g[3] + (xY + qY);
+        g[4] = g[4] + (xY - qY);
+        g[5] = g[5] + (xP + qP);
+        g[6] = g[6] + (xP - qP);
+        g[7] = g[7] + (xM + qM);
+        g[8] = g[8] + (xM - qM);
+        return;
+    }
+    float f10 = 0.f, f1X = 0.f, f1Y = 0.f, f1P = 0.f, f1M = 0.f;
+    if (op != ORC_OP_BGK) {
+        const float pxx = DX + (DP + DM);
+        const float pyy = DY + (DP + DM);
+        const float pxy = DP - DM;
+        const float tr = pxx + pyy;
+        f10 = (-2.f / 3.f) * tr;
+        f1X = fmaf(pxx, 1.f / 3.f, pyy * (-1.f / 6.f));
+        f1Y = fmaf(pyy, 1.f / 3.f, pxx * (-1.f / 6.f));
+        const float t12 = tr * (1.f / 12.f);
+        f1P = fmaf(pxy, 0.25f, t12);
+        f1M = fmaf(pxy, -0.25f, t12);
+    }
+    g[0] = rest_update(g[0], de0, f10, d1, kd, op);
+    pair_update(&g[1], &g[2], DX, DOX, f1X, d1, kd, op);
+    pair_update(&g[3], &g[4], DY, DOY, f1Y, d1, kd, op);
+    pair_update(&g[5], &g[6], DP, DOP, f1P, d1, kd, op);
+    pair_update(&g[7], &g[8], DM, DOM, f1M, d1, kd, op);
+}
+
+int orc32_periodic_d2q9(int nx, int ny, int op, double tau, double tau_nh, const double *f_in, int n_steps,
+                        double *f_out)
+{
+    if (nx < 1 || ny < 1 || n_steps < 0 || !f_in || !f_out) return -1;
+    const size_t n = (size_t)nx * ny;
+    float *a = malloc(n * 9 * sizeof(float)), *b = malloc(n * 9 * sizeof(float));
+    if (!a || !b) {
+        free(a);
+        free(b);
+        return -2;
+    }
+    const float d1 = (float)(2.0 - 1.0 / tau);
+    const float kd = (op == ORC_OP_BGK || op == ORC_OP_MRT) ? 0.f
+                     : op == ORC_OP_REG                      ? -1.f
+                                                             : (float)((1.0 - 1.0 / tau_nh) - 1.0);
+    for (size_t p = 0; p < n; p++)
+        for (int i = 0; i < 9; i++) a[p * 9 + i] = (float)(f_in[p * 9 + i] - w9(i));
+    for (int s = 0; s < n_steps; s++) {
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                float g[9];
+                for (int i = 0; i < 9; i++) {
+                    if (s == 0) {
+                        g[i] = a[((size_t)y * nx + x) * 9 + i];
+                    } else {
+                        const int xs = (x - CX9[i] + nx) % nx, ys = (y - CY9[i] + ny) % ny;
+                        g[i] = a[((size_t)ys * nx + xs) * 9 + i];
+                    }
+                }
+                collide9_f32(g, d1, kd, op);
+                memcpy(&b[((size_t)y * nx + x) * 9], g, sizeof g);
+            }
+        float *t = a;
+        a = b;
+        b = t;
+    }
+    for (size_t p = 0; p < n; p++)
+        for (int i = 0; i < 9; i++) f_out[p * 9 + i] = (double)a[p * 9 + i] + w9(i);
+    free(a);
+    free(b);
+    return 0;
+}

@@ -40,8 +40,8 @@ def orc_bc(bc: dict) -> OrcBC:
 
 def build(force: bool = False) -> str:
     so = os.path.join(HERE, "liberlbm_oracle.so")
-    src = os.path.join(HERE, "erlbm_oracle.c")
-    if force or not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("erlbm_oracle.c", "fp32_shifted.c", "erlbm_oracle.h")]
+    if force or not os.path.exists(so) or os.path.getmtime(so) < max(os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-s", "-C", HERE, "liberlbm_oracle.so"], check=True)
     return so
 
@@ -258,6 +258,19 @@ def write_vtk(q, nx, ny, nz, solid, aos, kind, fmt, path):
                               os.fsencode(path))
     if rc:
         raise OSError(f"cannot write {path}")
+
+
+def fp32_periodic_d2q9(nx, ny, op, tau, tau_nh, f_in, n_steps):
+    """The engine's FP32-shifted D2Q9 periodic update restated on the CPU (fp32_shifted.c): the
+    post-collision populations after n_steps steps, the first colliding in place."""
+    f_in = np.ascontiguousarray(f_in, dtype=np.float64)
+    out = np.empty_like(f_in)
+    fn = load().orc32_periodic_d2q9
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _dp, C.c_int, _dp]
+    if fn(nx, ny, op, tau, tau_nh, f_in, n_steps, out):
+        raise ValueError("orc32_periodic_d2q9: bad arguments")
+    return out
 
 
 def read_geo(path, pts_in=0, pts_out=0, wall=True):

@@ -297,3 +297,22 @@ def test_d3q19_box_wraps_in_every_axis(with_solid):
         lat.step(13)
         assert np.array_equal(lat.get_populations(eg().STAGE_POST_COLLISION), ref.get(1))
         assert np.array_equal(lat.get_populations(eg().STAGE_POST_STREAM), ref.get(0))
+
+
+@pytest.mark.parametrize("op", [1, 2, 3, 4])
+@pytest.mark.parametrize("nx,ny,steps", [(128, 128, 30), (256, 66, 71)])
+def test_fp32_kernels_equal_their_cpu_restatement(op, nx, ny, steps):
+    """The FP32-shifted D2Q9 periodic kernels (one, two and three steps per launch, with a graph block
+    at 71 steps) give bit for bit the populations of the engine's FP32 update restated on the CPU in
+    IEEE single precision (oracle/fp32_shifted.c)."""
+    rng = np.random.default_rng(op * 100 + ny)
+    w = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+    f0 = (w[None, :] * (1.0 + 0.05 * rng.standard_normal((nx * ny, 9)))).ravel()
+    tau, tnh = 0.53, 0.65
+    want = O.fp32_periodic_d2q9(nx, ny, op, tau, tnh, f0, steps)
+    for per in (1, 2, 3):
+        with eg().Lattice(9, nx, ny, 1, None, tau, tnh, op, eg().FP32_SHIFTED) as lat:
+            lat.set_launch(128, False, per == 2, per == 3)
+            lat.set_populations(f0)
+            lat.step(steps)
+            assert np.array_equal(lat.get_populations(eg().STAGE_POST_COLLISION), want), per
