@@ -409,14 +409,40 @@ int job_admit(erlbm_server *s, int64_t ticket, const erlbm_request &q, Job **out
             if (!solid[k]) nof.push_back((int)k);
         j->n_fluid = (long long)nof.size();
     }
-    const size_t need = 2 * pop + ((size_t)j->n_fluid + 4096) * 8 + 1024 + solid.size() + nof.size() * 4 + 4096 * 8;
+    // the initial state's table of sines and cosines along x (Taylor-Green kinds)
+    std::vector<double> tab;
+    int kind = 0;
+    double k = 0;
+    const double L = (double)j->g.nx;
+    if (q.kind == ERLBM_REQ_TG2D) {
+        kind = 1;
+        const int n = j->g.nx;
+        k = 2. * M_PI / L;
+        tab.resize(4 * n);
+        for (int x = 0; x < n; x++) {
+            tab[x] = sin(2. * M_PI * x / L);
+            tab[n + x] = cos(2. * M_PI * x / L);
+            tab[2 * n + x] = cos(4. * M_PI * x / L);
+            tab[3 * n + x] = cos(k * x);
+        }
+    } else if (q.kind == ERLBM_REQ_TG3D || q.kind == ERLBM_REQ_TG_MAP_POINT) {
+        kind = 4;
+        const int n = j->g.nx;
+        tab.resize(2 * n);
+        for (int x = 0; x < n; x++) {
+            tab[x] = sin(2. * M_PI * (double)x / L);
+            tab[n + x] = cos(2. * M_PI * (double)x / L);
+        }
+    }
+    const size_t tab_bytes = std::max<size_t>(tab.size(), 1) * 8;
+    const size_t need = 2 * pop + ((size_t)j->n_fluid + 4096) * 8 + 256 + solid.size() + nof.size() * 4 + tab_bytes;
     if (need > s->arena.size()) return ERLBM_E_OOM;
     if (s->arena.size() - s->arena.used() < need) return 1;
     j->buf[0] = job_alloc(s, j.get(), pop);
     j->buf[1] = job_alloc(s, j.get(), pop);
     j->scr = (double *)job_alloc(s, j.get(), ((size_t)j->n_fluid + 4096) * 8);
     j->status = (RunStatus *)job_alloc(s, j.get(), 256);
-    j->tab = (double *)job_alloc(s, j.get(), 4096 * 8);
+    j->tab = (double *)job_alloc(s, j.get(), tab_bytes);
     if (!solid.empty()) {
         j->solid = (uint8_t *)job_alloc(s, j.get(), solid.size());
         j->nof = (int *)job_alloc(s, j.get(), nof.size() * 4);
@@ -456,42 +482,12 @@ int job_admit(erlbm_server *s, int64_t ticket, const erlbm_request &q, Job **out
     RunStatus st0{0, 0x7fffffff, 0ull};
     cudaMemcpyAsync(j->status, &st0, sizeof(st0), cudaMemcpyHostToDevice, st);
     // initial populations on the device
-    std::vector<double> tab;
-    int kind = 0;
-    double k = 0;
-    const double L = (double)j->g.nx;
-    if (q.kind == ERLBM_REQ_TG2D) {
-        kind = 1;
-        const int n = j->g.nx;
-        k = 2. * M_PI / L;
-        tab.resize(4 * n);
-        for (int x = 0; x < n; x++) {
-            tab[x] = sin(2. * M_PI * x / L);
-            tab[n + x] = cos(2. * M_PI * x / L);
-            tab[2 * n + x] = cos(4. * M_PI * x / L);
-            tab[3 * n + x] = cos(k * x);
-        }
-    } else if (q.kind == ERLBM_REQ_TG3D || q.kind == ERLBM_REQ_TG_MAP_POINT) {
-        kind = 4;
-        const int n = j->g.nx;
-        tab.resize(2 * n);
-        for (int x = 0; x < n; x++) {
-            tab[x] = sin(2. * M_PI * (double)x / L);
-            tab[n + x] = cos(2. * M_PI * (double)x / L);
-        }
-    }
-    if (!tab.empty()) {
-        if (tab.size() > 4096) {
-            s->streams.push_back(j->slot);
-            job_free(s, j.get());
-            return ERLBM_E_INVAL;
-        }
-        cudaMemcpyAsync(j->tab, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, st);
-        cudaStreamSynchronize(st);  // the host table is a local vector
-    }
+    if (!tab.empty()) cudaMemcpyAsync(j->tab, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, st);
     const int irc = j->prec == ERLBM_FP64
                         ? launch_init_fp64(kind, j->q, j->g, (double *)j->buf[0], j->tab, q.u0, q.tau, k, 1.0, st)
                         : launch_init_fp32(kind, j->q, j->g, (float *)j->buf[0], j->tab, q.u0, q.tau, k, 1.0, st);
+    // the copies above read local host vectors: they finish before this returns
+    cudaStreamSynchronize(st);
     if (irc) {
         s->streams.push_back(j->slot);
         job_free(s, j.get());

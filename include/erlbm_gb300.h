@@ -328,7 +328,7 @@ typedef struct erlbm_server_desc {
 typedef struct erlbm_request {
     int kind;                   /* ERLBM_REQ_* */
     int precision, op;
-    int L;                      /* TG2D / TG3D side */
+    int L;                      /* side: TG2D 2..4096, TG3D 2..512 (ERLBM_E_INVAL otherwise) */
     int sx, sy;                 /* obstacle scale */
     double tau, tau_nh, u0;
     int n_steps;                /* step budget */

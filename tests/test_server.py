@@ -142,3 +142,22 @@ def test_stream_lane_admits_the_shortest_runs_first():
         assert all(r["status"] == 0 for r in rs + [rb, r0])
         assert max(r["t_admit"] for r in rs) <= rb["t_admit"]
         assert r0["t_admit"] <= rb["t_admit"]
+
+
+def test_large_2d_lattice_through_the_stream_lane():
+    """A D2Q9 Taylor-Green side above 1024 (its initial-state table holds 4 L entries) is admitted and
+    gives the oracle's energy bit for bit; a side above 4096 is refused at submission."""
+    m = E()
+    L, u0 = 1536, 2.0 / 1536
+    tau = 0.5 + 3 * u0 * L / 50
+    with m.Server(hbm_budget_bytes=1 << 30) as srv:
+        r = srv.wait(srv.submit(m.REQ_TG2D, m.FP64, op=m.OP_EXTREG, L=L, tau=tau, tau_nh=0.65, u0=u0, n_steps=3),
+                     timeout=600)
+        with pytest.raises(m.ErlbmError) as ei:
+            srv.submit(m.REQ_TG2D, m.FP64, L=4097, tau=tau, u0=u0, n_steps=3)
+        assert ei.value.code == -1
+    assert r["status"] == 0 and r["steps_done"] == 3 and r["lane"] == 1
+    lat = O.Lattice(9, L, L, 1, None, tau, 0.65, O.OP_EXTREG)
+    lat.set(O.init_taylor_green(9, L, u0, tau))
+    lat.step(3)
+    assert r["energy"] == lat.kinetic_energy(0)
