@@ -80,12 +80,14 @@ int orc_read_geo(const char *path, int pts_in, int pts_out, int wall, int *nx, i
 int orc_velocity_error(int nx, int ny, const double *vel, int nx_ref, int ny_ref, const double *vel_ref,
                        int text_digits, double *e_vec, double *e_mod);
 
-/* fp32_shifted.c: the engine's own FP32-shifted D2Q9 periodic update restated on the CPU (the checker
- * of the GPU FP32 kernels' bits): n_steps steps from the AoS populations f_in (post-stream), the first
+/* fp32_shifted.c: the engine's own FP32-shifted periodic update restated on the CPU (the checker of
+ * the GPU FP32 kernels' bits): n_steps steps from the AoS populations f_in (post-stream), the first
  * colliding in place; f_out = the post-collision populations.  Returns 0, or -1 / -2 on bad arguments
- * / allocation failure. */
+ * (MRT is D2Q9 only) / allocation failure. */
 int orc32_periodic_d2q9(int nx, int ny, int op, double tau, double tau_nh, const double *f_in, int n_steps,
                         double *f_out);
+int orc32_periodic_d3q19(int nx, int ny, int nz, int op, double tau, double tau_nh, const double *f_in,
+                         int n_steps, double *f_out);
 
 #ifdef __cplusplus
 }

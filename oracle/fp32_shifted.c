@@ -1,6 +1,6 @@
 /*
- * fp32_shifted.c -- test infrastructure: the GPU engine's FP32-shifted D2Q9 periodic update restated
- * for the CPU, operation for operation.
+ * fp32_shifted.c -- test infrastructure: the GPU engine's FP32-shifted periodic update (D2Q9 and
+ * D3Q19) restated for the CPU, operation for operation.
  *
  * This is not the reference's algorithm (that is erlbm_oracle.c, in FP64).  It is the checker for the
  * engine's own FP32 formulation.  The populations are stored as g_i = (float)(f_i - w_i).  The collision
@@ -13,8 +13,9 @@
  *
  * Step semantics are those of the engine's erlbm_step on a periodic box:
  *   - the first step after setting the populations collides them in place;
- *   - every later step pulls g_i from node (x - c_ix, y - c_iy) (periodic) and collides.
- * The result is the post-collision populations, returned as f = (double)g + w.
+ *   - every later step pulls g_i from node (x - c_ix, y - c_iy, z - c_iz) (periodic) and collides.
+ * The result is the post-collision populations, returned as f = (double)g + w, nodes in x-fastest
+ * order.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -116,12 +117,97 @@ static void collide9_f32(float g[9], float d1, float kd, int op)
     pair_update(&g[7], &g[8], DM, DOM, f1M, d1, kd, op);
 }
 
-int orc32_periodic_d2q9(int nx, int ny, int op, double tau, double tau_nh, const double *f_in, int n_steps,
-                        double *f_out)
+/* D3Q19: pairs X = (1,2), Y = (3,4), Z = (5,6), A = (7,8) c = (1,1,0), B = (9,10) c = (1,-1,0),
+ * C = (11,12) c = (1,0,1), D = (13,14) c = (1,0,-1), E = (16,15) c = (0,1,1), F = (17,18) c = (0,-1,1) */
+static const int CX19[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+static const int CY19[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, -1, 1, -1, 1};
+static const int CZ19[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, -1, 1, 1, -1};
+
+static double w19(int i) { return i == 0 ? 1. / 3. : (i < 7 ? 1. / 18. : 1. / 36.); }
+
+static void collide19_f32(float g[19], float d1, float kd, int op)
 {
-    if (nx < 1 || ny < 1 || n_steps < 0 || !f_in || !f_out) return -1;
-    const size_t n = (size_t)nx * ny;
-    float *a = malloc(n * 9 * sizeof(float)), *b = malloc(n * 9 * sizeof(float));
+    const float W1 = 1.f / 18.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
+    const float EX = g[1] + g[2], OX = g[1] - g[2];
+    const float EY = g[3] + g[4], OY = g[3] - g[4];
+    const float EZ = g[5] + g[6], OZ = g[5] - g[6];
+    const float EA = g[7] + g[8], OA = g[7] - g[8];
+    const float EB = g[9] + g[10], OB = g[9] - g[10];
+    const float EC = g[11] + g[12], OC = g[11] - g[12];
+    const float ED = g[13] + g[14], OD = g[13] - g[14];
+    const float EE = g[16] + g[15], OE = g[16] - g[15];
+    const float EF = g[17] + g[18], OF = g[17] - g[18];
+    const float drho = (((EX + EY) + (EZ + EA)) + ((EB + EC) + (ED + (EE + EF)))) + g[0];
+    const float mx = (OX + (OA + OB)) + (OC + OD);
+    const float my = (OY + (OA - OB)) + (OE - OF);
+    const float mz = (OZ + (OC - OD)) + (OE + OF);
+    const float inv = 1.f / (1.f + drho);
+    const float ux = mx * inv, uy = my * inv, uz = mz * inv;
+    const float mu15 = -1.5f * fmaf(mx, ux, fmaf(my, uy, mz * uz));
+    const float mw1x2 = -2.f * W1, mw2x2 = -2.f * W2, k45 = 4.5f;
+    const float R1 = mw1x2 * drho, R2 = mw2x2 * drho;
+    const float DX = fmaf(mw1x2, fmaf(k45 * mx, ux, mu15), EX + R1);
+    const float DY = fmaf(mw1x2, fmaf(k45 * my, uy, mu15), EY + R1);
+    const float DZ = fmaf(mw1x2, fmaf(k45 * mz, uz, mu15), EZ + R1);
+    const float cmA = mx + my, cmB = mx - my, cmC = mx + mz, cmD = mx - mz;
+    const float cmE = my + mz, cmF = mz - my;
+    const float DA = fmaf(mw2x2, fmaf(k45 * cmA, ux + uy, mu15), EA + R2);
+    const float DB = fmaf(mw2x2, fmaf(k45 * cmB, ux - uy, mu15), EB + R2);
+    const float DC = fmaf(mw2x2, fmaf(k45 * cmC, ux + uz, mu15), EC + R2);
+    const float DD = fmaf(mw2x2, fmaf(k45 * cmD, ux - uz, mu15), ED + R2);
+    const float DE = fmaf(mw2x2, fmaf(k45 * cmE, uy + uz, mu15), EE + R2);
+    const float DF = fmaf(mw2x2, fmaf(k45 * cmF, uz - uy, mu15), EF + R2);
+    const float de0 = -(((DX + DY) + (DZ + DA)) + ((DB + DC) + (DD + (DE + DF))));
+    const float m3w2x2 = 2.f * M3W2;
+    const float DOA = fmaf(m3w2x2, cmA, OA), DOB = fmaf(m3w2x2, cmB, OB);
+    const float DOC = fmaf(m3w2x2, cmC, OC), DOD = fmaf(m3w2x2, cmD, OD);
+    const float DOE = fmaf(m3w2x2, cmE, OE), DOF = fmaf(m3w2x2, cmF, OF);
+    const float DOX = -((DOA + DOB) + (DOC + DOD));
+    const float DOY = -((DOA - DOB) + (DOE - DOF));
+    const float DOZ = -((DOC - DOD) + (DOE + DOF));
+    float f10 = 0.f, f1X = 0.f, f1Y = 0.f, f1Z = 0.f, f1A = 0.f, f1B = 0.f, f1C = 0.f, f1D = 0.f, f1E = 0.f,
+          f1F = 0.f;
+    if (op != ORC_OP_BGK) {
+        const float pxx = (DX + (DA + DB)) + (DC + DD);
+        const float pyy = (DY + (DA + DB)) + (DE + DF);
+        const float pzz = (DZ + (DC + DD)) + (DE + DF);
+        const float pxy = DA - DB, pxz = DC - DD, pyz = DE - DF;
+        const float tr3 = ((pxx + pyy) + pzz) * (1.f / 3.f);
+        f10 = -1.5f * tr3;
+        f1X = 0.25f * (pxx - tr3);
+        f1Y = 0.25f * (pyy - tr3);
+        f1Z = 0.25f * (pzz - tr3);
+        const float bxy = 0.125f * ((pxx + pyy) - tr3);
+        const float bxz = 0.125f * ((pxx + pzz) - tr3);
+        const float byz = 0.125f * ((pyy + pzz) - tr3);
+        f1A = fmaf(0.25f, pxy, bxy);
+        f1B = fmaf(-0.25f, pxy, bxy);
+        f1C = fmaf(0.25f, pxz, bxz);
+        f1D = fmaf(-0.25f, pxz, bxz);
+        f1E = fmaf(0.25f, pyz, byz);
+        f1F = fmaf(-0.25f, pyz, byz);
+    }
+    g[0] = rest_update(g[0], de0, f10, d1, kd, op);
+    pair_update(&g[1], &g[2], DX, DOX, f1X, d1, kd, op);
+    pair_update(&g[3], &g[4], DY, DOY, f1Y, d1, kd, op);
+    pair_update(&g[5], &g[6], DZ, DOZ, f1Z, d1, kd, op);
+    pair_update(&g[7], &g[8], DA, DOA, f1A, d1, kd, op);
+    pair_update(&g[9], &g[10], DB, DOB, f1B, d1, kd, op);
+    pair_update(&g[11], &g[12], DC, DOC, f1C, d1, kd, op);
+    pair_update(&g[13], &g[14], DD, DOD, f1D, d1, kd, op);
+    pair_update(&g[16], &g[15], DE, DOE, f1E, d1, kd, op);
+    pair_update(&g[17], &g[18], DF, DOF, f1F, d1, kd, op);
+}
+
+/* The stepping loop shared by both lattices: q populations per node, AoS, x fastest. */
+static int run_periodic(int q, int nx, int ny, int nz, int op, double tau, double tau_nh, const double *f_in,
+                        int n_steps, double *f_out)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || n_steps < 0 || !f_in || !f_out) return -1;
+    if (op != ORC_OP_BGK && op != ORC_OP_REG && op != ORC_OP_EXTREG && !(op == ORC_OP_MRT && q == 9)) return -1;
+    const int *cx = q == 9 ? CX9 : CX19, *cy = q == 9 ? CY9 : CY19, *cz = q == 9 ? NULL : CZ19;
+    const size_t n = (size_t)nx * ny * nz;
+    float *a = malloc(n * q * sizeof(float)), *b = malloc(n * q * sizeof(float));
     if (!a || !b) {
         free(a);
         free(b);
@@ -132,29 +218,46 @@ int orc32_periodic_d2q9(int nx, int ny, int op, double tau, double tau_nh, const
                      : op == ORC_OP_REG                      ? -1.f
                                                              : (float)((1.0 - 1.0 / tau_nh) - 1.0);
     for (size_t p = 0; p < n; p++)
-        for (int i = 0; i < 9; i++) a[p * 9 + i] = (float)(f_in[p * 9 + i] - w9(i));
+        for (int i = 0; i < q; i++) a[p * q + i] = (float)(f_in[p * q + i] - (q == 9 ? w9(i) : w19(i)));
     for (int s = 0; s < n_steps; s++) {
-        for (int y = 0; y < ny; y++)
-            for (int x = 0; x < nx; x++) {
-                float g[9];
-                for (int i = 0; i < 9; i++) {
-                    if (s == 0) {
-                        g[i] = a[((size_t)y * nx + x) * 9 + i];
-                    } else {
-                        const int xs = (x - CX9[i] + nx) % nx, ys = (y - CY9[i] + ny) % ny;
-                        g[i] = a[((size_t)ys * nx + xs) * 9 + i];
+        for (int z = 0; z < nz; z++)
+            for (int y = 0; y < ny; y++)
+                for (int x = 0; x < nx; x++) {
+                    float g[19];
+                    for (int i = 0; i < q; i++) {
+                        size_t src = ((size_t)z * ny + y) * nx + x;
+                        if (s > 0) {
+                            const int xs = (x - cx[i] + nx) % nx, ys = (y - cy[i] + ny) % ny;
+                            const int zs = cz ? (z - cz[i] + nz) % nz : z;
+                            src = ((size_t)zs * ny + ys) * nx + xs;
+                        }
+                        g[i] = a[src * q + i];
                     }
+                    if (q == 9)
+                        collide9_f32(g, d1, kd, op);
+                    else
+                        collide19_f32(g, d1, kd, op);
+                    memcpy(&b[(((size_t)z * ny + y) * nx + x) * q], g, (size_t)q * sizeof(float));
                 }
-                collide9_f32(g, d1, kd, op);
-                memcpy(&b[((size_t)y * nx + x) * 9], g, sizeof g);
-            }
         float *t = a;
         a = b;
         b = t;
     }
     for (size_t p = 0; p < n; p++)
-        for (int i = 0; i < 9; i++) f_out[p * 9 + i] = (double)a[p * 9 + i] + w9(i);
+        for (int i = 0; i < q; i++) f_out[p * q + i] = (double)a[p * q + i] + (q == 9 ? w9(i) : w19(i));
     free(a);
     free(b);
     return 0;
+}
+
+int orc32_periodic_d2q9(int nx, int ny, int op, double tau, double tau_nh, const double *f_in, int n_steps,
+                        double *f_out)
+{
+    return run_periodic(9, nx, ny, 1, op, tau, tau_nh, f_in, n_steps, f_out);
+}
+
+int orc32_periodic_d3q19(int nx, int ny, int nz, int op, double tau, double tau_nh, const double *f_in,
+                         int n_steps, double *f_out)
+{
+    return run_periodic(19, nx, ny, nz, op, tau, tau_nh, f_in, n_steps, f_out);
 }

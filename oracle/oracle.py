@@ -273,6 +273,18 @@ def fp32_periodic_d2q9(nx, ny, op, tau, tau_nh, f_in, n_steps):
     return out
 
 
+def fp32_periodic_d3q19(nx, ny, nz, op, tau, tau_nh, f_in, n_steps):
+    """The same restatement for D3Q19 (BGK, RLBM, E-RLBM) on an nx x ny x nz periodic box."""
+    f_in = np.ascontiguousarray(f_in, dtype=np.float64)
+    out = np.empty_like(f_in)
+    fn = load().orc32_periodic_d3q19
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _dp, C.c_int, _dp]
+    if fn(nx, ny, nz, op, tau, tau_nh, f_in, n_steps, out):
+        raise ValueError("orc32_periodic_d3q19: bad arguments")
+    return out
+
+
 def read_geo(path, pts_in=0, pts_out=0, wall=True):
     """read_geo's solid mask: (nx, ny, nz, solid uint8 array, fluid count)."""
     nx, ny, nz = C.c_int(), C.c_int(), C.c_int()

@@ -316,3 +316,28 @@ def test_fp32_kernels_equal_their_cpu_restatement(op, nx, ny, steps):
             lat.set_populations(f0)
             lat.step(steps)
             assert np.array_equal(lat.get_populations(eg().STAGE_POST_COLLISION), want), per
+
+
+GENERIC_FP32_CASES = [(19, (12, 10, 8), 37, op) for op in (1, 3, 4)] + \
+    [(19, (32, 32, 32), 12, 4)] + [(9, (50, 34, 1), 41, op) for op in (1, 2, 3, 4)]
+
+
+@pytest.mark.parametrize("q,shape,steps,op", GENERIC_FP32_CASES)
+def test_generic_fp32_kernel_equals_its_cpu_restatement(q, shape, steps, op):
+    """The generic FP32-shifted step kernel (D3Q19 boxes, and D2Q9 boxes whose width is not a multiple
+    of 128, which the fused kernels do not take) gives bit for bit the populations of the FP32 update
+    restated on the CPU in IEEE single precision (oracle/fp32_shifted.c)."""
+    nx, ny, nz = shape
+    n = nx * ny * nz
+    rng = np.random.default_rng(op * 1000 + n)
+    w = O.equilibrium(q, 0, 0, 0, 1.0)
+    f0 = (w[None, :] * (1.0 + 0.05 * rng.standard_normal((n, q)))).ravel()
+    tau, tnh = 0.53, 0.65
+    if q == 9:
+        want = O.fp32_periodic_d2q9(nx, ny, op, tau, tnh, f0, steps)
+    else:
+        want = O.fp32_periodic_d3q19(nx, ny, nz, op, tau, tnh, f0, steps)
+    with eg().Lattice(q, nx, ny, nz, None, tau, tnh, op, eg().FP32_SHIFTED) as lat:
+        lat.set_populations(f0)
+        lat.step(steps)
+        assert np.array_equal(lat.get_populations(eg().STAGE_POST_COLLISION), want)

@@ -146,7 +146,9 @@ def test_stream_lane_admits_the_shortest_runs_first():
 
 def test_large_2d_lattice_through_the_stream_lane():
     """A D2Q9 Taylor-Green side above 1024 (its initial-state table holds 4 L entries) is admitted and
-    gives the oracle's energy bit for bit; a side above 4096 is refused at submission."""
+    gives the oracle's energy; a side above 4096 is refused at submission.  The populations are the
+    oracle's bit for bit (FP64), but the energy of 2.36 M nodes is a tree reduction on the device and a
+    sequential sum in the oracle, so the two differ in the last digits (1.6e-14 relative measured)."""
     m = E()
     L, u0 = 1536, 2.0 / 1536
     tau = 0.5 + 3 * u0 * L / 50
@@ -160,4 +162,5 @@ def test_large_2d_lattice_through_the_stream_lane():
     lat = O.Lattice(9, L, L, 1, None, tau, 0.65, O.OP_EXTREG)
     lat.set(O.init_taylor_green(9, L, u0, tau))
     lat.step(3)
-    assert r["energy"] == lat.kinetic_energy(0)
+    want = lat.kinetic_energy(0)
+    assert abs(r["energy"] - want) <= 1e-12 * want
