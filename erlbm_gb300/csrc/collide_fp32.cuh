@@ -13,8 +13,8 @@
 //   f* = f + [delta d - 2 d],  delta = 2 - 1/tau           (BGK)
 //
 // Each opposite pair (i, j) is split into an even part e = (g_i + g_j)/2 and an odd part
-// o = (g_i - g_j)/2 (both exact; the D2Q9 update carries them, and the non-equilibrium parts, at twice
-// this scale, which rounds identically and saves the scalings).  Then
+// o = (g_i - g_j)/2 (both exact; the updates carry them, and the non-equilibrium parts, at twice this
+// scale, which rounds identically and saves the scalings).  Then
 //   drho = g_0 + 2 sum e,   m = 2 sum c o,   u = m / (1 + drho),
 //   non-equilibrium even part  de = e - w (drho + 4.5 (c.m)(c.u) - 1.5 m.u),
 //   non-equilibrium odd part   do = o - 3 w (c.m),
@@ -247,9 +247,9 @@ __device__ __forceinline__ void moments19(const float g[19], float &drho, float 
     uz = mz * inv;
 }
 
-// The D3Q19 update in lane arithmetic (explicitly rounded operations).
-// The D3Q19 update with the pair sums, differences and non-equilibrium parts at twice their scale,
-// as the D2Q9 one: the same bits, 28 multiplications fewer.
+// The D3Q19 update in lane arithmetic (explicitly rounded operations), with the pair sums, differences
+// and non-equilibrium parts at twice their scale as in the D2Q9 one: the same bits, 28 multiplications
+// fewer.
 template <class M, int OP>
 __device__ __forceinline__ void collide19l(typename M::V g[19], const Coef &k)
 {
