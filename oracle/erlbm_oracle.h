@@ -88,6 +88,10 @@ int orc32_periodic_d2q9(int nx, int ny, int op, double tau, double tau_nh, const
                         double *f_out);
 int orc32_periodic_d3q19(int nx, int ny, int nz, int op, double tau, double tau_nh, const double *f_in,
                          int n_steps, double *f_out);
+/* the same with a solid mask (nx * ny * nz bytes, NULL = none; halfway bounce-back at solid nodes):
+ * f_in and f_out hold every node of the box, solid nodes included (left as given) */
+int orc32_periodic_solid(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
+                         const double *f_in, int n_steps, double *f_out);
 
 #ifdef __cplusplus
 }

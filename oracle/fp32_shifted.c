@@ -11,13 +11,17 @@
  * __fmaf_rn, __frcp_rn), so the two agree bit for bit.  This file is compiled with
  * -ffp-contract=off, so the compiler fuses nothing.
  *
- * Step semantics are those of the engine's erlbm_step on a periodic box:
+ * Step semantics are those of the engine's erlbm_step on a periodic box, optionally with solid nodes:
  *   - the first step after setting the populations collides them in place;
- *   - every later step pulls g_i from node (x - c_ix, y - c_iy, z - c_iz) (periodic) and collides.
- * The result is the post-collision populations, returned as f = (double)g + w, nodes in x-fastest
- * order.
+ *   - every later step pulls g_i from node (x - c_ix, y - c_iy, z - c_iz) (periodic) and collides;
+ *     when that node is solid, g_i is the population of the opposite direction that this node sent
+ *     towards it in the previous step (halfway bounce-back);
+ *   - solid nodes are never updated.
+ * The result is the post-collision populations, returned as f = (double)g + w for every node of the box
+ * in x-fastest order (solid nodes carry their input).
  */
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -199,9 +203,11 @@ static void collide19_f32(float g[19], float d1, float kd, int op)
     pair_update(&g[17], &g[18], DF, DOF, f1F, d1, kd, op);
 }
 
+static int opp(int i) { return i == 0 ? 0 : (i % 2 ? i + 1 : i - 1); }
+
 /* The stepping loop shared by both lattices: q populations per node, AoS, x fastest. */
-static int run_periodic(int q, int nx, int ny, int nz, int op, double tau, double tau_nh, const double *f_in,
-                        int n_steps, double *f_out)
+static int run_periodic(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
+                        const double *f_in, int n_steps, double *f_out)
 {
     if (nx < 1 || ny < 1 || nz < 1 || n_steps < 0 || !f_in || !f_out) return -1;
     if (op != ORC_OP_BGK && op != ORC_OP_REG && op != ORC_OP_EXTREG && !(op == ORC_OP_MRT && q == 9)) return -1;
@@ -223,21 +229,27 @@ static int run_periodic(int q, int nx, int ny, int nz, int op, double tau, doubl
         for (int z = 0; z < nz; z++)
             for (int y = 0; y < ny; y++)
                 for (int x = 0; x < nx; x++) {
+                    const size_t node = ((size_t)z * ny + y) * nx + x;
                     float g[19];
+                    if (solid && solid[node]) {
+                        memcpy(&b[node * q], &a[node * q], (size_t)q * sizeof(float));
+                        continue;
+                    }
                     for (int i = 0; i < q; i++) {
-                        size_t src = ((size_t)z * ny + y) * nx + x;
-                        if (s > 0) {
-                            const int xs = (x - cx[i] + nx) % nx, ys = (y - cy[i] + ny) % ny;
-                            const int zs = cz ? (z - cz[i] + nz) % nz : z;
-                            src = ((size_t)zs * ny + ys) * nx + xs;
+                        if (s == 0) {
+                            g[i] = a[node * q + i];
+                            continue;
                         }
-                        g[i] = a[src * q + i];
+                        const int xs = (x - cx[i] + nx) % nx, ys = (y - cy[i] + ny) % ny;
+                        const int zs = cz ? (z - cz[i] + nz) % nz : z;
+                        const size_t src = ((size_t)zs * ny + ys) * nx + xs;
+                        g[i] = (solid && solid[src]) ? a[node * q + opp(i)] : a[src * q + i];
                     }
                     if (q == 9)
                         collide9_f32(g, d1, kd, op);
                     else
                         collide19_f32(g, d1, kd, op);
-                    memcpy(&b[(((size_t)z * ny + y) * nx + x) * q], g, (size_t)q * sizeof(float));
+                    memcpy(&b[node * q], g, (size_t)q * sizeof(float));
                 }
         float *t = a;
         a = b;
@@ -253,11 +265,18 @@ static int run_periodic(int q, int nx, int ny, int nz, int op, double tau, doubl
 int orc32_periodic_d2q9(int nx, int ny, int op, double tau, double tau_nh, const double *f_in, int n_steps,
                         double *f_out)
 {
-    return run_periodic(9, nx, ny, 1, op, tau, tau_nh, f_in, n_steps, f_out);
+    return run_periodic(9, nx, ny, 1, NULL, op, tau, tau_nh, f_in, n_steps, f_out);
 }
 
 int orc32_periodic_d3q19(int nx, int ny, int nz, int op, double tau, double tau_nh, const double *f_in,
                          int n_steps, double *f_out)
 {
-    return run_periodic(19, nx, ny, nz, op, tau, tau_nh, f_in, n_steps, f_out);
+    return run_periodic(19, nx, ny, nz, NULL, op, tau, tau_nh, f_in, n_steps, f_out);
+}
+
+int orc32_periodic_solid(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
+                         const double *f_in, int n_steps, double *f_out)
+{
+    if ((q != 9 && q != 19) || (q == 9 && nz != 1)) return -1;
+    return run_periodic(q, nx, ny, nz, solid, op, tau, tau_nh, f_in, n_steps, f_out);
 }

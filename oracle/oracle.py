@@ -273,6 +273,26 @@ def fp32_periodic_d2q9(nx, ny, op, tau, tau_nh, f_in, n_steps):
     return out
 
 
+def fp32_periodic_solid(q, nx, ny, nz, solid, op, tau, tau_nh, f_in, n_steps):
+    """The restatement with a solid mask (halfway bounce-back): f_in and the result hold every node of
+    the box in x-fastest order; solid nodes are left as given."""
+    f_in = np.ascontiguousarray(f_in, dtype=np.float64)
+    out = np.empty_like(f_in)
+    fn = load().orc32_periodic_solid
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double, _dp, C.c_int,
+                   _dp]
+    sp = None
+    if solid is not None:
+        solid = np.ascontiguousarray(solid, dtype=np.uint8)
+        if solid.size != nx * ny * nz:
+            raise ValueError("solid mask size")
+        sp = solid.ctypes.data
+    if f_in.size != nx * ny * nz * q or fn(q, nx, ny, nz, sp, op, tau, tau_nh, f_in, n_steps, out):
+        raise ValueError("orc32_periodic_solid: bad arguments")
+    return out
+
+
 def fp32_periodic_d3q19(nx, ny, nz, op, tau, tau_nh, f_in, n_steps):
     """The same restatement for D3Q19 (BGK, RLBM, E-RLBM) on an nx x ny x nz periodic box."""
     f_in = np.ascontiguousarray(f_in, dtype=np.float64)

@@ -341,3 +341,28 @@ def test_generic_fp32_kernel_equals_its_cpu_restatement(q, shape, steps, op):
         lat.set_populations(f0)
         lat.step(steps)
         assert np.array_equal(lat.get_populations(eg().STAGE_POST_COLLISION), want)
+
+
+@pytest.mark.parametrize("q,shape,op", [(9, (256, 40, 1), op) for op in (1, 2, 3, 4)] +
+                         [(19, (14, 12, 6), op) for op in (1, 3, 4)] + [(19, (22, 12, 1), 4)])
+def test_generic_fp32_kernel_with_solids_equals_its_cpu_restatement(q, shape, op):
+    """With solid nodes (halfway bounce-back in the gather) the generic FP32-shifted step kernel gives
+    bit for bit the populations of the FP32 restatement: a random mask on a D2Q9 box of width 256 (which
+    the fused periodic kernels would otherwise take), a random mask on a D3Q19 box, and the obstacle
+    channel's walls and obstacle (scale 1, periodic in x)."""
+    nx, ny, nz = shape
+    n = nx * ny * nz
+    rng = np.random.default_rng(op * 10 + q)
+    if shape == (22, 12, 1):
+        solid = O.obstacle_geometry(1, 1)[2].astype(np.uint8)
+    else:
+        solid = (rng.random(n) < 0.15).astype(np.uint8)
+    w = O.equilibrium(q, 0, 0, 0, 1.0)
+    f0 = w[None, :] * (1.0 + 0.05 * rng.standard_normal((n, q)))
+    tau, tnh, steps = 0.53, 0.65, 29
+    want = O.fp32_periodic_solid(q, nx, ny, nz, solid, op, tau, tnh, f0.ravel(), steps).reshape(n, q)
+    with eg().Lattice(q, nx, ny, nz, solid, tau, tnh, op, eg().FP32_SHIFTED) as lat:
+        lat.set_populations(f0[solid == 0].ravel())
+        lat.step(steps)
+        got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, q)
+    assert np.array_equal(got, want[solid == 0])
