@@ -16,7 +16,10 @@
  *   - every later step pulls g_i from node (x - c_ix, y - c_iy, z - c_iz) (periodic) and collides;
  *     when that node is solid, g_i is the population of the opposite direction that this node sent
  *     towards it in the previous step (halfway bounce-back);
- *   - solid nodes are never updated.
+ *   - solid nodes are never updated;
+ *   - optionally (orc32_channel) a D3Q19 Zou-He velocity inlet plane and a density outlet plane
+ *     (devnull_rho_x: the inner neighbour's populations rescaled to rho_out), applied after the pull and
+ *     before the collision, in the same FP32 / FP64 split as the engine.
  * The result is the post-collision populations, returned as f = (double)g + w for every node of the box
  * in x-fastest order (solid nodes carry their input).
  */
@@ -205,13 +208,74 @@ static void collide19_f32(float g[19], float d1, float kd, int op)
 
 static int opp(int i) { return i == 0 ? 0 : (i % 2 ? i + 1 : i - 1); }
 
+typedef struct {
+    int inlet_x, outlet_x;
+    double u_in, rho_out;
+    double inv_1mvx, vx3, vx6; /* formed once per run, as the engine's zou_he_prep */
+} Planes;
+
+/* Zou-He velocity inlet on shifted D3Q19 populations: rho = (1 + 2 G_minus + G_zero) / (1 - vx) in
+ * FP64, the population sums and the transverse corrections in FP32 (ZouHeD3Q19_vx_x's closure). */
+static void zou_he19(float g[19], const Planes *pl, int left)
+{
+    const float ty = ((((g[18] + g[3]) + g[16]) - g[15]) - g[4]) - g[17];
+    const float tz = ((((g[17] + g[5]) + g[16]) - g[15]) - g[6]) - g[18];
+    const float gz = (((g[0] + g[3]) + (g[4] + g[5])) + ((g[6] + g[15]) + (g[16] + g[17]))) + g[18];
+    if (left) {
+        const float gm = ((g[1] + g[7]) + (g[9] + g[11])) + g[13];
+        const double rho = (1.0 + (2.0 * (double)gm + (double)gz)) * pl->inv_1mvx;
+        const float a3 = (float)(rho * pl->vx3), a6 = (float)(rho * pl->vx6);
+        g[1] = g[1] + a3;
+        g[7] = g[7] + fmaf(-0.5f, ty, a6);
+        g[9] = g[9] + fmaf(0.5f, ty, a6);
+        g[11] = g[11] + fmaf(-0.5f, tz, a6);
+        g[13] = g[13] + fmaf(0.5f, tz, a6);
+    } else {
+        const float gp = ((g[2] + g[8]) + (g[10] + g[12])) + g[14];
+        const double rho = (1.0 + (2.0 * (double)gp + (double)gz)) * pl->inv_1mvx;
+        const float a3 = (float)(rho * pl->vx3), a6 = (float)(rho * pl->vx6);
+        g[2] = g[2] - a3;
+        g[10] = g[10] - fmaf(0.5f, ty, a6);
+        g[8] = g[8] - fmaf(-0.5f, ty, a6);
+        g[14] = g[14] - fmaf(0.5f, tz, a6);
+        g[12] = g[12] - fmaf(-0.5f, tz, a6);
+    }
+}
+
+/* devnull_rho_x on shifted populations: g = g_adj + (s - 1)(g_adj + w) with
+ * s - 1 = ((rho_out - 1) - drho) / (1 + drho), all in FP32. */
+static void outlet_rescale(float *g, int q, double rho_out)
+{
+    float drho = 0.f;
+    for (int i = 0; i < q; i++) drho += g[i];
+    const float sm1 = ((float)(rho_out - 1.0) - drho) / (1.f + drho);
+    for (int i = 0; i < q; i++) g[i] = fmaf(sm1, g[i] + (float)(q == 9 ? w9(i) : w19(i)), g[i]);
+}
+
+/* populations of node (x, y, z) after the pull (or in place on the first step) */
+static void pull_node(const float *a, int q, int nx, int ny, int nz, const uint8_t *solid, int first, int x, int y,
+                      int z, float *g)
+{
+    const int *cx = q == 9 ? CX9 : CX19, *cy = q == 9 ? CY9 : CY19, *cz = q == 9 ? NULL : CZ19;
+    const size_t node = ((size_t)z * ny + y) * nx + x;
+    for (int i = 0; i < q; i++) {
+        if (first) {
+            g[i] = a[node * q + i];
+            continue;
+        }
+        const int xs = (x - cx[i] + nx) % nx, ys = (y - cy[i] + ny) % ny;
+        const int zs = cz ? (z - cz[i] + nz) % nz : z;
+        const size_t src = ((size_t)zs * ny + ys) * nx + xs;
+        g[i] = (solid && solid[src]) ? a[node * q + opp(i)] : a[src * q + i];
+    }
+}
+
 /* The stepping loop shared by both lattices: q populations per node, AoS, x fastest. */
-static int run_periodic(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
-                        const double *f_in, int n_steps, double *f_out)
+static int run_periodic(int q, int nx, int ny, int nz, const uint8_t *solid, const Planes *pl, int op, double tau,
+                        double tau_nh, const double *f_in, int n_steps, double *f_out)
 {
     if (nx < 1 || ny < 1 || nz < 1 || n_steps < 0 || !f_in || !f_out) return -1;
     if (op != ORC_OP_BGK && op != ORC_OP_REG && op != ORC_OP_EXTREG && !(op == ORC_OP_MRT && q == 9)) return -1;
-    const int *cx = q == 9 ? CX9 : CX19, *cy = q == 9 ? CY9 : CY19, *cz = q == 9 ? NULL : CZ19;
     const size_t n = (size_t)nx * ny * nz;
     float *a = malloc(n * q * sizeof(float)), *b = malloc(n * q * sizeof(float));
     if (!a || !b) {
@@ -235,15 +299,23 @@ static int run_periodic(int q, int nx, int ny, int nz, const uint8_t *solid, int
                         memcpy(&b[node * q], &a[node * q], (size_t)q * sizeof(float));
                         continue;
                     }
-                    for (int i = 0; i < q; i++) {
-                        if (s == 0) {
-                            g[i] = a[node * q + i];
-                            continue;
+                    if (pl && x == pl->outlet_x) {
+                        /* the inner neighbour's populations, rescaled to rho_out (a solid neighbour
+                         * gives the rest state w rho_out, i.e. g = 0 at rho_out = 1) */
+                        const int xn = x + (pl->outlet_x < nx / 2 ? 1 : -1);
+                        if (solid && solid[node + (size_t)(xn - x)]) {
+                            for (int i = 0; i < q; i++) {
+                                const double w = q == 9 ? w9(i) : w19(i);
+                                g[i] = (float)(w * pl->rho_out - w);
+                            }
+                        } else {
+                            pull_node(a, q, nx, ny, nz, solid, s == 0, xn, y, z, g);
+                            if (xn == pl->inlet_x) zou_he19(g, pl, pl->inlet_x < nx / 2);
+                            outlet_rescale(g, q, pl->rho_out);
                         }
-                        const int xs = (x - cx[i] + nx) % nx, ys = (y - cy[i] + ny) % ny;
-                        const int zs = cz ? (z - cz[i] + nz) % nz : z;
-                        const size_t src = ((size_t)zs * ny + ys) * nx + xs;
-                        g[i] = (solid && solid[src]) ? a[node * q + opp(i)] : a[src * q + i];
+                    } else {
+                        pull_node(a, q, nx, ny, nz, solid, s == 0, x, y, z, g);
+                        if (pl && x == pl->inlet_x) zou_he19(g, pl, pl->inlet_x < nx / 2);
                     }
                     if (q == 9)
                         collide9_f32(g, d1, kd, op);
@@ -265,18 +337,39 @@ static int run_periodic(int q, int nx, int ny, int nz, const uint8_t *solid, int
 int orc32_periodic_d2q9(int nx, int ny, int op, double tau, double tau_nh, const double *f_in, int n_steps,
                         double *f_out)
 {
-    return run_periodic(9, nx, ny, 1, NULL, op, tau, tau_nh, f_in, n_steps, f_out);
+    return run_periodic(9, nx, ny, 1, NULL, NULL, op, tau, tau_nh, f_in, n_steps, f_out);
 }
 
 int orc32_periodic_d3q19(int nx, int ny, int nz, int op, double tau, double tau_nh, const double *f_in,
                          int n_steps, double *f_out)
 {
-    return run_periodic(19, nx, ny, nz, NULL, op, tau, tau_nh, f_in, n_steps, f_out);
+    return run_periodic(19, nx, ny, nz, NULL, NULL, op, tau, tau_nh, f_in, n_steps, f_out);
 }
 
 int orc32_periodic_solid(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
                          const double *f_in, int n_steps, double *f_out)
 {
     if ((q != 9 && q != 19) || (q == 9 && nz != 1)) return -1;
-    return run_periodic(q, nx, ny, nz, solid, op, tau, tau_nh, f_in, n_steps, f_out);
+    return run_periodic(q, nx, ny, nz, solid, NULL, op, tau, tau_nh, f_in, n_steps, f_out);
+}
+
+int orc32_channel(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
+                  int inlet_x, double u_in, int outlet_x, double rho_out, const double *f_in, int n_steps,
+                  double *f_out)
+{
+    if ((q != 9 && q != 19) || (q == 9 && nz != 1)) return -1;
+    if (inlet_x >= nx || outlet_x >= nx || (inlet_x >= 0 && q != 19)) return -1;
+    if (outlet_x >= 0) {
+        const int xn = outlet_x + (outlet_x < nx / 2 ? 1 : -1);
+        if (xn < 0 || xn >= nx) return -1;
+    }
+    Planes pl;
+    pl.inlet_x = inlet_x < 0 ? -1 : inlet_x;
+    pl.outlet_x = outlet_x < 0 ? -1 : outlet_x;
+    pl.u_in = u_in;
+    pl.rho_out = rho_out;
+    pl.inv_1mvx = 1.0 / (1.0 - u_in);
+    pl.vx3 = u_in / 3.0;
+    pl.vx6 = u_in / 6.0;
+    return run_periodic(q, nx, ny, nz, solid, &pl, op, tau, tau_nh, f_in, n_steps, f_out);
 }

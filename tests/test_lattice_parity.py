@@ -366,3 +366,28 @@ def test_generic_fp32_kernel_with_solids_equals_its_cpu_restatement(q, shape, op
         lat.step(steps)
         got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, q)
     assert np.array_equal(got, want[solid == 0])
+
+
+@pytest.mark.parametrize("sx,op,mirrored,steps", [(1, 1, False, 300), (1, 3, False, 300), (1, 4, False, 300),
+                                                  (2, 4, False, 200), (1, 4, True, 300)])
+def test_fp32_obstacle_channel_equals_its_cpu_restatement(sx, op, mirrored, steps):
+    """The obstacle channel in FP32 through the generic step kernel (bounce-back at the walls and the
+    obstacle, the D3Q19 Zou-He inlet, the density outlet) gives bit for bit the populations of the FP32
+    restatement (oracle/fp32_shifted.c); mirrored, the inlet is on the right and the flow runs to -x."""
+    nx, ny, solid = O.obstacle_geometry(sx, sx)
+    inlet, outlet, u = 1, nx - 2, 0.05
+    if mirrored:
+        solid = solid.reshape(ny, nx)[:, ::-1].ravel().copy()
+        inlet, outlet, u = nx - 2, 1, -0.05
+    tau = 0.6 if op == 1 else 0.52
+    n = nx * ny
+    w = O.equilibrium(19, 0, 0, 0, 1.0)
+    rng = np.random.default_rng(sx * 10 + op)
+    f0 = w[None, :] * (1.0 + 0.02 * rng.standard_normal((n, 19)))
+    want = O.fp32_channel(19, nx, ny, 1, solid, op, tau, 0.65, f0.ravel(), steps, inlet, u, outlet,
+                          1.0).reshape(n, 19)
+    with eg().Lattice(19, nx, ny, 1, solid, tau, 0.65, op, eg().FP32_SHIFTED) as lat:
+        lat.set_populations(f0[solid == 0].ravel())
+        lat.step(steps, dict(inlet_x=inlet, u_in=u, outlet_x=outlet, rho_out=1.0))
+        got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, 19)
+    assert np.array_equal(got, want[solid == 0])

@@ -325,3 +325,27 @@ def test_fp32_restatement_with_solids_tracks_the_fp64_oracle(q, shape):
         # solid nodes are left as given
         assert np.array_equal(got[solid == 1],
                               (f0[solid == 1] - w).astype(np.float32).astype(np.float64) + w)
+
+
+@pytest.mark.parametrize("op,mirrored", [(1, False), (3, False), (4, False), (4, True)])
+def test_fp32_channel_restatement_tracks_the_fp64_oracle(op, mirrored):
+    """The FP32 restatement of the obstacle channel (walls and obstacle with halfway bounce-back, the
+    D3Q19 Zou-He inlet, the density outlet) stays within 2e-6 relative of the FP64 oracle after 300
+    steps from rest; mirrored, the inlet is on the right and the flow runs towards -x."""
+    nx, ny, solid = O.obstacle_geometry(1, 1)
+    inlet, outlet, u = 1, nx - 2, 0.05
+    if mirrored:
+        solid = solid.reshape(ny, nx)[:, ::-1].ravel().copy()
+        inlet, outlet, u = nx - 2, 1, -0.05
+    tau = 0.6 if op == 1 else 0.52
+    n = nx * ny
+    w = O.equilibrium(19, 0, 0, 0, 1.0)
+    f0 = np.tile(w, (n, 1))
+    got = O.fp32_channel(19, nx, ny, 1, solid, op, tau, 0.65, f0.ravel(), 300, inlet, u, outlet, 1.0).reshape(n, 19)
+    ref = O.Lattice(19, nx, ny, 1, solid, tau, 0.65, op)
+    ref.set(f0[solid == 0].ravel())
+    ref.step(300, dict(inlet_x=inlet, u_in=u, outlet_x=outlet, rho_out=1.0))
+    want = ref.get(1).reshape(-1, 19)
+    assert np.linalg.norm(got[solid == 0] - want) / np.linalg.norm(want - w[None, :]) < 2e-6
+    with pytest.raises(ValueError):  # the Zou-He inlet of the restatement is D3Q19's
+        O.fp32_channel(9, 8, 8, 1, None, 4, 0.6, 0.65, np.zeros(8 * 8 * 9), 1, 1, 0.05, -1, 1.0)
