@@ -223,3 +223,23 @@ def test_ctypes_structs_match_the_header(tmp_path):
         assert got[(pyname, "size")] == C.sizeof(cls), pyname
         for fname, _ in cls._fields_:
             assert got[(pyname, fname)] == getattr(cls, fname).offset, (pyname, fname)
+
+
+def test_product_never_loads_the_oracle():
+    """The package is the product and the oracle is only the checker: importing erlbm_gb300 and loading
+    its library in a fresh interpreter imports no oracle module and maps no oracle library, and no source
+    of the package names the oracle."""
+    import subprocess
+    import sys
+    code = ("import sys, erlbm_gb300 as m; m.lib(); "
+            "maps = open('/proc/self/maps').read() if sys.platform.startswith('linux') else ''; "
+            "print(any(k == 'oracle' or k.startswith('oracle.') for k in sys.modules), 'erlbm_oracle' in maps)")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, check=True)
+    assert out.stdout.split() == ["False", "False"], out.stdout
+    pkg = os.path.join(ROOT, "erlbm_gb300")
+    for d, _, files in os.walk(pkg):
+        if "_build" in d:
+            continue
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h")):
+                assert "oracle" not in open(os.path.join(d, f)).read(), f
