@@ -421,12 +421,15 @@ __device__ __forceinline__ void zou_he(float g[19], const ZouHe &z, bool left)
 
 // ZouHeD2Q9_vx_x (Boundary_conditions.cpp:710-744) on shifted populations: the weights of the
 // closure's index set sum to 1, so rho = (1 + G) / (1 - vx) with G = g0 + g3 + g4 + 2 (g2 + g8 + g6),
-// and g_i = w_i (rho P - 1) with P = 1 + 3 vx + 3 vx^2 for the +x movers (rho P - 1 in FP64).
+// and g_i = w_i (rho P - 1) with P = 1 + 3 vx + 3 vx^2 for the +x movers (rho P - 1 in FP64).  The
+// FP64 products and sums are explicitly rounded, so no contraction changes them.
 __device__ __forceinline__ void zou_he_d2q9(float g[9], double vx)
 {
     const float G = ((g[0] + g[3]) + g[4]) + 2.f * ((g[2] + g[8]) + g[6]);
     const double rho = (1.0 + (double)G) / (1.0 - vx);
-    const double e = rho * ((1.0 + 3.0 * vx) + 3.0 * vx * vx) - 1.0;
+    const double vx3 = __dmul_rn(3.0, vx);
+    const double P = __dadd_rn(__dadd_rn(1.0, vx3), __dmul_rn(vx3, vx));
+    const double e = __dadd_rn(__dmul_rn(rho, P), -1.0);
     g[1] = (float)(e / 9.0);
     g[5] = (float)(e / 36.0);
     g[7] = (float)(e / 36.0);

@@ -92,11 +92,12 @@ int orc32_periodic_d3q19(int nx, int ny, int nz, int op, double tau, double tau_
  * f_in and f_out hold every node of the box, solid nodes included (left as given) */
 int orc32_periodic_solid(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
                          const double *f_in, int n_steps, double *f_out);
-/* the same with boundary planes: a D3Q19 Zou-He velocity inlet u_in at inlet_x and a density outlet
- * (devnull_rho_x, rho_out) at outlet_x; -1 = none */
+/* the same with boundary planes (-1 = none): a Zou-He velocity inlet u_in at inlet_x; an outlet at
+ * outlet_x of kind 0 (devnull_rho_x to rho_out), 1 (OpenBoundaryD2Q9_x) or 2 (convective_x); the
+ * open y plane open_y of D2Q9 (OpenBoundaryD2Q9_y) */
 int orc32_channel(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
-                  int inlet_x, double u_in, int outlet_x, double rho_out, const double *f_in, int n_steps,
-                  double *f_out);
+                  int inlet_x, double u_in, int outlet_x, int outlet_kind, double rho_out, int open_y,
+                  const double *f_in, int n_steps, double *f_out);
 
 #ifdef __cplusplus
 }

@@ -17,9 +17,10 @@
  *     when that node is solid, g_i is the population of the opposite direction that this node sent
  *     towards it in the previous step (halfway bounce-back);
  *   - solid nodes are never updated;
- *   - optionally (orc32_channel) a D3Q19 Zou-He velocity inlet plane and a density outlet plane
- *     (devnull_rho_x: the inner neighbour's populations rescaled to rho_out), applied after the pull and
- *     before the collision, in the same FP32 / FP64 split as the engine.
+ *   - optionally (orc32_channel) boundary planes, applied after the pull and before the collision, in
+ *     the same FP32 / FP64 split as the engine: a Zou-He velocity inlet (D3Q19 or D2Q9); an outlet
+ *     that is the inner neighbour rescaled to rho_out (devnull_rho_x), open (OpenBoundaryD2Q9_x) or
+ *     convective (convective_x); and the open y plane of D2Q9 (OpenBoundaryD2Q9_y).
  * The result is the post-collision populations, returned as f = (double)g + w for every node of the box
  * in x-fastest order (solid nodes carry their input).
  */
@@ -209,10 +210,51 @@ static void collide19_f32(float g[19], float d1, float kd, int op)
 static int opp(int i) { return i == 0 ? 0 : (i % 2 ? i + 1 : i - 1); }
 
 typedef struct {
-    int inlet_x, outlet_x;
+    int inlet_x, outlet_x, outlet_kind, open_y;
     double u_in, rho_out;
     double inv_1mvx, vx3, vx6; /* formed once per run, as the engine's zou_he_prep */
 } Planes;
+
+enum { OUTLET_DENSITY = 0, OUTLET_OPEN = 1, OUTLET_CONVECTIVE = 2 };
+
+/* ZouHeD2Q9_vx_x on shifted populations: rho = (1 + G) / (1 - vx), g_i = w_i (rho P - 1) for the +x
+ * movers with P = (1 + 3 vx) + (3 vx) vx, in FP64 with every operation rounded separately. */
+static void zou_he9(float g[9], double vx)
+{
+    const float G = ((g[0] + g[3]) + g[4]) + 2.f * ((g[2] + g[8]) + g[6]);
+    const double rho = (1.0 + (double)G) / (1.0 - vx);
+    const double vx3 = 3.0 * vx;
+    const double P = (1.0 + vx3) + vx3 * vx;
+    const double e = rho * P - 1.0;
+    g[1] = (float)(e / 9.0);
+    g[5] = (float)(e / 36.0);
+    g[7] = (float)(e / 36.0);
+}
+
+/* x velocity of a node in FP32, as the engine's moments: u_x = m_x / (1 + drho) */
+static float node_ux(const float *g, int q)
+{
+    float drho, mx;
+    if (q == 9) {
+        const float eX = g[1] + g[2], eY = g[3] + g[4], eP = g[5] + g[6], eM = g[7] + g[8];
+        drho = g[0] + ((eX + eY) + (eP + eM));
+        mx = (g[1] - g[2]) + ((g[5] - g[6]) + (g[7] - g[8]));
+    } else {
+        const float e1 = (g[1] + g[2]) + (g[3] + g[4]), e2 = (g[5] + g[6]) + (g[7] + g[8]);
+        const float e3 = (g[9] + g[10]) + (g[11] + g[12]), e4 = (g[13] + g[14]) + (g[15] + g[16]);
+        drho = (g[0] + (e1 + e2)) + ((e3 + e4) + (g[17] + g[18]));
+        mx = ((g[1] - g[2]) + ((g[7] - g[8]) + (g[9] - g[10]))) + ((g[11] - g[12]) + (g[13] - g[14]));
+    }
+    const float inv = 1.f / (1.f + drho);
+    return mx * inv;
+}
+
+/* convective_x on shifted populations: g = (g + U g_a) / (1 + U), U the inner neighbour's u_x */
+static void convective(float *g, const float *a, int q)
+{
+    const float u = node_ux(a, q), factor = 1.f / (1.f + u);
+    for (int i = 0; i < q; i++) g[i] = factor * fmaf(u, a[i], g[i]);
+}
 
 /* Zou-He velocity inlet on shifted D3Q19 populations: rho = (1 + 2 G_minus + G_zero) / (1 - vx) in
  * FP64, the population sums and the transverse corrections in FP32 (ZouHeD3Q19_vx_x's closure). */
@@ -270,6 +312,81 @@ static void pull_node(const float *a, int q, int nx, int ny, int nz, const uint8
     }
 }
 
+static void apply_inlet(float *g, int q, int nx, const Planes *pl)
+{
+    if (q == 19)
+        zou_he19(g, pl, pl->inlet_x < nx / 2);
+    else
+        zou_he9(g, pl->u_in);
+}
+
+/* populations of fluid node (x, y, z) after this step's inlet and outlet planes */
+static void after_x_planes(const float *a, int q, int nx, int ny, int nz, const uint8_t *solid, const Planes *pl,
+                           int first, int x, int y, int z, float *g)
+{
+    const size_t node = ((size_t)z * ny + y) * nx + x;
+    if (pl && x == pl->outlet_x) {
+        const int xn = x + (pl->outlet_x < nx / 2 ? 1 : -1);
+        const int nsolid = solid && solid[node + (size_t)(xn - x)];
+        if (pl->outlet_kind == OUTLET_DENSITY) {
+            if (nsolid) { /* the rest state w rho_out */
+                for (int i = 0; i < q; i++) {
+                    const double w = q == 9 ? w9(i) : w19(i);
+                    g[i] = (float)(w * pl->rho_out - w);
+                }
+                return;
+            }
+            pull_node(a, q, nx, ny, nz, solid, first, xn, y, z, g);
+            if (xn == pl->inlet_x) apply_inlet(g, q, nx, pl);
+            outlet_rescale(g, q, pl->rho_out);
+            return;
+        }
+        pull_node(a, q, nx, ny, nz, solid, first, x, y, z, g);
+        if (nsolid) return;
+        float an[19];
+        pull_node(a, q, nx, ny, nz, solid, first, xn, y, z, an);
+        if (xn == pl->inlet_x) apply_inlet(an, q, nx, pl);
+        if (pl->outlet_kind == OUTLET_OPEN) { /* the populations entering from outside */
+            if (xn > x) {
+                g[1] = an[1];
+                g[5] = an[5];
+                g[7] = an[7];
+            } else {
+                g[2] = an[2];
+                g[6] = an[6];
+                g[8] = an[8];
+            }
+        } else {
+            convective(g, an, q);
+        }
+        return;
+    }
+    pull_node(a, q, nx, ny, nz, solid, first, x, y, z, g);
+    if (pl && x == pl->inlet_x) apply_inlet(g, q, nx, pl);
+}
+
+/* the x planes, then the open y plane (D2Q9): the populations entering through it are the inner
+ * neighbour's, taken after that neighbour's own x planes */
+static void after_planes(const float *a, int q, int nx, int ny, int nz, const uint8_t *solid, const Planes *pl,
+                         int first, int x, int y, int z, float *g)
+{
+    after_x_planes(a, q, nx, ny, nz, solid, pl, first, x, y, z, g);
+    if (!pl || q != 9 || y != pl->open_y) return;
+    const int yn = y + (pl->open_y < ny / 2 ? 1 : -1);
+    if (solid && solid[(size_t)yn * nx + x]) return;
+    float an[9];
+    after_x_planes(a, q, nx, ny, nz, solid, pl, first, x, yn, z, an);
+    if (yn > y) {
+        g[3] = an[3];
+        g[5] = an[5];
+        g[8] = an[8];
+    } else {
+        g[4] = an[4];
+        g[6] = an[6];
+        g[7] = an[7];
+    }
+}
+
 /* The stepping loop shared by both lattices: q populations per node, AoS, x fastest. */
 static int run_periodic(int q, int nx, int ny, int nz, const uint8_t *solid, const Planes *pl, int op, double tau,
                         double tau_nh, const double *f_in, int n_steps, double *f_out)
@@ -299,24 +416,7 @@ static int run_periodic(int q, int nx, int ny, int nz, const uint8_t *solid, con
                         memcpy(&b[node * q], &a[node * q], (size_t)q * sizeof(float));
                         continue;
                     }
-                    if (pl && x == pl->outlet_x) {
-                        /* the inner neighbour's populations, rescaled to rho_out (a solid neighbour
-                         * gives the rest state w rho_out, i.e. g = 0 at rho_out = 1) */
-                        const int xn = x + (pl->outlet_x < nx / 2 ? 1 : -1);
-                        if (solid && solid[node + (size_t)(xn - x)]) {
-                            for (int i = 0; i < q; i++) {
-                                const double w = q == 9 ? w9(i) : w19(i);
-                                g[i] = (float)(w * pl->rho_out - w);
-                            }
-                        } else {
-                            pull_node(a, q, nx, ny, nz, solid, s == 0, xn, y, z, g);
-                            if (xn == pl->inlet_x) zou_he19(g, pl, pl->inlet_x < nx / 2);
-                            outlet_rescale(g, q, pl->rho_out);
-                        }
-                    } else {
-                        pull_node(a, q, nx, ny, nz, solid, s == 0, x, y, z, g);
-                        if (pl && x == pl->inlet_x) zou_he19(g, pl, pl->inlet_x < nx / 2);
-                    }
+                    after_planes(a, q, nx, ny, nz, solid, pl, s == 0, x, y, z, g);
                     if (q == 9)
                         collide9_f32(g, d1, kd, op);
                     else
@@ -354,18 +454,26 @@ int orc32_periodic_solid(int q, int nx, int ny, int nz, const uint8_t *solid, in
 }
 
 int orc32_channel(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
-                  int inlet_x, double u_in, int outlet_x, double rho_out, const double *f_in, int n_steps,
-                  double *f_out)
+                  int inlet_x, double u_in, int outlet_x, int outlet_kind, double rho_out, int open_y,
+                  const double *f_in, int n_steps, double *f_out)
 {
     if ((q != 9 && q != 19) || (q == 9 && nz != 1)) return -1;
-    if (inlet_x >= nx || outlet_x >= nx || (inlet_x >= 0 && q != 19)) return -1;
+    if (inlet_x >= nx || outlet_x >= nx || open_y >= ny) return -1;
+    if (outlet_kind < OUTLET_DENSITY || outlet_kind > OUTLET_CONVECTIVE) return -1;
+    if (q == 19 && ((outlet_x >= 0 && outlet_kind == OUTLET_OPEN) || open_y >= 0)) return -1; /* D2Q9 planes */
     if (outlet_x >= 0) {
         const int xn = outlet_x + (outlet_x < nx / 2 ? 1 : -1);
         if (xn < 0 || xn >= nx) return -1;
     }
+    if (open_y >= 0) {
+        const int yn = open_y + (open_y < ny / 2 ? 1 : -1);
+        if (yn < 0 || yn >= ny) return -1;
+    }
     Planes pl;
     pl.inlet_x = inlet_x < 0 ? -1 : inlet_x;
     pl.outlet_x = outlet_x < 0 ? -1 : outlet_x;
+    pl.outlet_kind = outlet_kind;
+    pl.open_y = open_y < 0 ? -1 : open_y;
     pl.u_in = u_in;
     pl.rho_out = rho_out;
     pl.inv_1mvx = 1.0 / (1.0 - u_in);

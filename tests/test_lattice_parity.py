@@ -391,3 +391,47 @@ def test_fp32_obstacle_channel_equals_its_cpu_restatement(sx, op, mirrored, step
         lat.step(steps, dict(inlet_x=inlet, u_in=u, outlet_x=outlet, rho_out=1.0))
         got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, 19)
     assert np.array_equal(got, want[solid == 0])
+
+
+@pytest.mark.parametrize("outlet_kind,open_top,op", [(k, t, op) for k in (0, 1, 2) for t in (False, True)
+                                                     for op in (1, 4)] + [(1, True, 2), (2, False, 3)])
+def test_fp32_d2q9_planes_equal_their_cpu_restatement(outlet_kind, open_top, op):
+    """A D2Q9 channel in FP32 through the generic step kernel (the Zou-He inlet; the density, open or
+    convective outlet; the open y plane at the top; walls and a block obstacle) gives bit for bit the
+    populations of the FP32 restatement (oracle/fp32_shifted.c)."""
+    nx, ny = 40, 18
+    solid = np.zeros((ny, nx), np.uint8)
+    solid[0, :] = 1
+    if not open_top:
+        solid[ny - 1, :] = 1
+    solid[7:11, 10:13] = 1
+    solid = solid.ravel()
+    n = nx * ny
+    open_y = ny - 1 if open_top else -1
+    w = O.equilibrium(9, 0, 0, 0, 1.0)
+    rng = np.random.default_rng(outlet_kind * 10 + op + 100 * open_top)
+    f0 = w[None, :] * (1.0 + 0.02 * rng.standard_normal((n, 9)))
+    tau = 0.6 if op in (1, 2) else 0.53
+    want = O.fp32_channel(9, nx, ny, 1, solid, op, tau, 0.65, f0.ravel(), 250, 1, 0.05, nx - 2, 1.0, outlet_kind,
+                          open_y).reshape(n, 9)
+    with eg().Lattice(9, nx, ny, 1, solid, tau, 0.65, op, eg().FP32_SHIFTED) as lat:
+        lat.set_populations(f0[solid == 0].ravel())
+        lat.step(250, dict(inlet_x=1, u_in=0.05, outlet_x=nx - 2, outlet_kind=outlet_kind, rho_out=1.0,
+                           open_y=open_y))
+        got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, 9)
+    assert np.array_equal(got, want[solid == 0])
+
+
+def test_fp32_d3q19_convective_outlet_equals_its_cpu_restatement():
+    """The obstacle channel in FP32 with a convective outlet: bit for bit the FP32 restatement."""
+    nx, ny, solid = O.obstacle_geometry(1, 1)
+    n = nx * ny
+    w = O.equilibrium(19, 0, 0, 0, 1.0)
+    f0 = w[None, :] * (1.0 + 0.02 * np.random.default_rng(5).standard_normal((n, 19)))
+    want = O.fp32_channel(19, nx, ny, 1, solid, 4, 0.52, 0.65, f0.ravel(), 300, 1, 0.05, nx - 2, 1.0,
+                          2).reshape(n, 19)
+    with eg().Lattice(19, nx, ny, 1, solid, 0.52, 0.65, 4, eg().FP32_SHIFTED) as lat:
+        lat.set_populations(f0[solid == 0].ravel())
+        lat.step(300, dict(inlet_x=1, u_in=0.05, outlet_x=nx - 2, outlet_kind=2, rho_out=1.0))
+        got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, 19)
+    assert np.array_equal(got, want[solid == 0])

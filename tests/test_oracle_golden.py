@@ -347,5 +347,55 @@ def test_fp32_channel_restatement_tracks_the_fp64_oracle(op, mirrored):
     ref.step(300, dict(inlet_x=inlet, u_in=u, outlet_x=outlet, rho_out=1.0))
     want = ref.get(1).reshape(-1, 19)
     assert np.linalg.norm(got[solid == 0] - want) / np.linalg.norm(want - w[None, :]) < 2e-6
-    with pytest.raises(ValueError):  # the Zou-He inlet of the restatement is D3Q19's
-        O.fp32_channel(9, 8, 8, 1, None, 4, 0.6, 0.65, np.zeros(8 * 8 * 9), 1, 1, 0.05, -1, 1.0)
+    with pytest.raises(ValueError):  # the open outlet is a D2Q9 plane
+        O.fp32_channel(19, 8, 8, 2, None, 4, 0.6, 0.65, np.zeros(8 * 8 * 2 * 19), 1, outlet_x=6, outlet_kind=1)
+
+
+def _d2q9_channel(open_top):
+    """40 x 18 channel: walls at y = 0 and y = 17 (none at the top when it is the open y plane) and a
+    3 x 4 block obstacle."""
+    nx, ny = 40, 18
+    solid = np.zeros((ny, nx), np.uint8)
+    solid[0, :] = 1
+    if not open_top:
+        solid[ny - 1, :] = 1
+    solid[7:11, 10:13] = 1
+    return nx, ny, solid.ravel()
+
+
+@pytest.mark.parametrize("outlet_kind", [0, 1, 2])
+@pytest.mark.parametrize("open_top", [False, True])
+def test_fp32_d2q9_planes_restatement_tracks_the_fp64_oracle(outlet_kind, open_top):
+    """The FP32 restatement of a D2Q9 channel (Zou-He inlet; density, open or convective outlet; the open
+    y plane at the top) stays within 2e-6 relative of the FP64 oracle after 300 steps, every operator."""
+    nx, ny, solid = _d2q9_channel(open_top)
+    n = nx * ny
+    w = O.equilibrium(9, 0, 0, 0, 1.0)
+    f0 = np.tile(w, (n, 1))
+    open_y = ny - 1 if open_top else -1
+    bc = dict(inlet_x=1, u_in=0.05, outlet_x=nx - 2, outlet_kind=outlet_kind, rho_out=1.0, open_y=open_y)
+    for op in (1, 2, 3, 4):
+        tau = 0.6 if op in (1, 2) else 0.53
+        got = O.fp32_channel(9, nx, ny, 1, solid, op, tau, 0.65, f0.ravel(), 300, 1, 0.05, nx - 2, 1.0,
+                             outlet_kind, open_y).reshape(n, 9)
+        ref = O.Lattice(9, nx, ny, 1, solid, tau, 0.65, op)
+        ref.set(f0[solid == 0].ravel())
+        ref.step(300, bc)
+        want = ref.get(1).reshape(-1, 9)
+        assert np.linalg.norm(got[solid == 0] - want) / np.linalg.norm(want - w[None, :]) < 2e-6, op
+
+
+def test_fp32_d3q19_convective_restatement_tracks_the_fp64_oracle():
+    """The obstacle channel with a convective outlet instead of the density outlet: the FP32 restatement
+    stays within 2e-6 relative of the FP64 oracle after 300 steps."""
+    nx, ny, solid = O.obstacle_geometry(1, 1)
+    n = nx * ny
+    w = O.equilibrium(19, 0, 0, 0, 1.0)
+    f0 = np.tile(w, (n, 1))
+    got = O.fp32_channel(19, nx, ny, 1, solid, 4, 0.52, 0.65, f0.ravel(), 300, 1, 0.05, nx - 2, 1.0,
+                         2).reshape(n, 19)
+    ref = O.Lattice(19, nx, ny, 1, solid, 0.52, 0.65, 4)
+    ref.set(f0[solid == 0].ravel())
+    ref.step(300, dict(inlet_x=1, u_in=0.05, outlet_x=nx - 2, outlet_kind=2, rho_out=1.0))
+    want = ref.get(1).reshape(-1, 19)
+    assert np.linalg.norm(got[solid == 0] - want) / np.linalg.norm(want - w[None, :]) < 2e-6
