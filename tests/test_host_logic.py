@@ -243,3 +243,23 @@ def test_product_never_loads_the_oracle():
         for f in files:
             if f.endswith((".py", ".cu", ".cuh", ".h")):
                 assert "oracle" not in open(os.path.join(d, f)).read(), f
+
+
+def test_reference_arm_prints_the_contract_line():
+    """bench.py --impl reference times the reference's CPU path (the reference compiled from its sources
+    where present, else the oracle port) without a GPU and prints one JSON line with the arm's keys: the
+    metric of the engine's arm, a cpu_baseline describing the run and an e2e with no copies."""
+    import json
+    import subprocess
+    import sys
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3"],
+                         cwd=ROOT, capture_output=True, text=True, check=True, timeout=600)
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == "MLUPS" and line["unit"] == "MLUPS"
+    assert line["value"] > 0 and line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 3
+    cb = line["cpu_baseline"]
+    assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert cb["unit"] == "MLUPS" and cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["config"]["L"] == 2048
