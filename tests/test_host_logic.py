@@ -263,3 +263,22 @@ def test_reference_arm_prints_the_contract_line():
     assert line["e2e"] == {"value": line["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert line["config"]["L"] == 2048
+
+
+def test_reference_arm_under_torchrun_prints_once():
+    """Launched as the multi-GPU bench is (torchrun, two ranks), the reference arm runs on rank 0 alone:
+    one JSON line, n_gpus = 2, and every rank exits 0."""
+    import json
+    import socket
+    import subprocess
+    import sys
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                          "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl",
+                          "reference", "--gpus", "2", "--steps", "1", "--warmup", "3"],
+                         cwd=ROOT, capture_output=True, text=True, check=True, timeout=600)
+    lines = [json.loads(x) for x in out.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1, out.stdout
+    assert lines[0]["impl"] == "reference" and lines[0]["n_gpus"] == 2 and lines[0]["value"] > 0
