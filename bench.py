@@ -12,6 +12,11 @@ run on, with the populations already resident in HBM.  The working set (2 x 9 x 
 initial populations from pinned host memory (erlbm_set_populations, AoS doubles), runs `inner`
 steps (erlbm_step) and reads the kinetic energy back (erlbm_kinetic_energy), wall-clock timed.
 
+`fp64` is the plain FP64 path on the same lattice, the drop-in that reproduces the reference's FP64
+results bit for bit: device-timed MLUPS, its own `e2e` through the C ABI, and its roofline against
+the GPU's FP64 add / multiply rate (measured in the run) and against the HBM copy peak.  It is the
+like-for-like comparison with the reference arm, which computes in FP64 too.
+
 `cpu_baseline` times the CPU restatement of the reference's algorithm (oracle/, AoS + push map,
 OpenMP over all host cores) on a bounded sample of the same workload.  `--impl reference` runs the
 reference's own CPU code when it could be compiled from its sources here (oracle/_ref), otherwise
@@ -68,6 +73,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--L", type=int, default=2048)
     p.add_argument("--inner", type=int, default=1000, help="LBM steps per bench step")
+    p.add_argument("--inner-fp64", type=int, default=100,
+                   help="dsl: LBM steps per bench step of the plain FP64 block beside the FP32-shifted line")
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "refined"],
                    help="refined (map workloads): the whole map-points x map-points grid screened in FP32 with "
                         "the boundary points re-run in FP64")
@@ -184,66 +191,96 @@ class Clocks:
 # CPU legs (the only places bench.py executes oracle/)
 # ------------------------------------------------------------------------------------------------
 
+class CpuDsl:
+    """The reference's CPU algorithm for the double shear layer on this host's cores: the reference
+    library compiled from its sources (oracle/_ref, only where it was built) or the oracle's
+    restatement of it.  run(n) advances n steps and returns the seconds they took."""
+
+    def __init__(self, L: int, prefer_reference: bool, op_name: str = "erlbm"):
+        from oracle import oracle as O
+        self.L = L
+        self.threads = os.cpu_count() or 1
+        self.tau = tau_of(L)
+        self.op, self.tnh, self.label = DSL_OPS[op_name]
+        self.f0 = O.init_double_shear(L)
+        self.kind = "port"
+        self.overhead = 0.0
+        if prefer_reference and O.ref_available(9):
+            import ctypes as C
+            lib = O.load_ref(9)
+            fn = lib.ref9_run_threads
+            fn.restype = C.c_int
+            fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_void_p,
+                           C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
+                           C.c_int]
+            self._fn = fn
+            self.kind = "reference"
+            # each harness call sets the lattice up and copies its output: that fixed cost (a 1-step call
+            # less one step, the step time taken from a 1-step and a 5-step call) is taken out of every sample
+            t1 = self._call(1)
+            t5 = self._call(5)
+            self.step_s = max((t5 - t1) / 4, 1e-6)
+            self.overhead = max(0.0, t1 - self.step_s)
+        else:
+            self._lat = O.Lattice(9, L, L, 1, None, self.tau, self.tnh, self.op)
+            self._lat.set(self.f0)
+
+    def _call(self, n: int) -> float:
+        t = time.perf_counter()
+        self._fn(self.L, self.L, 1, None, self.op, self.tau, self.tnh, self.f0.ctypes.data, n, -1, 0.0, -1, 1.0,
+                 None, None, None, self.threads)
+        return time.perf_counter() - t
+
+    def run(self, n: int) -> float:
+        if self.kind == "reference":
+            return max(self._call(n) - self.overhead, 1e-9)
+        t = time.perf_counter()
+        self._lat.step(n, threads=self.threads)
+        return time.perf_counter() - t
+
+    def steps_for(self, seconds: float) -> int:
+        """LBM steps that take about `seconds` here (from a short probe)."""
+        t1 = self.step_s if self.kind == "reference" else self.run(2) / 2
+        return max(2, min(2000, int(seconds / max(t1, 1e-6))))
+
+    def describe(self, n: int) -> str:
+        return (f"double shear layer D2Q9 {self.label} FP64, L={self.L}, {n} steps, "
+                f"{self.threads} OpenMP threads")
+
+
 def cpu_sample(L: int, seconds: float, prefer_reference: bool, op_name: str = "erlbm"):
-    """Time the reference's CPU algorithm on this host's cores: the reference library compiled from
-    its sources (oracle/_ref, only where it was built) or the oracle's restatement of it."""
-    import numpy as np
-    from oracle import oracle as O
-    threads = os.cpu_count() or 1
-    tau = tau_of(L)
-    op, tnh, label = DSL_OPS[op_name]
-    f0 = O.init_double_shear(L)
-    kind = "port"
-    if prefer_reference and O.ref_available(9):
-        import ctypes as C
-        lib = O.load_ref(9)
-        fn = lib.ref9_run_threads
-        fn.restype = C.c_int
-        fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_int,
-                       C.c_int, C.c_double, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
-
-        def run(n):
-            t = time.perf_counter()
-            fn(L, L, 1, None, op, tau, tnh, f0.ctypes.data, n, -1, 0.0, -1, 1.0, None, None, None, threads)
-            return time.perf_counter() - t
-        kind = "reference"
-    else:
-        lat = O.Lattice(9, L, L, 1, None, tau, tnh, op)
-        lat.set(f0)
-
-        def run(n):
-            t = time.perf_counter()
-            lat.step(n, threads=threads)
-            return time.perf_counter() - t
-    t1 = run(2) / 2
-    n = max(2, min(2000, int(seconds / max(t1, 1e-6))))
-    dt = run(n)
-    if kind == "reference":  # the harness includes set-up and output copies; subtract a 1-step run
-        dt = max(dt - run(1) + t1, 1e-9)
-    mlups = L * L * n / dt / 1e6
-    return {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": kind,
-            "sample": f"double shear layer D2Q9 {label} FP64, L={L}, {n} steps, {threads} OpenMP threads"}
+    """One bounded sample (about `seconds` of CPU work) of the reference's CPU algorithm."""
+    cpu = CpuDsl(L, prefer_reference, op_name)
+    n = cpu.steps_for(seconds)
+    dt = cpu.run(n)
+    return {"value": L * L * n / dt / 1e6, "unit": "MLUPS", "cores": cpu.threads, "kind": cpu.kind,
+            "sample": cpu.describe(n)}
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU path on the host cores.  Every bench step runs the same
+    bounded number of LBM steps (chosen once, so that the whole run takes a few minutes), and the line
+    reports exactly that count and the measured time per bench step."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    W, K = args.warmup, args.steps
-    # each bench step is a bounded sample; warm-up samples are shorter
-    per = max(1.0, min(8.0, 120.0 / max(1, K + W)))
+    W, K, L = args.warmup, args.steps, args.L
+    cpu = CpuDsl(L, True, args.op)
+    per = max(1.0, min(8.0, 120.0 / max(1, K + W)))  # seconds of CPU work per bench step
+    n = cpu.steps_for(per)
     for _ in range(W):
-        cpu_sample(args.L, per / 4, True, args.op)
-    vals = [cpu_sample(args.L, per, True, args.op) for _ in range(K)]
-    v = statistics.median(x["value"] for x in vals)
-    cb = dict(vals[-1])
-    cb["value"] = v
-    L = args.L
+        cpu.run(max(1, n // 4))
+    times = [cpu.run(n) for _ in range(K)]
+    total = sum(times)
+    v = L * L * n * K / total / 1e6
+    cb = {"value": v, "unit": "MLUPS", "cores": cpu.threads, "kind": cpu.kind,
+          "sample": cpu.describe(n) + f" per bench step, {K} bench steps"}
     line = {"metric": "MLUPS", "value": v, "unit": "MLUPS", "n_gpus": args.gpus, "steps": K, "warmup": W,
-            "ms_per_step": L * L * args.inner / (v * 1e6) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": total / K * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (double shear layer initial condition)",
             "config": {"workload": f"double shear layer D2Q9 {DSL_OPS[args.op][2]} Re=80000 L={L}", "L": L,
-                       "lbm_steps_per_step": args.inner, "precision": "fp64 (reference CPU path)"},
+                       "lbm_steps_per_step": n, "precision": "fp64 (reference CPU path)",
+                       "warmup_lbm_steps_per_step": max(1, n // 4)},
             "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -341,10 +378,12 @@ def run_ours(args):
     e2e = {"value": world * L * L * inner * K / t_e2e / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": int(f0.nbytes),
            "d2h_bytes_per_step": 8}
 
-    extras = {}
+    lat.close()
+    extras, fp64 = {}, None
     if not args.no_extras and rank == 0:
         extras = gpu_extras(E, torch, L, f0, tau, op, tnh)
-    lat.close()
+        if args.precision == "fp32":
+            fp64 = fp64_block(E, torch, L, f0, tau, op, tnh, K, W, args.inner_fp64)
 
     if rank != 0:
         if dist:
@@ -387,6 +426,8 @@ def run_ours(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if fp64:
+        line["fp64"] = fp64
     if extras:
         line["extras"] = extras
     print(json.dumps(line), flush=True)
@@ -395,34 +436,87 @@ def run_ours(args):
     return 0
 
 
-def gpu_extras(E, torch, L, f0, tau, op, tnh):
-    """Secondary figures of the metric line: the plain FP64 path on the same lattice and the
-    FP32-shifted velocity error against it after a short common run."""
-    import numpy as np
-    out = {}
-    n64 = 200
+def fp64_ops_per_lu(L: int):
+    """FP64 add and multiply operations per lattice update of the plain kernel, from the committed ncu
+    instruction counts of the same kernel (profiles/dsl_periodic_d2q9_traffic.json, "fp64")."""
+    path = os.path.join(ROOT, "profiles", "dsl_periodic_d2q9_traffic.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["fp64"]["fp64_ops_per_lu"])
+    except Exception:
+        return None
+
+
+def fp64_block(E, torch, L, f0, tau, op, tnh, K, W, inner):
+    """The plain FP64 path (bit-identical to the reference) on the same lattice: device-timed MLUPS over
+    K bench steps of `inner` LBM steps, the same end to end through the C ABI (populations from pinned
+    host memory, steps, energy back), and its roofline against this GPU's FP64 add / multiply rate
+    (measured here with erlbm_fp64_rate) and against the HBM copy peak."""
     s = torch.cuda.Stream()
-    with E.Lattice(9, L, L, 1, None, tau, tnh, op, E.FP64) as l64:
-        l64.set_stream(s.cuda_stream)
-        l64.set_populations(f0)
-        l64.step(1 + 10)
-        l64.sync()
+    out = {"lbm_steps_per_step": inner, "steps": K, "warmup": W}
+    with E.Lattice(9, L, L, 1, None, tau, tnh, op, E.FP64) as lat:
+        lat.set_stream(s.cuda_stream)
+        lat.set_populations(f0)
+        lat.step(1)
+        for _ in range(W):
+            lat.step(inner)
+        lat.sync()
+        torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(s)
-        l64.step(n64)
+        for _ in range(K):
+            lat.step(inner)
         b.record(s)
         s.synchronize()
         ms = a.elapsed_time(b)
-        out["fp64_plain_mlups"] = L * L * n64 / (ms / 1e3) / 1e6
-        out["fp64_plain_launch_us"] = ms / n64 * 1e3
-        # velocity error of FP32-shifted vs FP64 after the same 1 + 10 + n64 steps
+        value = L * L * inner * K / (ms / 1e3) / 1e6
+        launch_us = ms / (K * inner) * 1e3
+        pinned = torch.empty(f0.size, dtype=torch.float64, pin_memory=True)
+        pinned.numpy()[:] = f0
+        host = pinned.numpy()
+        lat.set_populations(host)
+        lat.step(inner)
+        lat.kinetic_energy(E.STAGE_POST_COLLISION)
+        t0 = time.perf_counter()
+        for _ in range(K):
+            lat.set_populations(host)
+            lat.step(inner)
+            lat.kinetic_energy(E.STAGE_POST_COLLISION)
+        t_e2e = time.perf_counter() - t0
+    rate = E.fp64_rate()
+    ops = fp64_ops_per_lu(L)
+    hbm, hbm_kind = peaks()
+    out.update({
+        "value": value, "unit": "MLUPS", "dtype": "f64", "ms_per_step": ms / K,
+        "kernel": f"k_step<PrecExact64,9,{op}>",
+        "e2e": {"value": L * L * inner * K / t_e2e / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": int(f0.nbytes),
+                "d2h_bytes_per_step": 8},
+        "roofline": {"bound": "fp64", "unit": "Gop/s",
+                     "achieved": None if ops is None else ops * value * 1e6 / 1e9,
+                     "peak": rate / 1e9, "peak_kind": "measured in this run (erlbm_fp64_rate: unfused DADD/DMUL)",
+                     "frac": None if ops is None else ops * value * 1e6 / rate,
+                     "fp64_ops_per_lu": ops, "launch_us": launch_us},
+        "hbm": {"bytes_per_lu": BYTES_PER_LU["fp64"], "achieved_gbs": value * 1e6 * BYTES_PER_LU["fp64"] / 1e9,
+                "peak_gbs": hbm, "frac": value * 1e6 * BYTES_PER_LU["fp64"] / 1e9 / hbm, "peak_kind": hbm_kind},
+    })
+    return out
+
+
+def gpu_extras(E, torch, L, f0, tau, op, tnh):
+    """The FP32-shifted velocity error against the plain FP64 path after a short common run."""
+    import numpy as np
+    out = {}
+    n = 1 + 10 + 200
+    with E.Lattice(9, L, L, 1, None, tau, tnh, op, E.FP64) as l64:
+        l64.set_populations(f0)
+        l64.step(n)
         _, u64 = l64.macroscopic(E.STAGE_POST_COLLISION)
     with E.Lattice(9, L, L, 1, None, tau, tnh, op, E.FP32_SHIFTED) as l32:
         l32.set_populations(f0)
-        l32.step(1 + 10 + n64)
+        l32.step(n)
         _, u32 = l32.macroscopic(E.STAGE_POST_COLLISION)
     out["fp32_vs_fp64_rel_l2_velocity"] = float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64))
-    out["fp32_vs_fp64_steps"] = 1 + 10 + n64
+    out["fp32_vs_fp64_steps"] = n
     return out
 
 

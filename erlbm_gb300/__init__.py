@@ -239,6 +239,13 @@ def taylor_green_error(q: int, L: int, f, u0: float, visc: float, step: int, var
     return out
 
 
+def fp64_rate() -> float:
+    """FP64 add / multiply operations per second of the current GPU (erlbm_fp64_rate)."""
+    v = C.c_double()
+    check(lib().erlbm_fp64_rate(C.byref(v)), "erlbm_fp64_rate")
+    return v.value
+
+
 def tg_map_params(i: int, j: int, n_ma: int = 400, n_nu: int = 400, op: int = OP_EXTREG, tau_nh: float = 0.65):
     fn = _fn("erlbm_tg_map_params", C.c_int, [C.c_int] * 5 + [C.c_double] + [C.POINTER(C.c_double)] * 3)
     a, b, c = C.c_double(), C.c_double(), C.c_double()

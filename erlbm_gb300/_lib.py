@@ -123,6 +123,7 @@ _SIGS = {
                                        C.POINTER(C.c_double)]),
     "erlbm_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(BC), C.POINTER(Checks), C.POINTER(RunResult)]),
     "erlbm_sync": (C.c_int, [C.c_void_p]),
+    "erlbm_fp64_rate": (C.c_int, [C.POINTER(C.c_double)]),
     "erlbm_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "erlbm_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "erlbm_batch_run": (C.c_int, [C.POINTER(BatchDesc), C.c_int, C.POINTER(RunSpec), C.c_void_p, C.c_size_t,

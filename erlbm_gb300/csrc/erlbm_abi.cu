@@ -665,6 +665,13 @@ int erlbm_set_stream(erlbm_handle *h, void *stream)
     return ERLBM_OK;
 }
 
+int erlbm_fp64_rate(double *ops_per_s)
+{
+    if (!ops_per_s) return ERLBM_E_INVAL;
+    if (measure_fp64_rate(ops_per_s)) return cuda_fail(cudaGetLastError(), "FP64 rate probe");
+    return ERLBM_OK;
+}
+
 int erlbm_sync(erlbm_handle *h)
 {
     int rc = check_handle(h);

@@ -155,3 +155,65 @@ int launch_init_fp64(int kind, int q, const Geo &g, double *buf, const double *t
 }
 
 }  // namespace erlbm
+
+// ------------------------------------------------------------------------------------------------
+// FP64 add / multiply issue rate (the roofline of the exact path, which issues them unfused)
+// ------------------------------------------------------------------------------------------------
+
+namespace erlbm {
+namespace {
+
+constexpr int RATE_CHAINS = 8;
+
+// Eight independent multiply-then-add chains per thread; with --fmad=false each is one DMUL and one
+// DADD.  The values stay bounded (x -> a x + b with a < 1); the final test keeps the work alive.
+__global__ void __launch_bounds__(256) k_fp64_rate(double *out, int iters, double a, double b)
+{
+    double x[RATE_CHAINS];
+#pragma unroll
+    for (int k = 0; k < RATE_CHAINS; k++) x[k] = 1.0 + 1e-9 * (double)(threadIdx.x + 37 * k);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < RATE_CHAINS; k++) x[k] = x[k] * a + b;
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < RATE_CHAINS; k++) s = s + x[k];
+    if (s == -1.0 && out) out[blockIdx.x] = s;  // never true: every x stays near 1
+}
+
+}  // namespace
+
+// FP64 operations (each DADD and DMUL counted once, per thread) per second over one full wave of
+// resident CTAs, timed with events on a private stream after one warm-up launch.
+int measure_fp64_rate(double *ops_per_s)
+{
+    int dev = 0, sms = 0, occ = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fp64_rate, 256, 0);
+    if (e != cudaSuccess) return -3;
+    if (occ < 1) occ = 1;
+    const int grid = sms * occ, iters = 4096;
+    cudaStream_t s = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    int rc = -3;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess && cudaEventCreate(&a) == cudaSuccess &&
+        cudaEventCreate(&b) == cudaSuccess) {
+        k_fp64_rate<<<grid, 256, 0, s>>>(nullptr, iters / 8, 0.999999, 1e-6);
+        cudaEventRecord(a, s);
+        k_fp64_rate<<<grid, 256, 0, s>>>(nullptr, iters, 0.999999, 1e-6);
+        cudaEventRecord(b, s);
+        float ms = 0.f;
+        if (cudaEventSynchronize(b) == cudaSuccess && cudaEventElapsedTime(&ms, a, b) == cudaSuccess && ms > 0.f) {
+            *ops_per_s = (double)grid * 256.0 * iters * RATE_CHAINS * 2.0 / (ms * 1e-3);
+            rc = 0;
+        }
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (s) cudaStreamDestroy(s);
+    return rc == 0 && cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+}  // namespace erlbm

@@ -169,4 +169,7 @@ int launch_init_fp64(int kind, int q, const Geo &g, double *buf, const double *t
 int launch_init_fp32(int kind, int q, const Geo &g, float *buf, const double *tab, double u0, double tau, double k,
                      double rho, cudaStream_t s);
 
+// FP64 add / multiply rate of the current GPU (operations per second), k_fp64.cu
+int measure_fp64_rate(double *ops_per_s);
+
 }  // namespace erlbm

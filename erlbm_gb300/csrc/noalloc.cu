@@ -10,7 +10,10 @@
 //
 // The array is NOALLOC_SCRATCH_BYTES (about 1.2 MB) on every GPU that loads the library, for as
 // long as the process lives.  Host code must not use its name as a device address: the address is
-// taken once per device with cudaGetSymbolAddress and passed to the kernels.
+// taken with cudaGetSymbolAddress by the first call on a device (and again after that device's
+// context was replaced, e.g. by cudaDeviceReset) and passed to the kernels.
+#include <cuda.h>
+
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -39,9 +42,49 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH
 
 std::mutex g_mu;
 constexpr int MAX_DEVICES = 64;
-void *g_scratch_addr[MAX_DEVICES] = {};
+struct ScratchSlot {
+    void *addr;
+    unsigned long long ctx_id;  // context the address belongs to (0: not looked up yet)
+};
+ScratchSlot g_scratch[MAX_DEVICES] = {};
 
-// Device address of the scratch array on the current device (looked up on first use per device).
+// Identity of the current context (0 when none is current yet).  The driver API is reached through
+// the runtime's entry-point query, so the library does not link libcuda itself.
+int current_context_id(unsigned long long *id)
+{
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    if (!get_current || !get_id) {
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSuccess, q2 = cudaDriverEntryPointSuccess;
+        void *a = nullptr, *b = nullptr;
+        cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &q1);
+        cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &q2);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+            q2 != cudaDriverEntryPointSuccess || !a || !b) {
+            set_error("the driver's context queries (cuCtxGetCurrent, cuCtxGetId) are unavailable%s%s", "", "");
+            return ERLBM_E_CUDA;
+        }
+        get_current = (GetCurrent)a;
+        get_id = (GetId)b;
+    }
+    CUcontext ctx = nullptr;
+    *id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS) {
+        set_error("cuCtxGetCurrent failed in erlbm_batch_run_noalloc%s%s", "", "");
+        return ERLBM_E_CUDA;
+    }
+    if (ctx && get_id(ctx, id) != CUDA_SUCCESS) {
+        set_error("cuCtxGetId failed in erlbm_batch_run_noalloc%s%s", "", "");
+        return ERLBM_E_CUDA;
+    }
+    return ERLBM_OK;
+}
+
+// Device address of the scratch array on the current device.  Looked up by the first call on a
+// device (cudaGetSymbolAddress, with that device current; it also brings up the runtime's context if
+// none is current), and again if the current context is not the one the address was taken in.
 int scratch_address(unsigned char **out)
 {
     int dev = 0;
@@ -51,14 +94,20 @@ int scratch_address(unsigned char **out)
         set_error("device index %s beyond the supported range%s", std::to_string(dev).c_str(), "");
         return ERLBM_E_UNSUPPORTED;
     }
+    unsigned long long id = 0;
+    int rc = current_context_id(&id);
+    if (rc) return rc;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_addr[dev]) {
+    ScratchSlot &slot = g_scratch[dev];
+    if (!slot.addr || id == 0 || slot.ctx_id != id) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
-        g_scratch_addr[dev] = p;
+        if ((rc = current_context_id(&id))) return rc;
+        slot.addr = p;
+        slot.ctx_id = id;
     }
-    *out = (unsigned char *)g_scratch_addr[dev];
+    *out = (unsigned char *)slot.addr;
     return ERLBM_OK;
 }
 
@@ -135,7 +184,16 @@ extern "C" int erlbm_batch_run_noalloc(const erlbm_batch_desc *d, int n_runs, co
     density_bounds(g);
     cudaError_t e;
     if (d->init == ERLBM_INIT_TG_MAP) {
-        // the same tables erlbm_batch_run builds, staged from a stack buffer
+        // The same tables erlbm_batch_run builds, copied from host memory.  A pageable copy cannot be
+        // recorded into a graph, so a stream under capture is refused here rather than left with a
+        // broken capture.
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if ((e = cudaStreamIsCapturing(s, &cs)) != cudaSuccess) return cuda_fail(e, "cudaStreamIsCapturing");
+        if (cs != cudaStreamCaptureStatusNone) {
+            set_error("erlbm_batch_run_noalloc with ERLBM_INIT_TG_MAP copies its tables from host memory and "
+                      "cannot run on a stream under capture%s%s", "", "");
+            return ERLBM_E_UNSUPPORTED;
+        }
         const int n = d->nx > d->ny ? d->nx : d->ny;
         const double L = (double)d->nx;
         double h[2 * MAX_SIDE];

@@ -168,6 +168,10 @@ int erlbm_velocity_error(erlbm_handle *sim, int sim_stage, erlbm_handle *ref, in
 int erlbm_run(erlbm_handle *h, int n_steps, const erlbm_bc *bc, const erlbm_checks *chk, erlbm_run_result *res);
 /* wait for the handle's queued work */
 int erlbm_sync(erlbm_handle *h);
+/* FP64 add and multiply operations per second that the current GPU issues (independent unfused chains
+ * over one wave of resident blocks): the roofline of the plain FP64 path, which issues its operations
+ * unfused to round as the reference's build does.  No counterpart in the reference. */
+int erlbm_fp64_rate(double *ops_per_s);
 /* launch shape of the fused periodic D2Q9 FP32 kernel (the double-shear-layer lattices): threads per
  * block of the one-step kernel (128, 256, 512; 0 = default 256) and flags
  *   ERLBM_LAUNCH_STREAMING_STORES  evict-first stores (one-step kernel);
@@ -222,7 +226,10 @@ typedef struct erlbm_batch_result {
     int label;                  /* 1 unstable */
     int decided_step;           /* failing step, or n_steps */
     int steps_done;
-    int status;                 /* bit 0 |rho| > limit, bit 1 non-finite density, bit 2 energy check */
+    int status;                 /* bit 0 |rho| > limit, bit 1 non-finite density, bit 2 energy check;
+                                   bit 3 (value 8, erlbm_batch_run_noalloc only): the run was refused
+                                   (bad op, tau, tau_nh or n_steps) and not stepped, its label means
+                                   nothing */
     double margin;              /* as in erlbm_run_result */
     double energy;              /* last kinetic energy computed (E0 if no check ran) */
 } erlbm_batch_result;
@@ -238,11 +245,17 @@ int erlbm_batch_run(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec 
  * entries owned by the caller; d->solid, when set, is a DEVICE pointer; d->init must be
  * ERLBM_INIT_REST or ERLBM_INIT_TG_MAP.  At most ERLBM_NOALLOC_MAX_RUNS runs per call (more is
  * ERLBM_E_INVAL).  The work is queued on `stream` (a cudaStream_t; NULL = the default stream) and
- * the call returns without waiting; results follow the stream's order.  Runs are taken in the
- * caller's order (erlbm_batch_run starts the longest first); results are the same.  The first call
- * on a device looks up the array's device address: make that first call before any stream capture.
- * Every call shares the one array, so calls that overlap on the GPU (different streams, or several
- * host threads) race: order them on one stream. */
+ * the call does not wait for the runs; with ERLBM_INIT_TG_MAP it copies its sin/cos tables from
+ * pageable host memory, which may wait for the stream's earlier work, and it returns
+ * ERLBM_E_UNSUPPORTED when `stream` is being captured.  Runs are taken in the caller's order
+ * (erlbm_batch_run starts the longest first); results are the same.  The run table is read on the
+ * device, so a run with a bad operator, tau, tau_nh or n_steps cannot fail the call as it fails
+ * erlbm_batch_run (ERLBM_E_INVAL / ERLBM_E_UNSUPPORTED for the whole call): it is refused on its
+ * own, not stepped, and its result has status 8 and label 0.  The first call on a device looks up
+ * the array's device address (and again after that device's context was replaced, e.g. by
+ * cudaDeviceReset): make that first call before any stream capture.  Every call shares the one
+ * array, so calls that overlap on the GPU (different streams, or several host threads) race: order
+ * them on one stream. */
 #define ERLBM_NOALLOC_MAX_RUNS 16384
 int erlbm_batch_run_noalloc(const erlbm_batch_desc *d, int n_runs, const erlbm_run_spec *runs,
                             erlbm_batch_result *out, void *stream);

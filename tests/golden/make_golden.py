@@ -1,6 +1,8 @@
 """Generates the golden fixtures in this folder.  Run where the reference tree is present:
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py [--reference PATH]
+
+PATH defaults to $ERLBM_REFERENCE, else a "reference" directory beside the repository.
 
 It reads the reference's published tables (data/*.csv, data/*.vtk) and runs the reference's own
 library and program functions, compiled from their sources by oracle/Makefile (target `ref`), to
@@ -113,7 +115,8 @@ def _ref_ob_point(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("ERLBM_REFERENCE")
+                    or os.path.join(os.path.dirname(os.path.realpath(ROOT)), "reference"))
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--vectors-only", action="store_true", help="rewrite reference_vectors.npz only")
     a = ap.parse_args()
