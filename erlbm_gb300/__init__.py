@@ -109,11 +109,13 @@ class Lattice:
               "erlbm_set_stream")
 
     def set_launch(self, block_threads: int = 0, streaming_stores: bool = False, two_step: bool = False,
-                   three_step: bool = False) -> None:
+                   three_step: bool = False, wide_strips: bool = False) -> None:
         """Launch shape of the fused periodic D2Q9 FP32 kernel (see erlbm_gb300.autotune): two_step or
-        three_step run two or three consecutive steps as one launch (nx % 128 == 0, ny even); the same
-        bits in every shape."""
-        flags = (1 if streaming_stores else 0) | (2 if two_step else 0) | (4 if three_step else 0)
+        three_step run two or three consecutive steps as one launch (nx % 128 == 0, ny even);
+        wide_strips (with three_step) uses 64-column strips over column pairs; the same bits in every
+        shape."""
+        flags = ((1 if streaming_stores else 0) | (2 if two_step else 0) | (4 if three_step else 0) |
+                 (8 if wide_strips else 0))
         check(lib().erlbm_set_launch(self._h, int(block_threads), flags), "erlbm_set_launch")
 
     def kinetic_energy(self, stage: int = STAGE_POST_STREAM) -> float:

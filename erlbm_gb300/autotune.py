@@ -61,7 +61,7 @@ def _time_steps(lat, stream, n: int) -> float:
 PERIODIC_CANDIDATES = [(128, False), (256, False), (512, False), (128, True), (256, True), (512, True)]
 # two and three steps per launch: one kernel shape each (warp strips in 128-thread CTAs); the block size
 # given with them is the one-step shape used for the steps a call has left over
-MULTI_STEP_CANDIDATES = [(128, False, 2), (128, False, 3)]
+MULTI_STEP_CANDIDATES = [(128, False, 2), (128, False, 3), (128, True, 3)]  # (block, wide strips, steps)
 
 
 def tune_periodic(L: int, steps: int = 200, force: bool = False) -> dict:
@@ -69,7 +69,7 @@ def tune_periodic(L: int, steps: int = 200, force: bool = False) -> dict:
     L x L lattice."""
     import torch
     import erlbm_gb300 as E
-    key = f"{_device_key()}/periodic_d2q9_fp32/shapes3/L{L}"
+    key = f"{_device_key()}/periodic_d2q9_fp32/shapes4/L{L}"
     hit = _load().get(key)
     if hit and not force:
         return hit
@@ -81,15 +81,15 @@ def tune_periodic(L: int, steps: int = 200, force: bool = False) -> dict:
         lat.set_stream(stream.cuda_stream)
         lat.set_populations(E.init_double_shear(L))
         lat.step(1)
-        cands = [(b, s, 1) for b, s in PERIODIC_CANDIDATES]
+        cands = [(b, s, False, 1) for b, s in PERIODIC_CANDIDATES]
         if L % 2 == 0 and L >= 4:
-            cands += list(MULTI_STEP_CANDIDATES)
-        for block, st, per in cands:
-            lat.set_launch(block, st, per == 2, per == 3)
+            cands += [(b, False, w, per) for b, w, per in MULTI_STEP_CANDIDATES if not w or L >= 16]
+        for block, st, wide, per in cands:
+            lat.set_launch(block, st, per == 2, per == 3, wide)
             lat.step(20)
             t = min(_time_steps(lat, stream, steps) for _ in range(3))
             results.append(dict(block_threads=block, streaming_stores=st, two_step=per == 2, three_step=per == 3,
-                                mlups=L * L * steps / t / 1e6))
+                                wide_strips=wide, mlups=L * L * steps / t / 1e6))
     best = max(results, key=lambda r: r["mlups"])
     out = dict(best, candidates=results)
     _store(key, out)
@@ -102,7 +102,7 @@ def apply_periodic(lat) -> dict | None:
         return None
     best = tune_periodic(lat.nx)
     lat.set_launch(best["block_threads"], best["streaming_stores"], best.get("two_step", False),
-                   best.get("three_step", False))
+                   best.get("three_step", False), best.get("wide_strips", False))
     return best
 
 

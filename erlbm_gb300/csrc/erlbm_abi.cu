@@ -82,6 +82,7 @@ struct erlbm_handle {
     int shape = 0;                      // launch shape of the fused periodic kernel (erlbm_set_launch)
     bool two_step = false;              // pairs of fused periodic steps as one launch (erlbm_set_launch)
     bool three_step = false;            // triples of fused periodic steps as one launch (erlbm_set_launch)
+    bool wide_strips = false;           // the three-step launches use 64-column strips over column pairs
     std::vector<uint8_t> h_solid;       // host copy of the solid mask (empty for periodic boxes)
     std::vector<double> h_profile;      // parabolic inlet velocity per (y, z) of the inlet plane
     double *d_profile = nullptr;
@@ -351,7 +352,8 @@ int graph_steps(erlbm_handle *h, int per_launch)
         for (int k = 0; k < n_steps / per_launch && lrc == 0; k++) {
             const float *src = (const float *)h->d_buf[c];
             float *dst = (float *)h->d_buf[c ^ 1];
-            lrc = per_launch == 3   ? launch_periodic_d2q9_fp32_x3(h->op, h->g, h->R, src, dst, h->capture_stream)
+            lrc = per_launch == 3   ? launch_periodic_d2q9_fp32_x3(h->op, h->g, h->R, src, dst, h->capture_stream,
+                                                                 h->wide_strips)
                   : per_launch == 2 ? launch_periodic_d2q9_fp32_x2(h->op, h->g, h->R, src, dst, h->capture_stream)
                                     : launch_periodic_d2q9_fp32(h->op, h->g, h->R, src, dst, h->capture_stream,
                                                                 h->shape);
@@ -602,7 +604,8 @@ int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc)
     if ((rc = validate_bc(h, bc, &b))) return rc;
     const bool plain = h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && b.inlet_x < 0 && b.outlet_x < 0 &&
                        b.open_y < 0 && periodic_d2q9_fp32_ok(h->g);
-    const bool fused3 = plain && h->three_step && periodic_d2q9_x2_ok(h->g);
+    const bool fused3 = plain && h->three_step && periodic_d2q9_x2_ok(h->g) &&
+                        (!h->wide_strips || periodic_d2q9_x3p_ok(h->g));
     const bool fused2 = plain && h->two_step && periodic_d2q9_x2_ok(h->g);
     const int per_launch = fused3 ? 3 : (fused2 ? 2 : 1);
     for (int s = 0; s < n_steps;) {
@@ -614,7 +617,7 @@ int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc)
         if (fused3 && h->kind == 1 && n_steps - s >= 3) {
             // three plain periodic steps in one launch
             CKL(launch_periodic_d2q9_fp32_x3(h->op, h->g, h->R, (const float *)h->d_buf[h->cur],
-                                             (float *)h->d_buf[h->cur ^ 1], h->stream),
+                                             (float *)h->d_buf[h->cur ^ 1], h->stream, h->wide_strips),
                 "periodic_d2q9_x3");
             h->cur ^= 1;
             h->steps_done += 3;
@@ -645,14 +648,22 @@ int erlbm_set_launch(erlbm_handle *h, int block_threads, int flags)
         set_error("block_threads must be 0, 128, 256 or 512%s%s", "", "");
         return ERLBM_E_INVAL;
     }
-    if (flags & ~(ERLBM_LAUNCH_STREAMING_STORES | ERLBM_LAUNCH_TWO_STEP | ERLBM_LAUNCH_THREE_STEP)) return ERLBM_E_INVAL;
+    if (flags & ~(ERLBM_LAUNCH_STREAMING_STORES | ERLBM_LAUNCH_TWO_STEP | ERLBM_LAUNCH_THREE_STEP |
+                  ERLBM_LAUNCH_WIDE_STRIPS))
+        return ERLBM_E_INVAL;
+    if ((flags & ERLBM_LAUNCH_WIDE_STRIPS) && !(flags & ERLBM_LAUNCH_THREE_STEP)) {
+        set_error("set_launch: ERLBM_LAUNCH_WIDE_STRIPS applies to ERLBM_LAUNCH_THREE_STEP%s%s", "", "");
+        return ERLBM_E_INVAL;
+    }
     if ((flags & ERLBM_LAUNCH_TWO_STEP) && (flags & ERLBM_LAUNCH_THREE_STEP)) {
         set_error("set_launch: at most one of ERLBM_LAUNCH_TWO_STEP and ERLBM_LAUNCH_THREE_STEP%s%s", "", "");
         return ERLBM_E_INVAL;
     }
-    h->shape = block_threads | ((flags & ERLBM_LAUNCH_STREAMING_STORES) ? 0x1000 : 0);
+    h->shape = block_threads | ((flags & ERLBM_LAUNCH_STREAMING_STORES) ? 0x1000 : 0) |
+               ((flags & ERLBM_LAUNCH_WIDE_STRIPS) ? 0x2000 : 0);  // part of the graph key
     h->two_step = (flags & ERLBM_LAUNCH_TWO_STEP) != 0;
     h->three_step = (flags & ERLBM_LAUNCH_THREE_STEP) != 0;
+    h->wide_strips = (flags & ERLBM_LAUNCH_WIDE_STRIPS) != 0;
     return ERLBM_OK;  // graphs of another shape are rebuilt on their next use (graph_key)
 }
 

@@ -464,6 +464,164 @@ __global__ void __launch_bounds__(128, 4) k_periodic_d2q9_x3s(const float *__res
     }
 }
 
+
+// Three steps per launch over column pairs.  Lane l holds the columns xs - 2 + 2l and xs - 1 + 2l of a
+// 64-column strip as the two halves of a float2, so each packed FP32x2 operation of the collision
+// works on two neighbouring nodes of one row and every operand pair is formed where it is produced.
+// The strip walks down its chunk one row per iteration:
+//   - the first stage P' is valid in all 64 columns (lane 0 loads column xs - 3 and lane 31 column
+//     xs + 62 for the three populations that cross the strip's edges), P'' in columns 1 .. 62, the
+//     output in columns 2 .. 61: 60 output columns per 64 (the x3s strips: 28 per 32);
+//   - the x pull of a direction with c_x = +1 takes the left half from the lane below (one shuffle)
+//     and the right half from the lane's own left half, and the reverse for c_x = -1;
+//   - the y pull of row r takes the c_y = +1 group (3, 5, 8) from row r - 1, the c_y = 0 group (0, 1,
+//     2) from row r and the c_y = -1 group (4, 6, 7) from row r + 1.
+// The first stage pulls straight from memory: for P' row j + 2 it loads the c_y = +1 group of P row
+// j + 1, the c_y = 0 group of row j + 2 and the c_y = -1 group of row j + 3 (one iteration ahead), so
+// every input population is still read once.  The two later stages carry the c_y = +1 groups of
+// their two newest input rows and the c_y = 0 group of the newest one in registers; those rotate
+// through three and two register slots, so the loop body is unrolled six times and no group is copied
+// between iterations.  Per iteration P' row j + 2, P'' row j + 1 and output row j are collided; the
+// first four iterations of a chunk are its prologue, in which only the stages whose inputs exist run.
+// Bit-identical to three one-step launches: every node is collided by collide9x2 as by collide9.
+constexpr int XP_W = 60;   // output columns per strip
+constexpr int XP_SPAN = 6; // rows per unrolled group
+
+template <int I>
+struct IntC {
+    static constexpr int value = I;
+};
+
+template <int OP, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_periodic_d2q9_x3p(const float *__restrict__ src, float *__restrict__ dst,
+                                                                int nx, int ny, long long plane, int hc, int strips,
+                                                                int n_warps, shifted::Coef k)
+{
+    const int lane = threadIdx.x & 31;
+    const int wid = (int)blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
+    if (wid >= n_warps) return;  // the whole warp leaves together
+    const int xs = (wid % strips) * XP_W;
+    const int y0 = (wid / strips) * hc;
+    const int y1 = min(y0 + hc, ny);
+    int c = xs - 2 + 2 * lane;  // even, in [-2, nx + 60]
+    const bool store = lane >= 1 && lane <= 30 && c < nx;
+    c = c < 0 ? c + nx : (c >= nx ? c - nx : c);
+    // lane 0 pulls populations 1 (c_y = 0), 5 (c_y = +1), 7 (c_y = -1) across the left edge from column
+    // xs - 3; lane 31 pulls 2 (c_y = 0), 6 (c_y = -1), 8 (c_y = +1) across the right edge from xs + 62
+    const bool halo = lane == 0 || lane == 31;
+    int hcol = lane == 0 ? xs - 3 : xs + 62;
+    hcol = hcol < 0 ? hcol + nx : (hcol >= nx ? hcol - nx : hcol);
+    const int hp0 = lane == 0 ? 1 : 2, hp1 = lane == 0 ? 5 : 6, hp2 = lane == 0 ? 7 : 8;
+    const int hd1 = lane == 0 ? -1 : 1, hd2 = lane == 0 ? 1 : -1;  // row offsets of halo 1, 2 from c_y = 0's
+
+    auto wrap = [&](int r) { return r < 0 ? r + ny : (r >= ny ? r - ny : r); };
+    // P' row r's inputs: groups c_y = +1 of P row r - 1, c_y = 0 of row r, c_y = -1 of row r + 1
+    float2 ld[9];
+    float hv[3] = {0.f, 0.f, 0.f};
+    auto load = [&](int r) {
+        const float *pm = src + (long long)wrap(r - 1) * nx + c;
+        const float *pz = src + (long long)wrap(r) * nx + c;
+        const float *pp = src + (long long)wrap(r + 1) * nx + c;
+        ld[3] = __ldg(reinterpret_cast<const float2 *>(pm + 3 * plane));
+        ld[5] = __ldg(reinterpret_cast<const float2 *>(pm + 5 * plane));
+        ld[8] = __ldg(reinterpret_cast<const float2 *>(pm + 8 * plane));
+        ld[0] = __ldg(reinterpret_cast<const float2 *>(pz + 0 * plane));
+        ld[1] = __ldg(reinterpret_cast<const float2 *>(pz + 1 * plane));
+        ld[2] = __ldg(reinterpret_cast<const float2 *>(pz + 2 * plane));
+        ld[4] = __ldg(reinterpret_cast<const float2 *>(pp + 4 * plane));
+        ld[6] = __ldg(reinterpret_cast<const float2 *>(pp + 6 * plane));
+        ld[7] = __ldg(reinterpret_cast<const float2 *>(pp + 7 * plane));
+        if (halo) {
+            hv[0] = __ldg(src + (long long)wrap(r) * nx + hcol + hp0 * plane);
+            hv[1] = __ldg(src + (long long)wrap(r + hd1) * nx + hcol + hp1 * plane);
+            hv[2] = __ldg(src + (long long)wrap(r + hd2) * nx + hcol + hp2 * plane);
+        }
+    };
+    // x pulls: c_x = +1 takes column 2l - 1 (the lane below's right half) and 2l (own left half)
+    auto pull_p = [&](float2 v) { return make_float2(__shfl_up_sync(XS_FULL, v.y, 1), v.x); };
+    auto pull_m = [&](float2 v) { return make_float2(v.y, __shfl_down_sync(XS_FULL, v.x, 1)); };
+    auto pull_p_halo = [&](float2 v, float h) {
+        const float u = __shfl_up_sync(XS_FULL, v.y, 1);
+        return make_float2(lane == 0 ? h : u, v.x);
+    };
+    auto pull_m_halo = [&](float2 v, float h) {
+        const float u = __shfl_down_sync(XS_FULL, v.x, 1);
+        return make_float2(v.y, lane == 31 ? h : u);
+    };
+
+    // carried groups of stages 1 and 2 (index 0, 1): s1[.][slot] c_y = +1 (3, 5, 8), s0[.][slot] c_y = 0 (0, 1, 2)
+    float2 s1[2][3][3], s0[2][2][3];
+    float2 g[9], nm[3];
+
+    // one iteration at rotation phase T: stage 0, 1, 2 collide P' row j + 2, P'' row j + 1 and output
+    // row j where C1, C2 say their inputs exist (stage 0 always runs)
+    auto step = [&](auto T, auto C1, auto C2, int j) {
+        constexpr int t = decltype(T)::value;
+        constexpr int a = t % 3, n = (t + 2) % 3, z = (t + 1) % 2;
+        constexpr bool c1 = decltype(C1)::value, c2 = decltype(C2)::value;
+        g[3] = ld[3];
+        g[5] = pull_p_halo(ld[5], hv[1]);
+        g[8] = pull_m_halo(ld[8], hv[2]);
+        g[0] = ld[0];
+        g[1] = pull_p_halo(ld[1], hv[0]);
+        g[2] = pull_m_halo(ld[2], hv[0]);
+        g[4] = ld[4];
+        g[6] = pull_m_halo(ld[6], hv[1]);
+        g[7] = pull_p_halo(ld[7], hv[2]);
+        load(j + 3);  // the inputs of the next iteration's P' row
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
+            if (s == 1 && !c1) break;
+            if (s == 2 && !c2) break;
+            if (s > 0) {
+                g[3] = s1[s - 1][a][0];
+                g[5] = s1[s - 1][a][1];
+                g[8] = s1[s - 1][a][2];
+                g[0] = s0[s - 1][z ^ 1][0];
+                g[1] = s0[s - 1][z ^ 1][1];
+                g[2] = s0[s - 1][z ^ 1][2];
+                g[4] = nm[0];
+                g[6] = nm[1];
+                g[7] = nm[2];
+            }
+            shifted::collide9x2<OP>(g, k);
+            if (s == 2) {
+                if (store && j < y1) {
+                    float *d = dst + (long long)j * nx + c;
+#pragma unroll
+                    for (int i = 0; i < 9; i++) *reinterpret_cast<float2 *>(d + i * plane) = g[i];
+                }
+            } else {  // the collided row is the next stage's newest input row
+                s1[s][n][0] = g[3];
+                s1[s][n][1] = pull_p(g[5]);
+                s1[s][n][2] = pull_m(g[8]);
+                s0[s][z][0] = g[0];
+                s0[s][z][1] = pull_p(g[1]);
+                s0[s][z][2] = pull_m(g[2]);
+                nm[0] = g[4];
+                nm[1] = pull_m(g[6]);
+                nm[2] = pull_p(g[7]);
+            }
+        }
+    };
+    using F = IntC<0>;
+    using N = IntC<1>;
+    // prologue: P' rows y0 - 2 .. y0 + 1, P'' rows y0 - 1, y0 (phases 2 .. 5, so the loop starts at 0)
+    load(y0 - 2);
+    step(IntC<2>{}, F{}, F{}, y0 - 4);
+    step(IntC<3>{}, F{}, F{}, y0 - 3);
+    step(IntC<4>{}, N{}, F{}, y0 - 2);
+    step(IntC<5>{}, N{}, F{}, y0 - 1);
+    for (int j = y0; j < y1; j += XP_SPAN) {
+        step(IntC<0>{}, N{}, N{}, j);
+        step(IntC<1>{}, N{}, N{}, j + 1);
+        step(IntC<2>{}, N{}, N{}, j + 2);
+        step(IntC<3>{}, N{}, N{}, j + 3);
+        step(IntC<4>{}, N{}, N{}, j + 4);
+        step(IntC<5>{}, N{}, N{}, j + 5);
+    }
+}
+
 }  // namespace
 
 bool periodic_d2q9_x2_ok(const Geo &g)
@@ -535,11 +693,60 @@ static void go_x3(const Geo &g, const shifted::Coef &k, const float *src, float 
     kern<<<(unsigned)((n_warps + 3) / 4), 128, 0, s>>>(src, dst, g.nx, g.ny, g.plane, (int)hc, strips, n_warps, k);
 }
 
-// Three steps of the fused periodic D2Q9 FP32 update in one launch (periodic_d2q9_x2_ok(g) required).
-int launch_periodic_d2q9_fp32_x3(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s)
+// Three-step launch over column pairs: ceil(nx / 60) strips, chunks of a multiple of six rows, as many
+// chunks per strip as one wave of resident warps holds (no second, partial wave).
+// resident 128-thread CTAs per SM (the register cap follows from it); a build option for tuning
+#ifndef ERLBM_XP_MINB
+#define ERLBM_XP_MINB 3
+#endif
+constexpr int XP_MINB = ERLBM_XP_MINB;
+
+template <int OP>
+static void go_x3p(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
 {
-    if (!periodic_d2q9_x2_ok(g)) return -1;
+    auto kern = k_periodic_d2q9_x3p<OP, XP_MINB>;
+    constexpr int MAXDEV = 64;
+    static std::atomic<int> warps_cache[MAXDEV];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int d = dev >= 0 && dev < MAXDEV ? dev : 0;
+    int resident = warps_cache[d].load(std::memory_order_relaxed);
+    if (resident <= 0) {
+        int o = 0, n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, 128, 0) != cudaSuccess || o < 1) o = 1;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        resident = o * 4 * (n > 0 ? n : 1);
+        warps_cache[d].store(resident, std::memory_order_relaxed);
+    }
+    const int strips = (g.nx + XP_W - 1) / XP_W;
+    long long chunks = resident / strips;
+    if (chunks < 1) chunks = 1;
+    long long hc = (g.ny + chunks - 1) / chunks;
+    hc = (hc + XP_SPAN - 1) / XP_SPAN * XP_SPAN;
+    if (hc < 2 * XP_SPAN) hc = 2 * XP_SPAN;
+    const int n_warps = strips * (int)((g.ny + hc - 1) / hc);
+    kern<<<(unsigned)((n_warps + 3) / 4), 128, 0, s>>>(src, dst, g.nx, g.ny, g.plane, (int)hc, strips, n_warps, k);
+}
+
+bool periodic_d2q9_x3p_ok(const Geo &g) { return periodic_d2q9_fp32_ok(g) && g.ny >= 16 && g.nx >= 128; }
+
+// Three steps of the fused periodic D2Q9 FP32 update in one launch (periodic_d2q9_x2_ok(g) required;
+// wide = the column-pair kernel, which needs periodic_d2q9_x3p_ok(g)).
+int launch_periodic_d2q9_fp32_x3(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s,
+                                 bool wide)
+{
+    if (!periodic_d2q9_x2_ok(g) || (wide && !periodic_d2q9_x3p_ok(g))) return -1;
     const shifted::Coef k = shifted::make_coef(R);
+    if (wide) {
+        switch (op) {
+        case OP_BGK: go_x3p<OP_BGK>(g, k, src, dst, s); break;
+        case OP_MRT: go_x3p<OP_MRT>(g, k, src, dst, s); break;
+        case OP_REG: go_x3p<OP_REG>(g, k, src, dst, s); break;
+        case OP_EXTREG: go_x3p<OP_EXTREG>(g, k, src, dst, s); break;
+        default: return -1;
+        }
+        return cudaGetLastError() == cudaSuccess ? 0 : -3;
+    }
     switch (op) {
     case OP_BGK: go_x3<OP_BGK>(g, k, src, dst, s); break;
     case OP_MRT: go_x3<OP_MRT>(g, k, src, dst, s); break;

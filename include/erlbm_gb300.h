@@ -177,13 +177,17 @@ int erlbm_fp64_rate(double *ops_per_s);
  *   ERLBM_LAUNCH_STREAMING_STORES  evict-first stores (one-step kernel);
  *   ERLBM_LAUNCH_TWO_STEP          two consecutive steps per launch, the intermediate step kept on
  *                                  chip (nx % 128 == 0, ny even): half the HBM traffic per update;
- *   ERLBM_LAUNCH_THREE_STEP        three steps per launch (same conditions): a third of the traffic.
+ *   ERLBM_LAUNCH_THREE_STEP        three steps per launch (same conditions): a third of the traffic;
+ *   ERLBM_LAUNCH_WIDE_STRIPS       with ERLBM_LAUNCH_THREE_STEP: 64-column warp strips in which a lane
+ *                                  holds two neighbouring columns (60 outputs per 64 columns instead
+ *                                  of 28 per 32; ny >= 16).
  * The results are the same bits in every shape; at most one of the two multi-step flags.  Steps left
  * over (fewer than a launch takes) run one at a time.  Chosen by erlbm_gb300.autotune; no
  * counterpart in the reference. */
 #define ERLBM_LAUNCH_STREAMING_STORES 1
 #define ERLBM_LAUNCH_TWO_STEP 2
 #define ERLBM_LAUNCH_THREE_STEP 4
+#define ERLBM_LAUNCH_WIDE_STRIPS 8
 int erlbm_set_launch(erlbm_handle *h, int block_threads, int flags);
 /* run the handle's work on the caller's CUDA stream (a cudaStream_t; NULL = the handle's own
  * stream).  Waits for the work queued so far first.  No counterpart in the reference, whose loops

@@ -180,6 +180,15 @@ def test_run_energy_check_matches_oracle():
         assert r["margin"] == mg
 
 
+# launch shapes of the fused periodic D2Q9 FP32 kernels: steps per launch, "w" = three steps over
+# 64-column strips of column pairs (ERLBM_LAUNCH_WIDE_STRIPS)
+SHAPES = (1, 2, 3, "w")
+
+
+def set_shape(lat, per, block=256):
+    lat.set_launch(block, False, per == 2, per in (3, "w"), per == "w")
+
+
 @pytest.mark.parametrize("op", [1, 2, 3, 4])
 @pytest.mark.parametrize("L,steps", [(256, 17), (512, 40)])
 def test_multi_step_kernels_equal_one_step(op, L, steps):
@@ -188,9 +197,9 @@ def test_multi_step_kernels_equal_one_step(op, L, steps):
     tau = 0.5 + 3 * (1 / 32) * L / 80000
     f0 = eg().init_double_shear(L)
     outs = []
-    for per in (1, 2, 3):
+    for per in SHAPES:
         with eg().Lattice(9, L, L, 1, None, tau, 0.65, op, eg().FP32_SHIFTED) as lat:
-            lat.set_launch(256, False, per == 2, per == 3)
+            set_shape(lat, per)
             lat.set_populations(f0)
             lat.step(steps)
             lat.step(3)
@@ -200,7 +209,7 @@ def test_multi_step_kernels_equal_one_step(op, L, steps):
         assert np.array_equal(outs[0][0], o[0]) and np.array_equal(outs[0][1], o[1])
 
 
-@pytest.mark.parametrize("per", [1, 2, 3])
+@pytest.mark.parametrize("per", SHAPES)
 def test_graph_replay_equals_single_launches(per):
     """Blocks of 64 (or, three steps per launch, 66) plain periodic steps run as a replayed CUDA graph
     (captured once per buffer parity); the populations equal those of the same steps launched one call
@@ -212,7 +221,7 @@ def test_graph_replay_equals_single_launches(per):
     outs = []
     for blocks in (True, False):
         with eg().Lattice(9, L, L, 1, None, tau1, 0.65, eg().OP_EXTREG, eg().FP32_SHIFTED) as lat:
-            lat.set_launch(256, False, per == 2, per == 3)
+            set_shape(lat, per)
             lat.set_populations(f0)
             run = (lambda n: lat.step(n)) if blocks else (lambda n: [lat.step(1) for _ in range(n)])
             run(1)
@@ -228,23 +237,25 @@ def test_graph_replay_equals_single_launches(per):
         assert np.array_equal(x, y)
 
 
-@pytest.mark.parametrize("nx,ny", [(128, 4), (128, 6), (384, 10), (128, 130), (640, 258)])
+@pytest.mark.parametrize("nx,ny", [(128, 4), (128, 6), (384, 10), (128, 16), (256, 18), (128, 130), (640, 258),
+                                   (384, 100)])
 def test_multi_step_kernels_equal_one_step_on_uneven_strips(nx, ny):
-    """The two- and three-step kernels' warp strips are 30 and 28 columns wide, so nx = 128, 384 and 640
-    end in a partial strip; their chunks of rows are clamped at small ny.  Random near-equilibrium
-    populations, every wrap of the periodic box exercised: the one-step kernel's bits after ten steps,
-    which leave a remainder in both shapes."""
+    """The two- and three-step kernels' warp strips are 30, 28 and (wide) 60 columns wide, so nx = 128,
+    256, 384 and 640 end in a partial strip; their chunks of rows are clamped at small ny, and the wide
+    strips' chunks of six-row groups run past the last row.  Random near-equilibrium populations, every
+    wrap of the periodic box exercised: the one-step kernel's bits after ten steps, which leave a
+    remainder in every shape (below 16 rows the wide shape runs one step per launch)."""
     rng = np.random.default_rng(nx * 1000 + ny)
     w = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
     f0 = (w[None, :] * (1.0 + 0.05 * rng.standard_normal((nx * ny, 9)))).ravel()
     outs = []
-    for per in (1, 2, 3):
+    for per in SHAPES:
         with eg().Lattice(9, nx, ny, 1, None, 0.53, 0.65, eg().OP_EXTREG, eg().FP32_SHIFTED) as lat:
-            lat.set_launch(128, False, per == 2, per == 3)
+            set_shape(lat, per, 128)
             lat.set_populations(f0)
             lat.step(10)
             outs.append(lat.get_populations(0))
-    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
 
 
 def test_fused_kernel_launch_shapes_identical_and_tuned(tmp_path, monkeypatch):
@@ -255,17 +266,18 @@ def test_fused_kernel_launch_shapes_identical_and_tuned(tmp_path, monkeypatch):
     f0 = eg().init_double_shear(L)
     tau = 0.5 + 3 * (1 / 32) * L / 80000
     outs = []
-    shapes = [(b, s, 1) for b, s in autotune.PERIODIC_CANDIDATES] + list(autotune.MULTI_STEP_CANDIDATES)
-    for block, st, per in shapes:
+    shapes = [(b, s, False, 1) for b, s in autotune.PERIODIC_CANDIDATES] + \
+        [(b, False, w, per) for b, w, per in autotune.MULTI_STEP_CANDIDATES]
+    for block, st, wide, per in shapes:
         with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
-            lat.set_launch(block, st, per == 2, per == 3)
+            lat.set_launch(block, st, per == 2, per == 3, wide)
             lat.set_populations(f0)
             lat.step(30)  # 1 local step, then 29 as multi-step launches and single steps
             outs.append(lat.get_populations(1))
     assert all(np.array_equal(o, outs[0]) for o in outs[1:])
     best = autotune.tune_periodic(L, steps=50)
     per = 3 if best["three_step"] else (2 if best["two_step"] else 1)
-    assert (best["block_threads"], best["streaming_stores"], per) in shapes
+    assert (best["block_threads"], best["streaming_stores"], best["wide_strips"], per) in shapes
     assert autotune.tune_periodic(L)["mlups"] == best["mlups"]  # served from the cache
     with pytest.raises(eg().ErlbmError):  # two and three steps per launch at once
         with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
@@ -273,6 +285,9 @@ def test_fused_kernel_launch_shapes_identical_and_tuned(tmp_path, monkeypatch):
     with pytest.raises(eg().ErlbmError):
         with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
             lat.set_launch(100)
+    with pytest.raises(eg().ErlbmError):  # wide strips without three steps per launch
+        with eg().Lattice(9, L, L, 1, None, tau, 0.65, 4, eg().FP32_SHIFTED) as lat:
+            lat.set_launch(128, False, True, False, True)
 
 
 @pytest.mark.parametrize("with_solid", [False, True])
@@ -310,9 +325,9 @@ def test_fp32_kernels_equal_their_cpu_restatement(op, nx, ny, steps):
     f0 = (w[None, :] * (1.0 + 0.05 * rng.standard_normal((nx * ny, 9)))).ravel()
     tau, tnh = 0.53, 0.65
     want = O.fp32_periodic_d2q9(nx, ny, op, tau, tnh, f0, steps)
-    for per in (1, 2, 3):
+    for per in SHAPES:
         with eg().Lattice(9, nx, ny, 1, None, tau, tnh, op, eg().FP32_SHIFTED) as lat:
-            lat.set_launch(128, False, per == 2, per == 3)
+            set_shape(lat, per, 128)
             lat.set_populations(f0)
             lat.step(steps)
             assert np.array_equal(lat.get_populations(eg().STAGE_POST_COLLISION), want), per
