@@ -10,7 +10,12 @@
 // at the maps' lowest viscosity delta_1 is ~1e-4: as the sum of two O(1) FP32 coefficients it
 // would carry only ~4 significant digits.  So the update is written with delta_1 itself:
 //   f* = f + [delta_1 f1 + k_d (d - f1) - 2 f1]            (E-RLBM, RLBM: k_d = w_gt1 - 1)
+//      = f + [delta_1 f1 - k_c f1 + k_d d],  k_c = 2 + k_d = 1 + w_gt1 (formed in FP64, rounded once)
 //   f* = f + [delta d - 2 d],  delta = 2 - 1/tau           (BGK)
+// The second E-RLBM / RLBM form is the one evaluated: for an opposite pair with d = (D +- DO) / 2 the
+// part common to both members, delta_1 f1 - k_c f1 + (k_d / 2) D, is formed once and the odd part
+// (k_d / 2) DO added and subtracted by one fma each, so delta_1 f1 still enters as its own exactly
+// multiplied term.
 //
 // Each opposite pair (i, j) is split into an even part e = (g_i + g_j)/2 and an odd part
 // o = (g_i - g_j)/2 (both exact; the updates carry them, and the non-equilibrium parts, at twice this
@@ -34,23 +39,44 @@
 namespace erlbm {
 namespace shifted {
 
-// Increment coefficients, formed in FP64 and rounded once: kd = w_gt1 - 1 (unused by BGK) and
-// d1 = 2 - 1/tau (delta_1, or delta for BGK).
+// Increment coefficients, formed in FP64 and rounded once: kd = w_gt1 - 1 (unused by BGK and MRT),
+// d1 = 2 - 1/tau (delta_1, or delta for BGK), nkc = -(1 + w_gt1) = -(2 + kd); kh = kd / 2 (exact).
 struct Coef {
-    float kd, d1;
+    float kd, d1, nkc, kh;
 };
 
 __host__ __device__ inline Coef make_coef(const Relax &R)
 {
     Coef k;
     k.d1 = (float)(2.0 - R.inv_tau);
-    if (R.op == OP_BGK || R.op == OP_MRT)
+    if (R.op == OP_BGK || R.op == OP_MRT) {
         k.kd = 0.f;
-    else if (R.op == OP_REG)
+        k.nkc = 0.f;
+    } else if (R.op == OP_REG) {
         k.kd = -1.f;
-    else
+        k.nkc = -1.f;
+    } else {
         k.kd = (float)(R.omega_gt1 - 1.0);
+        k.nkc = (float)(-(1.0 + R.omega_gt1));
+    }
+    k.kh = 0.5f * k.kd;
     return k;
+}
+
+// 1 / b rounded to nearest: the hardware's approximate reciprocal refined by one fused correction step
+// (Markstein's method: e = 1 - b y, y' = y + y e, both as single roundings).  Checked against
+// __frcp_rn on every float whose exponent field lies in [1, 252] (|b| in [2^-126, 2^126)): identical
+// bits.  Outside that range (zero, subnormals, |b| >= 2^126, infinities, NaN) the approximation's
+// flush-to-zero and overflow would differ, so those take __frcp_rn.  3 FP32 operations instead of
+// the ~10 of __frcp_rn in the common case.
+__device__ __forceinline__ float rcp_rn(float b)
+{
+    const unsigned ex = (__float_as_uint(b) >> 23) & 0xffu;
+    if (ex - 1u > 251u) return __frcp_rn(b);
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(b));
+    const float e = __fmaf_rn(-b, y, 1.0f);
+    return __fmaf_rn(y, e, y);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -81,7 +107,7 @@ struct LaneF1 {
     static __device__ __forceinline__ V mul(V a, V b) { return __fmul_rn(a, b); }
     static __device__ __forceinline__ V fma(V a, V b, V d) { return __fmaf_rn(a, b, d); }
     static __device__ __forceinline__ V neg(V a) { return -a; }
-    static __device__ __forceinline__ V rcp(V a) { return __frcp_rn(a); }
+    static __device__ __forceinline__ V rcp(V a) { return rcp_rn(a); }
 };
 
 struct LaneF2 {
@@ -92,14 +118,24 @@ struct LaneF2 {
     static __device__ __forceinline__ V mul(V a, V b) { return __fmul2_rn(a, b); }
     static __device__ __forceinline__ V fma(V a, V b, V d) { return __ffma2_rn(a, b, d); }
     static __device__ __forceinline__ V neg(V a) { return make_float2(-a.x, -a.y); }
-    static __device__ __forceinline__ V rcp(V a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
+    // rcp_rn on both halves: one range test for the pair, the correction step in packed form
+    static __device__ __forceinline__ V rcp(V a)
+    {
+        const unsigned ex = (__float_as_uint(a.x) >> 23) & 0xffu, ey = (__float_as_uint(a.y) >> 23) & 0xffu;
+        if ((ex - 1u > 251u) | (ey - 1u > 251u)) return make_float2(rcp_rn(a.x), rcp_rn(a.y));
+        float2 y;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y.x) : "f"(a.x));
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y.y) : "f"(a.y));
+        const float2 e = __ffma2_rn(make_float2(-a.x, -a.y), y, make_float2(1.f, 1.f));
+        return __ffma2_rn(y, e, y);
+    }
 };
 
 // Update of one opposite pair from twice its even/odd non-equilibrium parts, D = 2 de and DO = 2 do,
 // and f1: the increment is formed from the small quantities first and added to the stored population
 // once, so only that last addition rounds at the scale of g.  The halving of D and DO is folded into
-// the fma that consumes them, which rounds exactly as the half-scale form would.  The rest population
-// (update_rest_l) takes its parts at their own scale.
+// the coefficient k_d / 2 (exact), which rounds exactly as the half-scale form would.  The rest
+// population (update_rest_l) takes its parts at their own scale.
 template <class M, int OP>
 __device__ __forceinline__ void update_pair2_l(typename M::V &gi, typename M::V &gj, typename M::V D,
                                                typename M::V DO, typename M::V f1, const Coef &k)
@@ -111,10 +147,11 @@ __device__ __forceinline__ void update_pair2_l(typename M::V &gi, typename M::V 
         gi = M::fma(half, M::fma(d1, DI, M::mul(m2, DI)), gi);
         gj = M::fma(half, M::fma(d1, DJ, M::mul(m2, DJ)), gj);
     } else {
-        const V kd = M::c(k.kd);
-        const V a = M::fma(half, D, M::neg(f1)), t = M::mul(m2, f1);
-        gi = M::add(gi, M::fma(d1, f1, M::fma(kd, M::fma(half, DO, a), t)));
-        gj = M::add(gj, M::fma(d1, f1, M::fma(kd, M::fma(M::c(-0.5f), DO, a), t)));
+        // every product here feeds an explicit fma, so there is nothing left for contraction to fuse
+        const V kh = M::c(k.kh);
+        const V cm = M::fma(d1, f1, M::fma(M::c(k.nkc), f1, M::mul(kh, D)));
+        gi = M::add(gi, M::fma(kh, DO, cm));
+        gj = M::add(gj, M::fma(M::c(-k.kh), DO, cm));
     }
 }
 
@@ -124,7 +161,7 @@ __device__ __forceinline__ typename M::V update_rest_l(typename M::V g0, typenam
 {
     const typename M::V d1 = M::c(k.d1), m2 = M::c(-2.f);
     if (OP == OP_BGK) return M::add(g0, M::fma(d1, de0, M::mul(m2, de0)));
-    return M::add(g0, M::fma(d1, f10, M::fma(M::c(k.kd), M::sub(de0, f10), M::mul(m2, f10))));
+    return M::add(g0, M::fma(d1, f10, M::fma(M::c(k.nkc), f10, M::mul(M::c(k.kd), de0))));
 }
 
 // The D2Q9 update with the pair sums and differences kept at twice their scale: E = g_i + g_j = 2e,
@@ -155,7 +192,6 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
     const V cmP = M::add(mx, my), cmM = M::sub(mx, my);
     const V DP = M::fma(mw2x2, M::fma(M::mul(k45, cmP), M::add(ux, uy), mu15), M::fma(mw2x2, drho, EP));
     const V DM = M::fma(mw2x2, M::fma(M::mul(k45, cmM), M::sub(ux, uy), mu15), M::fma(mw2x2, drho, EM));
-    const V de0 = M::neg(M::add(M::add(DX, DY), M::add(DP, DM)));
     // twice the odd non-equilibrium parts; the axis pairs close the momentum
     const V DOP = M::fma(M::c(2.f * M3W2), cmP, OP_);
     const V DOM = M::fma(M::c(2.f * M3W2), cmM, OM);
@@ -188,6 +224,7 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
     }
     const V zero = M::c(0.f);
     if constexpr (OP == OP_BGK) {
+        const V de0 = M::neg(M::add(M::add(DX, DY), M::add(DP, DM)));
         g[0] = update_rest_l<M, OP>(g[0], de0, zero, k);
         update_pair2_l<M, OP>(g[1], g[2], DX, DOX, zero, k);
         update_pair2_l<M, OP>(g[3], g[4], DY, DOY, zero, k);
@@ -195,14 +232,19 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
         update_pair2_l<M, OP>(g[7], g[8], DM, DOM, zero, k);
         return;
     }
-    const V pxx = M::add(DX, M::add(DP, DM));
-    const V pyy = M::add(DY, M::add(DP, DM));
+    // Pi^neq (twice), the rest population's closure de0 = -(sum of the D) from the same partial sums,
+    // and f1 (f1X = pxx / 3 - pyy / 6 written as (pxx - pyy) / 4 + tr / 12)
+    const V sd = M::add(DP, DM);
+    const V pxx = M::add(DX, sd);
+    const V pyy = M::add(DY, sd);
     const V pxy = M::sub(DP, DM);
     const V tr = M::add(pxx, pyy);
+    const V de0 = M::neg(M::add(pxx, DY));
     const V f10 = M::mul(M::c(-2.f / 3.f), tr);
-    const V f1X = M::fma(pxx, M::c(1.f / 3.f), M::mul(pyy, M::c(-1.f / 6.f)));
-    const V f1Y = M::fma(pyy, M::c(1.f / 3.f), M::mul(pxx, M::c(-1.f / 6.f)));
     const V t12 = M::mul(tr, M::c(1.f / 12.f));
+    const V dxy = M::sub(pxx, pyy);
+    const V f1X = M::fma(dxy, M::c(0.25f), t12);
+    const V f1Y = M::fma(dxy, M::c(-0.25f), t12);
     const V f1P = M::fma(pxy, M::c(0.25f), t12);
     const V f1M = M::fma(pxy, M::c(-0.25f), t12);
     g[0] = update_rest_l<M, OP>(g[0], de0, f10, k);

@@ -36,28 +36,36 @@ static const int CY9[9] = {0, 0, 0, 1, -1, 1, -1, -1, 1};
 
 static double w9(int i) { return i == 0 ? 4. / 9. : (i < 5 ? 1. / 9. : 1. / 36.); }
 
-/* one opposite pair from D = 2 de, DO = 2 do and f1 */
-static void pair_update(float *gi, float *gj, float D, float DO, float f1, float d1, float kd, int op)
+/* Increment coefficients, formed in double and rounded once (the engine's shifted::Coef): d1 = 2 - 1/tau,
+ * kd = w_gt1 - 1, nkc = -(1 + w_gt1), kh = kd / 2. */
+typedef struct {
+    float d1, kd, nkc, kh;
+} Coef32;
+
+/* one opposite pair from D = 2 de, DO = 2 do and f1: the increment delta_1 f1 - k_c f1 + k_d d with
+ * d = (D +- DO) / 2, the part common to both members formed once */
+static void pair_update(float *gi, float *gj, float D, float DO, float f1, const Coef32 *k, int op)
 {
     if (op == ORC_OP_BGK) {
-        const float DI = D + DO, DJ = D - DO;
+        const float d1 = k->d1, DI = D + DO, DJ = D - DO;
         *gi = fmaf(0.5f, fmaf(d1, DI, -2.f * DI), *gi);
         *gj = fmaf(0.5f, fmaf(d1, DJ, -2.f * DJ), *gj);
     } else {
-        const float a = fmaf(0.5f, D, -f1), t = -2.f * f1;
-        *gi = *gi + fmaf(d1, f1, fmaf(kd, fmaf(0.5f, DO, a), t));
-        *gj = *gj + fmaf(d1, f1, fmaf(kd, fmaf(-0.5f, DO, a), t));
+        const float cm = fmaf(k->d1, f1, fmaf(k->nkc, f1, k->kh * D));
+        *gi = *gi + fmaf(k->kh, DO, cm);
+        *gj = *gj + fmaf(-k->kh, DO, cm);
     }
 }
 
-static float rest_update(float g0, float de0, float f10, float d1, float kd, int op)
+static float rest_update(float g0, float de0, float f10, const Coef32 *k, int op)
 {
-    if (op == ORC_OP_BGK) return g0 + fmaf(d1, de0, -2.f * de0);
-    return g0 + fmaf(d1, f10, fmaf(kd, de0 - f10, -2.f * f10));
+    if (op == ORC_OP_BGK) return g0 + fmaf(k->d1, de0, -2.f * de0);
+    return g0 + fmaf(k->d1, f10, fmaf(k->nkc, f10, k->kd * de0));
 }
 
-static void collide9_f32(float g[9], float d1, float kd, int op)
+static void collide9_f32(float g[9], const Coef32 *k, int op)
 {
+    const float d1 = k->d1;
     const float W1 = 1.f / 9.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
     const float EX = g[1] + g[2], OX = g[1] - g[2];
     const float EY = g[3] + g[4], OY = g[3] - g[4];
@@ -75,7 +83,6 @@ static void collide9_f32(float g[9], float d1, float kd, int op)
     const float cmP = mx + my, cmM = mx - my;
     const float DP = fmaf(mw2x2, fmaf(k45 * cmP, ux + uy, mu15), fmaf(mw2x2, drho, EP));
     const float DM = fmaf(mw2x2, fmaf(k45 * cmM, ux - uy, mu15), fmaf(mw2x2, drho, EM));
-    const float de0 = -((DX + DY) + (DP + DM));
     const float DOP = fmaf(2.f * M3W2, cmP, OP);
     const float DOM = fmaf(2.f * M3W2, cmM, OM);
     const float DOX = -(DOP + DOM);
@@ -105,24 +112,29 @@ static void collide9_f32(float g[9], float d1, float kd, int op)
         g[8] = g[8] + (xM - qM);
         return;
     }
-    float f10 = 0.f, f1X = 0.f, f1Y = 0.f, f1P = 0.f, f1M = 0.f;
-    if (op != ORC_OP_BGK) {
-        const float pxx = DX + (DP + DM);
-        const float pyy = DY + (DP + DM);
+    float f10 = 0.f, f1X = 0.f, f1Y = 0.f, f1P = 0.f, f1M = 0.f, de0;
+    if (op == ORC_OP_BGK) {
+        de0 = -((DX + DY) + (DP + DM));
+    } else {
+        const float sd = DP + DM;
+        const float pxx = DX + sd;
+        const float pyy = DY + sd;
         const float pxy = DP - DM;
         const float tr = pxx + pyy;
+        de0 = -(pxx + DY);
         f10 = (-2.f / 3.f) * tr;
-        f1X = fmaf(pxx, 1.f / 3.f, pyy * (-1.f / 6.f));
-        f1Y = fmaf(pyy, 1.f / 3.f, pxx * (-1.f / 6.f));
         const float t12 = tr * (1.f / 12.f);
+        const float dxy = pxx - pyy;
+        f1X = fmaf(dxy, 0.25f, t12);
+        f1Y = fmaf(dxy, -0.25f, t12);
         f1P = fmaf(pxy, 0.25f, t12);
         f1M = fmaf(pxy, -0.25f, t12);
     }
-    g[0] = rest_update(g[0], de0, f10, d1, kd, op);
-    pair_update(&g[1], &g[2], DX, DOX, f1X, d1, kd, op);
-    pair_update(&g[3], &g[4], DY, DOY, f1Y, d1, kd, op);
-    pair_update(&g[5], &g[6], DP, DOP, f1P, d1, kd, op);
-    pair_update(&g[7], &g[8], DM, DOM, f1M, d1, kd, op);
+    g[0] = rest_update(g[0], de0, f10, k, op);
+    pair_update(&g[1], &g[2], DX, DOX, f1X, k, op);
+    pair_update(&g[3], &g[4], DY, DOY, f1Y, k, op);
+    pair_update(&g[5], &g[6], DP, DOP, f1P, k, op);
+    pair_update(&g[7], &g[8], DM, DOM, f1M, k, op);
 }
 
 /* D3Q19: pairs X = (1,2), Y = (3,4), Z = (5,6), A = (7,8) c = (1,1,0), B = (9,10) c = (1,-1,0),
@@ -133,7 +145,7 @@ static const int CZ19[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, -1,
 
 static double w19(int i) { return i == 0 ? 1. / 3. : (i < 7 ? 1. / 18. : 1. / 36.); }
 
-static void collide19_f32(float g[19], float d1, float kd, int op)
+static void collide19_f32(float g[19], const Coef32 *k, int op)
 {
     const float W1 = 1.f / 18.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
     const float EX = g[1] + g[2], OX = g[1] - g[2];
@@ -195,16 +207,16 @@ static void collide19_f32(float g[19], float d1, float kd, int op)
         f1E = fmaf(0.25f, pyz, byz);
         f1F = fmaf(-0.25f, pyz, byz);
     }
-    g[0] = rest_update(g[0], de0, f10, d1, kd, op);
-    pair_update(&g[1], &g[2], DX, DOX, f1X, d1, kd, op);
-    pair_update(&g[3], &g[4], DY, DOY, f1Y, d1, kd, op);
-    pair_update(&g[5], &g[6], DZ, DOZ, f1Z, d1, kd, op);
-    pair_update(&g[7], &g[8], DA, DOA, f1A, d1, kd, op);
-    pair_update(&g[9], &g[10], DB, DOB, f1B, d1, kd, op);
-    pair_update(&g[11], &g[12], DC, DOC, f1C, d1, kd, op);
-    pair_update(&g[13], &g[14], DD, DOD, f1D, d1, kd, op);
-    pair_update(&g[16], &g[15], DE, DOE, f1E, d1, kd, op);
-    pair_update(&g[17], &g[18], DF, DOF, f1F, d1, kd, op);
+    g[0] = rest_update(g[0], de0, f10, k, op);
+    pair_update(&g[1], &g[2], DX, DOX, f1X, k, op);
+    pair_update(&g[3], &g[4], DY, DOY, f1Y, k, op);
+    pair_update(&g[5], &g[6], DZ, DOZ, f1Z, k, op);
+    pair_update(&g[7], &g[8], DA, DOA, f1A, k, op);
+    pair_update(&g[9], &g[10], DB, DOB, f1B, k, op);
+    pair_update(&g[11], &g[12], DC, DOC, f1C, k, op);
+    pair_update(&g[13], &g[14], DD, DOD, f1D, k, op);
+    pair_update(&g[16], &g[15], DE, DOE, f1E, k, op);
+    pair_update(&g[17], &g[18], DF, DOF, f1F, k, op);
 }
 
 static int opp(int i) { return i == 0 ? 0 : (i % 2 ? i + 1 : i - 1); }
@@ -400,10 +412,20 @@ static int run_periodic(int q, int nx, int ny, int nz, const uint8_t *solid, con
         free(b);
         return -2;
     }
-    const float d1 = (float)(2.0 - 1.0 / tau);
-    const float kd = (op == ORC_OP_BGK || op == ORC_OP_MRT) ? 0.f
-                     : op == ORC_OP_REG                      ? -1.f
-                                                             : (float)((1.0 - 1.0 / tau_nh) - 1.0);
+    Coef32 k;
+    k.d1 = (float)(2.0 - 1.0 / tau);
+    if (op == ORC_OP_BGK || op == ORC_OP_MRT) {
+        k.kd = 0.f;
+        k.nkc = 0.f;
+    } else if (op == ORC_OP_REG) {
+        k.kd = -1.f;
+        k.nkc = -1.f;
+    } else {
+        const double omega_gt1 = 1.0 - 1.0 / tau_nh;
+        k.kd = (float)(omega_gt1 - 1.0);
+        k.nkc = (float)(-(1.0 + omega_gt1));
+    }
+    k.kh = 0.5f * k.kd;
     for (size_t p = 0; p < n; p++)
         for (int i = 0; i < q; i++) a[p * q + i] = (float)(f_in[p * q + i] - (q == 9 ? w9(i) : w19(i)));
     for (int s = 0; s < n_steps; s++) {
@@ -418,9 +440,9 @@ static int run_periodic(int q, int nx, int ny, int nz, const uint8_t *solid, con
                     }
                     after_planes(a, q, nx, ny, nz, solid, pl, s == 0, x, y, z, g);
                     if (q == 9)
-                        collide9_f32(g, d1, kd, op);
+                        collide9_f32(g, &k, op);
                     else
-                        collide19_f32(g, d1, kd, op);
+                        collide19_f32(g, &k, op);
                     memcpy(&b[node * q], g, (size_t)q * sizeof(float));
                 }
         float *t = a;
