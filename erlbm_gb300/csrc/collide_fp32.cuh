@@ -40,26 +40,32 @@ namespace erlbm {
 namespace shifted {
 
 // Increment coefficients, formed in FP64 and rounded once: kd = w_gt1 - 1 (unused by BGK and MRT),
-// d1 = 2 - 1/tau (delta_1, or delta for BGK), nkc = -(1 + w_gt1) = -(2 + kd); kh = kd / 2 (exact).
+// d1 = 2 - 1/tau (delta_1, or delta for BGK), nkc = -(1 + w_gt1) = -(2 + kd); kh = kd / 2 (exact);
+// d1t = -2/3 d1 and nkct = -2/3 nkc, the D2Q9 rest population's factors of the trace (its f1 is
+// -2/3 tr).
 struct Coef {
-    float kd, d1, nkc, kh;
+    float kd, d1, nkc, kh, d1t, nkct;
 };
 
 __host__ __device__ inline Coef make_coef(const Relax &R)
 {
     Coef k;
-    k.d1 = (float)(2.0 - R.inv_tau);
+    const double d1 = 2.0 - R.inv_tau;
+    double nkc = 0.0;
+    k.d1 = (float)d1;
     if (R.op == OP_BGK || R.op == OP_MRT) {
         k.kd = 0.f;
-        k.nkc = 0.f;
     } else if (R.op == OP_REG) {
         k.kd = -1.f;
-        k.nkc = -1.f;
+        nkc = -1.0;
     } else {
         k.kd = (float)(R.omega_gt1 - 1.0);
-        k.nkc = (float)(-(1.0 + R.omega_gt1));
+        nkc = -(1.0 + R.omega_gt1);
     }
+    k.nkc = (float)nkc;
     k.kh = 0.5f * k.kd;
+    k.d1t = (float)(-2.0 / 3.0 * d1);
+    k.nkct = (float)(-2.0 / 3.0 * nkc);
     return k;
 }
 
@@ -184,14 +190,20 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
     const V my = M::add(OY, M::sub(OP_, OM));
     const V inv = M::rcp(M::add(M::c(1.f), drho));
     const V ux = M::mul(mx, inv), uy = M::mul(my, inv);
-    const V mu15 = M::mul(M::c(-1.5f), M::fma(mx, ux, M::mul(my, uy)));
+    // the equilibrium's quadratic parts 4.5 (c.m)(c.u) - 1.5 m.u from a = m_x u_x, b = m_y u_y and
+    // c = m_x u_y + m_y u_x: 4.5 a - 1.5 (a + b) on the x axis, 3 (a + b) +- 4.5 c on the diagonals
+    const V a = M::mul(mx, ux), b = M::mul(my, uy);
+    const V sab = M::fma(mx, ux, b);  // a + b as one rounding (no product is left to an add)
+    const V mu15 = M::mul(M::c(-1.5f), sab);
+    const V cxy = M::fma(mx, uy, M::mul(my, ux));
+    const V s3 = M::mul(M::c(3.f), sab);
     const V k45 = M::c(4.5f), mw1x2 = M::c(-2.f * W1), mw2x2 = M::c(-2.f * W2);
     // twice the even non-equilibrium parts
-    const V DX = M::fma(mw1x2, M::fma(M::mul(k45, mx), ux, mu15), M::fma(mw1x2, drho, EX));
-    const V DY = M::fma(mw1x2, M::fma(M::mul(k45, my), uy, mu15), M::fma(mw1x2, drho, EY));
+    const V DX = M::fma(mw1x2, M::fma(k45, a, mu15), M::fma(mw1x2, drho, EX));
+    const V DY = M::fma(mw1x2, M::fma(k45, b, mu15), M::fma(mw1x2, drho, EY));
     const V cmP = M::add(mx, my), cmM = M::sub(mx, my);
-    const V DP = M::fma(mw2x2, M::fma(M::mul(k45, cmP), M::add(ux, uy), mu15), M::fma(mw2x2, drho, EP));
-    const V DM = M::fma(mw2x2, M::fma(M::mul(k45, cmM), M::sub(ux, uy), mu15), M::fma(mw2x2, drho, EM));
+    const V DP = M::fma(mw2x2, M::fma(k45, cxy, s3), M::fma(mw2x2, drho, EP));
+    const V DM = M::fma(mw2x2, M::fma(M::c(-4.5f), cxy, s3), M::fma(mw2x2, drho, EM));
     // twice the odd non-equilibrium parts; the axis pairs close the momentum
     const V DOP = M::fma(M::c(2.f * M3W2), cmP, OP_);
     const V DOM = M::fma(M::c(2.f * M3W2), cmM, OM);
@@ -232,22 +244,19 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
         update_pair2_l<M, OP>(g[7], g[8], DM, DOM, zero, k);
         return;
     }
-    // Pi^neq (twice), the rest population's closure de0 = -(sum of the D) from the same partial sums,
-    // and f1 (f1X = pxx / 3 - pyy / 6 written as (pxx - pyy) / 4 + tr / 12)
-    const V sd = M::add(DP, DM);
-    const V pxx = M::add(DX, sd);
-    const V pyy = M::add(DY, sd);
-    const V pxy = M::sub(DP, DM);
-    const V tr = M::add(pxx, pyy);
-    const V de0 = M::neg(M::add(pxx, DY));
-    const V f10 = M::mul(M::c(-2.f / 3.f), tr);
+    // Pi^neq (twice) through the sums sxy = D_X + D_Y and sd = D_P + D_M: tr = sxy + 2 sd,
+    // pxx - pyy = D_X - D_Y, the rest population's closure de0 = -(sxy + sd); f1 (f1X = pxx / 3 -
+    // pyy / 6 written as (pxx - pyy) / 4 + tr / 12; f1_0 = -2/3 tr enters through d1t and nkct)
+    const V sxy = M::add(DX, DY), sd = M::add(DP, DM);
+    const V tr = M::fma(M::c(2.f), sd, sxy);
+    const V de0 = M::neg(M::add(sxy, sd));
     const V t12 = M::mul(tr, M::c(1.f / 12.f));
-    const V dxy = M::sub(pxx, pyy);
+    const V dxy = M::sub(DX, DY), pxy = M::sub(DP, DM);
     const V f1X = M::fma(dxy, M::c(0.25f), t12);
     const V f1Y = M::fma(dxy, M::c(-0.25f), t12);
     const V f1P = M::fma(pxy, M::c(0.25f), t12);
     const V f1M = M::fma(pxy, M::c(-0.25f), t12);
-    g[0] = update_rest_l<M, OP>(g[0], de0, f10, k);
+    g[0] = M::add(g[0], M::fma(M::c(k.d1t), tr, M::fma(M::c(k.nkct), tr, M::mul(M::c(k.kd), de0))));
     update_pair2_l<M, OP>(g[1], g[2], DX, DOX, f1X, k);
     update_pair2_l<M, OP>(g[3], g[4], DY, DOY, f1Y, k);
     update_pair2_l<M, OP>(g[5], g[6], DP, DOP, f1P, k);

@@ -479,13 +479,13 @@ __global__ void __launch_bounds__(128, 4) k_periodic_d2q9_x3s(const float *__res
 // The first stage pulls straight from memory: for P' row j + 2 it loads the c_y = +1 group of P row
 // j + 1, the c_y = 0 group of row j + 2 and the c_y = -1 group of row j + 3 (one iteration ahead), so
 // every input population is still read once.  The two later stages carry the c_y = +1 groups of
-// their two newest input rows and the c_y = 0 group of the newest one in registers; those rotate
-// through three and two register slots, so the loop body is unrolled six times and no group is copied
-// between iterations.  Per iteration P' row j + 2, P'' row j + 1 and output row j are collided; the
+// their two newest input rows and the c_y = 0 group of the newest one in registers; the groups of a
+// row stay in the register slot they arrive in (three slots per group, used in turn), so the loop
+// body is unrolled three times and no group is copied between iterations.  Per iteration P' row j + 2, P'' row j + 1 and output row j are collided; the
 // first four iterations of a chunk are its prologue, in which only the stages whose inputs exist run.
 // Bit-identical to three one-step launches: every node is collided by collide9x2 as by collide9.
 constexpr int XP_W = 60;   // output columns per strip
-constexpr int XP_SPAN = 6; // rows per unrolled group
+constexpr int XP_SPAN = 3; // rows per unrolled group: one turn of the three register slots
 
 template <int I>
 struct IntC {
@@ -550,14 +550,15 @@ __global__ void __launch_bounds__(128, MINB) k_periodic_d2q9_x3p(const float *__
     };
 
     // carried groups of stages 1 and 2 (index 0, 1): s1[.][slot] c_y = +1 (3, 5, 8), s0[.][slot] c_y = 0 (0, 1, 2)
-    float2 s1[2][3][3], s0[2][2][3];
+    float2 s1[2][3][3], s0[2][3][3];
     float2 g[9], nm[3];
 
     // one iteration at rotation phase T: stage 0, 1, 2 collide P' row j + 2, P'' row j + 1 and output
     // row j where C1, C2 say their inputs exist (stage 0 always runs)
     auto step = [&](auto T, auto C1, auto C2, int j) {
-        constexpr int t = decltype(T)::value;
-        constexpr int a = t % 3, n = (t + 2) % 3, z = (t + 1) % 2;
+        // slots: the newest input row's groups go to n, the previous row's are in b, the one before in a
+        constexpr int t = decltype(T)::value % 3;
+        constexpr int a = t, b = (t + 1) % 3, n = (t + 2) % 3;
         constexpr bool c1 = decltype(C1)::value, c2 = decltype(C2)::value;
         g[3] = ld[3];
         g[5] = pull_p_halo(ld[5], hv[1]);
@@ -577,9 +578,9 @@ __global__ void __launch_bounds__(128, MINB) k_periodic_d2q9_x3p(const float *__
                 g[3] = s1[s - 1][a][0];
                 g[5] = s1[s - 1][a][1];
                 g[8] = s1[s - 1][a][2];
-                g[0] = s0[s - 1][z ^ 1][0];
-                g[1] = s0[s - 1][z ^ 1][1];
-                g[2] = s0[s - 1][z ^ 1][2];
+                g[0] = s0[s - 1][b][0];
+                g[1] = s0[s - 1][b][1];
+                g[2] = s0[s - 1][b][2];
                 g[4] = nm[0];
                 g[6] = nm[1];
                 g[7] = nm[2];
@@ -595,9 +596,9 @@ __global__ void __launch_bounds__(128, MINB) k_periodic_d2q9_x3p(const float *__
                 s1[s][n][0] = g[3];
                 s1[s][n][1] = pull_p(g[5]);
                 s1[s][n][2] = pull_m(g[8]);
-                s0[s][z][0] = g[0];
-                s0[s][z][1] = pull_p(g[1]);
-                s0[s][z][2] = pull_m(g[2]);
+                s0[s][n][0] = g[0];
+                s0[s][n][1] = pull_p(g[1]);
+                s0[s][n][2] = pull_m(g[2]);
                 nm[0] = g[4];
                 nm[1] = pull_m(g[6]);
                 nm[2] = pull_p(g[7]);
@@ -606,19 +607,16 @@ __global__ void __launch_bounds__(128, MINB) k_periodic_d2q9_x3p(const float *__
     };
     using F = IntC<0>;
     using N = IntC<1>;
-    // prologue: P' rows y0 - 2 .. y0 + 1, P'' rows y0 - 1, y0 (phases 2 .. 5, so the loop starts at 0)
+    // prologue: P' rows y0 - 2 .. y0 + 1, P'' rows y0 - 1, y0 (phases 2, 0, 1, 2, so the loop starts at 0)
     load(y0 - 2);
     step(IntC<2>{}, F{}, F{}, y0 - 4);
-    step(IntC<3>{}, F{}, F{}, y0 - 3);
-    step(IntC<4>{}, N{}, F{}, y0 - 2);
-    step(IntC<5>{}, N{}, F{}, y0 - 1);
+    step(IntC<0>{}, F{}, F{}, y0 - 3);
+    step(IntC<1>{}, N{}, F{}, y0 - 2);
+    step(IntC<2>{}, N{}, F{}, y0 - 1);
     for (int j = y0; j < y1; j += XP_SPAN) {
         step(IntC<0>{}, N{}, N{}, j);
         step(IntC<1>{}, N{}, N{}, j + 1);
         step(IntC<2>{}, N{}, N{}, j + 2);
-        step(IntC<3>{}, N{}, N{}, j + 3);
-        step(IntC<4>{}, N{}, N{}, j + 4);
-        step(IntC<5>{}, N{}, N{}, j + 5);
     }
 }
 
@@ -723,7 +721,7 @@ static void go_x3p(const Geo &g, const shifted::Coef &k, const float *src, float
     if (chunks < 1) chunks = 1;
     long long hc = (g.ny + chunks - 1) / chunks;
     hc = (hc + XP_SPAN - 1) / XP_SPAN * XP_SPAN;
-    if (hc < 2 * XP_SPAN) hc = 2 * XP_SPAN;
+    if (hc < 2 * XP_SPAN) hc = 2 * XP_SPAN;  // the prologue's six rows are not worth a shorter chunk
     const int n_warps = strips * (int)((g.ny + hc - 1) / hc);
     kern<<<(unsigned)((n_warps + 3) / 4), 128, 0, s>>>(src, dst, g.nx, g.ny, g.plane, (int)hc, strips, n_warps, k);
 }

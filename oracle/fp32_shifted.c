@@ -37,9 +37,9 @@ static const int CY9[9] = {0, 0, 0, 1, -1, 1, -1, -1, 1};
 static double w9(int i) { return i == 0 ? 4. / 9. : (i < 5 ? 1. / 9. : 1. / 36.); }
 
 /* Increment coefficients, formed in double and rounded once (the engine's shifted::Coef): d1 = 2 - 1/tau,
- * kd = w_gt1 - 1, nkc = -(1 + w_gt1), kh = kd / 2. */
+ * kd = w_gt1 - 1, nkc = -(1 + w_gt1), kh = kd / 2, d1t = -2/3 d1, nkct = -2/3 nkc. */
 typedef struct {
-    float d1, kd, nkc, kh;
+    float d1, kd, nkc, kh, d1t, nkct;
 } Coef32;
 
 /* one opposite pair from D = 2 de, DO = 2 do and f1: the increment delta_1 f1 - k_c f1 + k_d d with
@@ -76,13 +76,17 @@ static void collide9_f32(float g[9], const Coef32 *k, int op)
     const float my = OY + (OP - OM);
     const float inv = 1.f / (1.f + drho);
     const float ux = mx * inv, uy = my * inv;
-    const float mu15 = -1.5f * fmaf(mx, ux, my * uy);
+    const float a = mx * ux, b = my * uy;
+    const float sab = fmaf(mx, ux, b);
+    const float mu15 = -1.5f * sab;
+    const float cxy = fmaf(mx, uy, my * ux);
+    const float s3 = 3.f * sab;
     const float k45 = 4.5f, mw1x2 = -2.f * W1, mw2x2 = -2.f * W2;
-    const float DX = fmaf(mw1x2, fmaf(k45 * mx, ux, mu15), fmaf(mw1x2, drho, EX));
-    const float DY = fmaf(mw1x2, fmaf(k45 * my, uy, mu15), fmaf(mw1x2, drho, EY));
+    const float DX = fmaf(mw1x2, fmaf(k45, a, mu15), fmaf(mw1x2, drho, EX));
+    const float DY = fmaf(mw1x2, fmaf(k45, b, mu15), fmaf(mw1x2, drho, EY));
     const float cmP = mx + my, cmM = mx - my;
-    const float DP = fmaf(mw2x2, fmaf(k45 * cmP, ux + uy, mu15), fmaf(mw2x2, drho, EP));
-    const float DM = fmaf(mw2x2, fmaf(k45 * cmM, ux - uy, mu15), fmaf(mw2x2, drho, EM));
+    const float DP = fmaf(mw2x2, fmaf(k45, cxy, s3), fmaf(mw2x2, drho, EP));
+    const float DM = fmaf(mw2x2, fmaf(-4.5f, cxy, s3), fmaf(mw2x2, drho, EM));
     const float DOP = fmaf(2.f * M3W2, cmP, OP);
     const float DOM = fmaf(2.f * M3W2, cmM, OM);
     const float DOX = -(DOP + DOM);
@@ -112,25 +116,22 @@ static void collide9_f32(float g[9], const Coef32 *k, int op)
         g[8] = g[8] + (xM - qM);
         return;
     }
-    float f10 = 0.f, f1X = 0.f, f1Y = 0.f, f1P = 0.f, f1M = 0.f, de0;
+    float f1X = 0.f, f1Y = 0.f, f1P = 0.f, f1M = 0.f;
     if (op == ORC_OP_BGK) {
-        de0 = -((DX + DY) + (DP + DM));
+        const float de0 = -((DX + DY) + (DP + DM));
+        g[0] = rest_update(g[0], de0, 0.f, k, op);
     } else {
-        const float sd = DP + DM;
-        const float pxx = DX + sd;
-        const float pyy = DY + sd;
-        const float pxy = DP - DM;
-        const float tr = pxx + pyy;
-        de0 = -(pxx + DY);
-        f10 = (-2.f / 3.f) * tr;
+        const float sxy = DX + DY, sd = DP + DM;
+        const float tr = fmaf(2.f, sd, sxy);
+        const float de0 = -(sxy + sd);
         const float t12 = tr * (1.f / 12.f);
-        const float dxy = pxx - pyy;
+        const float dxy = DX - DY, pxy = DP - DM;
         f1X = fmaf(dxy, 0.25f, t12);
         f1Y = fmaf(dxy, -0.25f, t12);
         f1P = fmaf(pxy, 0.25f, t12);
         f1M = fmaf(pxy, -0.25f, t12);
+        g[0] = g[0] + fmaf(k->d1t, tr, fmaf(k->nkct, tr, k->kd * de0));
     }
-    g[0] = rest_update(g[0], de0, f10, k, op);
     pair_update(&g[1], &g[2], DX, DOX, f1X, k, op);
     pair_update(&g[3], &g[4], DY, DOY, f1Y, k, op);
     pair_update(&g[5], &g[6], DP, DOP, f1P, k, op);
@@ -413,19 +414,23 @@ static int run_periodic(int q, int nx, int ny, int nz, const uint8_t *solid, con
         return -2;
     }
     Coef32 k;
-    k.d1 = (float)(2.0 - 1.0 / tau);
+    const double d1 = 2.0 - 1.0 / tau;
+    double nkc = 0.0;
+    k.d1 = (float)d1;
     if (op == ORC_OP_BGK || op == ORC_OP_MRT) {
         k.kd = 0.f;
-        k.nkc = 0.f;
     } else if (op == ORC_OP_REG) {
         k.kd = -1.f;
-        k.nkc = -1.f;
+        nkc = -1.0;
     } else {
         const double omega_gt1 = 1.0 - 1.0 / tau_nh;
         k.kd = (float)(omega_gt1 - 1.0);
-        k.nkc = (float)(-(1.0 + omega_gt1));
+        nkc = -(1.0 + omega_gt1);
     }
+    k.nkc = (float)nkc;
     k.kh = 0.5f * k.kd;
+    k.d1t = (float)(-2.0 / 3.0 * d1);
+    k.nkct = (float)(-2.0 / 3.0 * nkc);
     for (size_t p = 0; p < n; p++)
         for (int i = 0; i < q; i++) a[p * q + i] = (float)(f_in[p * q + i] - (q == 9 ? w9(i) : w19(i)));
     for (int s = 0; s < n_steps; s++) {
