@@ -620,6 +620,159 @@ __global__ void __launch_bounds__(128, MINB) k_periodic_d2q9_x3p(const float *__
     }
 }
 
+
+// The column-pair kernel with its first-stage inputs brought in ahead by asynchronous copies into a
+// per-warp ring of shared memory (XA_DEPTH slots) instead of registers.  A slot holds, for each of the
+// nine populations, the 68 columns xs - 4 .. xs + 63 of the input row its c_y group comes from (c_y =
+// +1: row r - 1, 0: row r, -1: row r + 1 for P' row r), as 153 aligned 16-byte pieces spread over the
+// lanes.  The x pull is then a shifted shared-memory read: a lane's nodes sit at slot columns 2l + 2,
+// 2l + 3; c_x = +1 populations are read at 2l + 1, 2l + 2 and c_x = -1 ones at 2l + 3, 2l + 4, which
+// also covers the strip's edge columns, so the first stage needs no shuffle, select or edge load.  The
+// copies for P' row r + 2 are issued while row r is collided.  Everything after the first stage is the
+// x3p kernel's.
+constexpr int XA_DEPTH = 3;                // ring slots (two rows of copies in flight)
+constexpr int XA_ROW = 68;                 // columns per population row in a slot
+constexpr int XA_SLOT = 9 * XA_ROW;        // floats per slot
+constexpr int XA_PIECES = 9 * XA_ROW / 4;  // 16-byte pieces per slot (153)
+constexpr size_t XA_SMEM_PER_WARP = (size_t)XA_DEPTH * XA_SLOT * sizeof(float);
+
+__device__ __forceinline__ void cp_async16(float *dst_smem, const float *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <int OP, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_periodic_d2q9_x3a(const float *__restrict__ src, float *__restrict__ dst,
+                                                                int nx, int ny, int plane, int hc, int strips,
+                                                                int n_warps, shifted::Coef k)
+{
+    extern __shared__ __align__(16) float xa_smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = (int)(threadIdx.x >> 5);
+    const int wid = (int)blockIdx.x * (int)(blockDim.x >> 5) + wib;
+    if (wid >= n_warps) return;  // the whole warp leaves together
+    float *ring = xa_smem + (size_t)wib * (XA_DEPTH * XA_SLOT);
+    const int xs = (wid % strips) * XP_W;
+    const int y0 = (wid / strips) * hc;
+    const int y1 = min(y0 + hc, ny);
+    int c = xs - 2 + 2 * lane;  // even, in [-2, nx + 60]
+    const bool store = lane >= 1 && lane <= 30 && c < nx;
+    c = c < 0 ? c + nx : (c >= nx ? c - nx : c);
+    auto wrap = [&](int r) { return r < 0 ? r + ny : (r >= ny ? r - ny : r); };
+
+    // this lane's pieces q = lane + 32 m (q < 153): population q / 17, columns xs - 4 + 4 (q % 17) .. + 3
+    // (a piece never straddles the periodic seam: nx and the piece start are multiples of 4), offset
+    // within the population's plane, and the row of its c_y group (0: r - 1, 1: r, 2: r + 1)
+    int off[5];
+    unsigned rowsel = 0;  // 2 bits per piece
+#pragma unroll
+    for (int m = 0; m < 5; m++) {
+        const int q = lane + 32 * m;
+        const int pop = q / 17;
+        int col = xs - 4 + 4 * (q % 17);
+        col = col < 0 ? col + nx : (col >= nx ? col - nx : col);
+        off[m] = pop * plane + col;
+        const unsigned sel = (pop == 3 || pop == 5 || pop == 8) ? 0u : ((pop <= 2) ? 1u : 2u);
+        rowsel |= sel << (2 * m);
+    }
+    // copies of P' row r's inputs into a slot
+    auto issue = [&](int r, float *slot) {
+        const int ra = wrap(r - 1) * nx, rb = wrap(r) * nx, rc = wrap(r + 1) * nx;
+#pragma unroll
+        for (int m = 0; m < 5; m++) {
+            if (m == 4 && lane + 128 >= XA_PIECES) break;
+            const unsigned sel = (rowsel >> (2 * m)) & 3u;
+            const int ro = sel == 0 ? ra : (sel == 1 ? rb : rc);
+            cp_async16(slot + 4 * (lane + 32 * m), src + (unsigned)(ro + off[m]));
+        }
+        cp_async_commit();
+    };
+    // first-stage input of the lane's two nodes from a slot (x pull by the read offsets)
+    auto read = [&](const float *S, float2 g[9]) {
+        const int b = 2 * lane;
+        g[0] = *reinterpret_cast<const float2 *>(S + 0 * XA_ROW + b + 2);
+        g[3] = *reinterpret_cast<const float2 *>(S + 3 * XA_ROW + b + 2);
+        g[4] = *reinterpret_cast<const float2 *>(S + 4 * XA_ROW + b + 2);
+        g[1] = make_float2(S[1 * XA_ROW + b + 1], S[1 * XA_ROW + b + 2]);
+        g[5] = make_float2(S[5 * XA_ROW + b + 1], S[5 * XA_ROW + b + 2]);
+        g[7] = make_float2(S[7 * XA_ROW + b + 1], S[7 * XA_ROW + b + 2]);
+        g[2] = make_float2(S[2 * XA_ROW + b + 3], S[2 * XA_ROW + b + 4]);
+        g[6] = make_float2(S[6 * XA_ROW + b + 3], S[6 * XA_ROW + b + 4]);
+        g[8] = make_float2(S[8 * XA_ROW + b + 3], S[8 * XA_ROW + b + 4]);
+    };
+    auto pull_p = [&](float2 v) { return make_float2(__shfl_up_sync(XS_FULL, v.y, 1), v.x); };
+    auto pull_m = [&](float2 v) { return make_float2(v.y, __shfl_down_sync(XS_FULL, v.x, 1)); };
+
+    float2 s1[2][3][3], s0[2][3][3];
+    float2 g[9], nm[3];
+
+    // one iteration at rotation phase T (P' row j + 2 from ring slot (T + 1) % 3; the copies for P' row
+    // j + 4 go to slot T, which every lane finished reading one iteration earlier)
+    auto step = [&](auto T, auto C1, auto C2, int j) {
+        constexpr int t = decltype(T)::value % 3;
+        constexpr int a = t, b = (t + 1) % 3, n = (t + 2) % 3;
+        constexpr bool c1 = decltype(C1)::value, c2 = decltype(C2)::value;
+        cp_async_wait<XA_DEPTH - 2>();
+        __syncwarp();
+        read(ring + ((t + 1) % 3) * XA_SLOT, g);
+        issue(j + 4, ring + t * XA_SLOT);
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
+            if (s == 1 && !c1) break;
+            if (s == 2 && !c2) break;
+            if (s > 0) {
+                g[3] = s1[s - 1][a][0];
+                g[5] = s1[s - 1][a][1];
+                g[8] = s1[s - 1][a][2];
+                g[0] = s0[s - 1][b][0];
+                g[1] = s0[s - 1][b][1];
+                g[2] = s0[s - 1][b][2];
+                g[4] = nm[0];
+                g[6] = nm[1];
+                g[7] = nm[2];
+            }
+            shifted::collide9x2<OP>(g, k);
+            if (s == 2) {
+                if (store && j < y1) {
+                    float *d = dst + (long long)j * nx + c;
+#pragma unroll
+                    for (int i = 0; i < 9; i++) *reinterpret_cast<float2 *>(d + (long long)i * plane) = g[i];
+                }
+            } else {
+                s1[s][n][0] = g[3];
+                s1[s][n][1] = pull_p(g[5]);
+                s1[s][n][2] = pull_m(g[8]);
+                s0[s][n][0] = g[0];
+                s0[s][n][1] = pull_p(g[1]);
+                s0[s][n][2] = pull_m(g[2]);
+                nm[0] = g[4];
+                nm[1] = pull_m(g[6]);
+                nm[2] = pull_p(g[7]);
+            }
+        }
+    };
+    using F = IntC<0>;
+    using N = IntC<1>;
+    // P' rows y0 - 2 and y0 - 1 go to slots 0 and 1; the prologue runs phases 2, 0, 1, 2
+    issue(y0 - 2, ring);
+    issue(y0 - 1, ring + XA_SLOT);
+    step(IntC<2>{}, F{}, F{}, y0 - 4);
+    step(IntC<0>{}, F{}, F{}, y0 - 3);
+    step(IntC<1>{}, N{}, F{}, y0 - 2);
+    step(IntC<2>{}, N{}, F{}, y0 - 1);
+    for (int j = y0; j < y1; j += XP_SPAN) {
+        step(IntC<0>{}, N{}, N{}, j);
+        step(IntC<1>{}, N{}, N{}, j + 1);
+        step(IntC<2>{}, N{}, N{}, j + 2);
+    }
+    cp_async_wait_all();  // the copies issued for rows past the chunk land before the warp leaves
+}
+
 }  // namespace
 
 bool periodic_d2q9_x2_ok(const Geo &g)
@@ -726,7 +879,50 @@ static void go_x3p(const Geo &g, const shifted::Coef &k, const float *src, float
     kern<<<(unsigned)((n_warps + 3) / 4), 128, 0, s>>>(src, dst, g.nx, g.ny, g.plane, (int)hc, strips, n_warps, k);
 }
 
-bool periodic_d2q9_x3p_ok(const Geo &g) { return periodic_d2q9_fp32_ok(g) && g.ny >= 16 && g.nx >= 128; }
+// The wide three-step launch: the asynchronous-copy kernel (default; its offsets are 32-bit) or the
+// register-prefetch one (ERLBM_XP_ASYNC=0 at build time).
+#ifndef ERLBM_XP_ASYNC
+#define ERLBM_XP_ASYNC 1
+#endif
+// resident 128-thread CTAs per SM of the asynchronous-copy kernel (its register cap follows from it)
+#ifndef ERLBM_XA_MINB
+#define ERLBM_XA_MINB 4
+#endif
+
+template <int OP>
+static void go_x3a(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
+{
+    auto kern = k_periodic_d2q9_x3a<OP, ERLBM_XA_MINB>;
+    const size_t smem = 4 * XA_SMEM_PER_WARP;
+    constexpr int MAXDEV = 64;
+    static std::atomic<int> warps_cache[MAXDEV];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int d = dev >= 0 && dev < MAXDEV ? dev : 0;
+    int resident = warps_cache[d].load(std::memory_order_relaxed);
+    if (resident <= 0) {
+        int o = 0, n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, 128, smem) != cudaSuccess || o < 1) o = 1;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        resident = o * 4 * (n > 0 ? n : 1);
+        warps_cache[d].store(resident, std::memory_order_relaxed);
+    }
+    const int strips = (g.nx + XP_W - 1) / XP_W;
+    long long chunks = resident / strips;
+    if (chunks < 1) chunks = 1;
+    long long hc = (g.ny + chunks - 1) / chunks;
+    hc = (hc + XP_SPAN - 1) / XP_SPAN * XP_SPAN;
+    if (hc < 2 * XP_SPAN) hc = 2 * XP_SPAN;
+    const int n_warps = strips * (int)((g.ny + hc - 1) / hc);
+    kern<<<(unsigned)((n_warps + 3) / 4), 128, smem, s>>>(src, dst, g.nx, g.ny, (int)g.plane, (int)hc, strips, n_warps,
+                                                         k);
+}
+
+bool periodic_d2q9_x3p_ok(const Geo &g)
+{
+    // 64-column strips need ny >= 16; the asynchronous form addresses the nine planes with 32-bit offsets
+    return periodic_d2q9_fp32_ok(g) && g.ny >= 16 && g.nx >= 128 && (!ERLBM_XP_ASYNC || 9 * g.plane < (1LL << 31));
+}
 
 // Three steps of the fused periodic D2Q9 FP32 update in one launch (periodic_d2q9_x2_ok(g) required;
 // wide = the column-pair kernel, which needs periodic_d2q9_x3p_ok(g)).
@@ -735,6 +931,16 @@ int launch_periodic_d2q9_fp32_x3(int op, const Geo &g, const Relax &R, const flo
 {
     if (!periodic_d2q9_x2_ok(g) || (wide && !periodic_d2q9_x3p_ok(g))) return -1;
     const shifted::Coef k = shifted::make_coef(R);
+    if (wide && ERLBM_XP_ASYNC) {
+        switch (op) {
+        case OP_BGK: go_x3a<OP_BGK>(g, k, src, dst, s); break;
+        case OP_MRT: go_x3a<OP_MRT>(g, k, src, dst, s); break;
+        case OP_REG: go_x3a<OP_REG>(g, k, src, dst, s); break;
+        case OP_EXTREG: go_x3a<OP_EXTREG>(g, k, src, dst, s); break;
+        default: return -1;
+        }
+        return cudaGetLastError() == cudaSuccess ? 0 : -3;
+    }
     if (wide) {
         switch (op) {
         case OP_BGK: go_x3p<OP_BGK>(g, k, src, dst, s); break;
