@@ -349,6 +349,7 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     per = 3 if (shape and shape.get("three_step")) else (2 if (shape and shape.get("two_step")) else 1)
+    wide = bool(per == 3 and shape.get("wide_strips"))
     launches = K * launches_of(inner, per)
     value = world * L * L * inner * K / (ms / 1e3) / 1e6
     launch_ms = ms / launches
@@ -404,15 +405,17 @@ def run_ours(args):
                          "no flush",
                    "launch_shape": None if shape is None else {"block_threads": shape["block_threads"],
                                                                "streaming_stores": shape["streaming_stores"],
-                                                               "steps_per_launch": per}},
+                                                               "steps_per_launch": per, "wide_strips": wide}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
-                     "traffic": ncu_traffic(L, {1: args.precision, 2: "fp32_x2", 3: "fp32_x3"}[per])
+                     "traffic": ncu_traffic(L, "fp32_x3a" if wide else
+                                            {1: args.precision, 2: "fp32_x2", 3: "fp32_x3"}[per])
                      if args.op == "erlbm" else None,
                      "algorithmic_bytes_per_launch": algo_bytes, "launch_us": launch_ms * 1e3,
                      "lattice_updates_per_launch": L * L * per,
-                     "kernel": {1: f"k_periodic_d2q9<{op}>", 2: f"k_periodic_d2q9_x2s<{op}>",
-                                3: f"k_periodic_d2q9_x3s<{op}>"}[per]
+                     "kernel": (f"k_periodic_d2q9_x3a<{op}>" if wide else
+                                {1: f"k_periodic_d2q9<{op}>", 2: f"k_periodic_d2q9_x2s<{op}>",
+                                 3: f"k_periodic_d2q9_x3s<{op}>"}[per])
                      if args.precision == "fp32" else f"k_step<PrecExact64,9,{op}>",
                      # the update rate against the roofline of one step per launch, where every
                      # update reads and writes each population once (2 Q sizeof(real) bytes): the

@@ -605,7 +605,7 @@ int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc)
     const bool plain = h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && b.inlet_x < 0 && b.outlet_x < 0 &&
                        b.open_y < 0 && periodic_d2q9_fp32_ok(h->g);
     const bool fused3 = plain && h->three_step && periodic_d2q9_x2_ok(h->g) &&
-                        (!h->wide_strips || periodic_d2q9_x3p_ok(h->g));
+                        (!h->wide_strips || periodic_d2q9_x3a_ok(h->g));
     const bool fused2 = plain && h->two_step && periodic_d2q9_x2_ok(h->g);
     const int per_launch = fused3 ? 3 : (fused2 ? 2 : 1);
     for (int s = 0; s < n_steps;) {

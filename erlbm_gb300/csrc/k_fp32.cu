@@ -7,8 +7,8 @@
 // lane; it comes from the adjacent lane by a warp shuffle, and only the two warp-edge lanes
 // issue an extra 4-byte load (an L2 hit: the neighbouring warp reads that line too).
 // Algorithmic traffic is 2 * 9 * 4 = 72 bytes per lattice update.  The two- and three-step kernels
-// (k_periodic_d2q9_x2s, k_periodic_d2q9_x3s) advance every node by two or three steps per launch in
-// independent warp strips: 36 and 24 bytes per lattice update.
+// (k_periodic_d2q9_x2s, k_periodic_d2q9_x3s, and k_periodic_d2q9_x3a over column pairs) advance every
+// node by two or three steps per launch in independent warp strips: 36 and 24 bytes per lattice update.
 #include <atomic>
 
 #include "lattice_kernels.cuh"
@@ -465,23 +465,20 @@ __global__ void __launch_bounds__(128, 4) k_periodic_d2q9_x3s(const float *__res
 }
 
 
-// Three steps per launch over column pairs.  Lane l holds the columns xs - 2 + 2l and xs - 1 + 2l of a
-// 64-column strip as the two halves of a float2, so each packed FP32x2 operation of the collision
-// works on two neighbouring nodes of one row and every operand pair is formed where it is produced.
-// The strip walks down its chunk one row per iteration:
-//   - the first stage P' is valid in all 64 columns (lane 0 loads column xs - 3 and lane 31 column
-//     xs + 62 for the three populations that cross the strip's edges), P'' in columns 1 .. 62, the
-//     output in columns 2 .. 61: 60 output columns per 64 (the x3s strips: 28 per 32);
-//   - the x pull of a direction with c_x = +1 takes the left half from the lane below (one shuffle)
-//     and the right half from the lane's own left half, and the reverse for c_x = -1;
+// Three steps per launch over column pairs (k_periodic_d2q9_x3a).  Lane l holds the columns xs - 2 + 2l
+// and xs - 1 + 2l of a 64-column strip as the two halves of a float2, so each packed FP32x2 operation
+// of the collision works on two neighbouring nodes of one row and every operand pair is formed where it
+// is produced.  The strip walks down its chunk one row per iteration:
+//   - the first stage P' is valid in all 64 columns, P'' in columns 1 .. 62, the output in columns
+//     2 .. 61: 60 output columns per 64 (the x3s strips: 28 per 32);
+//   - the x pull of a collided row's direction with c_x = +1 takes the left half from the lane below
+//     (one shuffle) and the right half from the lane's own left half, and the reverse for c_x = -1;
 //   - the y pull of row r takes the c_y = +1 group (3, 5, 8) from row r - 1, the c_y = 0 group (0, 1,
 //     2) from row r and the c_y = -1 group (4, 6, 7) from row r + 1.
-// The first stage pulls straight from memory: for P' row j + 2 it loads the c_y = +1 group of P row
-// j + 1, the c_y = 0 group of row j + 2 and the c_y = -1 group of row j + 3 (one iteration ahead), so
-// every input population is still read once.  The two later stages carry the c_y = +1 groups of
-// their two newest input rows and the c_y = 0 group of the newest one in registers; the groups of a
-// row stay in the register slot they arrive in (three slots per group, used in turn), so the loop
-// body is unrolled three times and no group is copied between iterations.  Per iteration P' row j + 2, P'' row j + 1 and output row j are collided; the
+// The two later stages carry the c_y = +1 groups of their two newest input rows and the c_y = 0 group
+// of the newest one in registers; the groups of a row stay in the register slot they arrive in (three
+// slots per group, used in turn), so the loop body is unrolled three times and no group is copied
+// between iterations.  Per iteration P' row j + 2, P'' row j + 1 and output row j are collided; the
 // first four iterations of a chunk are its prologue, in which only the stages whose inputs exist run.
 // Bit-identical to three one-step launches: every node is collided by collide9x2 as by collide9.
 constexpr int XP_W = 60;   // output columns per strip
@@ -492,144 +489,15 @@ struct IntC {
     static constexpr int value = I;
 };
 
-template <int OP, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_periodic_d2q9_x3p(const float *__restrict__ src, float *__restrict__ dst,
-                                                                int nx, int ny, long long plane, int hc, int strips,
-                                                                int n_warps, shifted::Coef k)
-{
-    const int lane = threadIdx.x & 31;
-    const int wid = (int)blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
-    if (wid >= n_warps) return;  // the whole warp leaves together
-    const int xs = (wid % strips) * XP_W;
-    const int y0 = (wid / strips) * hc;
-    const int y1 = min(y0 + hc, ny);
-    int c = xs - 2 + 2 * lane;  // even, in [-2, nx + 60]
-    const bool store = lane >= 1 && lane <= 30 && c < nx;
-    c = c < 0 ? c + nx : (c >= nx ? c - nx : c);
-    // lane 0 pulls populations 1 (c_y = 0), 5 (c_y = +1), 7 (c_y = -1) across the left edge from column
-    // xs - 3; lane 31 pulls 2 (c_y = 0), 6 (c_y = -1), 8 (c_y = +1) across the right edge from xs + 62
-    const bool halo = lane == 0 || lane == 31;
-    int hcol = lane == 0 ? xs - 3 : xs + 62;
-    hcol = hcol < 0 ? hcol + nx : (hcol >= nx ? hcol - nx : hcol);
-    const int hp0 = lane == 0 ? 1 : 2, hp1 = lane == 0 ? 5 : 6, hp2 = lane == 0 ? 7 : 8;
-    const int hd1 = lane == 0 ? -1 : 1, hd2 = lane == 0 ? 1 : -1;  // row offsets of halo 1, 2 from c_y = 0's
-
-    auto wrap = [&](int r) { return r < 0 ? r + ny : (r >= ny ? r - ny : r); };
-    // P' row r's inputs: groups c_y = +1 of P row r - 1, c_y = 0 of row r, c_y = -1 of row r + 1
-    float2 ld[9];
-    float hv[3] = {0.f, 0.f, 0.f};
-    auto load = [&](int r) {
-        const float *pm = src + (long long)wrap(r - 1) * nx + c;
-        const float *pz = src + (long long)wrap(r) * nx + c;
-        const float *pp = src + (long long)wrap(r + 1) * nx + c;
-        ld[3] = __ldg(reinterpret_cast<const float2 *>(pm + 3 * plane));
-        ld[5] = __ldg(reinterpret_cast<const float2 *>(pm + 5 * plane));
-        ld[8] = __ldg(reinterpret_cast<const float2 *>(pm + 8 * plane));
-        ld[0] = __ldg(reinterpret_cast<const float2 *>(pz + 0 * plane));
-        ld[1] = __ldg(reinterpret_cast<const float2 *>(pz + 1 * plane));
-        ld[2] = __ldg(reinterpret_cast<const float2 *>(pz + 2 * plane));
-        ld[4] = __ldg(reinterpret_cast<const float2 *>(pp + 4 * plane));
-        ld[6] = __ldg(reinterpret_cast<const float2 *>(pp + 6 * plane));
-        ld[7] = __ldg(reinterpret_cast<const float2 *>(pp + 7 * plane));
-        if (halo) {
-            hv[0] = __ldg(src + (long long)wrap(r) * nx + hcol + hp0 * plane);
-            hv[1] = __ldg(src + (long long)wrap(r + hd1) * nx + hcol + hp1 * plane);
-            hv[2] = __ldg(src + (long long)wrap(r + hd2) * nx + hcol + hp2 * plane);
-        }
-    };
-    // x pulls: c_x = +1 takes column 2l - 1 (the lane below's right half) and 2l (own left half)
-    auto pull_p = [&](float2 v) { return make_float2(__shfl_up_sync(XS_FULL, v.y, 1), v.x); };
-    auto pull_m = [&](float2 v) { return make_float2(v.y, __shfl_down_sync(XS_FULL, v.x, 1)); };
-    auto pull_p_halo = [&](float2 v, float h) {
-        const float u = __shfl_up_sync(XS_FULL, v.y, 1);
-        return make_float2(lane == 0 ? h : u, v.x);
-    };
-    auto pull_m_halo = [&](float2 v, float h) {
-        const float u = __shfl_down_sync(XS_FULL, v.x, 1);
-        return make_float2(v.y, lane == 31 ? h : u);
-    };
-
-    // carried groups of stages 1 and 2 (index 0, 1): s1[.][slot] c_y = +1 (3, 5, 8), s0[.][slot] c_y = 0 (0, 1, 2)
-    float2 s1[2][3][3], s0[2][3][3];
-    float2 g[9], nm[3];
-
-    // one iteration at rotation phase T: stage 0, 1, 2 collide P' row j + 2, P'' row j + 1 and output
-    // row j where C1, C2 say their inputs exist (stage 0 always runs)
-    auto step = [&](auto T, auto C1, auto C2, int j) {
-        // slots: the newest input row's groups go to n, the previous row's are in b, the one before in a
-        constexpr int t = decltype(T)::value % 3;
-        constexpr int a = t, b = (t + 1) % 3, n = (t + 2) % 3;
-        constexpr bool c1 = decltype(C1)::value, c2 = decltype(C2)::value;
-        g[3] = ld[3];
-        g[5] = pull_p_halo(ld[5], hv[1]);
-        g[8] = pull_m_halo(ld[8], hv[2]);
-        g[0] = ld[0];
-        g[1] = pull_p_halo(ld[1], hv[0]);
-        g[2] = pull_m_halo(ld[2], hv[0]);
-        g[4] = ld[4];
-        g[6] = pull_m_halo(ld[6], hv[1]);
-        g[7] = pull_p_halo(ld[7], hv[2]);
-        load(j + 3);  // the inputs of the next iteration's P' row
-#pragma unroll
-        for (int s = 0; s < 3; s++) {
-            if (s == 1 && !c1) break;
-            if (s == 2 && !c2) break;
-            if (s > 0) {
-                g[3] = s1[s - 1][a][0];
-                g[5] = s1[s - 1][a][1];
-                g[8] = s1[s - 1][a][2];
-                g[0] = s0[s - 1][b][0];
-                g[1] = s0[s - 1][b][1];
-                g[2] = s0[s - 1][b][2];
-                g[4] = nm[0];
-                g[6] = nm[1];
-                g[7] = nm[2];
-            }
-            shifted::collide9x2<OP>(g, k);
-            if (s == 2) {
-                if (store && j < y1) {
-                    float *d = dst + (long long)j * nx + c;
-#pragma unroll
-                    for (int i = 0; i < 9; i++) *reinterpret_cast<float2 *>(d + i * plane) = g[i];
-                }
-            } else {  // the collided row is the next stage's newest input row
-                s1[s][n][0] = g[3];
-                s1[s][n][1] = pull_p(g[5]);
-                s1[s][n][2] = pull_m(g[8]);
-                s0[s][n][0] = g[0];
-                s0[s][n][1] = pull_p(g[1]);
-                s0[s][n][2] = pull_m(g[2]);
-                nm[0] = g[4];
-                nm[1] = pull_m(g[6]);
-                nm[2] = pull_p(g[7]);
-            }
-        }
-    };
-    using F = IntC<0>;
-    using N = IntC<1>;
-    // prologue: P' rows y0 - 2 .. y0 + 1, P'' rows y0 - 1, y0 (phases 2, 0, 1, 2, so the loop starts at 0)
-    load(y0 - 2);
-    step(IntC<2>{}, F{}, F{}, y0 - 4);
-    step(IntC<0>{}, F{}, F{}, y0 - 3);
-    step(IntC<1>{}, N{}, F{}, y0 - 2);
-    step(IntC<2>{}, N{}, F{}, y0 - 1);
-    for (int j = y0; j < y1; j += XP_SPAN) {
-        step(IntC<0>{}, N{}, N{}, j);
-        step(IntC<1>{}, N{}, N{}, j + 1);
-        step(IntC<2>{}, N{}, N{}, j + 2);
-    }
-}
-
-
-// The column-pair kernel with its first-stage inputs brought in ahead by asynchronous copies into a
-// per-warp ring of shared memory (XA_DEPTH slots) instead of registers.  A slot holds, for each of the
+// Its first-stage inputs are brought in ahead by asynchronous copies into a per-warp ring of shared
+// memory (XA_DEPTH slots), not into registers, which keeps the kernel at 122 registers (16 warps per
+// SM) and two rows of loads in flight.  A slot holds, for each of the
 // nine populations, the 68 columns xs - 4 .. xs + 63 of the input row its c_y group comes from (c_y =
 // +1: row r - 1, 0: row r, -1: row r + 1 for P' row r), as 153 aligned 16-byte pieces spread over the
 // lanes.  The x pull is then a shifted shared-memory read: a lane's nodes sit at slot columns 2l + 2,
 // 2l + 3; c_x = +1 populations are read at 2l + 1, 2l + 2 and c_x = -1 ones at 2l + 3, 2l + 4, which
 // also covers the strip's edge columns, so the first stage needs no shuffle, select or edge load.  The
-// copies for P' row r + 2 are issued while row r is collided.  Everything after the first stage is the
-// x3p kernel's.
+// copies for P' row r + 2 are issued while row r is collided.
 constexpr int XA_DEPTH = 3;                // ring slots (two rows of copies in flight)
 constexpr int XA_ROW = 68;                 // columns per population row in a slot
 constexpr int XA_SLOT = 9 * XA_ROW;        // floats per slot
@@ -844,55 +712,14 @@ static void go_x3(const Geo &g, const shifted::Coef &k, const float *src, float 
     kern<<<(unsigned)((n_warps + 3) / 4), 128, 0, s>>>(src, dst, g.nx, g.ny, g.plane, (int)hc, strips, n_warps, k);
 }
 
-// Three-step launch over column pairs: ceil(nx / 60) strips, chunks of a multiple of six rows, as many
+// Three-step launch over column pairs: ceil(nx / 60) strips, chunks of whole unrolled groups, as many
 // chunks per strip as one wave of resident warps holds (no second, partial wave).
-// resident 128-thread CTAs per SM (the register cap follows from it); a build option for tuning
-#ifndef ERLBM_XP_MINB
-#define ERLBM_XP_MINB 3
-#endif
-constexpr int XP_MINB = ERLBM_XP_MINB;
-
-template <int OP>
-static void go_x3p(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
-{
-    auto kern = k_periodic_d2q9_x3p<OP, XP_MINB>;
-    constexpr int MAXDEV = 64;
-    static std::atomic<int> warps_cache[MAXDEV];
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const int d = dev >= 0 && dev < MAXDEV ? dev : 0;
-    int resident = warps_cache[d].load(std::memory_order_relaxed);
-    if (resident <= 0) {
-        int o = 0, n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, 128, 0) != cudaSuccess || o < 1) o = 1;
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        resident = o * 4 * (n > 0 ? n : 1);
-        warps_cache[d].store(resident, std::memory_order_relaxed);
-    }
-    const int strips = (g.nx + XP_W - 1) / XP_W;
-    long long chunks = resident / strips;
-    if (chunks < 1) chunks = 1;
-    long long hc = (g.ny + chunks - 1) / chunks;
-    hc = (hc + XP_SPAN - 1) / XP_SPAN * XP_SPAN;
-    if (hc < 2 * XP_SPAN) hc = 2 * XP_SPAN;  // the prologue's six rows are not worth a shorter chunk
-    const int n_warps = strips * (int)((g.ny + hc - 1) / hc);
-    kern<<<(unsigned)((n_warps + 3) / 4), 128, 0, s>>>(src, dst, g.nx, g.ny, g.plane, (int)hc, strips, n_warps, k);
-}
-
-// The wide three-step launch: the asynchronous-copy kernel (default; its offsets are 32-bit) or the
-// register-prefetch one (ERLBM_XP_ASYNC=0 at build time).
-#ifndef ERLBM_XP_ASYNC
-#define ERLBM_XP_ASYNC 1
-#endif
-// resident 128-thread CTAs per SM of the asynchronous-copy kernel (its register cap follows from it)
-#ifndef ERLBM_XA_MINB
-#define ERLBM_XA_MINB 4
-#endif
+constexpr int XA_MINB = 4;  // resident 128-thread CTAs per SM (122 registers, no spills)
 
 template <int OP>
 static void go_x3a(const Geo &g, const shifted::Coef &k, const float *src, float *dst, cudaStream_t s)
 {
-    auto kern = k_periodic_d2q9_x3a<OP, ERLBM_XA_MINB>;
+    auto kern = k_periodic_d2q9_x3a<OP, XA_MINB>;
     const size_t smem = 4 * XA_SMEM_PER_WARP;
     constexpr int MAXDEV = 64;
     static std::atomic<int> warps_cache[MAXDEV];
@@ -918,35 +745,25 @@ static void go_x3a(const Geo &g, const shifted::Coef &k, const float *src, float
                                                          k);
 }
 
-bool periodic_d2q9_x3p_ok(const Geo &g)
+bool periodic_d2q9_x3a_ok(const Geo &g)
 {
-    // 64-column strips need ny >= 16; the asynchronous form addresses the nine planes with 32-bit offsets
-    return periodic_d2q9_fp32_ok(g) && g.ny >= 16 && g.nx >= 128 && (!ERLBM_XP_ASYNC || 9 * g.plane < (1LL << 31));
+    // 64-column strips need ny >= 16; the nine planes are addressed with 32-bit offsets
+    return periodic_d2q9_fp32_ok(g) && g.ny >= 16 && g.nx >= 128 && 9 * g.plane < (1LL << 31);
 }
 
 // Three steps of the fused periodic D2Q9 FP32 update in one launch (periodic_d2q9_x2_ok(g) required;
-// wide = the column-pair kernel, which needs periodic_d2q9_x3p_ok(g)).
+// wide = the column-pair kernel, which needs periodic_d2q9_x3a_ok(g)).
 int launch_periodic_d2q9_fp32_x3(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s,
                                  bool wide)
 {
-    if (!periodic_d2q9_x2_ok(g) || (wide && !periodic_d2q9_x3p_ok(g))) return -1;
+    if (!periodic_d2q9_x2_ok(g) || (wide && !periodic_d2q9_x3a_ok(g))) return -1;
     const shifted::Coef k = shifted::make_coef(R);
-    if (wide && ERLBM_XP_ASYNC) {
+    if (wide) {
         switch (op) {
         case OP_BGK: go_x3a<OP_BGK>(g, k, src, dst, s); break;
         case OP_MRT: go_x3a<OP_MRT>(g, k, src, dst, s); break;
         case OP_REG: go_x3a<OP_REG>(g, k, src, dst, s); break;
         case OP_EXTREG: go_x3a<OP_EXTREG>(g, k, src, dst, s); break;
-        default: return -1;
-        }
-        return cudaGetLastError() == cudaSuccess ? 0 : -3;
-    }
-    if (wide) {
-        switch (op) {
-        case OP_BGK: go_x3p<OP_BGK>(g, k, src, dst, s); break;
-        case OP_MRT: go_x3p<OP_MRT>(g, k, src, dst, s); break;
-        case OP_REG: go_x3p<OP_REG>(g, k, src, dst, s); break;
-        case OP_EXTREG: go_x3p<OP_EXTREG>(g, k, src, dst, s); break;
         default: return -1;
         }
         return cudaGetLastError() == cudaSuccess ? 0 : -3;

@@ -62,10 +62,10 @@ bool periodic_d2q9_fp32_ok(const Geo &g);
 int launch_periodic_d2q9_fp32_x2(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s);
 bool periodic_d2q9_x2_ok(const Geo &g);
 // Three steps per launch: 32-column warp strips (wide = false) or 64-column strips over column pairs
-// (wide = true, also needs periodic_d2q9_x3p_ok: ny >= 16).
+// (wide = true, also needs periodic_d2q9_x3a_ok: ny >= 16, nine planes within 32-bit offsets).
 int launch_periodic_d2q9_fp32_x3(int op, const Geo &g, const Relax &R, const float *src, float *dst, cudaStream_t s,
                                  bool wide);
-bool periodic_d2q9_x3p_ok(const Geo &g);
+bool periodic_d2q9_x3a_ok(const Geo &g);
 
 // Stream only: dst = post-stream populations of the post-collision state src (no BC, no collision).
 int launch_stream_only_fp64(int q, const Geo &g, const double *src, double *dst, cudaStream_t s);

@@ -180,7 +180,8 @@ int erlbm_fp64_rate(double *ops_per_s);
  *   ERLBM_LAUNCH_THREE_STEP        three steps per launch (same conditions): a third of the traffic;
  *   ERLBM_LAUNCH_WIDE_STRIPS       with ERLBM_LAUNCH_THREE_STEP: 64-column warp strips in which a lane
  *                                  holds two neighbouring columns (60 outputs per 64 columns instead
- *                                  of 28 per 32; ny >= 16).
+ *                                  of 28 per 32; ny >= 16 and 9 nx ny < 2^31, else one step per
+ *                                  launch).
  * The results are the same bits in every shape; at most one of the two multi-step flags.  Steps left
  * over (fewer than a launch takes) run one at a time.  Chosen by erlbm_gb300.autotune; no
  * counterpart in the reference. */
