@@ -26,8 +26,9 @@ Multi-GPU: one lattice does not shard, so N GPUs run N independent replicas (wea
 
 Other workloads (--workload; the default is the one above):
   tg-map, obstacle-map   stability maps (main_stability-map_*.cpp) on an evenly spaced P x P subset
-                         of the 400 x 400 grid; one bench step = one batched map launch; runs/s.
-                         The Taylor-Green map runs every point with RLBM and with E-RLBM.
+                         of the 400 x 400 grid; one bench step = one batched map launch per GPU; runs/s.
+                         The Taylor-Green map runs every point with RLBM and with E-RLBM.  Under
+                         torchrun the points are sharded over the ranks (weak in GPUs, strong in points).
   serve                  a seeded Poisson stream of mixed requests (Taylor-Green D2Q9 L = 32..512,
                          map points, obstacle channels scaled 1-4x, 3-D Taylor-Green 32^3 / 64^3;
                          FP32 or FP64; budgets 1..10000 steps) through the request server; runs/s
@@ -529,12 +530,27 @@ def map_points(P):
 
 
 def run_map(args):
+    """Map points are independent runs: under torchrun each rank (one GPU) runs a strided share of the
+    points and the labels are gathered (erlbm_gb300.sharding.map_run_sharded); `value` is the runs of all
+    ranks over the slowest rank's time."""
     import numpy as np
     import torch
     import erlbm_gb300 as E
-    torch.cuda.set_device(0)
+    from erlbm_gb300.sharding import map_run_sharded
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
     kind = E.MAP_TAYLOR_GREEN if args.workload == "tg-map" else E.MAP_OBSTACLE
     refined = args.precision == "refined"
+    if refined and world > 1:
+        raise SystemExit("the refined map's FP64 passes follow label changes across the whole grid; it runs on one GPU")
     prec = E.FP64 if args.precision == "fp64" else E.FP32_SHIFTED
     pts = map_points(args.map_points)
     P = args.map_points
@@ -544,7 +560,7 @@ def run_map(args):
             lab, dec, _, ref, passes = E.map_run_refined(kind, op=op, n_i=P, n_j=P, max_steps=args.max_steps,
                                                          slots=-1, return_passes=True)
             return lab, dec, int(ref.sum()), passes
-        lab, dec, _ = E.map_run(kind, points, precision=prec, op=op, max_steps=args.max_steps, slots=-1)
+        lab, dec, _ = map_run_sharded(kind, points, precision=prec, op=op, max_steps=args.max_steps, slots=-1)
         return lab, dec, 0, 0
 
     op = 0 if kind == E.MAP_TAYLOR_GREEN else E.OP_EXTREG
@@ -556,7 +572,9 @@ def run_map(args):
     if refined:
         autotune.tune_map(kind, E.FP64)
     torch.cuda.synchronize()
-    clocks = Clocks(0)
+    if dist:
+        dist.barrier()
+    clocks = Clocks(torch.cuda.current_device())
     clocks.start()
     t0 = time.perf_counter()
     runs, lus, n_ref, n_pass = 0, 0, 0, 0
@@ -566,17 +584,26 @@ def run_map(args):
         n_ref += nr
         n_pass += npass
         lus += int(np.sum(dec.astype(np.int64))) * nodes
+    torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     clk = clocks.stop()
-    value = runs / dt
-    line = {"metric": "map runs/s", "value": value, "unit": "runs/s", "n_gpus": 1, "steps": args.steps,
+    if dist:
+        t = torch.tensor([dt], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dt = float(t.item())
+        dist.destroy_process_group()
+        if rank != 0:
+            return 0
+    value = runs / dt  # the gathered label arrays hold every rank's runs
+    line = {"metric": "map runs/s", "value": value, "unit": "runs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if refined else ("f32" if prec else "f64"),
             "data": "synthetic (the reference's map axes)",
             "config": {"workload": f"{args.workload} D3Q19, "
                                    + (f"whole {P}x{P} grid" if refined else f"{P}x{P} points of the 400x400 grid")
                                    + f"{' x {RLBM, E-RLBM}' if op == 0 else ''}, max_steps={args.max_steps}",
-                       "precision": args.precision, "slots_per_sm": tuned["slots"]},
+                       "precision": args.precision, "slots_per_sm": tuned["slots"],
+                       "parallelism": f"points sharded over {world} GPU(s), labels gathered"},
             "lattice_updates_per_s": lus / dt, "roofline": None,
             "e2e": {"value": value, "unit": "runs/s", "h2d_bytes_per_step": len(pts) * 48,
                     "d2h_bytes_per_step": len(pts) * 32},
@@ -584,7 +611,7 @@ def run_map(args):
     if refined:
         line["refined_fraction"] = n_ref / runs
         line["fp64_passes_per_map"] = n_pass / args.steps
-    if not args.no_cpu:
+    if not args.no_cpu and world == 1:
         from oracle import oracle as O
         few = pts[:: max(1, len(pts) // 16)]
         t = time.perf_counter()

@@ -88,17 +88,23 @@ def _gloo_worker(rank, world, port, out):
     import torch.distributed as dist
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    from erlbm_gb300.sharding import run_sharded
+    from erlbm_gb300.sharding import map_run_sharded
     pts = [(i, j) for i in range(0, 400, 57) for j in range(0, 400, 91)]
 
-    def runner(mine):  # the oracle stands in for this rank's GPU map run
-        lab, dec, mg = O.tg_map(mine, op=O.OP_EXTREG, tau_nh=0.65, max_steps=1500, threads=1)
-        return lab, dec, mg
+    def oracle_map(kind, points, op, tau_nh, max_steps):
+        """The oracle in map_run's place (no GPU here): same call, same result layout (op = 0: all RLBM
+        results, then all E-RLBM results)."""
+        ops = [O.OP_REG, O.OP_EXTREG] if op == 0 else [op]
+        res = [O.tg_map(points, op=o, tau_nh=tau_nh if o == O.OP_EXTREG else 1.0, max_steps=max_steps, threads=1)
+               for o in ops]
+        return tuple(np.concatenate([r[k] for r in res]) for k in range(3))
 
-    lab, dec, mg = run_sharded(pts, runner)
+    # the same call bench.py makes on each GPU rank, with the oracle as the map
+    lab, dec, mg = map_run_sharded(1, pts, map_fn=oracle_map, op=0, tau_nh=0.65, max_steps=1500)
     if rank == 0:
-        ref = O.tg_map(pts, op=O.OP_EXTREG, tau_nh=0.65, max_steps=1500, threads=1)
-        out.put((np.array_equal(lab, ref[0]), np.array_equal(dec, ref[1]), np.array_equal(mg, ref[2])))
+        ref = oracle_map(1, pts, 0, 0.65, 1500)
+        out.put((np.array_equal(lab, ref[0]) and lab.dtype == ref[0].dtype, np.array_equal(dec, ref[1]),
+                 np.array_equal(mg, ref[2])))
     dist.barrier()
     dist.destroy_process_group()
 

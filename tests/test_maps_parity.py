@@ -93,3 +93,16 @@ def test_batch_run_aos_init_matches_lattice_runs():
         lat2.set(blocks[k])
         lat2.step(last)
         assert res[k]["energy"] == (lat2.kinetic_energy(0) if last > 0 else e0)
+
+
+def test_sharded_map_world1_equals_map_run():
+    """map_run_sharded, the multi-GPU map of bench.py, in a one-rank run: the same labels, decided
+    steps and margins as map_run on the same points, both operators of the Taylor-Green map."""
+    import erlbm_gb300 as m
+    from erlbm_gb300.sharding import map_run_sharded
+    pts = [(i, j) for i in range(0, 400, 53) for j in range(0, 400, 67)]
+    for kind, op in ((m.MAP_TAYLOR_GREEN, 0), (m.MAP_OBSTACLE, m.OP_EXTREG)):
+        a = m.map_run(kind, pts, precision=m.FP64, op=op, max_steps=1200)
+        b = map_run_sharded(kind, pts, precision=m.FP64, op=op, max_steps=1200)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)

@@ -164,3 +164,56 @@ def test_large_2d_lattice_through_the_stream_lane():
     lat.step(3)
     want = lat.kinetic_energy(0)
     assert abs(r["energy"] - want) <= 1e-12 * want
+
+
+def tg3d_init(L, u0):
+    """The server's 3-D Taylor-Green initial state restated on the host: rho = 1,
+    u = u0 (sin kx cos ky cos kz, -cos kx sin ky cos kz, 0), dist_eq at every node (x fastest)."""
+    x = np.arange(L, dtype=np.float64)
+    s, c = np.sin(2. * np.pi * x / L), np.cos(2. * np.pi * x / L)
+    f = np.empty((L, L, L, 19))
+    for z in range(L):
+        for y in range(L):
+            for xx in range(L):
+                ux = u0 * s[xx] * c[y] * c[z]
+                uy = -u0 * c[xx] * s[y] * c[z]
+                f[z, y, xx] = O.equilibrium(19, ux, uy, 0.0, 1.0)
+    return f.reshape(-1)
+
+
+@pytest.mark.parametrize("L,steps,exact", [(32, 40, True), (64, 6, False)])
+def test_tg3d_requests_match_oracle(L, steps, exact):
+    """Config-5 3-D Taylor-Green requests (D3Q19, L^3, FP64) through the server's stream lane: the
+    kinetic energy after the run equals the oracle's.  Up to 65536 nodes the device sums the energy
+    serially in node order, as kinectic_energy does, so L = 32 matches bit for bit; L = 64 is a tree
+    reduction, which agrees to the last digits only."""
+    m = E()
+    tau, tnh, u0 = 0.55, 0.65, 0.05
+    with m.Server(hbm_budget_bytes=1 << 30) as srv:
+        r = srv.wait(srv.submit(m.REQ_TG3D, m.FP64, op=m.OP_EXTREG, L=L, tau=tau, tau_nh=tnh, u0=u0, n_steps=steps),
+                     timeout=600)
+    assert r["status"] == 0 and r["steps_done"] == steps and r["lane"] == 1
+    lat = O.Lattice(19, L, L, L, None, tau, tnh, O.OP_EXTREG)
+    lat.set(tg3d_init(L, u0))
+    lat.step(steps)
+    want = lat.kinetic_energy(0)
+    if exact:
+        assert r["energy"] == want
+    else:
+        assert abs(r["energy"] - want) <= 1e-12 * want
+
+
+@pytest.mark.parametrize("scale", [3, 4])
+def test_scaled_obstacle_requests_match_oracle(scale):
+    """Config-5 obstacle channels scaled 3x and 4x in each dimension (FP64, Zou-He inlet, density
+    outlet, bounce-back, density checks every step): label, decided step and margin equal the oracle's
+    roda_ponto on the same geometry, for a stable and an unstable point."""
+    m = E()
+    with m.Server(hbm_budget_bytes=1 << 30) as srv:
+        for i, j, n in ((200, 399, 700), (10, 0, 700)):
+            u, tau, tnh = m.obstacle_map_params(i, j)
+            r = srv.wait(srv.submit(m.REQ_OBSTACLE, m.FP64, sx=scale, sy=scale, tau=tau, tau_nh=tnh, u0=u,
+                                    n_steps=n), timeout=600)
+            lab, dec, mg = O.obstacle_map_point(tau, tnh, u, sx=scale, sy=scale, max_steps=n)
+            assert r["status"] == 0
+            assert (r["label"], r["decided_step"], r["margin"]) == (lab, dec, mg), (i, j, r, lab, dec, mg)
