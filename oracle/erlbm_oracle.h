@@ -99,6 +99,15 @@ int orc32_channel(int q, int nx, int ny, int nz, const uint8_t *solid, int op, d
                   int inlet_x, double u_in, int outlet_x, int outlet_kind, double rho_out, int open_y,
                   const double *f_in, int n_steps, double *f_out);
 
+/* one run of the engine's batched FP32 map kernel restated (fp32_shifted.c): a block of `block` threads
+ * with npt nodes each; init 0 = rest state w rho0, 1 = the Taylor-Green map equilibrium with amplitude u0
+ * (u0 is also the Zou-He inlet velocity); out4 = label, decided step, steps done, status; out2 = margin,
+ * energy */
+int orc32_batch_run(int q, int nx, int ny, const uint8_t *solid, int inlet_x, int outlet_x, double rho0,
+                    int energy_every, double energy_factor, int density_check, double density_limit, int init,
+                    int op, double tau, double tau_nh, double u0, int n_steps, int block, int npt, int *out4,
+                    double *out2);
+
 #ifdef __cplusplus
 }
 #endif

@@ -508,3 +508,249 @@ int orc32_channel(int q, int nx, int ny, int nz, const uint8_t *solid, int op, d
     pl.vx6 = u_in / 6.0;
     return run_periodic(q, nx, ny, nz, solid, &pl, op, tau, tau_nh, f_in, n_steps, f_out);
 }
+
+/* ------------------------------------------------------------------------------------------------
+ * One run of the engine's batched FP32 map kernel (k_batch over PrecShifted32; a D3Q19 or D2Q9 lattice
+ * of nx x ny x 1 nodes held by one CTA of `block` threads with `npt` nodes each), restated with every
+ * operation of the kernel in the kernel's order, so that label, decided step, steps done, status,
+ * margin and energy agree bit for bit:
+ *   - thread slots: the fluid nodes in node order, the boundary-plane nodes first; thread t holds
+ *     slots t, t + block, ..., t + (npt - 1) block;
+ *   - initial state: the Taylor-Green map's equilibrium formed in FP32 from the FP64 velocity
+ *     (init 1), or the rest state w rho0 (init 0);
+ *   - a step: pull (in place on the first step) with bounce-back and the outlet's copy of its inner
+ *     neighbour; the energy check on those post-stream populations when step > 0 and step % every == 0;
+ *     the inlet and outlet closures; the collision; the density check drho > hi or drho < lo (float
+ *     bounds equivalent to |1 + drho| > limit) or non-finite at any node, the step finished first;
+ *   - energy: per node (double)(0.5f |u|^2) from FP32 moments, summed per thread over its slots
+ *     (0.0 + ...), then across each warp by the xor butterfly (strides 16, 8, 4, 2, 1), then over the
+ *     warps in order;
+ *   - margin: max over checks of E / (factor E0) (+inf for a non-finite E), or max |1 + drho| / limit
+ *     over every node and step seen (+inf when a density was non-finite).
+ * ------------------------------------------------------------------------------------------------ */
+
+#define ORC32_PI 3.14159265358979323846 /* the value of M_PI, which strict C11 does not declare */
+
+static double node_energy32(const float *g, int q)
+{
+    float drho, mx, my, mz = 0.f;
+    if (q == 9) {
+        const float eX = g[1] + g[2], eY = g[3] + g[4], eP = g[5] + g[6], eM = g[7] + g[8];
+        const float oX = g[1] - g[2], oY = g[3] - g[4], oP = g[5] - g[6], oM = g[7] - g[8];
+        drho = g[0] + ((eX + eY) + (eP + eM));
+        mx = oX + (oP + oM);
+        my = oY + (oP - oM);
+    } else {
+        const float oX = g[1] - g[2], oY = g[3] - g[4], oZ = g[5] - g[6], oA = g[7] - g[8], oB = g[9] - g[10];
+        const float oC = g[11] - g[12], oD = g[13] - g[14], oE = g[16] - g[15], oF = g[17] - g[18];
+        const float e1 = (g[1] + g[2]) + (g[3] + g[4]), e2 = (g[5] + g[6]) + (g[7] + g[8]);
+        const float e3 = (g[9] + g[10]) + (g[11] + g[12]), e4 = (g[13] + g[14]) + (g[15] + g[16]);
+        drho = (g[0] + (e1 + e2)) + ((e3 + e4) + (g[17] + g[18]));
+        mx = (oX + (oA + oB)) + (oC + oD);
+        my = (oY + (oA - oB)) + (oE - oF);
+        mz = (oZ + (oC - oD)) + (oE + oF);
+    }
+    const float inv = 1.f / (1.f + drho);
+    const float ux = mx * inv, uy = my * inv, uz = mz * inv;
+    if (q == 9) return (double)(0.5f * fmaf(ux, ux, uy * uy));
+    return (double)(0.5f * fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
+}
+
+static float node_drho32(const float *g, int q)
+{
+    float s = 0.f;
+    for (int i = 0; i < q; i++) s += g[i];
+    return s;
+}
+
+/* the kernel's block sum: per-thread values v[0 .. block-1], xor butterfly per warp, warps in order */
+static double block_sum32(double *v, int block)
+{
+    double s = 0.0;
+    for (int w = 0; w < block / 32; w++) {
+        double *l = v + 32 * w;
+        for (int o = 16; o > 0; o >>= 1) {
+            double t[32];
+            for (int k = 0; k < 32; k++) t[k] = l[k] + l[k ^ o];
+            memcpy(l, t, sizeof(t));
+        }
+        s += l[0];
+    }
+    return s;
+}
+
+int orc32_batch_run(int q, int nx, int ny, const uint8_t *solid, int inlet_x, int outlet_x, double rho0,
+                    int energy_every, double energy_factor, int density_check, double density_limit, int init,
+                    int op, double tau, double tau_nh, double u0, int n_steps, int block, int npt, int *out4,
+                    double *out2)
+{
+    if ((q != 9 && q != 19) || nx < 1 || ny < 1 || block < 32 || block % 32 || npt < 1 || n_steps < 0) return -1;
+    if (op != ORC_OP_BGK && op != ORC_OP_REG && op != ORC_OP_EXTREG && !(op == ORC_OP_MRT && q == 9)) return -1;
+    if (inlet_x >= 0 && q != 19) return -1;
+    const int nb = nx * ny;
+    if (nb > block * npt) return -1;
+    float *a = malloc((size_t)nb * q * sizeof(float)), *b = malloc((size_t)nb * q * sizeof(float));
+    float *f = malloc((size_t)nb * q * sizeof(float));
+    int *order = malloc((size_t)nb * sizeof(int));
+    double *tv = malloc((size_t)block * sizeof(double));
+    if (!a || !b || !f || !order || !tv) {
+        free(a), free(b), free(f), free(order), free(tv);
+        return -2;
+    }
+    /* thread slots */
+    int n_fluid = 0;
+    for (int pass = 0; pass < 2; pass++)
+        for (int n = 0; n < nb; n++) {
+            if (solid && solid[n]) continue;
+            const int x = n % nx;
+            const int plane = x == inlet_x || x == outlet_x;
+            if (plane == (pass == 0)) order[n_fluid++] = n;
+        }
+    /* coefficients (as the host prepares a run) and the planes */
+    Coef32 k;
+    const double d1 = 2.0 - 1.0 / tau;
+    double nkc = 0.0;
+    k.d1 = (float)d1;
+    if (op == ORC_OP_BGK || op == ORC_OP_MRT) {
+        k.kd = 0.f;
+    } else if (op == ORC_OP_REG) {
+        k.kd = -1.f;
+        nkc = -1.0;
+    } else {
+        const double omega_gt1 = 1.0 - 1.0 / tau_nh;
+        k.kd = (float)(omega_gt1 - 1.0);
+        nkc = -(1.0 + omega_gt1);
+    }
+    k.nkc = (float)nkc;
+    k.kh = 0.5f * k.kd;
+    k.d1t = (float)(-2.0 / 3.0 * d1);
+    k.nkct = (float)(-2.0 / 3.0 * nkc);
+    Planes pl;
+    pl.inlet_x = inlet_x;
+    pl.outlet_x = outlet_x;
+    pl.outlet_kind = OUTLET_DENSITY;
+    pl.open_y = -1;
+    pl.u_in = u0;
+    pl.rho_out = rho0;
+    pl.inv_1mvx = 1.0 / (1.0 - u0);
+    pl.vx3 = u0 / 3.0;
+    pl.vx6 = u0 / 6.0;
+    const Planes *plp = (inlet_x >= 0 || outlet_x >= 0) ? &pl : NULL;
+    /* density bounds: |1 + (double)d| > limit  <=>  d > hi or d < lo for a float d */
+    const double hi = density_limit - 1.0, lo = -density_limit - 1.0;
+    float fh = (float)hi, fl = (float)lo;
+    if ((double)fh > hi) fh = nextafterf(fh, -INFINITY);
+    if ((double)fl < lo) fl = nextafterf(fl, INFINITY);
+    /* initial populations */
+    const double L = (double)nx;
+    for (int n = 0; n < nb; n++) {
+        float *g = &a[(size_t)n * q];
+        const int x = n % nx, y = n / nx;
+        for (int i = 0; i < q; i++) {
+            const double w = q == 9 ? w9(i) : w19(i);
+            if (init == 1) {
+                const double sx = sin(2. * ORC32_PI * (double)x / L), cx_ = cos(2. * ORC32_PI * (double)x / L);
+                const double sy = sin(2. * ORC32_PI * (double)y / L), cy_ = cos(2. * ORC32_PI * (double)y / L);
+                const float ux = (float)(u0 * sx * cy_), uy = (float)(-u0 * cx_ * sy);
+                const float mu = -1.5f * fmaf(ux, ux, uy * uy);
+                const int ci = q == 9 ? CX9[i] : CX19[i], cj = q == 9 ? CY9[i] : CY19[i];
+                const float cu = (float)ci * ux + (float)cj * uy;
+                g[i] = (float)w * fmaf(cu, fmaf(4.5f, cu, 3.f), mu);
+            } else {
+                g[i] = (float)(w * rho0 - w);
+            }
+        }
+    }
+    /* per-thread energy of a population set (f: every node's populations) */
+#define THREAD_ENERGY(POP)                                                                        \
+    do {                                                                                          \
+        for (int t = 0; t < block; t++) {                                                         \
+            double e = 0.0;                                                                       \
+            for (int s = 0; s < npt; s++) {                                                       \
+                const int slot = t + s * block;                                                   \
+                if (slot < n_fluid) e += node_energy32(&(POP)[(size_t)order[slot] * q], q);      \
+            }                                                                                     \
+            tv[t] = e;                                                                            \
+        }                                                                                         \
+    } while (0)
+    double E0 = 0.0, E = 0.0, margin = 0.0, max_rho = 0.0;
+    float dmax = -INFINITY, dmin = INFINITY;
+    int label = 0, decided = n_steps, status = 0, steps_done = n_steps;
+    if (energy_every > 0) {
+        THREAD_ENERGY(a);
+        E0 = block_sum32(tv, block);
+        E = E0;
+    }
+    for (int step = 0; step < n_steps; step++) {
+        /* post-stream populations (the outlet node holds its inner neighbour's) */
+        for (int n = 0; n < nb; n++) {
+            if (solid && solid[n]) continue;
+            const int x = n % nx, y = n / nx;
+            int xp = x;
+            if (x == outlet_x) xp = x + (outlet_x < nx / 2 ? 1 : -1);
+            pull_node(a, q, nx, ny, 1, solid, step == 0, xp, y, 0, &f[(size_t)n * q]);
+        }
+        if (energy_every > 0 && step > 0 && step % energy_every == 0) {
+            THREAD_ENERGY(f);
+            E = block_sum32(tv, block);
+            const double lim = energy_factor * E0;
+            const double rr = isfinite(E) ? E / lim : INFINITY;
+            margin = fmax(margin, rr);
+            if (E > lim || !isfinite(E)) {
+                label = 1;
+                decided = step;
+                steps_done = step;
+                status |= 4;
+                break;
+            }
+        }
+        int flag = 0;
+        for (int n = 0; n < nb; n++) {
+            if (solid && solid[n]) {
+                memcpy(&b[(size_t)n * q], &a[(size_t)n * q], (size_t)q * sizeof(float));
+                continue;
+            }
+            float g[19];
+            const int x = n % nx, y = n / nx;
+            after_planes(a, q, nx, ny, 1, solid, plp, step == 0, x, y, 0, g);
+            if (q == 9)
+                collide9_f32(g, &k, op);
+            else
+                collide19_f32(g, &k, op);
+            if (density_check) {
+                const float d = node_drho32(g, q);
+                if (!isfinite(d)) {
+                    flag |= 2;
+                } else {
+                    dmax = fmaxf(dmax, d);
+                    dmin = fminf(dmin, d);
+                    if (d > fh || d < fl) flag |= 1;
+                }
+            }
+            memcpy(&b[(size_t)n * q], g, (size_t)q * sizeof(float));
+        }
+        float *t = a;
+        a = b;
+        b = t;
+        if (density_check && flag) {
+            label = 1;
+            decided = step;
+            steps_done = step + 1;
+            status |= (flag & 2) ? 3 : 1;
+            break;
+        }
+    }
+#undef THREAD_ENERGY
+    if (density_check) {
+        if (dmax >= dmin) max_rho = fmax(fabs(1.0 + (double)dmax), fabs(1.0 + (double)dmin));
+        margin = (status & 2) ? INFINITY : max_rho / density_limit;
+    }
+    out4[0] = label;
+    out4[1] = decided;
+    out4[2] = steps_done;
+    out4[3] = status;
+    out2[0] = margin;
+    out2[1] = E;
+    free(a), free(b), free(f), free(order), free(tv);
+    return 0;
+}

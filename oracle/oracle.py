@@ -316,6 +316,27 @@ def fp32_channel(q, nx, ny, nz, solid, op, tau, tau_nh, f_in, n_steps, inlet_x=-
     return out
 
 
+def fp32_batch_run(q, nx, ny, op, tau, tau_nh, u0, n_steps, block, npt, solid=None, inlet_x=-1, outlet_x=-1,
+                   rho0=1.0, energy_every=0, energy_factor=2.0, density_check=False, density_limit=10.0, init=0):
+    """One run of the engine's batched FP32 map kernel restated bit for bit (orc32_batch_run): the CTA
+    shape (block threads, npt nodes each) fixes the energy sum's order.  Returns the result fields."""
+    fn = load().orc32_batch_run
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int,
+                   C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                   C.c_void_p, C.c_void_p]
+    sp = None
+    if solid is not None:
+        solid = np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1)
+        sp = solid.ctypes.data
+    o4, o2 = np.zeros(4, np.int32), np.zeros(2, np.float64)
+    if fn(q, nx, ny, sp, inlet_x, outlet_x, rho0, energy_every, energy_factor, int(bool(density_check)),
+          density_limit, init, op, tau, tau_nh, u0, n_steps, block, npt, o4.ctypes.data, o2.ctypes.data):
+        raise ValueError("orc32_batch_run: bad arguments")
+    return dict(label=int(o4[0]), decided_step=int(o4[1]), steps_done=int(o4[2]), status=int(o4[3]),
+                margin=float(o2[0]), energy=float(o2[1]))
+
+
 def fp32_periodic_d3q19(nx, ny, nz, op, tau, tau_nh, f_in, n_steps):
     """The same restatement for D3Q19 (BGK, RLBM, E-RLBM) on an nx x ny x nz periodic box."""
     f_in = np.ascontiguousarray(f_in, dtype=np.float64)

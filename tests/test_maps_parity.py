@@ -106,3 +106,57 @@ def test_sharded_map_world1_equals_map_run():
         b = map_run_sharded(kind, pts, precision=m.FP64, op=op, max_steps=1200)
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
+
+
+def fp32_cta_shape(nb):
+    """The FP32 batched kernel's CTA for an nb-node lattice (two nodes per thread, whole warps)."""
+    return ((nb + 1) // 2 + 31) // 32 * 32, 2
+
+
+def same_result(gpu, cpu):
+    for k in ("label", "decided_step", "steps_done", "status", "margin", "energy"):
+        a, b = gpu[k], cpu[k]
+        if not (a == b or (a != a and b != b)):
+            return False
+    return True
+
+
+def test_fp32_map_kernel_equals_its_cpu_restatement():
+    """The FP32-shifted batched map kernel (k_batch over PrecShifted32) against its CPU restatement
+    (oracle/fp32_shifted.c, orc32_batch_run): label, decided step, steps done, status, margin and energy
+    bit for bit, on 40 Taylor-Green map points (RLBM and E-RLBM, energy checks every 100 steps, whose
+    sum follows the kernel's thread slots and reduction tree) and 24 obstacle points (Zou-He inlet,
+    density outlet, bounce-back, FP32 density check every step), each run to a capped budget.  The runs
+    are roda_ponto of main_stability-map_taylor-green.cpp:41-104 and main_stability-map_obstacle.cpp:75-123."""
+    import erlbm_gb300 as m
+    runs = []
+    for k in range(40):
+        op = m.OP_EXTREG if k % 2 else m.OP_REG
+        u0, tau, tnh = m.tg_map_params((31 * k + 7) % 400, (83 * k + 11) % 400, 400, 400, op, 0.65)
+        runs.append(dict(op=op, tau=tau, tau_nh=tnh, u0=u0, n_steps=4000))
+    got = m.batch_run(19, 16, 16, runs, precision=m.FP32_SHIFTED, energy_every=100, energy_factor=2.0,
+                      init=m.INIT_TG_MAP)
+    block, npt = fp32_cta_shape(256)
+    unstable = 0
+    for r, g in zip(runs, got):
+        want = O.fp32_batch_run(19, 16, 16, r["op"], r["tau"], r["tau_nh"], r["u0"], r["n_steps"], block, npt,
+                                energy_every=100, energy_factor=2.0, init=1)
+        assert same_result(g, want), (r, g, want)
+        unstable += g["label"]
+    assert 0 < unstable < len(runs)
+    nx, ny, solid = m.obstacle_geometry()
+    runs = []
+    for k in range(24):
+        u, tau, tnh = m.obstacle_map_params((53 * k + 3) % 400, (29 * k + 7) % 400)
+        runs.append(dict(op=m.OP_EXTREG, tau=tau, tau_nh=tnh, u0=u, n_steps=3000))
+    got = m.batch_run(19, nx, ny, runs, precision=m.FP32_SHIFTED, solid=solid, inlet_x=1, outlet_x=nx - 2,
+                      density_check=True, density_limit=10.0, init=m.INIT_REST)
+    block, npt = fp32_cta_shape(nx * ny)
+    unstable = 0
+    for r, g in zip(runs, got):
+        want = O.fp32_batch_run(19, nx, ny, r["op"], r["tau"], r["tau_nh"], r["u0"], r["n_steps"], block, npt,
+                                solid=solid, inlet_x=1, outlet_x=nx - 2, density_check=True, density_limit=10.0,
+                                init=0)
+        assert same_result(g, want), (r, g, want)
+        unstable += g["label"]
+    assert 0 < unstable < len(runs)
