@@ -82,3 +82,35 @@ def fig4_table(Ls=(64, 128, 256, 512, 1024), L_ref: int = 2048, models=FIG4_MODE
                 if log:
                     log(rows[-1])
     return rows
+
+
+def precision_error(L: int, t_stars=(0.125, 0.25, 0.5, 1.0), precision: int = FP32_SHIFTED, op: int = OP_EXTREG,
+                    tau_nh: float = 0.65, log=None):
+    """The double shear layer of main_double-shear-layer.cpp (Re = 80000, U0 = 1/32) run in `precision`
+    and in FP64 (the reference's results) from the same initial populations: the relative L2 error of
+    the post-collision velocity of step 32 L t*, ||u - u64|| / ||u64|| over all nodes (the formula of
+    tools/error_calculator.cpp:88-105, in memory), for each t*.  Returns {t*: error}."""
+    import numpy as np
+    tau = 0.5 + 3.0 * U0 * L / 80000.0
+    tnh = 1.0 if op == OP_REG else tau_nh
+    f0 = init_double_shear(L)
+    out = {}
+    with Lattice(9, L, L, 1, None, tau, tnh, op, FP64) as l64, Lattice(9, L, L, 1, None, tau, tnh, op,
+                                                                        precision) as lp:
+        if precision == FP32_SHIFTED and L % 128 == 0:
+            from . import autotune
+            autotune.apply_periodic(lp)
+        l64.set_populations(f0)
+        lp.set_populations(f0)
+        done = 0
+        for t in sorted(t_stars):
+            s = int(round(t * L / U0))
+            l64.step(s + 1 - done)
+            lp.step(s + 1 - done)
+            done = s + 1
+            _, u64 = l64.macroscopic(STAGE_POST_COLLISION)
+            _, up = lp.macroscopic(STAGE_POST_COLLISION)
+            out[t] = float(np.linalg.norm(up - u64) / np.linalg.norm(u64))
+            if log:
+                log(L, t, out[t])
+    return out
