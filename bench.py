@@ -57,7 +57,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-BYTES_PER_LU = {"fp32": 2 * 9 * 4, "fp64": 2 * 9 * 8}
+BYTES_PER_LU = {"fp32": 2 * 9 * 4, "fp64": 2 * 9 * 8, "pair": 2 * 9 * 8}
 
 
 # DSL operators as main_double-shear-layer.cpp takes them (--collision; tau_nh = 1 for reg, :89):
@@ -76,8 +76,9 @@ def parse():
     p.add_argument("--inner", type=int, default=1000, help="LBM steps per bench step")
     p.add_argument("--inner-fp64", type=int, default=100,
                    help="dsl: LBM steps per bench step of the plain FP64 block beside the FP32-shifted line")
-    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "refined"],
-                   help="refined (map workloads): the whole map-points x map-points grid screened in FP32 with "
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "pair", "refined"],
+                   help="pair (dsl): the compensated FP32 form (float-pair populations, float-float collision); "
+                        "refined (map workloads): the whole map-points x map-points grid screened in FP32 with "
                         "the boundary points re-run in FP64")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
@@ -310,7 +311,7 @@ def run_ours(args):
     dev = torch.cuda.current_device()
 
     L, inner, K, W = args.L, args.inner, args.steps, args.warmup
-    prec = E.FP32_SHIFTED if args.precision == "fp32" else E.FP64
+    prec = {"fp32": E.FP32_SHIFTED, "fp64": E.FP64, "pair": E.FP32_PAIR}[args.precision]
     tau = tau_of(L)
     f0 = E.init_double_shear(L)
     stream = torch.cuda.Stream()
@@ -397,10 +398,10 @@ def run_ours(args):
     line = {
         "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32" if args.precision == "fp32" else "f64",
+        "dtype": {"fp32": "f32", "fp64": "f64", "pair": "f32x2"}[args.precision],
         "data": "synthetic (double shear layer initial condition, main_double-shear-layer.cpp:48-66)",
         "config": {"workload": f"double shear layer D2Q9 {op_label} Re=80000 L={L}, "
-                               f"{'FP32-shifted' if args.precision == 'fp32' else 'FP64 plain'}",
+                               f"{dict(fp32='FP32-shifted', fp64='FP64 plain', pair='compensated FP32 pairs')[args.precision]}",
                    "L": L, "lbm_steps_per_step": inner, "parallelism": f"replicas x{world}",
                    "l2": f"working set {2 * BYTES_PER_LU[args.precision] // 2 * L * L / 1e6:.0f} MB > 129 MB L2, "
                          "no flush",
@@ -417,7 +418,8 @@ def run_ours(args):
                      "kernel": (f"k_periodic_d2q9_x3a<{op}>" if wide else
                                 {1: f"k_periodic_d2q9<{op}>", 2: f"k_periodic_d2q9_x2s<{op}>",
                                  3: f"k_periodic_d2q9_x3s<{op}>"}[per])
-                     if args.precision == "fp32" else f"k_step<PrecExact64,9,{op}>",
+                     if args.precision == "fp32" else (f"k_step<PrecExact64,9,{op}>" if args.precision == "fp64"
+                                                       else f"k_step_pair<{op}>"),
                      # the update rate against the roofline of one step per launch, where every
                      # update reads and writes each population once (2 Q sizeof(real) bytes): the
                      # multi-step kernels move a half or a third of those bytes, so this fraction can exceed 1

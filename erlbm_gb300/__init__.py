@@ -14,7 +14,7 @@ import os
 import numpy as np
 
 from . import _lib
-from ._lib import (FIELD_DENSITY, FIELD_VELOCITY, FIELD_VORTICITY, FP32_SHIFTED, FP64, INIT_AOS, INIT_REST,
+from ._lib import (FIELD_DENSITY, FIELD_VELOCITY, FIELD_VORTICITY, FP32_PAIR, FP32_SHIFTED, FP64, INIT_AOS, INIT_REST,
                    INIT_TG_MAP, INLET_PARABOLIC, INLET_ZOUHE, MAP_OBSTACLE, MAP_TAYLOR_GREEN, OP_BGK, OP_EXTREG,
                    OP_MRT, OP_REG, OUTLET_CONVECTIVE, OUTLET_DENSITY, OUTLET_OPEN, REQ_OBSTACLE,
                    REQ_TG2D, REQ_TG3D, REQ_TG_MAP_POINT, STAGE_POST_COLLISION, STAGE_POST_STREAM, VTK_ASCII,

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(HERE, "liberlbm_gb300.so")
 
 OK, E_INVAL, E_OOM, E_CUDA, E_TIMEOUT, E_NONFINITE, E_UNSUPPORTED, E_STATE = 0, -1, -2, -3, -4, -5, -6, -7
 OP_BGK, OP_MRT, OP_REG, OP_EXTREG = 1, 2, 3, 4
-FP64, FP32_SHIFTED = 0, 1
+FP64, FP32_SHIFTED, FP32_PAIR = 0, 1, 2
 STAGE_POST_STREAM, STAGE_POST_COLLISION = 0, 1
 MAP_TAYLOR_GREEN, MAP_OBSTACLE = 1, 2
 INIT_REST, INIT_TG_MAP, INIT_AOS = 0, 1, 2

@@ -108,6 +108,10 @@ __device__ __forceinline__ void moments9(const float g[9], float &drho, float &m
 struct LaneF1 {
     using V = float;
     static __device__ __forceinline__ V c(float x) { return x; }
+    static __device__ __forceinline__ V ck(float x) { return x; }  // a relaxation coefficient
+    // a lattice constant: its FP32 value (fv, as the expression the FP32 update has always used) or,
+    // for a wider lane, the exact value dv
+    static __device__ __forceinline__ V kc(float fv, double) { return fv; }
     static __device__ __forceinline__ V add(V a, V b) { return __fadd_rn(a, b); }
     static __device__ __forceinline__ V sub(V a, V b) { return __fsub_rn(a, b); }
     static __device__ __forceinline__ V mul(V a, V b) { return __fmul_rn(a, b); }
@@ -119,6 +123,8 @@ struct LaneF1 {
 struct LaneF2 {
     using V = float2;
     static __device__ __forceinline__ V c(float x) { return make_float2(x, x); }
+    static __device__ __forceinline__ V ck(float x) { return make_float2(x, x); }
+    static __device__ __forceinline__ V kc(float fv, double) { return make_float2(fv, fv); }
     static __device__ __forceinline__ V add(V a, V b) { return __fadd2_rn(a, b); }
     static __device__ __forceinline__ V sub(V a, V b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
     static __device__ __forceinline__ V mul(V a, V b) { return __fmul2_rn(a, b); }
@@ -142,32 +148,32 @@ struct LaneF2 {
 // once, so only that last addition rounds at the scale of g.  The halving of D and DO is folded into
 // the coefficient k_d / 2 (exact), which rounds exactly as the half-scale form would.  The rest
 // population (update_rest_l) takes its parts at their own scale.
-template <class M, int OP>
+template <class M, int OP, class K>
 __device__ __forceinline__ void update_pair2_l(typename M::V &gi, typename M::V &gj, typename M::V D,
-                                               typename M::V DO, typename M::V f1, const Coef &k)
+                                               typename M::V DO, typename M::V f1, const K &k)
 {
     using V = typename M::V;
-    const V d1 = M::c(k.d1), m2 = M::c(-2.f), half = M::c(0.5f);
+    const V d1 = M::ck(k.d1), m2 = M::c(-2.f), half = M::c(0.5f);
     if (OP == OP_BGK) {
         const V DI = M::add(D, DO), DJ = M::sub(D, DO);
         gi = M::fma(half, M::fma(d1, DI, M::mul(m2, DI)), gi);
         gj = M::fma(half, M::fma(d1, DJ, M::mul(m2, DJ)), gj);
     } else {
         // every product here feeds an explicit fma, so there is nothing left for contraction to fuse
-        const V kh = M::c(k.kh);
-        const V cm = M::fma(d1, f1, M::fma(M::c(k.nkc), f1, M::mul(kh, D)));
+        const V kh = M::ck(k.kh);
+        const V cm = M::fma(d1, f1, M::fma(M::ck(k.nkc), f1, M::mul(kh, D)));
         gi = M::add(gi, M::fma(kh, DO, cm));
-        gj = M::add(gj, M::fma(M::c(-k.kh), DO, cm));
+        gj = M::add(gj, M::fma(M::neg(kh), DO, cm));
     }
 }
 
-template <class M, int OP>
+template <class M, int OP, class K>
 __device__ __forceinline__ typename M::V update_rest_l(typename M::V g0, typename M::V de0, typename M::V f10,
-                                                       const Coef &k)
+                                                       const K &k)
 {
-    const typename M::V d1 = M::c(k.d1), m2 = M::c(-2.f);
+    const typename M::V d1 = M::ck(k.d1), m2 = M::c(-2.f);
     if (OP == OP_BGK) return M::add(g0, M::fma(d1, de0, M::mul(m2, de0)));
-    return M::add(g0, M::fma(d1, f10, M::fma(M::c(k.nkc), f10, M::mul(M::c(k.kd), de0))));
+    return M::add(g0, M::fma(d1, f10, M::fma(M::ck(k.nkc), f10, M::mul(M::ck(k.kd), de0))));
 }
 
 // The D2Q9 update with the pair sums and differences kept at twice their scale: E = g_i + g_j = 2e,
@@ -175,8 +181,8 @@ __device__ __forceinline__ typename M::V update_rest_l(typename M::V g0, typenam
 // in binary floating point (the magnitudes here are far from the subnormal range), so every rounded
 // operation below yields exactly twice (or, for the moments, exactly) what the half-scale form yields:
 // the same bits with 13 multiplications fewer.  The final 1/2 is folded into the fma that consumes D.
-template <class M, int OP>
-__device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
+template <class M, int OP, class K = Coef>
+__device__ __forceinline__ void collide9l(typename M::V g[9], const K &k)
 {
     using V = typename M::V;
     constexpr float W1 = 1.f / 9.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
@@ -197,7 +203,7 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
     const V mu15 = M::mul(M::c(-1.5f), sab);
     const V cxy = M::fma(mx, uy, M::mul(my, ux));
     const V s3 = M::mul(M::c(3.f), sab);
-    const V k45 = M::c(4.5f), mw1x2 = M::c(-2.f * W1), mw2x2 = M::c(-2.f * W2);
+    const V k45 = M::c(4.5f), mw1x2 = M::kc(-2.f * W1, -2.0 / 9.0), mw2x2 = M::kc(-2.f * W2, -2.0 / 36.0);
     // twice the even non-equilibrium parts
     const V DX = M::fma(mw1x2, M::fma(k45, a, mu15), M::fma(mw1x2, drho, EX));
     const V DY = M::fma(mw1x2, M::fma(k45, b, mu15), M::fma(mw1x2, drho, EY));
@@ -205,8 +211,8 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
     const V DP = M::fma(mw2x2, M::fma(k45, cxy, s3), M::fma(mw2x2, drho, EP));
     const V DM = M::fma(mw2x2, M::fma(M::c(-4.5f), cxy, s3), M::fma(mw2x2, drho, EM));
     // twice the odd non-equilibrium parts; the axis pairs close the momentum
-    const V DOP = M::fma(M::c(2.f * M3W2), cmP, OP_);
-    const V DOM = M::fma(M::c(2.f * M3W2), cmM, OM);
+    const V DOP = M::fma(M::kc(2.f * M3W2, -1.0 / 6.0), cmP, OP_);
+    const V DOM = M::fma(M::kc(2.f * M3W2, -1.0 / 6.0), cmM, OM);
     const V DOX = M::neg(M::add(DOP, DOM));
     const V DOY = M::neg(M::sub(DOP, DOM));
     if constexpr (OP == OP_MRT) {
@@ -250,13 +256,13 @@ __device__ __forceinline__ void collide9l(typename M::V g[9], const Coef &k)
     const V sxy = M::add(DX, DY), sd = M::add(DP, DM);
     const V tr = M::fma(M::c(2.f), sd, sxy);
     const V de0 = M::neg(M::add(sxy, sd));
-    const V t12 = M::mul(tr, M::c(1.f / 12.f));
+    const V t12 = M::mul(tr, M::kc(1.f / 12.f, 1.0 / 12.0));
     const V dxy = M::sub(DX, DY), pxy = M::sub(DP, DM);
     const V f1X = M::fma(dxy, M::c(0.25f), t12);
     const V f1Y = M::fma(dxy, M::c(-0.25f), t12);
     const V f1P = M::fma(pxy, M::c(0.25f), t12);
     const V f1M = M::fma(pxy, M::c(-0.25f), t12);
-    g[0] = M::add(g[0], M::fma(M::c(k.d1t), tr, M::fma(M::c(k.nkct), tr, M::mul(M::c(k.kd), de0))));
+    g[0] = M::add(g[0], M::fma(M::ck(k.d1t), tr, M::fma(M::ck(k.nkct), tr, M::mul(M::ck(k.kd), de0))));
     update_pair2_l<M, OP>(g[1], g[2], DX, DOX, f1X, k);
     update_pair2_l<M, OP>(g[3], g[4], DY, DOY, f1Y, k);
     update_pair2_l<M, OP>(g[5], g[6], DP, DOP, f1P, k);

@@ -92,7 +92,7 @@ struct erlbm_handle {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long graph_key = -1;
     cudaStream_t capture_stream = nullptr;
-    size_t elem() const { return prec == ERLBM_FP64 ? sizeof(double) : sizeof(float); }
+    size_t elem() const { return prec == ERLBM_FP32_SHIFTED ? sizeof(float) : 8; }  // FP64 or a float pair
 };
 
 namespace {
@@ -170,6 +170,9 @@ int stage_buffer(erlbm_handle *h, int stage, const void **out)
     if (h->prec == ERLBM_FP64)
         CKL(launch_stream_only_fp64(h->q, h->g, (const double *)h->d_buf[h->cur], (double *)spare, h->stream),
             "stream_only");
+    else if (h->prec == ERLBM_FP32_PAIR)
+        CKL(launch_stream_only_pair(h->q, h->g, (const float2 *)h->d_buf[h->cur], (float2 *)spare, h->stream),
+            "stream_only");
     else
         CKL(launch_stream_only_fp32(h->q, h->g, (const float *)h->d_buf[h->cur], (float *)spare, h->stream),
             "stream_only");
@@ -181,6 +184,9 @@ int node_fields(erlbm_handle *h, const void *buf, double *e, double *rho, double
 {
     if (h->prec == ERLBM_FP64)
         CKL(launch_node_fields_fp64(h->q, h->g, h->n_fluid, h->d_nof, (const double *)buf, e, rho, u, h->stream),
+            "node_fields");
+    else if (h->prec == ERLBM_FP32_PAIR)
+        CKL(launch_node_fields_pair(h->q, h->g, h->n_fluid, h->d_nof, (const float2 *)buf, e, rho, u, h->stream),
             "node_fields");
     else
         CKL(launch_node_fields_fp32(h->q, h->g, h->n_fluid, h->d_nof, (const float *)buf, e, rho, u, h->stream),
@@ -315,7 +321,16 @@ int enqueue_step(erlbm_handle *h, const BCp &bc, int check_density, double densi
     void *src = h->d_buf[h->cur], *dst = h->d_buf[h->cur ^ 1];
     const bool plain =
         bc.inlet_x < 0 && bc.outlet_x < 0 && bc.open_y < 0 && !check_density && !stop_on_flag && a.mode == 0;
-    if (h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && plain && periodic_d2q9_fp32_ok(h->g)) {
+    if (h->prec == ERLBM_FP32_PAIR) {
+        if (!plain && !(a.mode == 1 && bc.inlet_x < 0 && bc.outlet_x < 0 && bc.open_y < 0 && !check_density &&
+                        !stop_on_flag)) {
+            set_error("the compensated FP32 form runs periodic lattices without boundary planes or per-step "
+                      "density checks%s%s", "", "");
+            return ERLBM_E_UNSUPPORTED;
+        }
+        CKL(launch_step_pair(h->q, h->op, h->g, h->R, a.mode, (const float2 *)src, (float2 *)dst, h->stream),
+            "step_pair");
+    } else if (h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && plain && periodic_d2q9_fp32_ok(h->g)) {
         CKL(launch_periodic_d2q9_fp32(h->op, h->g, h->R, (const float *)src, (float *)dst, h->stream, h->shape),
             "periodic_d2q9");
     } else if (h->prec == ERLBM_FP64) {
@@ -435,12 +450,16 @@ int erlbm_create(const erlbm_desc *d, erlbm_handle **out)
         set_error("lattice too large for 32-bit node indices%s%s", "", "");
         return ERLBM_E_INVAL;
     }
-    if (d->precision != ERLBM_FP64 && d->precision != ERLBM_FP32_SHIFTED) {
+    if (d->precision != ERLBM_FP64 && d->precision != ERLBM_FP32_SHIFTED && d->precision != ERLBM_FP32_PAIR) {
         set_error("unknown precision%s%s", "", "");
         return ERLBM_E_INVAL;
     }
     int rc = check_op(d->op, d->q);
     if (rc) return rc;
+    if (d->precision == ERLBM_FP32_PAIR && (d->q != 9 || d->solid || d->op == ERLBM_OP_MRT)) {
+        set_error("the compensated FP32 form runs periodic D2Q9 lattices with BGK, RLBM or E-RLBM%s%s", "", "");
+        return ERLBM_E_UNSUPPORTED;
+    }
     if (!(d->tau > 0) || !std::isfinite(d->tau) || !std::isfinite(d->tau_nh) || d->tau_nh == 0) {
         set_error("tau and tau_nh must be finite and non-zero%s%s", "", "");
         return ERLBM_E_INVAL;
@@ -538,6 +557,10 @@ int erlbm_set_params(erlbm_handle *h, double tau, double tau_nh, int op)
     int rc = check_handle(h);
     if (rc) return rc;
     if ((rc = check_op(op, h->q))) return rc;
+    if (h->prec == ERLBM_FP32_PAIR && op == ERLBM_OP_MRT) {
+        set_error("MRT has no compensated FP32 form%s%s", "", "");
+        return ERLBM_E_UNSUPPORTED;
+    }
     if (!(tau > 0) || !std::isfinite(tau) || !std::isfinite(tau_nh) || tau_nh == 0) {
         set_error("tau and tau_nh must be finite and non-zero%s%s", "", "");
         return ERLBM_E_INVAL;
@@ -563,6 +586,9 @@ int erlbm_set_populations(erlbm_handle *h, const double *aos, size_t n)
     if (h->prec == ERLBM_FP64)
         CKL(launch_aos_to_soa_fp64(h->q, h->g, h->n_fluid, h->d_nof, h->d_aos, (double *)h->d_buf[h->cur], h->stream),
             "aos_to_soa");
+    else if (h->prec == ERLBM_FP32_PAIR)
+        CKL(launch_aos_to_soa_pair(h->q, h->g, h->n_fluid, h->d_nof, h->d_aos, (float2 *)h->d_buf[h->cur], h->stream),
+            "aos_to_soa");
     else
         CKL(launch_aos_to_soa_fp32(h->q, h->g, h->n_fluid, h->d_nof, h->d_aos, (float *)h->d_buf[h->cur], h->stream),
             "aos_to_soa");
@@ -586,6 +612,9 @@ int erlbm_get_populations(erlbm_handle *h, double *aos, size_t n, int stage)
     if ((rc = stage_buffer(h, stage, &buf))) return rc;
     if (h->prec == ERLBM_FP64)
         CKL(launch_soa_to_aos_fp64(h->q, h->g, h->n_fluid, h->d_nof, (const double *)buf, h->d_aos, h->stream),
+            "soa_to_aos");
+    else if (h->prec == ERLBM_FP32_PAIR)
+        CKL(launch_soa_to_aos_pair(h->q, h->g, h->n_fluid, h->d_nof, (const float2 *)buf, h->d_aos, h->stream),
             "soa_to_aos");
     else
         CKL(launch_soa_to_aos_fp32(h->q, h->g, h->n_fluid, h->d_nof, (const float *)buf, h->d_aos, h->stream),
@@ -860,6 +889,8 @@ int field_on_device(erlbm_handle *h, int stage, int field, double *out)
     const int kind = field == 3 ? 3 : 1;
     if (h->prec == ERLBM_FP64)
         CKL(launch_box_field_fp64(h->q, h->g, (const double *)buf, kind, target, h->stream), "box_field");
+    else if (h->prec == ERLBM_FP32_PAIR)
+        CKL(launch_box_field_pair(h->q, h->g, (const float2 *)buf, kind, target, h->stream), "box_field");
     else
         CKL(launch_box_field_fp32(h->q, h->g, (const float *)buf, kind, target, h->stream), "box_field");
     if (field == 2) CKL(launch_vorticity(h->g, target, out, h->stream), "vorticity");

@@ -176,4 +176,18 @@ int launch_init_fp32(int kind, int q, const Geo &g, float *buf, const double *ta
 // FP64 add / multiply rate of the current GPU (operations per second), k_fp64.cu
 int measure_fp64_rate(double *ops_per_s);
 
+// The compensated FP32 form (k_pair.cu): populations as float pairs (hi, lo); periodic D2Q9 lattices
+// without boundary planes, BGK / RLBM / E-RLBM.
+bool step_pair_ok(int q, int op, const Geo &g);
+int launch_step_pair(int q, int op, const Geo &g, const Relax &R, int mode, const float2 *src, float2 *dst,
+                     cudaStream_t s);
+int launch_stream_only_pair(int q, const Geo &g, const float2 *src, float2 *dst, cudaStream_t s);
+int launch_aos_to_soa_pair(int q, const Geo &g, long long n_fluid, const int *node_of_fluid, const double *aos,
+                           float2 *soa, cudaStream_t s);
+int launch_soa_to_aos_pair(int q, const Geo &g, long long n_fluid, const int *node_of_fluid, const float2 *soa,
+                           double *aos, cudaStream_t s);
+int launch_node_fields_pair(int q, const Geo &g, long long n_fluid, const int *node_of_fluid, const float2 *buf,
+                            double *e, double *rho, double *u, cudaStream_t s);
+int launch_box_field_pair(int q, const Geo &g, const float2 *buf, int field, double *out, cudaStream_t s);
+
 }  // namespace erlbm

@@ -45,6 +45,11 @@ extern "C" {
 /* ---- precisions --------------------------------------------------------------------------- */
 #define ERLBM_FP64 0         /* plain path: bit-identical to the reference's FP64 CPU results */
 #define ERLBM_FP32_SHIFTED 1 /* populations stored and collided in FP32 as f_i - w_i */
+#define ERLBM_FP32_PAIR 2    /* compensated: f_i - w_i stored as a pair of floats (hi + lo, 8 bytes), the
+                                momentum and the pair differences collided in float-float arithmetic on
+                                the FP32 pipe, the small parts in FP32; periodic D2Q9 lattices without
+                                boundary planes or per-step density checks, BGK / RLBM / E-RLBM (others
+                                return ERLBM_E_UNSUPPORTED); no counterpart in the reference */
 
 /* ---- population stages (which populations a query reads) ---------------------------------- */
 #define ERLBM_STAGE_POST_STREAM 0    /* lattice.inif at the top of a driver's step loop */

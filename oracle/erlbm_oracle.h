@@ -108,6 +108,11 @@ int orc32_batch_run(int q, int nx, int ny, const uint8_t *solid, int inlet_x, in
                     int op, double tau, double tau_nh, double u0, int n_steps, int block, int npt, int *out4,
                     double *out2);
 
+/* the compensated FP32 form (float-pair populations, fp32_shifted.c) on a periodic D2Q9 box: the same
+ * contract as orc32_periodic_d2q9; BGK, RLBM and E-RLBM */
+int orc32p_periodic_d2q9(int nx, int ny, int op, double tau, double tau_nh, const double *f_in, int n_steps,
+                         double *f_out);
+
 #ifdef __cplusplus
 }
 #endif

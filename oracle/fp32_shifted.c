@@ -754,3 +754,197 @@ int orc32_batch_run(int q, int nx, int ny, const uint8_t *solid, int inlet_x, in
     free(a), free(b), free(f), free(order), free(tv);
     return 0;
 }
+
+/* ------------------------------------------------------------------------------------------------
+ * The engine's compensated FP32 form (ERLBM_FP32_PAIR) restated: g = f - w held as an unevaluated
+ * float pair (hi + lo); the D2Q9 collision with the pair sums and differences, the momentum, c.m on
+ * the diagonals, the diagonals' odd non-equilibrium parts and the increment's addition in float-float
+ * arithmetic (Knuth's two-sum, Dekker's fast two-sum, the fma-split product), the rest in FP32; every
+ * step of it as the engine's collide_pair.cuh orders it.
+ * ------------------------------------------------------------------------------------------------ */
+typedef struct {
+    float hi, lo;
+} DS32;
+
+static DS32 ds_two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    DS32 r = {s, (a - (s - bb)) + (b - bb)};
+    return r;
+}
+static DS32 ds_fast_two_sum(float a, float b)
+{
+    const float s = a + b;
+    DS32 r = {s, b - (s - a)};
+    return r;
+}
+static DS32 ds_add(DS32 a, DS32 b)
+{
+    const DS32 s = ds_two_sum(a.hi, b.hi);
+    return ds_fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+static DS32 ds_neg(DS32 a)
+{
+    DS32 r = {-a.hi, -a.lo};
+    return r;
+}
+static DS32 ds_sub(DS32 a, DS32 b) { return ds_add(a, ds_neg(b)); }
+static DS32 ds_c(float x)
+{
+    DS32 r = {x, 0.f};
+    return r;
+}
+static DS32 ds_split(double v)
+{
+    const float hi = (float)v;
+    DS32 r = {hi, (float)(v - (double)hi)};
+    return r;
+}
+/* Dekker's product: hi x hi split by an fma, the cross terms added */
+static DS32 ds_mul(DS32 a, DS32 b)
+{
+    const float p = a.hi * b.hi;
+    const float e = fmaf(a.lo, b.hi, fmaf(a.hi, b.lo, fmaf(a.hi, b.hi, -p)));
+    return ds_fast_two_sum(p, e);
+}
+static DS32 ds_fma(DS32 a, DS32 b, DS32 d) { return ds_add(ds_mul(a, b), d); }
+static DS32 ds_rcp(DS32 a)
+{
+    const DS32 y0 = ds_c(1.f / a.hi);
+    return ds_add(y0, ds_mul(y0, ds_sub(ds_c(1.f), ds_mul(a, y0))));
+}
+
+typedef struct {
+    DS32 kd, d1, nkc, kh, d1t, nkct;
+} CoefDS32;
+
+static void ds_pair_update(DS32 *gi, DS32 *gj, DS32 D, DS32 DO, DS32 f1, const CoefDS32 *k, int op)
+{
+    const DS32 d1 = k->d1, m2 = ds_c(-2.f), half = ds_c(0.5f);
+    if (op == ORC_OP_BGK) {
+        const DS32 DI = ds_add(D, DO), DJ = ds_sub(D, DO);
+        *gi = ds_fma(half, ds_fma(d1, DI, ds_mul(m2, DI)), *gi);
+        *gj = ds_fma(half, ds_fma(d1, DJ, ds_mul(m2, DJ)), *gj);
+    } else {
+        const DS32 kh = k->kh;
+        const DS32 cm = ds_fma(d1, f1, ds_fma(k->nkc, f1, ds_mul(kh, D)));
+        *gi = ds_add(*gi, ds_fma(kh, DO, cm));
+        *gj = ds_add(*gj, ds_fma(ds_neg(kh), DO, cm));
+    }
+}
+
+/* shifted::collide9l over the float-float lane (BGK, RLBM, E-RLBM), operation for operation */
+static void collide9_pair(DS32 g[9], const CoefDS32 *k, int op)
+{
+    const float W1 = 1.f / 9.f, W2 = 1.f / 36.f, M3W2 = -3.f * (1.f / 36.f);
+    (void)W1, (void)W2, (void)M3W2;
+    const DS32 EX = ds_add(g[1], g[2]), OX = ds_sub(g[1], g[2]);
+    const DS32 EY = ds_add(g[3], g[4]), OY = ds_sub(g[3], g[4]);
+    const DS32 EP = ds_add(g[5], g[6]), OP = ds_sub(g[5], g[6]);
+    const DS32 EM = ds_add(g[7], g[8]), OM = ds_sub(g[7], g[8]);
+    const DS32 drho = ds_add(ds_add(ds_add(EX, EY), ds_add(EP, EM)), g[0]);
+    const DS32 mx = ds_add(OX, ds_add(OP, OM));
+    const DS32 my = ds_add(OY, ds_sub(OP, OM));
+    const DS32 inv = ds_rcp(ds_add(ds_c(1.f), drho));
+    const DS32 ux = ds_mul(mx, inv), uy = ds_mul(my, inv);
+    const DS32 a = ds_mul(mx, ux), b = ds_mul(my, uy);
+    const DS32 sab = ds_fma(mx, ux, b);
+    const DS32 mu15 = ds_mul(ds_c(-1.5f), sab);
+    const DS32 cxy = ds_fma(mx, uy, ds_mul(my, ux));
+    const DS32 s3 = ds_mul(ds_c(3.f), sab);
+    const DS32 k45 = ds_c(4.5f), mw1x2 = ds_split(-2.0 / 9.0), mw2x2 = ds_split(-2.0 / 36.0);
+    const DS32 DX = ds_fma(mw1x2, ds_fma(k45, a, mu15), ds_fma(mw1x2, drho, EX));
+    const DS32 DY = ds_fma(mw1x2, ds_fma(k45, b, mu15), ds_fma(mw1x2, drho, EY));
+    const DS32 cmP = ds_add(mx, my), cmM = ds_sub(mx, my);
+    const DS32 DP = ds_fma(mw2x2, ds_fma(k45, cxy, s3), ds_fma(mw2x2, drho, EP));
+    const DS32 DM = ds_fma(mw2x2, ds_fma(ds_c(-4.5f), cxy, s3), ds_fma(mw2x2, drho, EM));
+    const DS32 DOP = ds_fma(ds_split(-1.0 / 6.0), cmP, OP);
+    const DS32 DOM = ds_fma(ds_split(-1.0 / 6.0), cmM, OM);
+    const DS32 DOX = ds_neg(ds_add(DOP, DOM));
+    const DS32 DOY = ds_neg(ds_sub(DOP, DOM));
+    const DS32 zero = ds_c(0.f);
+    if (op == ORC_OP_BGK) {
+        const DS32 de0 = ds_neg(ds_add(ds_add(DX, DY), ds_add(DP, DM)));
+        const DS32 d1 = k->d1, m2 = ds_c(-2.f);
+        g[0] = ds_add(g[0], ds_fma(d1, de0, ds_mul(m2, de0)));
+        ds_pair_update(&g[1], &g[2], DX, DOX, zero, k, op);
+        ds_pair_update(&g[3], &g[4], DY, DOY, zero, k, op);
+        ds_pair_update(&g[5], &g[6], DP, DOP, zero, k, op);
+        ds_pair_update(&g[7], &g[8], DM, DOM, zero, k, op);
+        return;
+    }
+    const DS32 sxy = ds_add(DX, DY), sd = ds_add(DP, DM);
+    const DS32 tr = ds_fma(ds_c(2.f), sd, sxy);
+    const DS32 de0 = ds_neg(ds_add(sxy, sd));
+    const DS32 t12 = ds_mul(tr, ds_split(1.0 / 12.0));
+    const DS32 dxy = ds_sub(DX, DY), pxy = ds_sub(DP, DM);
+    const DS32 f1X = ds_fma(dxy, ds_c(0.25f), t12), f1Y = ds_fma(dxy, ds_c(-0.25f), t12);
+    const DS32 f1P = ds_fma(pxy, ds_c(0.25f), t12), f1M = ds_fma(pxy, ds_c(-0.25f), t12);
+    g[0] = ds_add(g[0], ds_fma(k->d1t, tr, ds_fma(k->nkct, tr, ds_mul(k->kd, de0))));
+    ds_pair_update(&g[1], &g[2], DX, DOX, f1X, k, op);
+    ds_pair_update(&g[3], &g[4], DY, DOY, f1Y, k, op);
+    ds_pair_update(&g[5], &g[6], DP, DOP, f1P, k, op);
+    ds_pair_update(&g[7], &g[8], DM, DOM, f1M, k, op);
+}
+
+int orc32p_periodic_d2q9(int nx, int ny, int op, double tau, double tau_nh, const double *f_in, int n_steps,
+                         double *f_out)
+{
+    if (nx < 1 || ny < 1 || n_steps < 0 || !f_in || !f_out) return -1;
+    if (op != ORC_OP_BGK && op != ORC_OP_REG && op != ORC_OP_EXTREG) return -1;
+    const size_t n = (size_t)nx * ny;
+    DS32 *a = malloc(n * 9 * sizeof(DS32)), *b = malloc(n * 9 * sizeof(DS32));
+    if (!a || !b) {
+        free(a), free(b);
+        return -2;
+    }
+    CoefDS32 k;
+    const double d1 = 2.0 - 1.0 / tau;
+    double kd = 0.0, nkc = 0.0;
+    if (op == ORC_OP_REG) {
+        kd = -1.0;
+        nkc = -1.0;
+    } else if (op == ORC_OP_EXTREG) {
+        const double omega_gt1 = 1.0 - 1.0 / tau_nh;
+        kd = omega_gt1 - 1.0;
+        nkc = -(1.0 + omega_gt1);
+    }
+    k.kd = ds_split(kd);
+    k.d1 = ds_split(d1);
+    k.nkc = ds_split(nkc);
+    k.kh = ds_split(0.5 * kd);
+    k.d1t = ds_split(-2.0 / 3.0 * d1);
+    k.nkct = ds_split(-2.0 / 3.0 * nkc);
+    for (size_t p = 0; p < n; p++)
+        for (int i = 0; i < 9; i++) {
+            const double d = f_in[p * 9 + i] - w9(i);
+            const float hi = (float)d;
+            a[p * 9 + i].hi = hi;
+            a[p * 9 + i].lo = (float)(d - (double)hi);
+        }
+    for (int s = 0; s < n_steps; s++) {
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                const size_t node = (size_t)y * nx + x;
+                DS32 g[9];
+                for (int i = 0; i < 9; i++) {
+                    if (s == 0) {
+                        g[i] = a[node * 9 + i];
+                    } else {
+                        const int xs = (x - CX9[i] + nx) % nx, ys = (y - CY9[i] + ny) % ny;
+                        g[i] = a[((size_t)ys * nx + xs) * 9 + i];
+                    }
+                }
+                collide9_pair(g, &k, op);
+                memcpy(&b[node * 9], g, sizeof(g));
+            }
+        DS32 *t = a;
+        a = b;
+        b = t;
+    }
+    for (size_t p = 0; p < n; p++)
+        for (int i = 0; i < 9; i++) f_out[p * 9 + i] = ((double)a[p * 9 + i].hi + (double)a[p * 9 + i].lo) + w9(i);
+    free(a), free(b);
+    return 0;
+}

@@ -316,6 +316,20 @@ def fp32_channel(q, nx, ny, nz, solid, op, tau, tau_nh, f_in, n_steps, inlet_x=-
     return out
 
 
+def fp32_pair_periodic_d2q9(nx, ny, op, tau, tau_nh, f_in, n_steps):
+    """The compensated FP32 form (float-pair populations) restated on the CPU, periodic D2Q9: n_steps
+    steps from the post-stream populations f_in (the first colliding in place); the post-collision
+    populations f = w + hi + lo."""
+    f_in = np.ascontiguousarray(f_in, dtype=np.float64)
+    out = np.empty_like(f_in)
+    fn = load().orc32p_periodic_d2q9
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _dp, C.c_int, _dp]
+    if f_in.size != nx * ny * 9 or fn(nx, ny, op, tau, tau_nh, f_in, n_steps, out):
+        raise ValueError("orc32p_periodic_d2q9: bad arguments")
+    return out
+
+
 def fp32_batch_run(q, nx, ny, op, tau, tau_nh, u0, n_steps, block, npt, solid=None, inlet_x=-1, outlet_x=-1,
                    rho0=1.0, energy_every=0, energy_factor=2.0, density_check=False, density_limit=10.0, init=0):
     """One run of the engine's batched FP32 map kernel restated bit for bit (orc32_batch_run): the CTA
