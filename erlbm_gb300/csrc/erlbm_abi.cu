@@ -68,6 +68,7 @@ struct erlbm_handle {
     Geo g{};
     long long n_fluid = 0;
     uint8_t *d_solid = nullptr;
+    uint8_t *d_segflag = nullptr;    // D2Q9, nx % 128 == 0, solids: per 128-column segment, a solid in its stencil
     int *d_nof = nullptr;            // node of fluid index (null for periodic boxes)
     void *d_buf[2] = {nullptr, nullptr};
     int cur = 0;
@@ -133,6 +134,7 @@ void free_handle(erlbm_handle *h)
 {
     if (!h) return;
     cudaFree(h->d_solid);
+    cudaFree(h->d_segflag);
     cudaFree(h->d_profile);
     cudaFree(h->d_nof);
     cudaFree(h->d_buf[0]);
@@ -333,6 +335,10 @@ int enqueue_step(erlbm_handle *h, const BCp &bc, int check_density, double densi
     } else if (h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && plain && periodic_d2q9_fp32_ok(h->g)) {
         CKL(launch_periodic_d2q9_fp32(h->op, h->g, h->R, (const float *)src, (float *)dst, h->stream, h->shape),
             "periodic_d2q9");
+    } else if (h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && a.mode == 0 && !check_density && !stop_on_flag &&
+               d2q9_hybrid_ok(h->g)) {
+        CKL(launch_step_fp32_hybrid(h->op, h->g, bc, h->R, (const float *)src, (float *)dst, h->d_segflag, h->stream),
+            "d2q9_hybrid");
     } else if (h->prec == ERLBM_FP64) {
         CKL(launch_step_fp64(h->q, h->op, h->g, bc, h->R, a, (const double *)src, (double *)dst, h->stream), "step");
     } else {
@@ -513,6 +519,12 @@ int erlbm_create(const erlbm_desc *d, erlbm_handle **out)
             ok = cudaMemcpy(h->d_solid, d->solid, h->g.nbox, cudaMemcpyHostToDevice) == cudaSuccess &&
                  cudaMemcpy(h->d_nof, nof.data(), nof.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
             h->g.solid = h->d_solid;
+        }
+        if (ok && h->q == 9 && h->prec == ERLBM_FP32_SHIFTED && d2q9_hybrid_ok(h->g)) {
+            std::vector<uint8_t> flags((size_t)h->g.ny * (h->g.nx / 128));
+            d2q9_segment_flags(h->g, d->solid, flags.data());
+            ok = cudaMalloc(&h->d_segflag, flags.size()) == cudaSuccess &&
+                 cudaMemcpy(h->d_segflag, flags.data(), flags.size(), cudaMemcpyHostToDevice) == cudaSuccess;
         }
     }
     if (!ok) {

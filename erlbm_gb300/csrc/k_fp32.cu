@@ -828,6 +828,114 @@ int launch_step_fp32(int q, int op, const Geo &g, const BCp &bc, const Relax &R,
     return step_any<PrecShifted32>(q, op, g, bc, R, a, src, dst, s);
 }
 
+namespace {
+
+// One step of a D2Q9 lattice with solids and boundary planes, FP32-shifted, in the fused kernel's form
+// where it can be: a warp owns 128 columns of a row (four per lane, float4 accesses, x neighbours by
+// shuffle).  A segment whose pull stencil (its row and the rows above and below, one column beyond
+// each end) holds no solid node (segflag[warp] == 0) and none of whose nodes lies on a boundary plane
+// needs nothing else, and runs exactly k_periodic_d2q9's update.  The other warps -- next to walls and
+// obstacles, and on the planes -- run the generic per-node update (pull with bounce-back, the planes,
+// the collision) for their 128 nodes, skipping solid ones.  Both give the generic kernel's bits.
+template <int OP>
+__global__ void __launch_bounds__(256) k_d2q9_hybrid(const float *__restrict__ src, float *__restrict__ dst, Geo g,
+                                                     BCp bc, CollParams prm, const uint8_t *__restrict__ segflag)
+{
+    const int lane = threadIdx.x & 31;
+    const int wpr = g.nx >> 7;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= (long long)wpr * g.ny) return;  // whole warps only
+    const int y = (int)(gw / wpr);
+    const int xw = (int)(gw % wpr) << 7;
+    const bool planes = (bc.inlet_x >= xw && bc.inlet_x < xw + 128) || (bc.outlet_x >= xw && bc.outlet_x < xw + 128) ||
+                        y == bc.open_y;
+    if (planes || (segflag != nullptr && segflag[gw])) {
+#pragma unroll 1
+        for (int c = 0; c < 4; c++) {
+            const int x = xw + 4 * lane + c;
+            const long long node = (long long)y * g.nx + x;
+            if (g.solid != nullptr && g.solid[node]) continue;
+            float f[9];
+            state_after_planes<PrecShifted32, 9>(src, g, bc, 0, x, y, 0, node, f);
+            shifted::collide<9, OP>(f, prm.k);
+#pragma unroll
+            for (int i = 0; i < 9; i++) dst[(long long)i * g.plane + node] = f[i];
+        }
+        return;
+    }
+    const int nx = g.nx, ny = g.ny;
+    const long long plane = g.plane;
+    const int x0 = xw + 4 * lane;
+    const int ym = (y == 0) ? ny - 1 : y - 1;
+    const int yp = (y == ny - 1) ? 0 : y + 1;
+    const int xl = (xw == 0) ? nx - 1 : xw - 1;
+    const int xr = (xw + 128 == nx) ? 0 : xw + 128;
+    const long long ry = (long long)y * nx, rm = (long long)ym * nx, rp = (long long)yp * nx;
+    float4 v[9];
+    v[0] = pull4<0>(src + 0 * plane + ry, x0, xl, xr, lane);
+    v[1] = pull4<1>(src + 1 * plane + ry, x0, xl, xr, lane);
+    v[2] = pull4<-1>(src + 2 * plane + ry, x0, xl, xr, lane);
+    v[3] = pull4<0>(src + 3 * plane + rm, x0, xl, xr, lane);
+    v[4] = pull4<0>(src + 4 * plane + rp, x0, xl, xr, lane);
+    v[5] = pull4<1>(src + 5 * plane + rm, x0, xl, xr, lane);
+    v[6] = pull4<-1>(src + 6 * plane + rp, x0, xl, xr, lane);
+    v[7] = pull4<1>(src + 7 * plane + rp, x0, xl, xr, lane);
+    v[8] = pull4<-1>(src + 8 * plane + rm, x0, xl, xr, lane);
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        float gg[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) gg[i] = comp(v[i], c);
+        shifted::collide9<OP>(gg, prm.k);
+#pragma unroll
+        for (int i = 0; i < 9; i++) setc(v[i], c, gg[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; i++) *reinterpret_cast<float4 *>(dst + i * plane + ry + x0) = v[i];
+}
+
+}  // namespace
+
+bool d2q9_hybrid_ok(const Geo &g) { return g.nz == 1 && g.nx % 128 == 0 && g.ny >= 2 && g.plane % 4 == 0; }
+
+// Solid flags of the 128-column segments of a D2Q9 box (host): 1 where the segment's pull stencil holds a
+// solid node.  n = ny * nx / 128 bytes, one per warp of k_d2q9_hybrid in launch order.
+void d2q9_segment_flags(const Geo &g, const uint8_t *solid, uint8_t *flags)
+{
+    const int wpr = g.nx / 128;
+    for (int y = 0; y < g.ny; y++)
+        for (int w = 0; w < wpr; w++) {
+            uint8_t f = 0;
+            for (int dy = -1; dy <= 1 && !f; dy++) {
+                const int yy = (y + dy + g.ny) % g.ny;
+                for (int x = w * 128 - 1; x <= w * 128 + 128 && !f; x++) {
+                    const int xx = (x + g.nx) % g.nx;
+                    f = solid[(size_t)yy * g.nx + xx] ? 1 : 0;
+                }
+            }
+            flags[(size_t)y * wpr + w] = f;
+        }
+}
+
+int launch_step_fp32_hybrid(int op, const Geo &g, const BCp &bc, const Relax &R, const float *src, float *dst,
+                            const uint8_t *segflag, cudaStream_t s)
+{
+    if (!d2q9_hybrid_ok(g)) return -1;
+    CollParams prm;
+    prm.R = R;
+    prm.k = shifted::make_coef(R);
+    const long long warps = (long long)(g.nx / 128) * g.ny;
+    const unsigned nb = (unsigned)((warps * 32 + 255) / 256);
+    switch (op) {
+    case OP_BGK: k_d2q9_hybrid<OP_BGK><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag); break;
+    case OP_MRT: k_d2q9_hybrid<OP_MRT><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag); break;
+    case OP_REG: k_d2q9_hybrid<OP_REG><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag); break;
+    case OP_EXTREG: k_d2q9_hybrid<OP_EXTREG><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag); break;
+    default: return -1;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
 int launch_stream_only_fp32(int q, const Geo &g, const float *src, float *dst, cudaStream_t s)
 {
     return stream_only_any<PrecShifted32>(q, g, src, dst, s);

@@ -190,4 +190,11 @@ int launch_node_fields_pair(int q, const Geo &g, long long n_fluid, const int *n
                             double *e, double *rho, double *u, cudaStream_t s);
 int launch_box_field_pair(int q, const Geo &g, const float2 *buf, int field, double *out, cudaStream_t s);
 
+// D2Q9 FP32-shifted steps with solids and boundary planes, fused where a 128-column segment touches
+// neither (k_fp32.cu): nx % 128 == 0; segflag from d2q9_segment_flags (null: no solids).
+bool d2q9_hybrid_ok(const Geo &g);
+void d2q9_segment_flags(const Geo &g, const uint8_t *solid, uint8_t *flags);
+int launch_step_fp32_hybrid(int op, const Geo &g, const BCp &bc, const Relax &R, const float *src, float *dst,
+                            const uint8_t *segflag, cudaStream_t s);
+
 }  // namespace erlbm

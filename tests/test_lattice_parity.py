@@ -450,3 +450,50 @@ def test_fp32_d3q19_convective_outlet_equals_its_cpu_restatement():
         lat.step(300, dict(inlet_x=1, u_in=0.05, outlet_x=nx - 2, outlet_kind=2, rho_out=1.0))
         got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, 19)
     assert np.array_equal(got, want[solid == 0])
+
+
+@pytest.mark.parametrize("outlet_kind,open_top,op", [(0, False, 4), (2, False, 3), (1, True, 1), (2, True, 4)])
+def test_fp32_d2q9_hybrid_kernel_equals_its_cpu_restatement(outlet_kind, open_top, op):
+    """A D2Q9 channel 256 x 48 wide (nx a multiple of 128) in FP32 runs the hybrid step kernel: the
+    128-column segments whose stencil touches no solid and no plane take the fused path, the others the
+    generic per-node update.  Walls, a block obstacle, the Zou-He inlet and each outlet: bit for bit the
+    FP32 restatement (oracle/fp32_shifted.c)."""
+    nx, ny = 256, 48
+    solid = np.zeros((ny, nx), np.uint8)
+    solid[0, :] = 1
+    if not open_top:
+        solid[ny - 1, :] = 1
+    solid[20:26, 150:158] = 1
+    solid = solid.ravel()
+    n = nx * ny
+    open_y = ny - 1 if open_top else -1
+    w = O.equilibrium(9, 0, 0, 0, 1.0)
+    rng = np.random.default_rng(outlet_kind * 10 + op + 100 * open_top)
+    f0 = w[None, :] * (1.0 + 0.02 * rng.standard_normal((n, 9)))
+    tau = 0.6 if op in (1, 2) else 0.53
+    want = O.fp32_channel(9, nx, ny, 1, solid, op, tau, 0.65, f0.ravel(), 120, 1, 0.05, nx - 2, 1.0, outlet_kind,
+                          open_y).reshape(n, 9)
+    with eg().Lattice(9, nx, ny, 1, solid, tau, 0.65, op, eg().FP32_SHIFTED) as lat:
+        lat.set_populations(f0[solid == 0].ravel())
+        lat.step(120, dict(inlet_x=1, u_in=0.05, outlet_x=nx - 2, outlet_kind=outlet_kind, rho_out=1.0,
+                           open_y=open_y))
+        got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, 9)
+    assert np.array_equal(got, want[solid == 0])
+
+
+def test_fp32_d2q9_hybrid_kernel_periodic_with_solids_equals_restatement():
+    """Solid specks on a periodic 384 x 40 box (no planes): segments at the periodic seams and next to
+    the specks take the generic path, the rest the fused one; bit for bit the FP32 restatement."""
+    nx, ny = 384, 40
+    rng = np.random.default_rng(77)
+    solid = (rng.random((ny, nx)) < 0.002).astype(np.uint8)
+    solid[0, 0] = solid[ny - 1, nx - 1] = 1
+    solid = solid.ravel()
+    w = O.equilibrium(9, 0, 0, 0, 1.0)
+    f0 = w[None, :] * (1.0 + 0.03 * rng.standard_normal((nx * ny, 9)))
+    want = O.fp32_periodic_solid(9, nx, ny, 1, solid, 4, 0.53, 0.65, f0.ravel(), 60).reshape(-1, 9)
+    with eg().Lattice(9, nx, ny, 1, solid, 0.53, 0.65, 4, eg().FP32_SHIFTED) as lat:
+        lat.set_populations(f0[solid == 0].ravel())
+        lat.step(60)
+        got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, 9)
+    assert np.array_equal(got, want[solid == 0])
