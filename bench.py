@@ -40,7 +40,8 @@ Other workloads (--workload; the default is the one above):
                          beside the CPU restatement writing the same files from host populations.
   channel                a D2Q9 channel (the library's channel boundaries, Boundary_conditions.cpp:
                          456-806): walls, a circular cylinder, parabolic inlet, convective outlet,
-                         nx = 4 ny (ny = L / 4); `inner` steps per bench step; MLUPS over fluid nodes.
+                         nx = 4 ny (ny = L / 2: 4096 x 1024 at L = 2048, whose two population buffers
+                         exceed L2 in FP32); `inner` steps per bench step; MLUPS over fluid nodes.
 """
 from __future__ import annotations
 
@@ -830,7 +831,7 @@ def run_channel(args):
     import torch
     import erlbm_gb300 as E
     torch.cuda.set_device(0)
-    ny = max(64, args.L // 4)
+    ny = max(64, args.L // 2)
     nx, solid = channel_geometry(ny)
     prec = E.FP64 if args.precision == "fp64" else E.FP32_SHIFTED
     tau, tnh, op = 0.55, 0.7, E.OP_EXTREG
@@ -900,11 +901,12 @@ def run_channel(args):
             "config": {"workload": f"D2Q9 channel {nx}x{ny} with a cylinder, parabolic inlet, convective outlet, "
                                    f"E-RLBM tau=0.55 tau_nh=0.7", "nx": nx, "ny": ny, "n_fluid": n_fluid,
                        "lbm_steps_per_step": inner, "precision": args.precision,
-                       "l2": f"working set {bpl * n_fluid / 1e6:.0f} MB (two population buffers)"},
+                       "l2": f"working set {bpl * n_fluid / 1e6:.0f} MB (two population buffers) "
+                             f"{'>' if bpl * n_fluid > 129e6 else '<'} 129 MB L2, no flush"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": bpl * n_fluid,
                          "launch_us": launch_ms * 1e3, "lattice_updates_per_launch": n_fluid,
-                         "kernel": f"k_step<{'PrecExact64' if prec == E.FP64 else 'PrecShifted32'},9,4>"},
+                         "kernel": "k_step<PrecExact64,9,4>" if prec == E.FP64 else "k_d2q9_hybrid<4>"},
             "e2e": {"value": n_fluid * inner * K / t_e2e / 1e6, "unit": "MLUPS",
                     "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": 8},
             "gpu_launches": K * inner, "clocks": clk}

@@ -69,6 +69,9 @@ struct erlbm_handle {
     long long n_fluid = 0;
     uint8_t *d_solid = nullptr;
     uint8_t *d_segflag = nullptr;    // D2Q9, nx % 128 == 0, solids: per 128-column segment, a solid in its stencil
+    uint8_t *d_nodeflag = nullptr;   // and per node, a solid among its eight neighbours
+    int *d_fix = nullptr;            // the fluid nodes with a solid neighbour (n_fix)
+    int n_fix = 0;
     int *d_nof = nullptr;            // node of fluid index (null for periodic boxes)
     void *d_buf[2] = {nullptr, nullptr};
     int cur = 0;
@@ -92,6 +95,10 @@ struct erlbm_handle {
     // shape and parameters in graph_key (rebuilt when erlbm_set_launch or erlbm_set_params changes them)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long graph_key = -1;
+    // the same for blocks of D2Q9 FP32 steps with solids or planes (k_d2q9_hybrid), for the planes in
+    // bc_graph_bc (rebuilt when a call brings other planes)
+    cudaGraphExec_t bc_graph[2] = {nullptr, nullptr};
+    BCp bc_graph_bc{};
     cudaStream_t capture_stream = nullptr;
     size_t elem() const { return prec == ERLBM_FP32_SHIFTED ? sizeof(float) : 8; }  // FP64 or a float pair
 };
@@ -121,6 +128,14 @@ int check_op(int op, int q)
     return ERLBM_E_INVAL;
 }
 
+void drop_bc_graphs(erlbm_handle *h)
+{
+    for (cudaGraphExec_t &x : h->bc_graph) {
+        if (x) cudaGraphExecDestroy(x);
+        x = nullptr;
+    }
+}
+
 void drop_graphs(erlbm_handle *h)
 {
     for (cudaGraphExec_t &x : h->graph) {
@@ -128,6 +143,7 @@ void drop_graphs(erlbm_handle *h)
         x = nullptr;
     }
     h->graph_key = -1;
+    drop_bc_graphs(h);
 }
 
 void free_handle(erlbm_handle *h)
@@ -135,6 +151,8 @@ void free_handle(erlbm_handle *h)
     if (!h) return;
     cudaFree(h->d_solid);
     cudaFree(h->d_segflag);
+    cudaFree(h->d_nodeflag);
+    cudaFree(h->d_fix);
     cudaFree(h->d_profile);
     cudaFree(h->d_nof);
     cudaFree(h->d_buf[0]);
@@ -337,7 +355,8 @@ int enqueue_step(erlbm_handle *h, const BCp &bc, int check_density, double densi
             "periodic_d2q9");
     } else if (h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && a.mode == 0 && !check_density && !stop_on_flag &&
                d2q9_hybrid_ok(h->g)) {
-        CKL(launch_step_fp32_hybrid(h->op, h->g, bc, h->R, (const float *)src, (float *)dst, h->d_segflag, h->stream),
+        CKL(launch_step_fp32_hybrid(h->op, h->g, bc, h->R, (const float *)src, (float *)dst, h->d_segflag,
+                                    h->d_nodeflag, h->d_fix, h->n_fix, h->stream),
             "d2q9_hybrid");
     } else if (h->prec == ERLBM_FP64) {
         CKL(launch_step_fp64(h->q, h->op, h->g, bc, h->R, a, (const double *)src, (double *)dst, h->stream), "step");
@@ -397,6 +416,55 @@ int graph_steps(erlbm_handle *h, int per_launch)
     }
     CK(cudaGraphLaunch(x, h->stream));
     h->steps_done += n_steps;
+    h->kind = 1;
+    return ERLBM_OK;
+}
+
+bool same_planes(const BCp &a, const BCp &b)
+{
+    return a.inlet_x == b.inlet_x && a.u_in == b.u_in && a.outlet_x == b.outlet_x && a.rho_out == b.rho_out &&
+           a.inlet_kind == b.inlet_kind && a.outlet_kind == b.outlet_kind && a.open_y == b.open_y &&
+           a.profile == b.profile;
+}
+
+// A block of BC_GRAPH_STEPS steps of k_d2q9_hybrid as one CUDA graph launch, captured once per buffer
+// parity for the planes b.  The parabolic profile is read from h->d_profile when the graph runs, and
+// validate_bc rewrites it only after the stream has drained.
+constexpr int BC_GRAPH_STEPS = 64;
+
+int bc_graph_steps(erlbm_handle *h, const BCp &b)
+{
+    if (!same_planes(h->bc_graph_bc, b)) {
+        drop_bc_graphs(h);
+        h->bc_graph_bc = b;
+    }
+    cudaGraphExec_t &x = h->bc_graph[h->cur];
+    if (!x) {
+        if (!h->capture_stream) CK(cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking));
+        CK(cudaStreamBeginCapture(h->capture_stream, cudaStreamCaptureModeRelaxed));
+        int c = h->cur, lrc = 0;
+        for (int k = 0; k < BC_GRAPH_STEPS && lrc == 0; k++) {
+            lrc = launch_step_fp32_hybrid(h->op, h->g, b, h->R, (const float *)h->d_buf[c], (float *)h->d_buf[c ^ 1],
+                                          h->d_segflag, h->d_nodeflag, h->d_fix, h->n_fix, h->capture_stream);
+            c ^= 1;
+        }
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->capture_stream, &graph);
+        if (lrc != 0 || e != cudaSuccess || !graph) {
+            if (graph) cudaGraphDestroy(graph);
+            const cudaError_t le = cudaGetLastError();
+            return cuda_fail(e != cudaSuccess ? e : (le != cudaSuccess ? le : cudaErrorInvalidValue),
+                             "capture of the boundary step graph");
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&x, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            x = nullptr;
+            return cuda_fail(ie, "cudaGraphInstantiate");
+        }
+    }
+    CK(cudaGraphLaunch(x, h->stream));
+    h->steps_done += BC_GRAPH_STEPS;
     h->kind = 1;
     return ERLBM_OK;
 }
@@ -521,10 +589,19 @@ int erlbm_create(const erlbm_desc *d, erlbm_handle **out)
             h->g.solid = h->d_solid;
         }
         if (ok && h->q == 9 && h->prec == ERLBM_FP32_SHIFTED && d2q9_hybrid_ok(h->g)) {
-            std::vector<uint8_t> flags((size_t)h->g.ny * (h->g.nx / 128));
-            d2q9_segment_flags(h->g, d->solid, flags.data());
-            ok = cudaMalloc(&h->d_segflag, flags.size()) == cudaSuccess &&
-                 cudaMemcpy(h->d_segflag, flags.data(), flags.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+            std::vector<uint8_t> flags((size_t)h->g.ny * (h->g.nx / 128)), nflags((size_t)h->g.nbox);
+            d2q9_segment_flags(h->g, d->solid, flags.data(), nflags.data());
+            std::vector<int> fix;
+            for (long long k = 0; k < h->g.nbox; k++)
+                if (nflags[k] && !d->solid[k]) fix.push_back((int)k);
+            h->n_fix = (int)fix.size();
+            ok = cudaMalloc(&h->d_fix, std::max<size_t>(fix.size(), 1) * sizeof(int)) == cudaSuccess &&
+                 (fix.empty() || cudaMemcpy(h->d_fix, fix.data(), fix.size() * sizeof(int), cudaMemcpyHostToDevice) ==
+                                     cudaSuccess) &&
+                 cudaMalloc(&h->d_segflag, flags.size()) == cudaSuccess &&
+                 cudaMalloc(&h->d_nodeflag, nflags.size()) == cudaSuccess &&
+                 cudaMemcpy(h->d_segflag, flags.data(), flags.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+                 cudaMemcpy(h->d_nodeflag, nflags.data(), nflags.size(), cudaMemcpyHostToDevice) == cudaSuccess;
         }
     }
     if (!ok) {
@@ -649,7 +726,13 @@ int erlbm_step(erlbm_handle *h, int n_steps, const erlbm_bc *bc)
                         (!h->wide_strips || periodic_d2q9_x3a_ok(h->g));
     const bool fused2 = plain && h->two_step && periodic_d2q9_x2_ok(h->g);
     const int per_launch = fused3 ? 3 : (fused2 ? 2 : 1);
+    const bool hybrid = !plain && h->prec == ERLBM_FP32_SHIFTED && h->q == 9 && d2q9_hybrid_ok(h->g);
     for (int s = 0; s < n_steps;) {
+        if (hybrid && h->kind == 1 && n_steps - s >= BC_GRAPH_STEPS) {
+            if ((rc = bc_graph_steps(h, b))) return rc;
+            s += BC_GRAPH_STEPS;
+            continue;
+        }
         if (plain && h->kind == 1 && n_steps - s >= graph_steps_of(per_launch)) {
             if ((rc = graph_steps(h, per_launch))) return rc;
             s += graph_steps_of(per_launch);

@@ -830,41 +830,63 @@ int launch_step_fp32(int q, int op, const Geo &g, const BCp &bc, const Relax &R,
 
 namespace {
 
-// One step of a D2Q9 lattice with solids and boundary planes, FP32-shifted, in the fused kernel's form
-// where it can be: a warp owns 128 columns of a row (four per lane, float4 accesses, x neighbours by
-// shuffle).  A segment whose pull stencil (its row and the rows above and below, one column beyond
-// each end) holds no solid node (segflag[warp] == 0) and none of whose nodes lies on a boundary plane
-// needs nothing else, and runs exactly k_periodic_d2q9's update.  The other warps -- next to walls and
-// obstacles, and on the planes -- run the generic per-node update (pull with bounce-back, the planes,
-// the collision) for their 128 nodes, skipping solid ones.  Both give the generic kernel's bits.
+// One step of a D2Q9 lattice with solids and boundary planes, FP32-shifted.  Two kinds of blocks:
+//  - fix-up blocks (the first n_fix_blocks): one thread per node that needs the generic per-node update
+//    (pull with bounce-back, the planes, the collision): the fluid nodes next to a solid (the list
+//    `fix`, n_fix entries) and the nodes of the inlet column, the outlet column and the open y row;
+//  - fused blocks (the rest): k_periodic_d2q9's update, a warp per 128 columns of a row, four per lane,
+//    float4 accesses, x neighbours by shuffle.  It is the right update for every fluid node whose eight
+//    neighbours are fluid and which lies on no plane.  A segment whose stencil holds a solid (segflag)
+//    or which a plane crosses stores only its other nodes (nodeflag marks the nodes next to a solid).
+// The fix-up blocks come first, so their scattered loads overlap the fused stream instead of
+// lengthening its last wave.  No node is written by both kinds, and a node on a plane that is also
+// next to a solid is computed twice with the same result.  A solid node's storage is written by the
+// fused update but never read (the pull of a fluid node that faces a solid takes its own opposite
+// population), so what it holds does not matter.  Both updates give the generic kernel's bits.
 template <int OP>
 __global__ void __launch_bounds__(256) k_d2q9_hybrid(const float *__restrict__ src, float *__restrict__ dst, Geo g,
-                                                     BCp bc, CollParams prm, const uint8_t *__restrict__ segflag)
+                                                     BCp bc, CollParams prm, const uint8_t *__restrict__ segflag,
+                                                     const uint8_t *__restrict__ nodeflag,
+                                                     const int *__restrict__ fix, int n_fix, int n_fix_blocks)
 {
-    const int lane = threadIdx.x & 31;
-    const int wpr = g.nx >> 7;
-    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (gw >= (long long)wpr * g.ny) return;  // whole warps only
-    const int y = (int)(gw / wpr);
-    const int xw = (int)(gw % wpr) << 7;
-    const bool planes = (bc.inlet_x >= xw && bc.inlet_x < xw + 128) || (bc.outlet_x >= xw && bc.outlet_x < xw + 128) ||
-                        y == bc.open_y;
-    if (planes || (segflag != nullptr && segflag[gw])) {
-#pragma unroll 1
-        for (int c = 0; c < 4; c++) {
-            const int x = xw + 4 * lane + c;
-            const long long node = (long long)y * g.nx + x;
-            if (g.solid != nullptr && g.solid[node]) continue;
-            float f[9];
-            state_after_planes<PrecShifted32, 9>(src, g, bc, 0, x, y, 0, node, f);
-            shifted::collide<9, OP>(f, prm.k);
-#pragma unroll
-            for (int i = 0; i < 9; i++) dst[(long long)i * g.plane + node] = f[i];
-        }
-        return;
-    }
     const int nx = g.nx, ny = g.ny;
     const long long plane = g.plane;
+    if ((int)blockIdx.x < n_fix_blocks) {
+        int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+        int x, y;
+        if (t < n_fix) {
+            const int node = fix[t];
+            y = node / nx;
+            x = node - y * nx;
+        } else {
+            t -= n_fix;
+            if (bc.inlet_x >= 0) {
+                if (t < ny) { x = bc.inlet_x; y = t; goto have; }
+                t -= ny;
+            }
+            if (bc.outlet_x >= 0) {
+                if (t < ny) { x = bc.outlet_x; y = t; goto have; }
+                t -= ny;
+            }
+            if (bc.open_y >= 0 && t < nx) { x = t; y = bc.open_y; goto have; }
+            return;
+        }
+    have:
+        const long long node = (long long)y * nx + x;
+        if (g.solid != nullptr && g.solid[node]) return;
+        float f[9];
+        state_after_planes<PrecShifted32, 9>(src, g, bc, 0, x, y, 0, node, f);
+        shifted::collide<9, OP>(f, prm.k);
+#pragma unroll
+        for (int i = 0; i < 9; i++) dst[(long long)i * plane + node] = f[i];
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const int wpr = nx >> 7;
+    const long long gw = ((long long)(blockIdx.x - n_fix_blocks) * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= (long long)wpr * ny) return;  // whole warps only
+    const int y = (int)(gw / wpr);
+    const int xw = (int)(gw % wpr) << 7;
     const int x0 = xw + 4 * lane;
     const int ym = (y == 0) ? ny - 1 : y - 1;
     const int yp = (y == ny - 1) ? 0 : y + 1;
@@ -890,18 +912,58 @@ __global__ void __launch_bounds__(256) k_d2q9_hybrid(const float *__restrict__ s
 #pragma unroll
         for (int i = 0; i < 9; i++) setc(v[i], c, gg[i]);
     }
+    const bool planes = (bc.inlet_x >= xw && bc.inlet_x < xw + 128) || (bc.outlet_x >= xw && bc.outlet_x < xw + 128) ||
+                        y == bc.open_y;
+    if (!planes && !(segflag != nullptr && segflag[gw])) {
 #pragma unroll
-    for (int i = 0; i < 9; i++) *reinterpret_cast<float4 *>(dst + i * plane + ry + x0) = v[i];
+        for (int i = 0; i < 9; i++) *reinterpret_cast<float4 *>(dst + i * plane + ry + x0) = v[i];
+        return;
+    }
+    const uchar4 nf = nodeflag != nullptr ? *reinterpret_cast<const uchar4 *>(nodeflag + ry + x0) : make_uchar4(0, 0, 0, 0);
+    const bool open_row = y == bc.open_y;
+    const bool k0 = !(nf.x || open_row || x0 == bc.inlet_x || x0 == bc.outlet_x);
+    const bool k1 = !(nf.y || open_row || x0 + 1 == bc.inlet_x || x0 + 1 == bc.outlet_x);
+    const bool k2 = !(nf.z || open_row || x0 + 2 == bc.inlet_x || x0 + 2 == bc.outlet_x);
+    const bool k3 = !(nf.w || open_row || x0 + 3 == bc.inlet_x || x0 + 3 == bc.outlet_x);
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+        float *p = dst + i * plane + ry + x0;
+        if (k0 && k1 && k2 && k3) {
+            *reinterpret_cast<float4 *>(p) = v[i];
+        } else {
+            if (k0) p[0] = v[i].x;
+            if (k1) p[1] = v[i].y;
+            if (k2) p[2] = v[i].z;
+            if (k3) p[3] = v[i].w;
+        }
+    }
 }
 
 }  // namespace
 
-bool d2q9_hybrid_ok(const Geo &g) { return g.nz == 1 && g.nx % 128 == 0 && g.ny >= 2 && g.plane % 4 == 0; }
-
-// Solid flags of the 128-column segments of a D2Q9 box (host): 1 where the segment's pull stencil holds a
-// solid node.  n = ny * nx / 128 bytes, one per warp of k_d2q9_hybrid in launch order.
-void d2q9_segment_flags(const Geo &g, const uint8_t *solid, uint8_t *flags)
+bool d2q9_hybrid_ok(const Geo &g)
 {
+    // node indices of the fix-up list and the fix-up thread index are 32-bit
+    return g.nz == 1 && g.nx % 128 == 0 && g.ny >= 2 && g.plane % 4 == 0 && g.nbox + 3LL * (g.nx + g.ny) < (1LL << 31);
+}
+
+// Solid flags of a D2Q9 box for k_d2q9_hybrid (host).  segflags: ny * nx / 128 bytes, one per fused
+// warp in launch order, 1 where the 128-column segment's pull stencil holds a solid node.  nodeflags:
+// nx * ny bytes, 1 where one of the node's eight neighbours (periodic wrap) is solid; the fluid nodes
+// among those are the kernel's fix-up list.
+void d2q9_segment_flags(const Geo &g, const uint8_t *solid, uint8_t *flags, uint8_t *nodeflags)
+{
+    for (int y = 0; y < g.ny; y++)
+        for (int x = 0; x < g.nx; x++) {
+            uint8_t f = 0;
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    if (!dx && !dy) continue;
+                    const int xx = (x + dx + g.nx) % g.nx, yy = (y + dy + g.ny) % g.ny;
+                    f |= solid[(size_t)yy * g.nx + xx] ? 1 : 0;
+                }
+            nodeflags[(size_t)y * g.nx + x] = f;
+        }
     const int wpr = g.nx / 128;
     for (int y = 0; y < g.ny; y++)
         for (int w = 0; w < wpr; w++) {
@@ -918,19 +980,26 @@ void d2q9_segment_flags(const Geo &g, const uint8_t *solid, uint8_t *flags)
 }
 
 int launch_step_fp32_hybrid(int op, const Geo &g, const BCp &bc, const Relax &R, const float *src, float *dst,
-                            const uint8_t *segflag, cudaStream_t s)
+                            const uint8_t *segflag, const uint8_t *nodeflag, const int *fix, int n_fix, cudaStream_t s)
 {
-    if (!d2q9_hybrid_ok(g)) return -1;
+    if (!d2q9_hybrid_ok(g) || n_fix < 0) return -1;
     CollParams prm;
     prm.R = R;
     prm.k = shifted::make_coef(R);
     const long long warps = (long long)(g.nx / 128) * g.ny;
-    const unsigned nb = (unsigned)((warps * 32 + 255) / 256);
+    const long long n_generic =
+        (long long)n_fix + (bc.inlet_x >= 0 ? g.ny : 0) + (bc.outlet_x >= 0 ? g.ny : 0) + (bc.open_y >= 0 ? g.nx : 0);
+    const long long fix_blocks = (n_generic + 255) / 256;
+    const long long nb = fix_blocks + (warps * 32 + 255) / 256;
+    if (nb > 0x7fffffffLL) return -1;
+    const int fb = (int)fix_blocks;
     switch (op) {
-    case OP_BGK: k_d2q9_hybrid<OP_BGK><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag); break;
-    case OP_MRT: k_d2q9_hybrid<OP_MRT><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag); break;
-    case OP_REG: k_d2q9_hybrid<OP_REG><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag); break;
-    case OP_EXTREG: k_d2q9_hybrid<OP_EXTREG><<<nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag); break;
+    case OP_BGK: k_d2q9_hybrid<OP_BGK><<<(unsigned)nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag, nodeflag, fix, n_fix, fb); break;
+    case OP_MRT: k_d2q9_hybrid<OP_MRT><<<(unsigned)nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag, nodeflag, fix, n_fix, fb); break;
+    case OP_REG: k_d2q9_hybrid<OP_REG><<<(unsigned)nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag, nodeflag, fix, n_fix, fb); break;
+    case OP_EXTREG:
+        k_d2q9_hybrid<OP_EXTREG><<<(unsigned)nb, 256, 0, s>>>(src, dst, g, bc, prm, segflag, nodeflag, fix, n_fix, fb);
+        break;
     default: return -1;
     }
     return cudaGetLastError() == cudaSuccess ? 0 : -3;

@@ -191,10 +191,11 @@ int launch_node_fields_pair(int q, const Geo &g, long long n_fluid, const int *n
 int launch_box_field_pair(int q, const Geo &g, const float2 *buf, int field, double *out, cudaStream_t s);
 
 // D2Q9 FP32-shifted steps with solids and boundary planes, fused where a 128-column segment touches
-// neither (k_fp32.cu): nx % 128 == 0; segflag from d2q9_segment_flags (null: no solids).
+// neither (k_fp32.cu): nx % 128 == 0; segflag and nodeflag from d2q9_segment_flags (null: no solids);
+// fix: the n_fix fluid nodes with nodeflag set, in node order.
 bool d2q9_hybrid_ok(const Geo &g);
-void d2q9_segment_flags(const Geo &g, const uint8_t *solid, uint8_t *flags);
+void d2q9_segment_flags(const Geo &g, const uint8_t *solid, uint8_t *flags, uint8_t *nodeflags);
 int launch_step_fp32_hybrid(int op, const Geo &g, const BCp &bc, const Relax &R, const float *src, float *dst,
-                            const uint8_t *segflag, cudaStream_t s);
+                            const uint8_t *segflag, const uint8_t *nodeflag, const int *fix, int n_fix, cudaStream_t s);
 
 }  // namespace erlbm

@@ -98,6 +98,9 @@ int orc32_periodic_solid(int q, int nx, int ny, int nz, const uint8_t *solid, in
 int orc32_channel(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
                   int inlet_x, double u_in, int outlet_x, int outlet_kind, double rho_out, int open_y,
                   const double *f_in, int n_steps, double *f_out);
+int orc32_channel_ex(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
+                     int inlet_x, double u_in, int inlet_kind, int parabolic_L, int outlet_x, int outlet_kind,
+                     double rho_out, int open_y, const double *f_in, int n_steps, double *f_out);
 
 /* one run of the engine's batched FP32 map kernel restated (fp32_shifted.c): a block of `block` threads
  * with npt nodes each; init 0 = rest state w rho0, 1 = the Taylor-Green map equilibrium with amplitude u0

@@ -226,6 +226,7 @@ typedef struct {
     int inlet_x, outlet_x, outlet_kind, open_y;
     double u_in, rho_out;
     double inv_1mvx, vx3, vx6; /* formed once per run, as the engine's zou_he_prep */
+    const double *prof;        /* parabolic inlet: the x velocity per (y, z), else NULL */
 } Planes;
 
 enum { OUTLET_DENSITY = 0, OUTLET_OPEN = 1, OUTLET_CONVECTIVE = 2 };
@@ -325,8 +326,33 @@ static void pull_node(const float *a, int q, int nx, int ny, int nz, const uint8
     }
 }
 
-static void apply_inlet(float *g, int q, int nx, const Planes *pl)
+/* parabolic_D3Q19_x's node update on shifted populations: an opposite pair has one weight, so
+ * g_i = g_opp + rho vx / 3 (or / 6), rho in FP64 */
+static void parabolic19(float g[19], double vx)
 {
+    const float ty = ((((g[18] + g[3]) + g[16]) - g[15]) - g[4]) - g[17];
+    const float tz = ((((g[17] + g[5]) + g[16]) - g[15]) - g[6]) - g[18];
+    const float gz = (((g[0] + g[3]) + (g[4] + g[5])) + ((g[6] + g[15]) + (g[16] + g[17]))) + g[18];
+    const float gm = ((g[2] + g[8]) + (g[10] + g[12])) + g[14];
+    const double rho = (1.0 + (2.0 * (double)gm + (double)gz)) / (1.0 - vx);
+    const float a3 = (float)(rho * vx / 3.0), a6 = (float)(rho * vx / 6.0);
+    g[1] = g[2] + a3;
+    g[7] = g[8] + fmaf(-0.5f, ty, a6);
+    g[9] = g[10] + fmaf(0.5f, ty, a6);
+    g[11] = g[12] + fmaf(-0.5f, tz, a6);
+    g[13] = g[14] + fmaf(0.5f, tz, a6);
+}
+
+static void apply_inlet(float *g, int q, int nx, int ny, int y, int z, const Planes *pl)
+{
+    if (pl->prof) { /* parabolic_D2Q9_x is the D2Q9 Zou-He closure with the profile's velocity */
+        const double vx = pl->prof[y + (size_t)ny * z];
+        if (q == 19)
+            parabolic19(g, vx);
+        else
+            zou_he9(g, vx);
+        return;
+    }
     if (q == 19)
         zou_he19(g, pl, pl->inlet_x < nx / 2);
     else
@@ -350,7 +376,7 @@ static void after_x_planes(const float *a, int q, int nx, int ny, int nz, const 
                 return;
             }
             pull_node(a, q, nx, ny, nz, solid, first, xn, y, z, g);
-            if (xn == pl->inlet_x) apply_inlet(g, q, nx, pl);
+            if (xn == pl->inlet_x) apply_inlet(g, q, nx, ny, y, z, pl);
             outlet_rescale(g, q, pl->rho_out);
             return;
         }
@@ -358,7 +384,7 @@ static void after_x_planes(const float *a, int q, int nx, int ny, int nz, const 
         if (nsolid) return;
         float an[19];
         pull_node(a, q, nx, ny, nz, solid, first, xn, y, z, an);
-        if (xn == pl->inlet_x) apply_inlet(an, q, nx, pl);
+        if (xn == pl->inlet_x) apply_inlet(an, q, nx, ny, y, z, pl);
         if (pl->outlet_kind == OUTLET_OPEN) { /* the populations entering from outside */
             if (xn > x) {
                 g[1] = an[1];
@@ -375,7 +401,7 @@ static void after_x_planes(const float *a, int q, int nx, int ny, int nz, const 
         return;
     }
     pull_node(a, q, nx, ny, nz, solid, first, x, y, z, g);
-    if (pl && x == pl->inlet_x) apply_inlet(g, q, nx, pl);
+    if (pl && x == pl->inlet_x) apply_inlet(g, q, nx, ny, y, z, pl);
 }
 
 /* the x planes, then the open y plane (D2Q9): the populations entering through it are the inner
@@ -484,7 +510,24 @@ int orc32_channel(int q, int nx, int ny, int nz, const uint8_t *solid, int op, d
                   int inlet_x, double u_in, int outlet_x, int outlet_kind, double rho_out, int open_y,
                   const double *f_in, int n_steps, double *f_out)
 {
+    return orc32_channel_ex(q, nx, ny, nz, solid, op, tau, tau_nh, inlet_x, u_in, 0, 0, outlet_x, outlet_kind, rho_out,
+                            open_y, f_in, n_steps, f_out);
+}
+
+/* the parabolic profile of parabolic_D2Q9_x / parabolic_D3Q19_x (Boundary_conditions.cpp :759-764,
+ * :467-472) at the h-th fluid node of a column, counted from 1 */
+static double parabolic_vel32(int h, double vx_max, int Lw)
+{
+    const double d_h = (double)h - 0.5;
+    return -4.0 * vx_max / (Lw * Lw) * (d_h) * (d_h - Lw);
+}
+
+int orc32_channel_ex(int q, int nx, int ny, int nz, const uint8_t *solid, int op, double tau, double tau_nh,
+                     int inlet_x, double u_in, int inlet_kind, int parabolic_L, int outlet_x, int outlet_kind,
+                     double rho_out, int open_y, const double *f_in, int n_steps, double *f_out)
+{
     if ((q != 9 && q != 19) || (q == 9 && nz != 1)) return -1;
+    if (inlet_kind != 0 && inlet_kind != 1) return -1;
     if (inlet_x >= nx || outlet_x >= nx || open_y >= ny) return -1;
     if (outlet_kind < OUTLET_DENSITY || outlet_kind > OUTLET_CONVECTIVE) return -1;
     if (q == 19 && ((outlet_x >= 0 && outlet_kind == OUTLET_OPEN) || open_y >= 0)) return -1; /* D2Q9 planes */
@@ -506,7 +549,28 @@ int orc32_channel(int q, int nx, int ny, int nz, const uint8_t *solid, int op, d
     pl.inv_1mvx = 1.0 / (1.0 - u_in);
     pl.vx3 = u_in / 3.0;
     pl.vx6 = u_in / 6.0;
-    return run_periodic(q, nx, ny, nz, solid, &pl, op, tau, tau_nh, f_in, n_steps, f_out);
+    pl.prof = NULL;
+    double *prof = NULL;
+    if (inlet_kind == 1 && inlet_x >= 0) { /* the fluid nodes of each inlet column, counted up from y = 0 */
+        if (parabolic_L < 1 || parabolic_L >= ny) return -1;
+        prof = calloc((size_t)ny * nz, sizeof(double));
+        if (!prof) return -2;
+        for (int z = 0; z < nz; z++) {
+            int h = 0;
+            for (int y = 0; y < ny; y++) {
+                if (solid && solid[((size_t)z * ny + y) * nx + inlet_x]) continue;
+                if (++h > parabolic_L) {
+                    free(prof);
+                    return -1;
+                }
+                prof[y + (size_t)ny * z] = parabolic_vel32(h, u_in, parabolic_L);
+            }
+        }
+        pl.prof = prof;
+    }
+    const int rc = run_periodic(q, nx, ny, nz, solid, &pl, op, tau, tau_nh, f_in, n_steps, f_out);
+    free(prof);
+    return rc;
 }
 
 /* ------------------------------------------------------------------------------------------------
@@ -626,6 +690,7 @@ int orc32_batch_run(int q, int nx, int ny, const uint8_t *solid, int inlet_x, in
     k.d1t = (float)(-2.0 / 3.0 * d1);
     k.nkct = (float)(-2.0 / 3.0 * nkc);
     Planes pl;
+    memset(&pl, 0, sizeof(pl)); /* no parabolic profile */
     pl.inlet_x = inlet_x;
     pl.outlet_x = outlet_x;
     pl.outlet_kind = OUTLET_DENSITY;

@@ -294,25 +294,26 @@ def fp32_periodic_solid(q, nx, ny, nz, solid, op, tau, tau_nh, f_in, n_steps):
 
 
 def fp32_channel(q, nx, ny, nz, solid, op, tau, tau_nh, f_in, n_steps, inlet_x=-1, u_in=0.0, outlet_x=-1,
-                 rho_out=1.0, outlet_kind=0, open_y=-1):
-    """The restatement with a solid mask and boundary planes: a Zou-He velocity inlet at inlet_x; an
-    outlet at outlet_x of kind 0 (density, devnull_rho_x), 1 (open, D2Q9) or 2 (convective); the D2Q9
-    open y plane open_y.  f_in and the result hold every node of the box."""
+                 rho_out=1.0, outlet_kind=0, open_y=-1, inlet_kind=0, parabolic_L=0):
+    """The restatement with a solid mask and boundary planes: a velocity inlet at inlet_x, Zou-He
+    (inlet_kind 0) or parabolic with a channel width of parabolic_L fluid nodes (1); an outlet at
+    outlet_x of kind 0 (density, devnull_rho_x), 1 (open, D2Q9) or 2 (convective); the D2Q9 open y
+    plane open_y.  f_in and the result hold every node of the box."""
     f_in = np.ascontiguousarray(f_in, dtype=np.float64)
     out = np.empty_like(f_in)
-    fn = load().orc32_channel
+    fn = load().orc32_channel_ex
     fn.restype = C.c_int
     fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
-                   C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, _dp, C.c_int, _dp]
+                   C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _dp, C.c_int, _dp]
     sp = None
     if solid is not None:
         solid = np.ascontiguousarray(solid, dtype=np.uint8)
         if solid.size != nx * ny * nz:
             raise ValueError("solid mask size")
         sp = solid.ctypes.data
-    if f_in.size != nx * ny * nz * q or fn(q, nx, ny, nz, sp, op, tau, tau_nh, inlet_x, u_in, outlet_x,
-                                           outlet_kind, rho_out, open_y, f_in, n_steps, out):
-        raise ValueError("orc32_channel: bad arguments")
+    if f_in.size != nx * ny * nz * q or fn(q, nx, ny, nz, sp, op, tau, tau_nh, inlet_x, u_in, inlet_kind, parabolic_L,
+                                           outlet_x, outlet_kind, rho_out, open_y, f_in, n_steps, out):
+        raise ValueError("orc32_channel_ex: bad arguments")
     return out
 
 

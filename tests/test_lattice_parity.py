@@ -481,6 +481,56 @@ def test_fp32_d2q9_hybrid_kernel_equals_its_cpu_restatement(outlet_kind, open_to
     assert np.array_equal(got, want[solid == 0])
 
 
+@pytest.mark.parametrize("op", [1, 3, 4])
+def test_fp32_d2q9_hybrid_parabolic_channel_equals_its_cpu_restatement(op):
+    """The channel workload's form on a 384 x 40 box: walls on all four sides, a cylinder, the parabolic
+    inlet at x = 1 next to the wall, the convective outlet at x = 301 (inside a lane's four columns and a
+    segment with no solid in its stencil), a speck of solid two columns in front of the outlet and one
+    on the seam of two segments.  The hybrid kernel runs the nodes next to solids and the plane nodes
+    through the per-node update, 64-step blocks as CUDA graphs: bit for bit the FP32 restatement."""
+    nx, ny = 384, 40
+    solid = np.zeros((ny, nx), np.uint8)
+    solid[:, 0] = solid[:, nx - 1] = 1
+    solid[0, :] = solid[ny - 1, :] = 1
+    yy, xx = np.mgrid[0:ny, 0:nx]
+    solid[(xx - 60) ** 2 + (yy - 20) ** 2 <= 16] = 1
+    solid[12, 299] = 1
+    solid[30, 127] = solid[30, 128] = 1
+    solid = solid.ravel()
+    n = nx * ny
+    w = O.equilibrium(9, 0, 0, 0, 1.0)
+    rng = np.random.default_rng(op + 40)
+    f0 = w[None, :] * (1.0 + 0.02 * rng.standard_normal((n, 9)))
+    tau = 0.6 if op == 1 else 0.53
+    outlet_x = 301
+    want = O.fp32_channel(9, nx, ny, 1, solid, op, tau, 0.65, f0.ravel(), 140, 1, 0.05, outlet_x, 1.0, 2,
+                          inlet_kind=1, parabolic_L=ny - 2).reshape(n, 9)
+    bc = dict(inlet_x=1, u_in=0.05, inlet_kind=eg().INLET_PARABOLIC, parabolic_L=ny - 2, outlet_x=outlet_x,
+              outlet_kind=2, rho_out=1.0)
+    with eg().Lattice(9, nx, ny, 1, solid, tau, 0.65, op, eg().FP32_SHIFTED) as lat:
+        lat.set_populations(f0[solid == 0].ravel())
+        # 1 generic step, then blocks of 64 steps replayed as graphs from both buffer parities
+        for n_steps in (1, 65, 74):
+            lat.step(n_steps, bc)
+        got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, 9)
+    assert np.array_equal(got, want[solid == 0])
+
+
+def test_fp32_d2q9_hybrid_planes_without_solids_equals_restatement():
+    """No solid at all (periodic in y), a Zou-He inlet at x = 130 and a density outlet at x = 3 (the flow
+    planes inside segments away from the box edges): bit for bit the restatement."""
+    nx, ny = 256, 24
+    w = O.equilibrium(9, 0, 0, 0, 1.0)
+    rng = np.random.default_rng(11)
+    f0 = w[None, :] * (1.0 + 0.02 * rng.standard_normal((nx * ny, 9)))
+    want = O.fp32_channel(9, nx, ny, 1, None, 4, 0.53, 0.65, f0.ravel(), 50, 130, 0.03, 3, 1.0, 0).reshape(-1, 9)
+    with eg().Lattice(9, nx, ny, 1, None, 0.53, 0.65, 4, eg().FP32_SHIFTED) as lat:
+        lat.set_populations(f0.ravel())
+        lat.step(50, dict(inlet_x=130, u_in=0.03, outlet_x=3, outlet_kind=0, rho_out=1.0))
+        got = lat.get_populations(eg().STAGE_POST_COLLISION).reshape(-1, 9)
+    assert np.array_equal(got, want)
+
+
 def test_fp32_d2q9_hybrid_kernel_periodic_with_solids_equals_restatement():
     """Solid specks on a periodic 384 x 40 box (no planes): segments at the periodic seams and next to
     the specks take the generic path, the rest the fused one; bit for bit the FP32 restatement."""

@@ -385,6 +385,43 @@ def test_fp32_d2q9_planes_restatement_tracks_the_fp64_oracle(outlet_kind, open_t
         assert np.linalg.norm(got[solid == 0] - want) / np.linalg.norm(want - w[None, :]) < 2e-6, op
 
 
+@pytest.mark.parametrize("q", [9, 19])
+def test_fp32_parabolic_inlet_restatement_tracks_the_fp64_oracle(q):
+    """The parabolic inlet (parabolic_D2Q9_x / parabolic_D3Q19_x) with a convective outlet: the FP32
+    restatement stays within 2e-6 relative of the FP64 oracle after 300 steps from rest."""
+    if q == 9:
+        nx, ny, solid = _d2q9_channel(False)
+    else:  # the obstacle channel with walls at y = 0 and y = ny - 1
+        nx, ny, solid = O.obstacle_geometry(1, 1)
+        solid = solid.reshape(ny, nx).copy()
+        solid[0, :] = solid[ny - 1, :] = 1
+        solid = solid.ravel()
+    n = nx * ny
+    w = O.equilibrium(q, 0, 0, 0, 1.0)
+    f0 = np.tile(w, (n, 1))
+    Lw = ny - 2
+    got = O.fp32_channel(q, nx, ny, 1, solid, 4, 0.53, 0.65, f0.ravel(), 300, 1, 0.05, nx - 2, 1.0, 2,
+                         inlet_kind=1, parabolic_L=Lw).reshape(n, q)
+    ref = O.Lattice(q, nx, ny, 1, solid, 0.53, 0.65, 4)
+    ref.set(f0[solid == 0].ravel())
+    ref.step(300, dict(inlet_x=1, u_in=0.05, inlet_kind=1, parabolic_L=Lw, outlet_x=nx - 2, outlet_kind=2,
+                       rho_out=1.0))
+    want = ref.get(1).reshape(-1, q)
+    assert np.linalg.norm(got[solid == 0] - want) / np.linalg.norm(want - w[None, :]) < 2e-6
+    with pytest.raises(ValueError):  # a column with more fluid nodes than the profile's width
+        O.fp32_channel(q, nx, ny, 1, solid, 4, 0.53, 0.65, f0.ravel(), 1, 1, 0.05, nx - 2, 1.0, 2, inlet_kind=1,
+                       parabolic_L=Lw - 1)
+
+
+def test_fp32_batch_restatement_runs_a_stable_obstacle_point():
+    """The batched-map restatement with its Zou-He inlet and density outlet (orc32_batch_run) on a
+    stable obstacle point: 300 steps, no density flag, label stable, every step done."""
+    nx, ny, solid = O.obstacle_geometry(1, 1)
+    r = O.fp32_batch_run(19, nx, ny, 4, 0.6, 0.65, 0.02, 300, 256, 2, solid=solid, inlet_x=1, outlet_x=nx - 2,
+                         density_check=True, density_limit=10.0, init=0)
+    assert r["status"] == 0 and r["label"] == 0 and r["steps_done"] == 300, r
+
+
 def test_fp32_d3q19_convective_restatement_tracks_the_fp64_oracle():
     """The obstacle channel with a convective outlet instead of the density outlet: the FP32 restatement
     stays within 2e-6 relative of the FP64 oracle after 300 steps."""
