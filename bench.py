@@ -55,6 +55,9 @@ import sys
 import tempfile
 import time
 
+# before any CUDA context exists: the server's resident loops need their own hardware work queues
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -93,6 +96,9 @@ def parse():
     p.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
     p.add_argument("--rate", type=float, default=2000.0, help="serve: mean arrivals per second")
     p.add_argument("--plain-requests", type=int, default=24, help="serve: sampled requests run on the plain path")
+    p.add_argument("--team-ctas", type=int, default=0,
+                   help="serve: CTAs of each resident team loop (0 = one per SM; -1 = no team loop, those "
+                        "requests take the stream lane)")
     return p.parse_args()
 
 
@@ -693,7 +699,7 @@ def run_serve(args):
     import erlbm_gb300 as E
     torch.cuda.set_device(0)
     stream = serve_stream(E, args.requests, args.rate)
-    with E.Server(hbm_budget_bytes=16 << 30) as srv:
+    with E.Server(hbm_budget_bytes=16 << 30, team_ctas=args.team_ctas) as srv:
         # warm-up: one request of each kind
         for _, r in stream[:8]:
             srv.wait(srv.submit(**dict(r, n_steps=min(r["n_steps"], 10))))
@@ -723,10 +729,11 @@ def run_serve(args):
             "warmup": 8, "ms_per_step": span / max(1, len(ok)) * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded Poisson stream of config-5 requests)",
             "config": {"workload": f"serve {args.requests} requests, Poisson {args.rate:.0f}/s, mixed kinds",
-                       "requests": args.requests},
+                       "requests": args.requests, "team_ctas": args.team_ctas},
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "max": float(lat.max())},
             "failed": len(res) - len(ok), "lanes": {"resident": sum(1 for x in ok if x["lane"] == 0),
+                                                    "team": sum(1 for x in ok if x["lane"] == 2),
                                                     "stream": sum(1 for x in ok if x["lane"] == 1)},
             "plain_fp64_one_run_at_a_time": {"value": plain, "unit": "runs/s", "requests": len(sample),
                                              "sample": "every k-th request of the same stream"},

@@ -11,6 +11,11 @@ from __future__ import annotations
 import ctypes as C
 import os
 
+# The request server keeps persistent kernels resident on their own streams.  Streams share the
+# device's hardware work queues (8 unless this is set before the process creates its CUDA context),
+# and a kernel queued behind a resident loop on a shared queue waits until that loop leaves.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 import numpy as np
 
 from . import _lib
@@ -355,9 +360,10 @@ def batch_run(q: int, nx: int, ny: int, runs, precision: int = FP64, solid=None,
 class Server:
     """Continuous-batching server (erlbm_server_*): submit runs while others are on the GPU."""
 
-    def __init__(self, hbm_budget_bytes: int = 8 << 30, slot_ctas: int = 0, max_streams: int = 16,
-                 queue_capacity: int = 0):
-        d = _lib.ServerDesc(int(hbm_budget_bytes), int(slot_ctas), int(max_streams), int(queue_capacity))
+    def __init__(self, hbm_budget_bytes: int = 8 << 30, slot_ctas: int = 0, max_streams: int = 0,
+                 queue_capacity: int = 0, team_ctas: int = 0, team_max_nodes: int = 0):
+        d = _lib.ServerDesc(int(hbm_budget_bytes), int(slot_ctas), int(max_streams), int(queue_capacity),
+                            int(team_ctas), int(team_max_nodes))
         h = C.c_void_p()
         check(lib().erlbm_server_start(C.byref(d), C.byref(h)), "erlbm_server_start")
         self._h = h

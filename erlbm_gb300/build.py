@@ -24,7 +24,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off",
           f"-I{CSRC}", f"-I{INCLUDE}"]
-NO_FMA = {"k_fp64.cu", "k_map64.cu", "noalloc.cu", "fields.cu", "k_pair.cu"}
+NO_FMA = {"k_fp64.cu", "k_map64.cu", "noalloc.cu", "fields.cu", "k_pair.cu", "k_team64.cu"}
 
 
 def nvcc() -> str:

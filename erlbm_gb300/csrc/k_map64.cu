@@ -65,6 +65,10 @@ int launch_slot_server_fp64(const SlotRing &ring, int max_nb, int grid, int bloc
     auto k = k_slot_server<PrecExact64, 19, 1>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return -3;
+    // every resident loop asks for the largest shared-memory carveout: an SM runs CTAs of kernels with
+    // one carveout at a time, so loops with different ones would keep each other off the SMs
+    e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return -3;
     k<<<grid, block, smem, s>>>(ring, max_nb, dbl);
     return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
@@ -72,7 +76,9 @@ int launch_slot_server_fp64(const SlotRing &ring, int max_nb, int grid, int bloc
 int slot_server_occupancy_fp64(int block, size_t smem)
 {
     auto k = k_slot_server<PrecExact64, 19, 1>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared) !=
+            cudaSuccess) {
         cudaGetLastError();
         return 0;
     }

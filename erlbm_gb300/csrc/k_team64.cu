@@ -1,0 +1,44 @@
+// k_team64.cu -- the server's resident team loop over plain FP64 lattices (compiled with --fmad=false,
+// the rounding of k_fp64.cu, so that a run gives the stream lane's bits).
+#include "team_lane.cuh"
+
+namespace erlbm {
+
+int launch_team_server_fp64(const TeamRing &r, int grid, cudaStream_t s)
+{
+    if (grid < 2 || grid > TEAM_MAX_GRID) return -1;
+    // the slot loops' carveout (largest shared memory), so that the resident loops share SMs
+    if (cudaFuncSetAttribute(team::k_team_server<PrecExact64>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+        return -3;
+    team::k_team_server<PrecExact64><<<grid, team_threads<PrecExact64>(), 0, s>>>(r);
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+int team_server_occupancy_fp64()
+{
+    int n = 0;
+    if (cudaFuncSetAttribute(team::k_team_server<PrecExact64>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, team::k_team_server<PrecExact64>, team_threads<PrecExact64>(), 0) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+namespace {
+__global__ void k_team_clock(long long *out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) *out = team::now_ns();
+}
+}  // namespace
+
+int launch_team_clock(long long *out, cudaStream_t s)
+{
+    k_team_clock<<<1, 32, 0, s>>>(out);
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+}  // namespace erlbm

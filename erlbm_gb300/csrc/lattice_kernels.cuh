@@ -211,16 +211,28 @@ __device__ __forceinline__ void node_xyz(const Geo &g, long long node, int &x, i
     }
 }
 
+// Loads for kernels that read buffers they (or other CTAs of the same launch) wrote earlier in the
+// launch, as the resident team loop does across steps and runs: COH loads go through L2 (ld.global.cg),
+// never through the read-only path, whose lines may be stale within a launch.
+template <bool COH, class T>
+__device__ __forceinline__ T ldx(const T *p)
+{
+    if constexpr (COH)
+        return __ldcg(p);
+    else
+        return *p;
+}
+
 // Post-stream populations of node (x, y, z) gathered from the post-collision buffer.  The source of
 // direction i is node (x - c_x, y - c_y, z - c_z) with periodic wrap: its index is the node's plus
 // one offset per axis, set once for the node's position.
-template <class P, int Q>
+template <class P, int Q, bool COH = false>
 __device__ __forceinline__ void gather(const typename P::T *__restrict__ src, const Geo &g, int mode, int x, int y,
                                        int z, long long node, typename P::T *f)
 {
     if (mode == 1) {
 #pragma unroll
-        for (int i = 0; i < Q; i++) f[i] = src[(long long)i * g.plane + node];
+        for (int i = 0; i < Q; i++) f[i] = ldx<COH>(src + (long long)i * g.plane + node);
         return;
     }
     const long long nx = g.nx, nxy = (long long)g.nx * g.ny;
@@ -237,12 +249,12 @@ __device__ __forceinline__ void gather(const typename P::T *__restrict__ src, co
         const int cx = Lat<Q>::cx(i), cy = Lat<Q>::cy(i), cz = Lat<Q>::cz(i);
         const long long s = node + (cx == 1 ? xm : (cx == -1 ? xp : 0)) + (cy == 1 ? ym : (cy == -1 ? yp : 0)) +
                             (cz == 1 ? zm : (cz == -1 ? zp : 0));
-        const typename P::T pulled = src[(long long)i * g.plane + s];
+        const typename P::T pulled = ldx<COH>(src + (long long)i * g.plane + s);
         if (g.solid != nullptr) {
             // both candidates are loaded before the solid byte is known (every address is a node of
             // the box), so the loads do not wait for the mask
-            const typename P::T back = src[(long long)Lat<Q>::opp(i) * g.plane + node];
-            f[i] = g.solid[s] ? back : pulled;
+            const typename P::T back = ldx<COH>(src + (long long)Lat<Q>::opp(i) * g.plane + node);
+            f[i] = ldx<COH>(g.solid + s) ? back : pulled;
         } else {
             f[i] = pulled;
         }
@@ -281,7 +293,7 @@ __device__ __forceinline__ void apply_inlet(typename P::T *f, const Geo &g, cons
 }
 
 // Populations of fluid node (x, y, z) after this step's inlet and outlet planes.
-template <class P, int Q>
+template <class P, int Q, bool COH = false>
 __device__ void state_after_x_planes(const typename P::T *__restrict__ src, const Geo &g, const BCp &bc, int mode,
                                      int x, int y, int z, long long node, typename P::T *f)
 {
@@ -289,21 +301,21 @@ __device__ void state_after_x_planes(const typename P::T *__restrict__ src, cons
     if (x == bc.outlet_x) {
         const int xn = x + ((bc.outlet_x < g.nx / 2) ? 1 : -1);
         const long long nn = node + (xn - x);
-        const bool nsolid = g.solid != nullptr && g.solid[nn];
+        const bool nsolid = g.solid != nullptr && ldx<COH>(g.solid + nn);
         if (bc.outlet_kind == 0) {  // devnull_rho_x: the inner neighbour, rescaled
             if (nsolid) {
                 P::template rest<Q>(f, bc.rho_out);
                 return;
             }
-            gather<P, Q>(src, g, mode, xn, y, z, nn, f);
+            gather<P, Q, COH>(src, g, mode, xn, y, z, nn, f);
             if (xn == bc.inlet_x) apply_inlet<P, Q>(f, g, bc, y, z);
             P::template outlet<Q>(f, bc.rho_out);
             return;
         }
-        gather<P, Q>(src, g, mode, x, y, z, node, f);
+        gather<P, Q, COH>(src, g, mode, x, y, z, node, f);
         if (nsolid) return;  // the reference reads no neighbour there (it would read outside the array)
         T a[Q];
-        gather<P, Q>(src, g, mode, xn, y, z, nn, a);
+        gather<P, Q, COH>(src, g, mode, xn, y, z, nn, a);
         if (xn == bc.inlet_x) apply_inlet<P, Q>(a, g, bc, y, z);
         if (bc.outlet_kind == 1) {
             if constexpr (Q == 9) {  // OpenBoundaryD2Q9_x: the populations entering from outside
@@ -322,23 +334,23 @@ __device__ void state_after_x_planes(const typename P::T *__restrict__ src, cons
         }
         return;
     }
-    gather<P, Q>(src, g, mode, x, y, z, node, f);
+    gather<P, Q, COH>(src, g, mode, x, y, z, node, f);
     if (x == bc.inlet_x) apply_inlet<P, Q>(f, g, bc, y, z);
 }
 
 // Post-boundary populations of fluid node (x, y, z): the x planes, then OpenBoundaryD2Q9_y.
-template <class P, int Q>
+template <class P, int Q, bool COH = false>
 __device__ void state_after_planes(const typename P::T *__restrict__ src, const Geo &g, const BCp &bc, int mode, int x,
                                    int y, int z, long long node, typename P::T *f)
 {
-    state_after_x_planes<P, Q>(src, g, bc, mode, x, y, z, node, f);
+    state_after_x_planes<P, Q, COH>(src, g, bc, mode, x, y, z, node, f);
     if constexpr (Q == 9) {
         if (y != bc.open_y) return;
         const int yn = y + ((bc.open_y < g.ny / 2) ? 1 : -1);
         const long long nn = node + (long long)(yn - y) * g.nx;
-        if (g.solid != nullptr && g.solid[nn]) return;
+        if (g.solid != nullptr && ldx<COH>(g.solid + nn)) return;
         typename P::T a[Q];
-        state_after_x_planes<P, Q>(src, g, bc, mode, x, yn, z, nn, a);
+        state_after_x_planes<P, Q, COH>(src, g, bc, mode, x, yn, z, nn, a);
         if (yn > y) {
             f[3] = a[3];
             f[5] = a[5];
@@ -355,11 +367,54 @@ __device__ void state_after_planes(const typename P::T *__restrict__ src, const 
 // Generic step kernel: any box, solid mask, boundary planes, density check
 // ------------------------------------------------------------------------------------------------
 
+// One node of one step: state after the planes, collision, the density check, store.  rho_bits and
+// flag return the check's outcome (|rho| as a bit pattern; 1 above the limit, 2 non-finite).  The body
+// of k_step, shared with the resident team loop so that both give the same bits.
+template <class P, int Q, int OP, bool COH = false>
+__device__ __forceinline__ void step_node(const typename P::T *__restrict__ src, typename P::T *__restrict__ dst,
+                                          const Geo &g, const BCp &bc, const CollParams &prm, int mode,
+                                          int check_density, double density_limit, long long node,
+                                          unsigned long long &rho_bits, int &flag)
+{
+    using T = typename P::T;
+    int x, y, z;
+    node_xyz(g, node, x, y, z);
+    T f[Q];
+    state_after_planes<P, Q, COH>(src, g, bc, mode, x, y, z, node, f);
+    P::template collide<Q, OP>(f, prm);
+    if (check_density) {
+        const double rho = P::template density<Q>(f);
+        if (!isfinite(rho)) {
+            flag = 2;
+        } else {
+            const double ar = fabs(rho);
+            rho_bits = (unsigned long long)__double_as_longlong(ar);
+            if (ar > density_limit) flag = 1;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < Q; i++) dst[(long long)i * g.plane + node] = f[i];
+}
+
+// The density check's warp reduction: lane 0 folds the warp's outcome into the run status.  Every
+// lane of the warp calls it.
+__device__ __forceinline__ void report_density(RunStatus *status, int step_index, unsigned long long rho_bits, int flag)
+{
+    const unsigned long long m = warp_max_u64(rho_bits);
+    const int any = __reduce_or_sync(0xffffffffu, flag);
+    if ((threadIdx.x & 31) == 0) {
+        if (m) atomicMax(&status->max_abs_rho_bits, m);
+        if (any) {
+            atomicOr(&status->flags, any);
+            atomicMin(&status->decided_step, step_index);
+        }
+    }
+}
+
 template <class P, int Q, int OP>
 __global__ void __launch_bounds__(256) k_step(const typename P::T *__restrict__ src, typename P::T *__restrict__ dst,
                                               Geo g, BCp bc, CollParams prm, StepArgs a)
 {
-    using T = typename P::T;
     if (a.stop_on_flag && a.status != nullptr) {
         // A check failed in an EARLIER step: nothing to do.  (Blocks of the failing step itself
         // still finish it, as the reference finishes the step in which it flags a node.)  One
@@ -372,36 +427,9 @@ __global__ void __launch_bounds__(256) k_step(const typename P::T *__restrict__ 
     if (active && g.solid != nullptr && g.solid[node]) active = false;
     unsigned long long rho_bits = 0;
     int flag = 0;
-    if (active) {
-        int x, y, z;
-        node_xyz(g, node, x, y, z);
-        T f[Q];
-        state_after_planes<P, Q>(src, g, bc, a.mode, x, y, z, node, f);
-        P::template collide<Q, OP>(f, prm);
-        if (a.check_density) {
-            const double rho = P::template density<Q>(f);
-            if (!isfinite(rho)) {
-                flag = 2;
-            } else {
-                const double ar = fabs(rho);
-                rho_bits = (unsigned long long)__double_as_longlong(ar);
-                if (ar > a.density_limit) flag = 1;
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < Q; i++) dst[(long long)i * g.plane + node] = f[i];
-    }
-    if (a.check_density) {
-        const unsigned long long m = warp_max_u64(rho_bits);
-        const int any = __reduce_or_sync(0xffffffffu, flag);
-        if ((threadIdx.x & 31) == 0) {
-            if (m) atomicMax(&a.status->max_abs_rho_bits, m);
-            if (any) {
-                atomicOr(&a.status->flags, any);
-                atomicMin(&a.status->decided_step, a.step_index);
-            }
-        }
-    }
+    if (active)
+        step_node<P, Q, OP>(src, dst, g, bc, prm, a.mode, a.check_density, a.density_limit, node, rho_bits, flag);
+    if (a.check_density) report_density(a.status, a.step_index, rho_bits, flag);
 }
 
 template <class P, int Q>
@@ -444,6 +472,26 @@ __global__ void __launch_bounds__(256) k_soa_to_aos(Geo g, long long n_fluid, co
     const long long node = nof ? nof[p] : p;
 #pragma unroll
     for (int i = 0; i < Q; i++) aos[p * Q + i] = P::template to_f<Q>(soa[(long long)i * g.plane + node], i);
+}
+
+// Kinetic energy of fluid index p: of the post-stream state (pull from buf) when `stream`, else of the
+// populations in buf.  k_stream_only followed by k_node_fields, for one node.
+template <class P, int Q, bool COH = false>
+__device__ __forceinline__ double node_energy_at(const typename P::T *buf, const Geo &g, const int *nof, long long p,
+                                                 bool stream)
+{
+    using T = typename P::T;
+    const long long node = nof ? ldx<COH>(nof + p) : p;
+    T f[Q];
+    if (stream) {
+        int x, y, z;
+        node_xyz(g, node, x, y, z);
+        gather<P, Q, COH>(buf, g, 0, x, y, z, node, f);
+    } else {
+#pragma unroll
+        for (int i = 0; i < Q; i++) f[i] = ldx<COH>(buf + (long long)i * g.plane + node);
+    }
+    return P::template energy<Q>(f);
 }
 
 template <class P, int Q>
@@ -627,22 +675,20 @@ namespace erlbm {
 // inicializa_taylor_green (main_taylor-green.cpp:57-100), D2Q9, Poisson density and f_eq + f1.
 // tab: [s2 | c2 | c4 | ck] of L doubles each: sin(2 pi x / L), cos(2 pi x / L), cos(4 pi x / L),
 // cos(k x) with k = 2 pi / L, evaluated as the reference writes them.
-template <class P>
-__global__ void __launch_bounds__(256) k_init_tg2d(typename P::T *buf, Geo g, const double *__restrict__ tab,
-                                                   double u0, double tau, double k)
+template <class P, bool COH = false>
+__device__ __forceinline__ void init_tg2d_node(typename P::T *buf, const Geo &g, const double *tab, double u0,
+                                               double tau, double k, long long node)
 {
-    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int L = g.nx;
-    if (node >= g.nbox) return;
     const int x = (int)(node % L), y = (int)(node / L);
     const double *s2 = tab, *c2 = tab + L, *c4 = tab + 2 * L, *ck = tab + 3 * L;
     const double cs2 = 1. / 3.;
-    const double rho = 1.0 + 0.75 * u0 * u0 * (c4[x] + c4[y]);
-    const double ux = u0 * s2[x] * c2[y];
-    const double uy = -u0 * c2[x] * s2[y];
+    const double rho = 1.0 + 0.75 * u0 * u0 * (ldx<COH>(c4 + x) + ldx<COH>(c4 + y));
+    const double ux = u0 * ldx<COH>(s2 + x) * ldx<COH>(c2 + y);
+    const double uy = -u0 * ldx<COH>(c2 + x) * ldx<COH>(s2 + y);
     double f[9];
     exact::equilibrium9(rho, ux, uy, f);
-    const double Sxx = 2. * u0 * k * ck[x] * ck[y];
+    const double Sxx = 2. * u0 * k * ldx<COH>(ck + x) * ldx<COH>(ck + y);
     const double Pxx = -rho * cs2 * tau * Sxx;
     const double Pyy = -Pxx;
 #pragma unroll
@@ -654,35 +700,57 @@ __global__ void __launch_bounds__(256) k_init_tg2d(typename P::T *buf, Geo g, co
     for (int i = 0; i < 9; i++) buf[(long long)i * g.plane + node] = P::template from_f<9>(f[i], i);
 }
 
-// Three-dimensional Taylor-Green equilibrium (no driver in the reference; defined here):
-// rho = 1, u = U0 (sin kx cos ky cos kz, -cos kx sin ky cos kz, 0).  tab: [s | c] of L doubles.
 template <class P>
-__global__ void __launch_bounds__(256) k_init_tg3d(typename P::T *buf, Geo g, const double *__restrict__ tab,
-                                                   double u0)
+__global__ void __launch_bounds__(256) k_init_tg2d(typename P::T *buf, Geo g, const double *__restrict__ tab,
+                                                   double u0, double tau, double k)
 {
     const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= g.nbox) return;
+    init_tg2d_node<P>(buf, g, tab, u0, tau, k, node);
+}
+
+// Three-dimensional Taylor-Green equilibrium (no driver in the reference; defined here):
+// rho = 1, u = U0 (sin kx cos ky cos kz, -cos kx sin ky cos kz, 0).  tab: [s | c] of L doubles.
+template <class P, bool COH = false>
+__device__ __forceinline__ void init_tg3d_node(typename P::T *buf, const Geo &g, const double *tab, double u0,
+                                               long long node)
+{
     const int L = g.nx;
     const int x = (int)(node % L);
     const long long r = node / L;
     const int y = (int)(r % g.ny), z = (int)(r / g.ny);
     const double *s = tab, *c = tab + L;
-    const double ux = u0 * s[x] * c[y] * c[z];
-    const double uy = -u0 * c[x] * s[y] * c[z];
+    const double ux = u0 * ldx<COH>(s + x) * ldx<COH>(c + y) * ldx<COH>(c + z);
+    const double uy = -u0 * ldx<COH>(c + x) * ldx<COH>(s + y) * ldx<COH>(c + z);
     double f[19];
     exact::equilibrium19(1.0, ux, uy, 0.0, f);
 #pragma unroll
     for (int i = 0; i < 19; i++) buf[(long long)i * g.plane + node] = P::template from_f<19>(f[i], i);
 }
 
+template <class P>
+__global__ void __launch_bounds__(256) k_init_tg3d(typename P::T *buf, Geo g, const double *__restrict__ tab,
+                                                   double u0)
+{
+    const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= g.nbox) return;
+    init_tg3d_node<P>(buf, g, tab, u0, node);
+}
+
 // Rest equilibrium f_i = w_i rho on every fluid node (main_stability-map_obstacle.cpp:81-82).
+template <class P, int Q>
+__device__ __forceinline__ void init_rest_node(typename P::T *buf, const Geo &g, double rho, long long node)
+{
+#pragma unroll
+    for (int i = 0; i < Q; i++) buf[(long long)i * g.plane + node] = P::template from_f<Q>(Lat<Q>::w(i) * rho, i);
+}
+
 template <class P, int Q>
 __global__ void __launch_bounds__(256) k_init_rest(typename P::T *buf, Geo g, double rho)
 {
     const long long node = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= g.nbox) return;
-#pragma unroll
-    for (int i = 0; i < Q; i++) buf[(long long)i * g.plane + node] = P::template from_f<Q>(Lat<Q>::w(i) * rho, i);
+    init_rest_node<P, Q>(buf, g, rho, node);
 }
 
 template <class P>

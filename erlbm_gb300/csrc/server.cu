@@ -8,14 +8,21 @@
 //               claim requests from a ring in mapped pinned memory as soon as the host publishes
 //               them, run each to completion in shared memory and publish the result.  Idle CTAs
 //               poll with a bounded wait and exit; the scheduler relaunches the loop on demand.
+//  team lane    D2Q9 Taylor-Green up to 512^2, D3Q19 Taylor-Green up to 64^3, the obstacle channel
+//               scaled by more than 1 (team_lane.cuh).  A second persistent kernel per precision:
+//               its admitter claims requests from another ring and admits them on the device by
+//               HBM footprint (pages of the team arena); its CTAs join the admitted runs and work
+//               through their items (chunks of nodes per step), and publish the results.  No host
+//               launch per run or per step.
 //  stream lane  every larger lattice.  Each admitted run gets device memory from a fixed HBM arena
 //               (admission is by footprint: a request waits until its populations, scratch and
 //               status fit), its own non-blocking CUDA stream, and is advanced in chunks of steps;
 //               runs on different streams overlap on the device.
 //
 // One scheduler thread issues every CUDA call (no allocation or device-wide synchronisation after
-// start-up, so nothing ever waits for the resident loop).  Results are deterministic: the lane a
-// request takes depends only on the request, so a run gives the same result alone and in a mix.
+// start-up, so nothing ever waits for the resident loops).  Results are deterministic: the lane a
+// request takes depends only on the request and the server's configuration, and the team and stream
+// lanes give the same bits, so a run gives the same result alone and in a mix.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -35,6 +42,7 @@
 #include "abi_internal.h"
 #include "batch_kernels.cuh"
 #include "kernels_api.h"
+#include "team_lane.cuh"
 
 using namespace erlbm;
 
@@ -135,6 +143,27 @@ struct StreamSlot {
     double *h_out = nullptr;  // pinned: [0] energy, [2..3] RunStatus
 };
 
+// The team lane of one precision: its ring of requests and results in mapped pinned memory and the
+// device state of its resident launch.
+struct TeamLane {
+    int prec = 0;
+    TeamEntry *h_entries = nullptr;
+    unsigned char *h_payload = nullptr;  // mapped: TEAM_PAYLOAD bytes per ring entry
+    TeamDone *h_done = nullptr;
+    int *h_tail = nullptr;  // [0] tail, [1] stop
+    TeamRing ring{};
+    TeamCtl *d_ctl = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t exited = nullptr;
+    bool running = false;
+    int published = 0, grid = 0;
+    std::unordered_map<int, int64_t> ticket_of;  // ring index -> ticket
+    std::vector<int> outstanding;
+};
+
+constexpr int TEAM_CAPACITY = 128;            // ring entries per team lane
+constexpr long long TEAM_PAYLOAD = 64 << 10;  // payload bytes per ring entry
+
 struct Job {
     int64_t ticket = 0;
     StreamSlot *slot = nullptr;
@@ -178,6 +207,13 @@ struct erlbm_server {
     Clock::time_point t0;
     Arena arena;
     SlotLane lane[2];
+    TeamLane team[2];             // [0] FP64, [1] FP32-shifted
+    char *team_arena = nullptr;   // pages of the team lanes
+    unsigned *d_pages = nullptr;  // their bitmap
+    int team_pages = 0;
+    double team_clock = 0;        // server clock minus the device clock (s)
+    int team_jobs = TEAM_MAX_JOBS;  // runs admitted at a time per team loop
+    std::deque<std::pair<int64_t, erlbm_request>> pending_c[2];  // team-lane requests waiting for ring space
     BatchGeo geos_host[2]{};
     uint8_t *d_obst_solid = nullptr;
     double *d_tg_tab = nullptr;
@@ -298,8 +334,9 @@ int lane_launch(SlotLane &L)
 int lane_submit(erlbm_server *s, SlotLane &L, int64_t ticket, const erlbm_request &q)
 {
     const int cap = s->desc.queue_capacity;
-    if ((int)L.outstanding.size() >= cap) return 1;  // ring full: retry later
     const int idx = L.published;
+    // ring full, or the entry a lap back (whose slot this one reuses) not collected yet: retry later
+    if ((int)L.outstanding.size() >= cap || L.ticket_of.count(idx - cap)) return 1;
     SlotEntry &e = L.h_entries[idx % cap];
     memset(&e, 0, sizeof(e));
     e.run.R = make_relax(q.tau, q.tau_nh, q.op);
@@ -344,6 +381,241 @@ void lane_collect(erlbm_server *s, SlotLane &L)
     }
     if (L.running && cudaEventQuery(L.exited) == cudaSuccess) L.running = false;
     if (!L.running && !L.outstanding.empty() && !s->stopping.load()) lane_launch(L);
+}
+
+// ---- team lane --------------------------------------------------------------------------------
+
+int team_setup(erlbm_server *s, TeamLane &L, int prec)
+{
+    L.prec = prec;
+    const int occ = prec == ERLBM_FP64 ? team_server_occupancy_fp64() : team_server_occupancy_fp32();
+    // one CTA (128 threads, 128 registers) per SM and precision: with both loops resident, half of each
+    // SM's registers stay free for a slot loop's CTA
+    const int want = s->desc.team_ctas > 0 ? s->desc.team_ctas : s->sms;
+    L.grid = occ > 0 && s->desc.team_ctas >= 0 ? std::min(std::max(2, want), TEAM_MAX_GRID) : 0;
+    if (L.grid < 2) {
+        L.grid = 0;  // no resident team loop: these requests take the stream lane
+        return ERLBM_OK;
+    }
+    cudaError_t e;
+    if ((e = cudaHostAlloc(&L.h_entries, TEAM_CAPACITY * sizeof(TeamEntry), cudaHostAllocMapped)) != cudaSuccess ||
+        (e = cudaHostAlloc(&L.h_payload, TEAM_CAPACITY * TEAM_PAYLOAD, cudaHostAllocMapped)) != cudaSuccess ||
+
+        (e = cudaHostAlloc(&L.h_done, TEAM_CAPACITY * sizeof(TeamDone), cudaHostAllocMapped)) != cudaSuccess ||
+        (e = cudaHostAlloc(&L.h_tail, 64, cudaHostAllocMapped)) != cudaSuccess)
+        return cuda_fail(e, "team ring");
+    memset(L.h_done, 0, TEAM_CAPACITY * sizeof(TeamDone));
+    memset(L.h_tail, 0, 64);
+    L.d_ctl = (TeamCtl *)s->arena.alloc(sizeof(TeamCtl));
+    TeamQueue *q = (TeamQueue *)s->arena.alloc(sizeof(TeamQueue));
+    TeamJob *jobs = (TeamJob *)s->arena.alloc(TEAM_MAX_JOBS * sizeof(TeamJob));
+    if (!L.d_ctl || !q || !jobs) {
+        set_error("server arena too small for the team lane%s%s", "", "");
+        return ERLBM_E_OOM;
+    }
+    if ((e = cudaMemset(q, 0, sizeof(TeamQueue))) != cudaSuccess) return cuda_fail(e, "team queue");
+    TeamEntry *de;
+    unsigned char *dp;
+    TeamDone *dd;
+    int *dt;
+    if ((e = cudaHostGetDevicePointer(&de, L.h_entries, 0)) != cudaSuccess ||
+        (e = cudaHostGetDevicePointer(&dp, L.h_payload, 0)) != cudaSuccess ||
+        (e = cudaHostGetDevicePointer(&dd, L.h_done, 0)) != cudaSuccess ||
+        (e = cudaHostGetDevicePointer(&dt, L.h_tail, 0)) != cudaSuccess)
+        return cuda_fail(e, "team ring mapping");
+    TeamRing &r = L.ring;
+    r.tail = dt;
+    r.stop = dt + 1;
+    r.entries = de;
+    r.payload = dp;
+    r.done = dd;
+    r.payload_stride = TEAM_PAYLOAD;
+    r.capacity = TEAM_CAPACITY;
+    r.max_jobs = s->team_jobs;
+    r.queue = q;
+    r.ctl = L.d_ctl;
+    r.jobs = jobs;
+    r.pages = s->d_pages;
+    r.arena = s->team_arena;
+    r.n_pages = s->team_pages;
+    r.idle_ns = 300000000LL;  // an idle launch leaves after 0.3 s
+    r.sync_ns = 5000000000LL; // a team barrier gives up after 5 s
+    if ((e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&L.exited, cudaEventDisableTiming)) != cudaSuccess)
+        return cuda_fail(e, "team lane stream");
+    return ERLBM_OK;
+}
+
+int team_launch(TeamLane &L)
+{
+    cudaError_t e = cudaMemsetAsync(L.d_ctl, 0, sizeof(TeamCtl), L.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "team lane reset");
+    const int rc = L.prec == ERLBM_FP64 ? launch_team_server_fp64(L.ring, L.grid, L.stream)
+                                        : launch_team_server_fp32(L.ring, L.grid, L.stream);
+    if (rc) return cuda_fail(cudaGetLastError(), "team loop launch");
+    cudaEventRecord(L.exited, L.stream);
+    L.running = true;
+    return ERLBM_OK;
+}
+
+// Layout of a team-lane run: its arena bytes (buffers, energies, tables, mask, fluid list) and its
+// payload (tables, mask, fluid list) in the ring slot.  Returns false when the request does not go to
+// the team lane: too large for the lane, the payload slot or the team arena.
+bool team_plan(const erlbm_server *s, const erlbm_request &q, TeamEntry &e, std::vector<uint8_t> *solid_out)
+{
+    const TeamLane &L = s->team[q.precision == ERLBM_FP64 ? 0 : 1];
+    if (L.grid < 2) return false;
+    const long long max_nodes = s->desc.team_max_nodes > 0 ? s->desc.team_max_nodes : 65536;
+    memset(&e, 0, sizeof(e));
+    std::vector<uint8_t> solid;
+    switch (q.kind) {
+    case ERLBM_REQ_TG2D:
+        if (q.L > 512) return false;
+        e.q = 9;
+        e.nx = e.ny = q.L;
+        e.nz = 1;
+        e.init = 1;
+        e.tab_len = 4 * q.L;
+        e.k = 2. * M_PI / (double)q.L;
+        break;
+    case ERLBM_REQ_TG3D:
+        if (q.L > 64) return false;
+        e.q = 19;
+        e.nx = e.ny = e.nz = q.L;
+        e.init = 4;
+        e.tab_len = 2 * q.L;
+        break;
+    case ERLBM_REQ_OBSTACLE: {
+        int nx, ny;
+        erlbm_obstacle_geometry(std::max(1, q.sx), std::max(1, q.sy), &nx, &ny, nullptr);
+        if ((long long)nx * ny > (1 << 19)) return false;
+        solid.resize((size_t)nx * ny);
+        erlbm_obstacle_geometry(std::max(1, q.sx), std::max(1, q.sy), &nx, &ny, solid.data());
+        e.q = 19;
+        e.nx = nx;
+        e.ny = ny;
+        e.nz = 1;
+        e.init = 0;
+        e.check_density = 1;
+        e.inlet_x = 1;
+        e.outlet_x = nx - 2;
+        break;
+    }
+    default:
+        return false;
+    }
+    if (q.kind != ERLBM_REQ_OBSTACLE) e.inlet_x = e.outlet_x = -1;
+    const long long nbox = (long long)e.nx * e.ny * e.nz, plane = (nbox + 63) / 64 * 64;
+    if (nbox > max_nodes) return false;
+    long long n_fluid = nbox;
+    if (!solid.empty()) {
+        n_fluid = 0;
+        for (uint8_t v : solid) n_fluid += v ? 0 : 1;
+    }
+    auto al = [](long long b) { return (b + 255) / 256 * 256; };
+    auto al16 = [](long long b) { return (b + 15) / 16 * 16; };
+    const long long pop = (long long)e.q * plane * (q.precision == ERLBM_FP64 ? 8 : 4);
+    e.off_buf1 = al(pop);
+    e.off_scr = e.off_buf1 + al(pop);
+    e.off_pay = e.off_scr + al((n_fluid + 4096) * 8);  // energies, then the partial sums
+    e.solid_len = (int)solid.size();
+    e.pay_solid = al16(e.tab_len * 8LL);
+    e.pay_nof = e.pay_solid + al16(e.solid_len);
+    const long long pay = al16(solid.empty() ? e.tab_len * 8LL : e.pay_nof + n_fluid * 4);
+    if (pay > TEAM_PAYLOAD) return false;
+    e.pay_bytes = pay;
+    const long long bytes = e.off_pay + pay;
+    const long long pages = (bytes + TEAM_PAGE - 1) / TEAM_PAGE;
+    if (pages > s->team_pages) return false;
+    e.pages = (int)pages;
+    e.n_fluid = (int)n_fluid;
+    e.prm.R = make_relax(q.tau, q.tau_nh, q.op);
+    e.prm.k = shifted::make_coef(e.prm.R);
+    e.u0 = q.u0;
+    e.tau = q.tau;
+    e.op = q.op;
+    e.n_steps = q.n_steps;
+    // nodes per work item: 2 (FP64) or 8 (FP32) per thread of a CTA; small FP64 items spread a small
+    // lattice's step over more CTAs
+    e.chunk = q.precision == ERLBM_FP64 ? 256 : 1024;
+    if (solid_out) solid_out->swap(solid);
+    return true;
+}
+
+double estimate_seconds(const erlbm_request &q);
+
+int team_submit(erlbm_server *s, TeamLane &L, int64_t ticket, const erlbm_request &q)
+{
+    const int cap = TEAM_CAPACITY;
+    const int idx = L.published;
+    if ((int)L.outstanding.size() >= cap || L.ticket_of.count(idx - cap)) return 1;
+    TeamEntry e;
+    std::vector<uint8_t> solid;
+    if (!team_plan(s, q, e, &solid)) return -1;
+    e.est_ns = (long long)(estimate_seconds(q) * 1e9);
+    // the payload slot is free: its previous request was collected
+    unsigned char *pl = L.h_payload + (size_t)(idx % cap) * TEAM_PAYLOAD;
+    double *tab = (double *)pl;
+    const double Lx = (double)e.nx;
+    if (e.init == 1) {
+        const int n = e.nx;
+        for (int x = 0; x < n; x++) {  // the stream lane's tables (job_admit)
+            tab[x] = sin(2. * M_PI * x / Lx);
+            tab[n + x] = cos(2. * M_PI * x / Lx);
+            tab[2 * n + x] = cos(4. * M_PI * x / Lx);
+            tab[3 * n + x] = cos(e.k * x);
+        }
+    } else if (e.init == 4) {
+        const int n = e.nx;
+        for (int x = 0; x < n; x++) {
+            tab[x] = sin(2. * M_PI * (double)x / Lx);
+            tab[n + x] = cos(2. * M_PI * (double)x / Lx);
+        }
+    }
+    if (!solid.empty()) {
+        memcpy(pl + e.pay_solid, solid.data(), solid.size());
+        int *nof = (int *)(pl + e.pay_nof);
+        int k = 0;
+        for (size_t i = 0; i < solid.size(); i++)
+            if (!solid[i]) nof[k++] = (int)i;
+    }
+    L.h_entries[idx % cap] = e;
+    L.h_done[idx % cap].seq = 0;
+    L.published = idx + 1;
+    __atomic_store_n(&L.h_tail[0], L.published, __ATOMIC_RELEASE);
+    L.ticket_of[idx] = ticket;
+    L.outstanding.push_back(idx);
+    return 0;
+}
+
+void team_collect(erlbm_server *s, TeamLane &L)
+{
+    const int cap = TEAM_CAPACITY;
+    for (size_t k = 0; k < L.outstanding.size();) {
+        const int idx = L.outstanding[k];
+        TeamDone &d = L.h_done[idx % cap];
+        if (__atomic_load_n(&d.seq, __ATOMIC_ACQUIRE) == idx + 1) {
+            erlbm_result r;
+            memset(&r, 0, sizeof(r));
+            r.status = d.status ? ERLBM_E_CUDA : ERLBM_OK;
+            r.label = d.label;
+            r.steps_done = d.steps_done;
+            r.decided_step = d.decided_step;
+            r.energy = d.energy;
+            r.margin = d.margin;
+            r.lane = 2;
+            r.t_admit = (double)d.t_admit_ns * 1e-9 + s->team_clock;
+            const int64_t t = L.ticket_of[idx];
+            L.ticket_of.erase(idx);
+            finish(s, t, r);
+            L.outstanding[k] = L.outstanding.back();
+            L.outstanding.pop_back();
+        } else {
+            ++k;
+        }
+    }
+    if (L.running && cudaEventQuery(L.exited) == cudaSuccess) L.running = false;
+    if (!L.running && !L.outstanding.empty() && !s->stopping.load()) team_launch(L);
 }
 
 // ---- stream lane ------------------------------------------------------------------------------
@@ -710,7 +982,8 @@ void scheduler(erlbm_server *s)
             std::unique_lock<std::mutex> lk(s->mu);
             const bool idle = s->active.empty() && s->pending_b.empty() && s->pending_a[0].empty() &&
                               s->pending_a[1].empty() && s->lane[0].outstanding.empty() &&
-                              s->lane[1].outstanding.empty();
+                              s->lane[1].outstanding.empty() && s->pending_c[0].empty() && s->pending_c[1].empty() &&
+                              s->team[0].outstanding.empty() && s->team[1].outstanding.empty();
             if (idle && s->inbox.empty()) {
                 if (s->stopping.load()) break;
                 s->cv_work.wait_for(lk, std::chrono::milliseconds(2));
@@ -720,8 +993,11 @@ void scheduler(erlbm_server *s)
         }
         for (size_t k = 0; k < in.size(); k++) {
             auto &p = in[k];
+            TeamEntry te;
             if (slot_eligible(p.second)) {
                 s->pending_a[p.second.precision == ERLBM_FP64 ? 0 : 1].push_back(p);
+            } else if (team_plan(s, p.second, te, nullptr)) {
+                s->pending_c[p.second.precision == ERLBM_FP64 ? 0 : 1].push_back(p);
             } else {
                 Pending q;
                 q.ticket = p.first;
@@ -742,6 +1018,19 @@ void scheduler(erlbm_server *s)
             }
             if (any && !L.running) lane_launch(L);
         }
+        // publish team-lane requests while their ring has space; the device admits them
+        for (int l = 0; l < 2; l++) {
+            TeamLane &L = s->team[l];
+            bool any = false;
+            while (!s->pending_c[l].empty()) {
+                const int rc = team_submit(s, L, s->pending_c[l].front().first, s->pending_c[l].front().second);
+                if (rc == 1) break;
+                if (rc != 0) finish(s, s->pending_c[l].front().first, error_result(rc < 0 ? rc : ERLBM_E_INVAL, 2));
+                s->pending_c[l].pop_front();
+                any = true;
+            }
+            if (any && !L.running) team_launch(L);
+        }
         // admit stream-lane runs while memory and streams allow
         admit_stream_lane(s);
         for (size_t k = 0; k < s->active.size();) {
@@ -754,15 +1043,24 @@ void scheduler(erlbm_server *s)
         }
         lane_collect(s, s->lane[0]);
         lane_collect(s, s->lane[1]);
+        team_collect(s, s->team[0]);
+        team_collect(s, s->team[1]);
         if (s->stopping.load() && s->active.empty() && s->pending_b.empty() && s->pending_a[0].empty() &&
-            s->pending_a[1].empty() && s->lane[0].outstanding.empty() && s->lane[1].outstanding.empty()) {
+            s->pending_a[1].empty() && s->lane[0].outstanding.empty() && s->lane[1].outstanding.empty() &&
+            s->pending_c[0].empty() && s->pending_c[1].empty() && s->team[0].outstanding.empty() &&
+            s->team[1].outstanding.empty()) {
             std::lock_guard<std::mutex> lk(s->mu);
             if (s->inbox.empty()) break;
         }
-        if (!s->active.empty()) std::this_thread::yield();
+        if (!s->active.empty() || !s->team[0].outstanding.empty() || !s->team[1].outstanding.empty())
+            std::this_thread::yield();
     }
     // leave the resident loops
     for (auto &L : s->lane) {
+        if (L.h_tail) __atomic_store_n(&L.h_tail[1], 1, __ATOMIC_RELEASE);
+        if (L.stream) cudaStreamSynchronize(L.stream);
+    }
+    for (auto &L : s->team) {
         if (L.h_tail) __atomic_store_n(&L.h_tail[1], 1, __ATOMIC_RELEASE);
         if (L.stream) cudaStreamSynchronize(L.stream);
     }
@@ -779,6 +1077,8 @@ int erlbm_server_start(const erlbm_server_desc *d, erlbm_server **out)
     std::unique_ptr<erlbm_server> s(new erlbm_server());
     if (d) s->desc = *d;
     if (s->desc.hbm_budget_bytes <= 0) s->desc.hbm_budget_bytes = 8LL << 30;
+    // max_streams given: it caps the team loops' runs too; by default 16 streams and 64 team runs
+    if (s->desc.max_streams > 0) s->team_jobs = std::min(s->desc.max_streams, TEAM_MAX_JOBS);
     if (s->desc.max_streams <= 0) s->desc.max_streams = 16;
     if (s->desc.queue_capacity <= 0) s->desc.queue_capacity = 1 << 16;
     cudaError_t e;
@@ -831,6 +1131,26 @@ int erlbm_server_start(const erlbm_server_desc *d, erlbm_server **out)
     density_bounds(ob);
     if ((rc = lane_setup(s.get(), s->lane[0], ERLBM_FP64))) return rc;
     if ((rc = lane_setup(s.get(), s->lane[1], ERLBM_FP32_SHIFTED))) return rc;
+    // the team lanes' pages: half of the budget
+    s->team_pages = (int)std::min<long long>(s->desc.hbm_budget_bytes / 2 / TEAM_PAGE, 1 << 20);
+    if (s->team_pages > 0) {
+        s->team_arena = (char *)s->arena.alloc((size_t)s->team_pages * TEAM_PAGE);
+        const size_t words = ((size_t)s->team_pages + 31) / 32;
+        s->d_pages = (unsigned *)s->arena.alloc(words * 4);
+        if (!s->team_arena || !s->d_pages) return ERLBM_E_OOM;
+        if ((e = cudaMemset(s->d_pages, 0, words * 4)) != cudaSuccess) return cuda_fail(e, "team pages");
+        if ((rc = team_setup(s.get(), s->team[0], ERLBM_FP64))) return rc;
+        if ((rc = team_setup(s.get(), s->team[1], ERLBM_FP32_SHIFTED))) return rc;
+        // the device clock against the server clock, for the team lanes' admission times
+        long long *h_clk = nullptr;
+        if ((e = cudaMallocHost(&h_clk, 64)) != cudaSuccess) return cuda_fail(e, "team clock");
+        const double t0 = s->now();
+        const int crc = launch_team_clock(h_clk, s->team[0].stream ? s->team[0].stream : 0);
+        e = cudaDeviceSynchronize();
+        const double t1 = s->now();
+        if (crc == 0 && e == cudaSuccess) s->team_clock = 0.5 * (t0 + t1) - (double)h_clk[0] * 1e-9;
+        cudaFreeHost(h_clk);
+    }
     for (int k = 0; k < s->desc.max_streams; k++) {
         StreamSlot *sl = new StreamSlot();
         s->all_streams.push_back(sl);
@@ -909,6 +1229,14 @@ int erlbm_server_stop(erlbm_server *s)
         if (L.stream) cudaStreamDestroy(L.stream);
         if (L.exited) cudaEventDestroy(L.exited);
         if (L.h_entries) cudaFreeHost(L.h_entries);
+        if (L.h_done) cudaFreeHost(L.h_done);
+        if (L.h_tail) cudaFreeHost(L.h_tail);
+    }
+    for (auto &L : s->team) {
+        if (L.stream) cudaStreamDestroy(L.stream);
+        if (L.exited) cudaEventDestroy(L.exited);
+        if (L.h_entries) cudaFreeHost(L.h_entries);
+        if (L.h_payload) cudaFreeHost(L.h_payload);
         if (L.h_done) cudaFreeHost(L.h_done);
         if (L.h_tail) cudaFreeHost(L.h_tail);
     }

@@ -329,10 +329,17 @@ int erlbm_read_geo(const char *path, int pts_in, int pts_out, int wall, int *nx,
  * slice of device memory and a scheduler thread; requests are admitted while others run:
  *  - D3Q19 lattices of <= 288 nodes (Taylor-Green map points, the obstacle channel at scale 1) go to
  *    a device-resident loop whose CTAs claim them from a ring as soon as they are published;
+ *  - D2Q9 and D3Q19 Taylor-Green lattices and the scaled obstacle channels of up to team_max_nodes
+ *    nodes go to a second device-resident loop (one per precision) that claims them from its own ring
+ *    and admits them on the device by memory footprint (pages of half the budget); its CTAs join the
+ *    admitted runs and work through their steps in chunks of nodes (lane 2);
  *  - larger lattices are admitted by memory footprint and advanced on their own CUDA streams.
  * The lane a request takes depends only on the request, so its result does not depend on the mix.
  * While a server runs, avoid calls that synchronise the whole device (erlbm_destroy frees memory)
- * on the same GPU: they wait until the resident loop idles out (about a second). */
+ * on the same GPU: they wait until the resident loop idles out (about a second).  The resident loops
+ * run on their own streams; set CUDA_DEVICE_MAX_CONNECTIONS=32 in the environment before the process
+ * creates its CUDA context, or work on a stream that shares a hardware queue with a resident loop
+ * waits until that loop leaves (the Python package sets it when imported). */
 #define ERLBM_REQ_TG2D 1          /* D2Q9 Taylor-Green L x L, inicializa_taylor_green init (main_taylor-green.cpp:57-100) */
 #define ERLBM_REQ_TG_MAP_POINT 2  /* D3Q19 16 x 16 x 1 map point, energy checks every 100 steps (TG map roda_ponto) */
 #define ERLBM_REQ_OBSTACLE 3      /* D3Q19 obstacle channel scaled (sx, sy), Zou-He inlet with u0, density checks */
@@ -344,8 +351,13 @@ typedef struct erlbm_server erlbm_server;
 typedef struct erlbm_server_desc {
     int64_t hbm_budget_bytes;   /* device memory for admitted lattices (default 8 GiB) */
     int slot_ctas;              /* CTAs of each resident loop (one per precision); 0 = SMs / 2 */
-    int max_streams;            /* concurrent stream-lane runs; 0 = 16 */
+    int max_streams;            /* concurrent stream-lane runs, and team-loop runs per precision; 0 = 16
+                                   stream-lane runs and 64 team-loop runs */
     int queue_capacity;         /* ring entries per resident loop; 0 = 65536 */
+    int team_ctas;              /* CTAs of each team loop (one per precision); 0 = SMs; < 0: no team
+                                   loop, its requests take the stream lane */
+    int team_max_nodes;         /* largest lattice (nodes) the team loops take; 0 = 65536.  Larger ones
+                                   take the stream lane, whose whole-GPU step launches run them faster */
 } erlbm_server_desc;
 
 typedef struct erlbm_request {
@@ -364,7 +376,7 @@ typedef struct erlbm_result {
                                    the last energy check (map points) */
     double margin;
     double t_submit, t_admit, t_done; /* seconds on the server clock (t_admit < 0: resident loop) */
-    int lane;                   /* 0 resident loop, 1 stream lane */
+    int lane;                   /* 0 resident loop, 1 stream lane, 2 resident team loop */
 } erlbm_result;
 
 int erlbm_server_start(const erlbm_server_desc *d, erlbm_server **s);

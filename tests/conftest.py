@@ -1,6 +1,9 @@
 import os
 import sys
 
+# before any CUDA context exists: the server's resident loops need their own hardware work queues
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

@@ -131,7 +131,7 @@ def test_stream_lane_admits_the_shortest_runs_first():
     """With one stream the stream lane admits by estimated work (shortest first, aging with the
     wait), not by arrival: small lattices submitted after a large one start before it."""
     m = E()
-    with m.Server(hbm_budget_bytes=1 << 30, max_streams=1) as srv:
+    with m.Server(hbm_budget_bytes=1 << 30, max_streams=1, team_ctas=-1) as srv:
         blocker = srv.submit(m.REQ_TG2D, m.FP64, L=256, tau=0.6, tau_nh=0.65, u0=0.05, n_steps=3000)
         big = srv.submit(m.REQ_TG3D, m.FP64, op=m.OP_EXTREG, L=64, tau=0.55, tau_nh=0.65, u0=0.05, n_steps=2000)
         small = [srv.submit(m.REQ_TG2D, m.FP32_SHIFTED, L=128, tau=0.6, tau_nh=0.65, u0=0.05, n_steps=100)
@@ -183,8 +183,9 @@ def tg3d_init(L, u0):
 
 @pytest.mark.parametrize("L,steps,exact", [(32, 40, True), (64, 6, False)])
 def test_tg3d_requests_match_oracle(L, steps, exact):
-    """Config-5 3-D Taylor-Green requests (D3Q19, L^3, FP64) through the server's stream lane: the
-    kinetic energy after the run equals the oracle's.  Up to 65536 nodes the device sums the energy
+    """Config-5 3-D Taylor-Green requests (D3Q19, L^3, FP64): 32^3 through the server's resident team
+    loop, 64^3 (above its default size limit) through the stream lane.  The kinetic energy after the run
+    equals the oracle's.  Up to 65536 nodes the device sums the energy
     serially in node order, as kinectic_energy does, so L = 32 matches bit for bit; L = 64 is a tree
     reduction, which agrees to the last digits only."""
     m = E()
@@ -192,7 +193,7 @@ def test_tg3d_requests_match_oracle(L, steps, exact):
     with m.Server(hbm_budget_bytes=1 << 30) as srv:
         r = srv.wait(srv.submit(m.REQ_TG3D, m.FP64, op=m.OP_EXTREG, L=L, tau=tau, tau_nh=tnh, u0=u0, n_steps=steps),
                      timeout=600)
-    assert r["status"] == 0 and r["steps_done"] == steps and r["lane"] == 1
+    assert r["status"] == 0 and r["steps_done"] == steps and r["lane"] == (2 if L ** 3 <= 65536 else 1)
     lat = O.Lattice(19, L, L, L, None, tau, tnh, O.OP_EXTREG)
     lat.set(tg3d_init(L, u0))
     lat.step(steps)
@@ -217,3 +218,90 @@ def test_scaled_obstacle_requests_match_oracle(scale):
             lab, dec, mg = O.obstacle_map_point(tau, tnh, u, sx=scale, sy=scale, max_steps=n)
             assert r["status"] == 0
             assert (r["label"], r["decided_step"], r["margin"]) == (lab, dec, mg), (i, j, r, lab, dec, mg)
+
+
+def team_requests(m):
+    """Requests of the resident team loop: D2Q9 Taylor-Green (energy summed serially up to 65536
+    nodes, as a tree above), D3Q19 Taylor-Green, obstacle channels scaled 2x and 3x with a stable and
+    an unstable point (density checks every step), in both precisions."""
+    reqs = []
+    for prec in (m.FP64, m.FP32_SHIFTED):
+        for L, steps in ((64, 120), (256, 40), (512, 6)):
+            u0 = 2.0 / L
+            reqs.append(dict(kind=m.REQ_TG2D, precision=prec, op=m.OP_EXTREG, L=L, tau=0.5 + 3 * u0 * L / 50.0,
+                             tau_nh=0.65, u0=u0, n_steps=steps))
+        reqs.append(dict(kind=m.REQ_TG3D, precision=prec, op=m.OP_REG, L=32, tau=0.55, tau_nh=1.0, u0=0.05,
+                         n_steps=30))
+        for (i, j), s in (((200, 399), 2), ((10, 0), 3)):
+            u, tau, tnh = m.obstacle_map_params(i, j)
+            reqs.append(dict(kind=m.REQ_OBSTACLE, precision=prec, op=m.OP_EXTREG, sx=s, sy=s, tau=tau, tau_nh=tnh,
+                             u0=u, n_steps=600))
+    reqs.append(dict(kind=m.REQ_TG2D, precision=m.FP64, op=m.OP_MRT, L=128, tau=0.6, tau_nh=0.65, u0=0.02,
+                     n_steps=50))
+    return reqs
+
+
+RESULT_KEYS = ("status", "label", "steps_done", "decided_step", "energy", "margin")
+
+
+def same(a, b):
+    return all(a[k] == b[k] or (np.isnan(a[k]) and np.isnan(b[k])) for k in RESULT_KEYS)
+
+
+def test_team_loop_results_equal_the_stream_lane():
+    """The resident team loop gives the stream lane's results bit for bit (the same per-node update,
+    density fold and energy reduction shape): each request alone on a server without team loop
+    (team_ctas < 0, lane 1) and on one whose team loop takes lattices up to 2^19 nodes (lane 2)."""
+    m = E()
+    reqs = team_requests(m)
+    with m.Server(hbm_budget_bytes=1 << 30, team_ctas=-1) as srv:
+        want = [srv.wait(srv.submit(**r), timeout=600) for r in reqs]
+    with m.Server(hbm_budget_bytes=1 << 30, team_max_nodes=1 << 19) as srv:
+        got = [srv.wait(srv.submit(**r), timeout=600) for r in reqs]
+    assert all(w["lane"] == 1 for w in want) and all(g["lane"] == 2 for g in got)
+    for r, w, g in zip(reqs, want, got):
+        assert w["status"] == 0, (r, w)
+        assert same(w, g), (r, w, g)
+    assert any(g["label"] == 1 for g in got) and any(g["label"] == 0 and g["margin"] > 0 for g in got)
+
+
+def test_team_loop_results_do_not_depend_on_the_team_size_or_the_mix():
+    """The same requests one at a time on a team loop of three worker CTAs (team_ctas = 4), and all at
+    once on the default loop, where each run is worked on by as many CTAs as join it: equal results,
+    bit for bit."""
+    m = E()
+    reqs = team_requests(m)
+    with m.Server(hbm_budget_bytes=1 << 30, team_ctas=4, team_max_nodes=1 << 19) as srv:
+        small = [srv.wait(srv.submit(**r), timeout=600) for r in reqs]
+    with m.Server(hbm_budget_bytes=1 << 30, team_max_nodes=1 << 19) as srv:
+        tickets = [srv.submit(**r) for r in reqs]
+        mixed = [srv.wait(t, timeout=600) for t in tickets]
+    for r, a, b in zip(reqs, small, mixed):
+        assert a["status"] == 0 and a["lane"] == 2 and b["lane"] == 2, (r, a)
+        assert same(a, b), (r, a, b)
+
+
+def test_team_loop_admits_by_footprint():
+    """With a budget whose team pages hold one 512^2 FP64 lattice at a time (38 MB of populations in a
+    64 MB team region), three of them run one after the other, while small requests are admitted
+    beside them; every run completes with the result it has alone."""
+    m = E()
+    L = 512
+    u0 = 2.0 / L
+    big = dict(kind=m.REQ_TG2D, precision=m.FP64, op=m.OP_EXTREG, L=L, tau=0.5 + 3 * u0 * L / 50.0, tau_nh=0.65,
+               u0=u0, n_steps=20)
+    small = dict(kind=m.REQ_TG2D, precision=m.FP64, op=m.OP_EXTREG, L=64, tau=0.56, tau_nh=0.65, u0=2 / 64,
+                 n_steps=200)
+    with m.Server(hbm_budget_bytes=128 << 20, team_max_nodes=1 << 19) as srv:
+        alone_big = srv.wait(srv.submit(**big), timeout=600)
+        alone_small = srv.wait(srv.submit(**small), timeout=600)
+        tb = [srv.submit(**big) for _ in range(3)]
+        ts = [srv.submit(**small) for _ in range(6)]
+        rb = [srv.wait(t, timeout=600) for t in tb]
+        rs = [srv.wait(t, timeout=600) for t in ts]
+    assert alone_big["lane"] == 2 and alone_small["lane"] == 2
+    assert all(same(r, alone_big) for r in rb) and all(same(r, alone_small) for r in rs)
+    run = alone_big["t_done"] - alone_big["t_admit"]
+    admits = sorted(r["t_admit"] for r in rb)
+    assert admits[1] - admits[0] > 0.3 * run and admits[2] - admits[1] > 0.3 * run  # one big run at a time
+    assert max(r["t_admit"] for r in rs) < admits[2]  # the small runs did not wait behind the big ones
