@@ -99,6 +99,8 @@ def parse():
     p.add_argument("--team-ctas", type=int, default=0,
                    help="serve: CTAs of each resident team loop (0 = one per SM; -1 = no team loop, those "
                         "requests take the stream lane)")
+    p.add_argument("--team-max-nodes", type=int, default=0,
+                   help="serve: largest lattice the team loops take (0 = the server's default, 2^19)")
     return p.parse_args()
 
 
@@ -699,7 +701,7 @@ def run_serve(args):
     import erlbm_gb300 as E
     torch.cuda.set_device(0)
     stream = serve_stream(E, args.requests, args.rate)
-    with E.Server(hbm_budget_bytes=16 << 30, team_ctas=args.team_ctas) as srv:
+    with E.Server(hbm_budget_bytes=16 << 30, team_ctas=args.team_ctas, team_max_nodes=args.team_max_nodes) as srv:
         # warm-up: one request of each kind
         for _, r in stream[:8]:
             srv.wait(srv.submit(**dict(r, n_steps=min(r["n_steps"], 10))))
@@ -729,7 +731,8 @@ def run_serve(args):
             "warmup": 8, "ms_per_step": span / max(1, len(ok)) * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded Poisson stream of config-5 requests)",
             "config": {"workload": f"serve {args.requests} requests, Poisson {args.rate:.0f}/s, mixed kinds",
-                       "requests": args.requests, "team_ctas": args.team_ctas},
+                       "requests": args.requests, "team_ctas": args.team_ctas,
+                       "team_max_nodes": args.team_max_nodes},
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "max": float(lat.max())},
             "failed": len(res) - len(ok), "lanes": {"resident": sum(1 for x in ok if x["lane"] == 0),

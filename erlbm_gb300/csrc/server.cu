@@ -465,7 +465,7 @@ bool team_plan(const erlbm_server *s, const erlbm_request &q, TeamEntry &e, std:
 {
     const TeamLane &L = s->team[q.precision == ERLBM_FP64 ? 0 : 1];
     if (L.grid < 2) return false;
-    const long long max_nodes = s->desc.team_max_nodes > 0 ? s->desc.team_max_nodes : 65536;
+    const long long max_nodes = s->desc.team_max_nodes > 0 ? s->desc.team_max_nodes : (1 << 19);
     memset(&e, 0, sizeof(e));
     std::vector<uint8_t> solid;
     switch (q.kind) {

@@ -356,8 +356,10 @@ typedef struct erlbm_server_desc {
     int queue_capacity;         /* ring entries per resident loop; 0 = 65536 */
     int team_ctas;              /* CTAs of each team loop (one per precision); 0 = SMs; < 0: no team
                                    loop, its requests take the stream lane */
-    int team_max_nodes;         /* largest lattice (nodes) the team loops take; 0 = 65536.  Larger ones
-                                   take the stream lane, whose whole-GPU step launches run them faster */
+    int team_max_nodes;         /* largest lattice (nodes) the team loops take; 0 = 2^19 (D2Q9 512^2,
+                                   D3Q19 64^3).  Larger ones take the stream lane.  A lower limit (65536)
+                                   sends the large FP64 lattices to the stream lane's whole-GPU launches,
+                                   which run them faster: more runs/s on FP64-heavy streams, higher p50 */
 } erlbm_server_desc;
 
 typedef struct erlbm_request {

@@ -183,9 +183,8 @@ def tg3d_init(L, u0):
 
 @pytest.mark.parametrize("L,steps,exact", [(32, 40, True), (64, 6, False)])
 def test_tg3d_requests_match_oracle(L, steps, exact):
-    """Config-5 3-D Taylor-Green requests (D3Q19, L^3, FP64): 32^3 through the server's resident team
-    loop, 64^3 (above its default size limit) through the stream lane.  The kinetic energy after the run
-    equals the oracle's.  Up to 65536 nodes the device sums the energy
+    """Config-5 3-D Taylor-Green requests (D3Q19, L^3, FP64) through the server's resident team loop: the
+    kinetic energy after the run equals the oracle's.  Up to 65536 nodes the device sums the energy
     serially in node order, as kinectic_energy does, so L = 32 matches bit for bit; L = 64 is a tree
     reduction, which agrees to the last digits only."""
     m = E()
@@ -193,7 +192,7 @@ def test_tg3d_requests_match_oracle(L, steps, exact):
     with m.Server(hbm_budget_bytes=1 << 30) as srv:
         r = srv.wait(srv.submit(m.REQ_TG3D, m.FP64, op=m.OP_EXTREG, L=L, tau=tau, tau_nh=tnh, u0=u0, n_steps=steps),
                      timeout=600)
-    assert r["status"] == 0 and r["steps_done"] == steps and r["lane"] == (2 if L ** 3 <= 65536 else 1)
+    assert r["status"] == 0 and r["steps_done"] == steps and r["lane"] == 2
     lat = O.Lattice(19, L, L, L, None, tau, tnh, O.OP_EXTREG)
     lat.set(tg3d_init(L, u0))
     lat.step(steps)
