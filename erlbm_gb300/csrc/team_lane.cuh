@@ -111,6 +111,7 @@ struct TeamQueue {
     int idx[TEAM_PEND];
     long long claim_ns[TEAM_PEND], est_ns[TEAM_PEND];
     int active, hungry;            // admitted runs not yet freed; of those, runs with no member
+    int rescuers, pad;             // CTAs that left a run to join a hungry one and have not joined yet
     int job_state[TEAM_MAX_JOBS];  // 0 free, 1 admitted
 };
 
@@ -427,9 +428,10 @@ static __device__ int join_run(const TeamRing &r)
     return -1;
 }
 
-// The work of one CTA in run jid, until no item is left or another run needs it.
+// The work of one CTA in run jid, until no item is left or another run needs it.  Returns true when
+// the CTA left to join a hungry run (it holds one of the rescuers' places).
 template <class P>
-__device__ void work_run(const TeamRing &r, int jid)
+__device__ bool work_run(const TeamRing &r, int jid)
 {
     using T = typename P::T;
     constexpr int NT = team_threads<P>();
@@ -602,15 +604,30 @@ __device__ void work_run(const TeamRing &r, int jid)
             __threadfence();
             const unsigned long long d = atomicAdd(&J->done, add) + add;
             if ((long long)d == total) publish(r, J, e);
-            // make room for an admitted run that has no member yet
+            // make room for an admitted run that has no member yet: as many CTAs leave their runs as
+            // there are such runs, each taking a rescuer's place first
+            s_leave = 0;
             const int m = ld_acq_gpu(&J->members);
-            s_leave = ld_acq_gpu(&r.queue->hungry) > 0 && (m & ~TEAM_CLOSED) > 1;
+            if ((m & ~TEAM_CLOSED) > 1) {
+                int hungry = ld_acq_gpu(&r.queue->hungry), resc = ld_acq_gpu(&r.queue->rescuers);
+                for (int tries = 0; tries < 4 && resc < hungry; tries++) {
+                    const int old = atomicCAS(&r.queue->rescuers, resc, resc + 1);
+                    if (old == resc) {
+                        s_leave = 1;
+                        break;
+                    }
+                    resc = old;
+                    hungry = ld_acq_gpu(&r.queue->hungry);
+                }
+            }
         }
         __syncthreads();
         if (s_leave) break;
     }
+    const bool rescuer = s_leave != 0 && s_k < total;
     if (tid == 0) leave_run(r, jid, s_k >= total);
     __syncthreads();
+    return rescuer;
 }
 
 // Admission of ring entry idx: 0 admitted, 1 not now.  Called by the admitter thread only.
@@ -729,6 +746,8 @@ __device__ void work_loop(const TeamRing &r)
     TeamCtl *ctl = r.ctl;
     if (threadIdx.x == 0) atomicAdd(&ctl->live, 1);
     const long long t0 = now_ns();
+    __shared__ int s_rescuer;
+    if (threadIdx.x == 0) s_rescuer = 0;
     for (;;) {
         if (threadIdx.x == 0) {
             int job = -2;
@@ -736,6 +755,10 @@ __device__ void work_loop(const TeamRing &r)
                                   // do not load L2 with scans of the run table
             while (job == -2) {
                 const int j = ld_acq_gpu(&r.queue->active) > 0 ? join_run(r) : -1;
+                if (s_rescuer) {  // the place is given back whether or not a hungry run was left
+                    atomicSub(&r.queue->rescuers, 1);
+                    s_rescuer = 0;
+                }
                 if (j >= 0) {
                     job = j;
                     break;
@@ -752,7 +775,8 @@ __device__ void work_loop(const TeamRing &r)
         }
         __syncthreads();
         if (s_job < 0) break;
-        work_run<P>(r, s_job);
+        const bool rescuer = work_run<P>(r, s_job);
+        if (threadIdx.x == 0) s_rescuer = rescuer ? 1 : 0;
     }
     if (threadIdx.x == 0) atomicSub(&ctl->live, 1);
 }
