@@ -361,9 +361,9 @@ class Server:
     """Continuous-batching server (erlbm_server_*): submit runs while others are on the GPU."""
 
     def __init__(self, hbm_budget_bytes: int = 8 << 30, slot_ctas: int = 0, max_streams: int = 0,
-                 queue_capacity: int = 0, team_ctas: int = 0, team_max_nodes: int = 0):
+                 queue_capacity: int = 0, team_ctas: int = 0, team_max_nodes: int = 0, team_wait_us: int = 0):
         d = _lib.ServerDesc(int(hbm_budget_bytes), int(slot_ctas), int(max_streams), int(queue_capacity),
-                            int(team_ctas), int(team_max_nodes))
+                            int(team_ctas), int(team_max_nodes), int(team_wait_us))
         h = C.c_void_p()
         check(lib().erlbm_server_start(C.byref(d), C.byref(h)), "erlbm_server_start")
         self._h = h

@@ -83,7 +83,8 @@ class BatchResult(C.Structure):
 
 class ServerDesc(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_longlong), ("slot_ctas", C.c_int), ("max_streams", C.c_int),
-                ("queue_capacity", C.c_int), ("team_ctas", C.c_int), ("team_max_nodes", C.c_int)]
+                ("queue_capacity", C.c_int), ("team_ctas", C.c_int), ("team_max_nodes", C.c_int),
+                ("team_wait_us", C.c_int)]
 
 
 class Request(C.Structure):

@@ -439,7 +439,8 @@ int team_setup(erlbm_server *s, TeamLane &L, int prec)
     r.arena = s->team_arena;
     r.n_pages = s->team_pages;
     r.idle_ns = 300000000LL;  // an idle launch leaves after 0.3 s
-    r.sync_ns = 5000000000LL; // a team barrier gives up after 5 s
+    // a run waits at most this long for the previous phase of its steps
+    r.sync_ns = s->desc.team_wait_us > 0 ? 1000LL * s->desc.team_wait_us : 5000000000LL;
     if ((e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&L.exited, cudaEventDisableTiming)) != cudaSuccess)
         return cuda_fail(e, "team lane stream");
@@ -597,7 +598,7 @@ void team_collect(erlbm_server *s, TeamLane &L)
         if (__atomic_load_n(&d.seq, __ATOMIC_ACQUIRE) == idx + 1) {
             erlbm_result r;
             memset(&r, 0, sizeof(r));
-            r.status = d.status ? ERLBM_E_CUDA : ERLBM_OK;
+            r.status = d.status ? ERLBM_E_TIMEOUT : ERLBM_OK;  // TEAM_TIMEOUT: a phase wait ran out
             r.label = d.label;
             r.steps_done = d.steps_done;
             r.decided_step = d.decided_step;

@@ -29,7 +29,8 @@
 //
 // Every wait is bounded: free CTAs leave when the admitter has left or its heartbeat is older than the
 // idle limit; the admitter leaves after the idle limit without work; an item that waits longer than
-// sync_ns for the previous phase marks the run failed (TeamDone.status TEAM_TIMEOUT) and goes on.
+// sync_ns for the previous phase marks the run failed (TeamDone.status TEAM_TIMEOUT, reported to the
+// caller as ERLBM_E_TIMEOUT) and goes on without it, so the run still ends.
 // Buffers that the launch rewrites (populations, energies, the payload copies) are read with
 // L2-coherent loads, the host's ring memory with uncached ones.
 #pragma once

@@ -360,6 +360,8 @@ typedef struct erlbm_server_desc {
                                    D3Q19 64^3).  Larger ones take the stream lane.  A lower limit (65536)
                                    sends the large FP64 lattices to the stream lane's whole-GPU launches,
                                    which run them faster: more runs/s on FP64-heavy streams, higher p50 */
+    int team_wait_us;           /* longest wait of a team-loop run for the previous phase of its steps
+                                   before the run is reported failed (status ERLBM_E_TIMEOUT); 0 = 5 s */
 } erlbm_server_desc;
 
 typedef struct erlbm_request {

@@ -304,3 +304,18 @@ def test_team_loop_admits_by_footprint():
     admits = sorted(r["t_admit"] for r in rb)
     assert admits[1] - admits[0] > 0.3 * run and admits[2] - admits[1] > 0.3 * run  # one big run at a time
     assert max(r["t_admit"] for r in rs) < admits[2]  # the small runs did not wait behind the big ones
+
+
+def test_team_loop_reports_a_phase_wait_that_runs_out():
+    """A team-loop run whose phase waits are limited to 1 us (team_wait_us) cannot wait for its steps'
+    previous phases: the wait runs out, the run goes on without it and ends with ERLBM_E_TIMEOUT
+    (-4).  A run on a server with the default limit gives the result it has alone."""
+    m = E()
+    req = dict(kind=m.REQ_TG2D, precision=m.FP64, op=m.OP_EXTREG, L=256, tau=0.6, tau_nh=0.65, u0=0.02,
+               n_steps=200)
+    with m.Server(hbm_budget_bytes=1 << 30, team_wait_us=1) as srv:
+        r = srv.wait(srv.submit(**req), timeout=600)
+    assert r["lane"] == 2 and r["status"] == -4, r
+    with m.Server(hbm_budget_bytes=1 << 30) as srv:
+        ok = srv.wait(srv.submit(**req), timeout=600)
+    assert ok["lane"] == 2 and ok["status"] == 0 and ok["steps_done"] == 200
