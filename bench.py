@@ -701,25 +701,38 @@ def run_serve(args):
     import erlbm_gb300 as E
     torch.cuda.set_device(0)
     stream = serve_stream(E, args.requests, args.rate)
-    with E.Server(hbm_budget_bytes=16 << 30, team_ctas=args.team_ctas, team_max_nodes=args.team_max_nodes) as srv:
-        # warm-up: one request of each kind
-        for _, r in stream[:8]:
-            srv.wait(srv.submit(**dict(r, n_steps=min(r["n_steps"], 10))))
-        clocks = Clocks(0)
-        clocks.start()
-        t0 = time.perf_counter()
-        tickets = []
-        for at, r in stream:
-            now = time.perf_counter() - t0
-            if at > now:
-                time.sleep(at - now)
-            tickets.append(srv.submit(**r))
-        res = [srv.wait(t, 3600.0) for t in tickets]
-        clk = clocks.stop()
-    ok = [x for x in res if x["status"] == 0]
-    lat = np.array([x["t_done"] - x["t_submit"] for x in ok])
-    span = max(x["t_done"] for x in ok) - min(x["t_submit"] for x in ok)
+
+    def serve(team_ctas, clocked):
+        """The stream through one server: (results, clock record)."""
+        with E.Server(hbm_budget_bytes=16 << 30, team_ctas=team_ctas, team_max_nodes=args.team_max_nodes) as srv:
+            # warm-up: one request of each kind
+            for _, r in stream[:8]:
+                srv.wait(srv.submit(**dict(r, n_steps=min(r["n_steps"], 10))))
+            clocks = Clocks(0)
+            if clocked:
+                clocks.start()
+            t0 = time.perf_counter()
+            tickets = []
+            for at, r in stream:
+                now = time.perf_counter() - t0
+                if at > now:
+                    time.sleep(at - now)
+                tickets.append(srv.submit(**r))
+            res = [srv.wait(t, 3600.0) for t in tickets]
+            clk = clocks.stop() if clocked else None
+        ok = [x for x in res if x["status"] == 0]
+        lat = np.array([x["t_done"] - x["t_submit"] for x in ok])
+        span = max(x["t_done"] for x in ok) - min(x["t_submit"] for x in ok)
+        return res, ok, lat, span, clk
+
+    res, ok, lat, span, clk = serve(args.team_ctas, True)
     value = len(ok) / span
+    stream_only = None
+    if not args.no_extras and args.team_ctas >= 0:
+        # the same stream with every non-slot request on the host-launched stream lane
+        _, ok2, lat2, span2, _ = serve(-1, False)
+        stream_only = {"value": len(ok2) / span2, "unit": "runs/s", "p50": float(np.percentile(lat2, 50)),
+                       "p99": float(np.percentile(lat2, 99)), "failed": args.requests - len(ok2)}
     # the plain path on an evenly strided sample of the same stream, one run after another
     m = max(1, min(args.plain_requests, len(stream)))
     sample = stream[:: max(1, len(stream) // m)][:m]
@@ -740,6 +753,7 @@ def run_serve(args):
                                                     "stream": sum(1 for x in ok if x["lane"] == 1)},
             "plain_fp64_one_run_at_a_time": {"value": plain, "unit": "runs/s", "requests": len(sample),
                                              "sample": "every k-th request of the same stream"},
+            "stream_lane_only": stream_only,
             "roofline": None, "e2e": {"value": value, "unit": "runs/s", "h2d_bytes_per_step": 64,
                                       "d2h_bytes_per_step": 64},
             "gpu_launches": None, "clocks": clk}
