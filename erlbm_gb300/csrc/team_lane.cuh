@@ -480,9 +480,14 @@ __device__ bool work_run(const TeamRing &r, int jid)
     bc.open_y = -1;
     bc.profile = nullptr;
     const long long total = s_total, cn = e.chunk, nf = e.n_fluid;
+    // thread 0: the next item, claimed while this one is worked on (-1: none claimed), and the last
+    // count of finished items it read (the count only grows)
+    long long pf = -1, known_done = 0;
+    bool last_item = false;  // leaving after the item already claimed
     for (;;) {
         if (tid == 0) {
-            const long long k = (long long)atomicAdd(&J->next, 1ull);
+            const long long k = pf >= 0 ? pf : (long long)atomicAdd(&J->next, 1ull);
+            pf = -1;
             s_k = k;
             s_noop = 0;
             if (k < total) {
@@ -491,13 +496,15 @@ __device__ bool work_run(const TeamRing &r, int jid)
                 s_step = it.step;
                 s_chunk = it.chunk;
                 // every item of the previous phases done (the step barrier); bounded
-                const long long t0 = now_ns();
-                while ((long long)ld_acq_gpu64(&J->done) < it.start) {
-                    if (now_ns() - t0 > r.sync_ns) {
-                        atomicExch(&J->error, 1);
-                        break;
+                if (known_done < it.start) {
+                    const long long t0 = now_ns();
+                    while ((known_done = (long long)ld_acq_gpu64(&J->done)) < it.start) {
+                        if (now_ns() - t0 > r.sync_ns) {
+                            atomicExch(&J->error, 1);
+                            break;
+                        }
+                        __nanosleep(64);
                     }
-                    __nanosleep(64);
                 }
                 __threadfence();
                 // a density check failed in an earlier step: the run stopped there
@@ -505,6 +512,8 @@ __device__ bool work_run(const TeamRing &r, int jid)
                 if (e.check_density && ld_acq_gpu(&J->status.flags)) sd = ld_acq_gpu(&J->status.decided_step) + 1;
                 s_sd = sd;
                 if (it.kind == kSTEP && it.step >= sd) s_noop = 1;
+                // claim the next item now: the atomic's round trip overlaps this item's work
+                if (!last_item && !s_noop) pf = (long long)atomicAdd(&J->next, 1ull);
             }
         }
         __syncthreads();
@@ -606,15 +615,20 @@ __device__ bool work_run(const TeamRing &r, int jid)
             const unsigned long long d = atomicAdd(&J->done, add) + add;
             if ((long long)d == total) publish(r, J, e);
             // make room for an admitted run that has no member yet: as many CTAs leave their runs as
-            // there are such runs, each taking a rescuer's place first
+            // there are such runs, each taking a rescuer's place first.  A CTA that holds a claimed
+            // item works on it before it leaves.
             s_leave = 0;
-            const int m = ld_acq_gpu(&J->members);
-            if ((m & ~TEAM_CLOSED) > 1) {
+            if (last_item) {
+                s_leave = 1;
+            } else if (ld_acq_gpu(&r.queue->hungry) > 0 && (ld_acq_gpu(&J->members) & ~TEAM_CLOSED) > 1) {
                 int hungry = ld_acq_gpu(&r.queue->hungry), resc = ld_acq_gpu(&r.queue->rescuers);
                 for (int tries = 0; tries < 4 && resc < hungry; tries++) {
                     const int old = atomicCAS(&r.queue->rescuers, resc, resc + 1);
                     if (old == resc) {
-                        s_leave = 1;
+                        if (pf >= 0 && pf < total)
+                            last_item = true;
+                        else
+                            s_leave = 1;
                         break;
                     }
                     resc = old;
@@ -625,8 +639,9 @@ __device__ bool work_run(const TeamRing &r, int jid)
         __syncthreads();
         if (s_leave) break;
     }
+    // a claimed item past the end leaves the run closed; one that ended the loop by leaving was worked on
     const bool rescuer = s_leave != 0 && s_k < total;
-    if (tid == 0) leave_run(r, jid, s_k >= total);
+    if (tid == 0) leave_run(r, jid, s_k >= total || pf >= total);
     __syncthreads();
     return rescuer;
 }
