@@ -76,8 +76,8 @@ def test_pair_kernel_equals_its_cpu_restatement(op):
 @pytest.mark.gpu
 def test_pair_meets_the_velocity_error_target_on_the_double_shear_layer():
     """The double shear layer (Re = 80000, E-RLBM tau_nh = 0.65) at L = 512 to t* = 1: the compensated
-    form's relative L2 velocity error against FP64 is below 1e-5 (the benchmark spec's target), where the
-    FP32-shifted form's is above it."""
+    form's relative L2 velocity error against FP64 is below the 1e-5 target for the FP32 forms, where
+    the FP32-shifted form's is above it."""
     from erlbm_gb300 import programs as P
     pair = P.precision_error(512, t_stars=(0.5, 1.0), precision=E().FP32_PAIR)
     f32 = P.precision_error(512, t_stars=(1.0,), precision=E().FP32_SHIFTED)
