@@ -146,6 +146,17 @@ def ncu_traffic(L: int, precision: str):
         return None
 
 
+def channel_traffic(nx: int, ny: int):
+    """DRAM bytes per launch of the FP32 channel kernel from its committed ncu summary, scaled by the
+    box (the capture is of the bench's own 4096 x 1024 channel)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "channel_step_traffic.json")) as f:
+            rec = json.load(f)["fp32"]
+        return (rec["dram_bytes_read"] + rec["dram_bytes_write"]) * (nx * ny) / (rec["nx"] * rec["ny"])
+    except Exception:
+        return None
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
 
@@ -928,7 +939,8 @@ def run_channel(args):
                        "l2": f"working set {bpl * n_fluid / 1e6:.0f} MB (two population buffers) "
                              f"{'>' if bpl * n_fluid > 129e6 else '<'} 129 MB L2, no flush"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": bpl * n_fluid,
+                         "peak_kind": peak_kind, "traffic": channel_traffic(nx, ny) if prec != E.FP64 else None,
+                         "algorithmic_bytes_per_launch": bpl * n_fluid,
                          "launch_us": launch_ms * 1e3, "lattice_updates_per_launch": n_fluid,
                          "kernel": "k_step<PrecExact64,9,4>" if prec == E.FP64 else "k_d2q9_hybrid<4>"},
             "e2e": {"value": n_fluid * inner * K / t_e2e / 1e6, "unit": "MLUPS",
