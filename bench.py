@@ -402,11 +402,13 @@ def run_ours(args):
            "d2h_bytes_per_step": 8}
 
     lat.close()
-    extras, fp64 = {}, None
+    extras, fp64, pair = {}, None, None
     if not args.no_extras and rank == 0:
         extras = gpu_extras(E, torch, L, f0, tau, op, tnh)
         if args.precision == "fp32":
             fp64 = fp64_block(E, torch, L, f0, tau, op, tnh, K, W, args.inner_fp64)
+            if args.op in ("erlbm", "reg", "bgk"):  # the compensated form has no MRT
+                pair = pair_block(E, torch, L, f0, tau, op, tnh, K, W, 100)
 
     if rank != 0:
         if dist:
@@ -454,7 +456,12 @@ def run_ours(args):
         line["cpu_baseline"] = cpu
     if fp64:
         line["fp64"] = fp64
+    if pair:
+        line["pair"] = pair
     if extras:
+        acc = accuracy_t1()
+        if acc and args.precision == "fp32":
+            extras["fp32_vs_fp64_rel_l2_velocity_at_t1"] = acc.get("fp32")
         line["extras"] = extras
     print(json.dumps(line), flush=True)
     if dist:
@@ -473,14 +480,12 @@ def fp64_ops_per_lu(L: int):
         return None
 
 
-def fp64_block(E, torch, L, f0, tau, op, tnh, K, W, inner):
-    """The plain FP64 path (bit-identical to the reference) on the same lattice: device-timed MLUPS over
-    K bench steps of `inner` LBM steps, the same end to end through the C ABI (populations from pinned
-    host memory, steps, energy back), and its roofline against this GPU's FP64 add / multiply rate
-    (measured here with erlbm_fp64_rate) and against the HBM copy peak."""
+def time_lattice(E, torch, L, f0, tau, op, tnh, K, W, inner, prec):
+    """One DSL lattice in precision `prec`: device-timed MLUPS over K bench steps of `inner` LBM steps,
+    and the same end to end through the C ABI (populations from pinned host memory, steps, energy
+    back).  Returns (MLUPS, ms per bench step, us per launch, e2e MLUPS)."""
     s = torch.cuda.Stream()
-    out = {"lbm_steps_per_step": inner, "steps": K, "warmup": W}
-    with E.Lattice(9, L, L, 1, None, tau, tnh, op, E.FP64) as lat:
+    with E.Lattice(9, L, L, 1, None, tau, tnh, op, prec) as lat:
         lat.set_stream(s.cuda_stream)
         lat.set_populations(f0)
         lat.step(1)
@@ -496,7 +501,6 @@ def fp64_block(E, torch, L, f0, tau, op, tnh, K, W, inner):
         s.synchronize()
         ms = a.elapsed_time(b)
         value = L * L * inner * K / (ms / 1e3) / 1e6
-        launch_us = ms / (K * inner) * 1e3
         pinned = torch.empty(f0.size, dtype=torch.float64, pin_memory=True)
         pinned.numpy()[:] = f0
         host = pinned.numpy()
@@ -509,14 +513,22 @@ def fp64_block(E, torch, L, f0, tau, op, tnh, K, W, inner):
             lat.step(inner)
             lat.kinetic_energy(E.STAGE_POST_COLLISION)
         t_e2e = time.perf_counter() - t0
+    return value, ms / K, ms / (K * inner) * 1e3, L * L * inner * K / t_e2e / 1e6
+
+
+def fp64_block(E, torch, L, f0, tau, op, tnh, K, W, inner):
+    """The plain FP64 path (bit-identical to the reference) on the same lattice: device-timed and end to
+    end, with its roofline against this GPU's FP64 add / multiply rate (measured here with
+    erlbm_fp64_rate) and against the HBM copy peak."""
+    value, ms_step, launch_us, e2e = time_lattice(E, torch, L, f0, tau, op, tnh, K, W, inner, E.FP64)
     rate = E.fp64_rate()
     ops = fp64_ops_per_lu(L)
     hbm, hbm_kind = peaks()
-    out.update({
-        "value": value, "unit": "MLUPS", "dtype": "f64", "ms_per_step": ms / K,
+    return {
+        "lbm_steps_per_step": inner, "steps": K, "warmup": W,
+        "value": value, "unit": "MLUPS", "dtype": "f64", "ms_per_step": ms_step,
         "kernel": f"k_step<PrecExact64,9,{op}>",
-        "e2e": {"value": L * L * inner * K / t_e2e / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": int(f0.nbytes),
-                "d2h_bytes_per_step": 8},
+        "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": 8},
         "roofline": {"bound": "fp64", "unit": "Gop/s",
                      "achieved": None if ops is None else ops * value * 1e6 / 1e9,
                      "peak": rate / 1e9, "peak_kind": "measured in this run (erlbm_fp64_rate: unfused DADD/DMUL)",
@@ -524,8 +536,37 @@ def fp64_block(E, torch, L, f0, tau, op, tnh, K, W, inner):
                      "fp64_ops_per_lu": ops, "launch_us": launch_us},
         "hbm": {"bytes_per_lu": BYTES_PER_LU["fp64"], "achieved_gbs": value * 1e6 * BYTES_PER_LU["fp64"] / 1e9,
                 "peak_gbs": hbm, "frac": value * 1e6 * BYTES_PER_LU["fp64"] / 1e9 / hbm, "peak_kind": hbm_kind},
-    })
+    }
+
+
+def pair_block(E, torch, L, f0, tau, op, tnh, K, W, inner):
+    """The compensated FP32 form (float-pair populations, float-float collision), the FP32 variant that
+    meets the 1e-5 velocity-error target, on the same lattice: device-timed and end to end, against
+    the HBM copy peak at its 144 B per update, with its measured error at t* = 1."""
+    value, ms_step, launch_us, e2e = time_lattice(E, torch, L, f0, tau, op, tnh, K, W, inner, E.FP32_PAIR)
+    hbm, hbm_kind = peaks()
+    out = {
+        "lbm_steps_per_step": inner, "steps": K, "warmup": W,
+        "value": value, "unit": "MLUPS", "dtype": "f32x2", "ms_per_step": ms_step, "kernel": f"k_step_pair<{op}>",
+        "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": 8},
+        "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": value * 1e6 * BYTES_PER_LU["pair"] / 1e9,
+                     "peak": hbm, "frac": value * 1e6 * BYTES_PER_LU["pair"] / 1e9 / hbm, "peak_kind": hbm_kind,
+                     "bytes_per_lu": BYTES_PER_LU["pair"], "launch_us": launch_us},
+    }
+    acc = accuracy_t1()
+    if acc:
+        out["rel_l2_velocity_vs_fp64_at_t1"] = acc.get("pair")
     return out
+
+
+def accuracy_t1():
+    """Relative L2 velocity errors against FP64 at t* = 1 of the double shear layer (65 537 steps at
+    L = 2048, too long for a bench step), from the committed measurement (programs.precision_error)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "accuracy_t1.json")) as f:
+            return json.load(f)
+    except Exception:
+        return None
 
 
 def gpu_extras(E, torch, L, f0, tau, op, tnh):
