@@ -238,10 +238,13 @@ class CpuDsl:
             self._fn = fn
             self.kind = "reference"
             # each harness call sets the lattice up and copies its output: that fixed cost (a 1-step call
-            # less one step, the step time taken from a 1-step and a 5-step call) is taken out of every sample
+            # less one step, the step time taken from a 1-step and a 5-step call) is taken out of every
+            # sample.  The first call pays one-time costs (threads, pages) and is not used; the step time
+            # is at least a tenth of the 5-step call's, so that noise cannot make it vanish.
+            self._call(1)
             t1 = self._call(1)
             t5 = self._call(5)
-            self.step_s = max((t5 - t1) / 4, 1e-6)
+            self.step_s = max((t5 - t1) / 4, t5 / 10, 1e-6)
             self.overhead = max(0.0, t1 - self.step_s)
         else:
             self._lat = O.Lattice(9, L, L, 1, None, self.tau, self.tnh, self.op)
