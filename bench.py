@@ -101,6 +101,8 @@ def parse():
                         "requests take the stream lane)")
     p.add_argument("--team-max-nodes", type=int, default=0,
                    help="serve: largest lattice the team loops take (0 = the server's default, 2^19)")
+    p.add_argument("--single-runs", action="store_true",
+                   help="serve: also time single requests alone on the team loop and on the stream lane")
     return p.parse_args()
 
 
@@ -750,6 +752,39 @@ def plain_run(E, r):
         return lat.kinetic_energy()
 
 
+def serve_single_runs(E, args):
+    """Wall time (ms) from submission to result of single requests on an otherwise idle server, on the
+    team loop and on the stream lane, and of 16 copies of the 64^3 FP64 request submitted together."""
+    reqs = {
+        "tg3d64_fp64": dict(kind=E.REQ_TG3D, precision=E.FP64, op=E.OP_EXTREG, L=64, tau=0.55, tau_nh=0.65,
+                            u0=0.05, n_steps=500),
+        "tg2d512_fp64": dict(kind=E.REQ_TG2D, precision=E.FP64, op=E.OP_EXTREG, L=512, tau=0.56, tau_nh=0.65,
+                             u0=2 / 512, n_steps=500),
+        "tg3d64_fp32": dict(kind=E.REQ_TG3D, precision=E.FP32_SHIFTED, op=E.OP_EXTREG, L=64, tau=0.55, tau_nh=0.65,
+                            u0=0.05, n_steps=500),
+        "tg2d512_fp32": dict(kind=E.REQ_TG2D, precision=E.FP32_SHIFTED, op=E.OP_EXTREG, L=512, tau=0.56,
+                             tau_nh=0.65, u0=2 / 512, n_steps=500),
+        "tg2d64_fp64": dict(kind=E.REQ_TG2D, precision=E.FP64, op=E.OP_EXTREG, L=64, tau=0.56, tau_nh=0.65,
+                            u0=2 / 64, n_steps=500),
+        "obstacle3x3_fp64": dict(kind=E.REQ_OBSTACLE, precision=E.FP64, op=E.OP_EXTREG, sx=3, sy=3, tau=0.52,
+                                 tau_nh=0.6, u0=0.05, n_steps=500),
+    }
+    out = {}
+    for lane, team_ctas in (("team", args.team_ctas), ("stream", -1)):
+        with E.Server(hbm_budget_bytes=4 << 30, team_ctas=team_ctas, team_max_nodes=args.team_max_nodes) as srv:
+            for name, r in reqs.items():
+                srv.wait(srv.submit(**dict(r, n_steps=5)), 600.0)
+                t = time.perf_counter()
+                srv.wait(srv.submit(**r), 600.0)
+                out.setdefault(name, {})[lane + "_ms"] = (time.perf_counter() - t) * 1e3
+            t = time.perf_counter()
+            tickets = [srv.submit(**reqs["tg3d64_fp64"]) for _ in range(16)]
+            for x in tickets:
+                srv.wait(x, 600.0)
+            out.setdefault("16x_tg3d64_fp64", {})[lane + "_ms"] = (time.perf_counter() - t) * 1e3
+    return out
+
+
 def run_serve(args):
     import numpy as np
     import torch
@@ -782,6 +817,7 @@ def run_serve(args):
 
     res, ok, lat, span, clk = serve(args.team_ctas, True)
     value = len(ok) / span
+    singles = serve_single_runs(E, args) if args.single_runs else None
     stream_only = None
     if not args.no_extras and args.team_ctas >= 0:
         # the same stream with every non-slot request on the host-launched stream lane
@@ -809,6 +845,7 @@ def run_serve(args):
             "plain_fp64_one_run_at_a_time": {"value": plain, "unit": "runs/s", "requests": len(sample),
                                              "sample": "every k-th request of the same stream"},
             "stream_lane_only": stream_only,
+            "single_runs": singles,
             "roofline": None, "e2e": {"value": value, "unit": "runs/s", "h2d_bytes_per_step": 64,
                                       "d2h_bytes_per_step": 64},
             "gpu_launches": None, "clocks": clk}
