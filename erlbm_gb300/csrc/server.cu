@@ -331,6 +331,20 @@ int lane_launch(SlotLane &L)
     return ERLBM_OK;
 }
 
+// A resident loop that cannot be launched cannot serve what was published to it: those requests end
+// with the launch's error.
+template <class Lane>
+void fail_outstanding(erlbm_server *s, Lane &L, int rc, int lane)
+{
+    for (const int idx : L.outstanding) {
+        auto it = L.ticket_of.find(idx);
+        if (it == L.ticket_of.end()) continue;
+        finish(s, it->second, error_result(rc, lane));
+        L.ticket_of.erase(it);
+    }
+    L.outstanding.clear();
+}
+
 int lane_submit(erlbm_server *s, SlotLane &L, int64_t ticket, const erlbm_request &q)
 {
     const int cap = s->desc.queue_capacity;
@@ -380,7 +394,10 @@ void lane_collect(erlbm_server *s, SlotLane &L)
         }
     }
     if (L.running && cudaEventQuery(L.exited) == cudaSuccess) L.running = false;
-    if (!L.running && !L.outstanding.empty() && !s->stopping.load()) lane_launch(L);
+    if (!L.running && !L.outstanding.empty() && !s->stopping.load()) {
+        const int rc = lane_launch(L);
+        if (rc != ERLBM_OK) fail_outstanding(s, L, rc, 0);
+    }
 }
 
 // ---- team lane --------------------------------------------------------------------------------
@@ -616,7 +633,10 @@ void team_collect(erlbm_server *s, TeamLane &L)
         }
     }
     if (L.running && cudaEventQuery(L.exited) == cudaSuccess) L.running = false;
-    if (!L.running && !L.outstanding.empty() && !s->stopping.load()) team_launch(L);
+    if (!L.running && !L.outstanding.empty() && !s->stopping.load()) {
+        const int rc = team_launch(L);
+        if (rc != ERLBM_OK) fail_outstanding(s, L, rc, 2);
+    }
 }
 
 // ---- stream lane ------------------------------------------------------------------------------
@@ -1017,7 +1037,10 @@ void scheduler(erlbm_server *s)
                 s->pending_a[l].pop_front();
                 any = true;
             }
-            if (any && !L.running) lane_launch(L);
+            if (any && !L.running) {
+                const int rc = lane_launch(L);
+                if (rc != ERLBM_OK) fail_outstanding(s, L, rc, 0);
+            }
         }
         // publish team-lane requests while their ring has space; the device admits them
         for (int l = 0; l < 2; l++) {
@@ -1030,7 +1053,10 @@ void scheduler(erlbm_server *s)
                 s->pending_c[l].pop_front();
                 any = true;
             }
-            if (any && !L.running) team_launch(L);
+            if (any && !L.running) {
+                const int rc = team_launch(L);
+                if (rc != ERLBM_OK) fail_outstanding(s, L, rc, 2);
+            }
         }
         // admit stream-lane runs while memory and streams allow
         admit_stream_lane(s);
