@@ -1,10 +1,10 @@
 // team_lane.cuh -- the request server's resident team loop (server.cu): mixed-size lattices admitted
 // on the device by HBM footprint and stepped by the CTAs of one persistent launch.
 //
-// The reference has no serving path.  This lane takes the lattices that are too large for one CTA's
-// shared memory but small enough that a whole-GPU launch per step would be bound by launch latency:
-// D2Q9 Taylor-Green up to 512^2, D3Q19 Taylor-Green up to 64^3, the obstacle channel scaled by more
-// than 1.  One launch per precision stays resident while it has work:
+// The reference has no serving path.  This lane takes the lattices too large for one CTA's shared
+// memory, up to the server's team_max_nodes (by default D2Q9 Taylor-Green up to 512^2, D3Q19
+// Taylor-Green up to 64^3, the obstacle channels scaled by more than 1), and runs them with no host
+// launch per run or per step.  One launch per precision stays resident while it has work:
 //
 //  admitter  thread 0 of the CTA that wins the election.  It claims requests from a ring in mapped
 //            pinned memory as the host publishes them, keeps up to TEAM_PEND of them waiting, and
@@ -14,12 +14,13 @@
 //            precisions' launches, claimed with CAS.  The first request that does not fit stops the
 //            pass, so memory frees up for it.
 //  workers   every other CTA.  A run is a sequence of work items: the copy of its tables and solid
-//            mask from the ring, the initial state in chunks of nodes, each step in the same chunks, the final kinetic energy per node in chunks, its
-//            partial sums, the final sum.  A free CTA joins the run with the fewest CTAs for its
-//            size, and its members take the next item from the run's counter until none is left.
+//            mask from the ring, the initial state in chunks of nodes, each step in the same chunks,
+//            the final kinetic energy per node in chunks, its partial sums, the final sum.  A free
+//            CTA joins the run with the fewest CTAs for its size, and its members take the next item
+//            from the run's counter (claiming it while the previous one runs) until none is left.
 //            An item waits until every item of the previous phases is done, which is the step
-//            barrier.  A member leaves a run with other members whenever an admitted run has none,
-//            so small runs admitted behind large ones start at once.  The CTA that finishes the last
+//            barrier.  When admitted runs have no member, as many CTAs leave runs that have other
+//            members, so small runs admitted behind large ones start at once.  The CTA that finishes the last
 //            item publishes the result; the last member out frees the pages.
 //
 // Results do not depend on how many CTAs work on a run, nor on the mix: each node's update reads only
