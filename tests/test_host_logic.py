@@ -157,6 +157,20 @@ def test_channel_bench_geometry_fits_the_parabolic_inlet():
         assert s[ny // 2, ny] == 1 and s[ny // 2, 2 * ny] == 0  # the cylinder, and open channel behind it
 
 
+def test_bench_reads_its_committed_measurements():
+    """The bench line's `roofline.traffic` of the channel and the t* = 1 errors come from committed
+    ncu and accuracy measurements: the files parse, the channel traffic scales with the box from the
+    captured 4096 x 1024 channel, and the errors say which FP32 form meets the 1e-5 target."""
+    import bench
+    t = bench.channel_traffic(4096, 1024)
+    assert t is not None and 72 * 4096 * 1024 * 0.5 < t < 72 * 4096 * 1024 * 1.5
+    assert abs(bench.channel_traffic(2048, 512) - t / 4) < 1
+    acc = bench.accuracy_t1()
+    assert acc["fp32"]["met"] is False and acc["fp32"]["L2048"] > 1e-5
+    assert acc["pair"]["met"] is True and acc["pair"]["L2048"] < 1e-5
+    assert bench.ncu_traffic(2048, "fp32_x3a") > 0 and bench.fp64_ops_per_lu(2048) == 169
+
+
 def test_bench_launch_count_follows_erlbm_step():
     """bench.py's launch count per call of n steps: graph blocks of 64 steps (66 with three steps per
     launch), then multi-step launches, then single steps -- the decomposition erlbm_step makes."""
